@@ -1,0 +1,528 @@
+"""Drop-in replacement for GLASS's ``_glass_cuda_native`` extension module.
+
+GLASS loads its CUDA backend with ``importlib.import_module("_glass_cuda_native")``
+(src/glass_cuda.py:31-44) and reaches it through the names that the pybind11
+module exports (cpp/src/native_bindings.cpp:20383-21200).  This module offers
+those names on top of libglass_gb300.so (include/glass_gb300.h) through ctypes,
+so src/glass_cuda.py, src/glass/engine/resident_cuda.py and ``glass run
+--backend cuda`` run unchanged.  ``glass_gb300.install_drop_in()`` registers it
+under the reference's module name.
+
+Error behaviour follows the reference: argument errors raise ValueError
+(std::invalid_argument), bad frame indices IndexError (std::out_of_range),
+state and CUDA failures RuntimeError (check_cuda, native_bindings.cpp:1011).
+Callers feature-gate with ``hasattr`` (glass_cuda.py:2740-2760), so methods
+that are not provided here make the façade raise its own clear RuntimeError.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import weakref
+from time import perf_counter
+from typing import Any
+
+import numpy as np
+
+from glass_gb300 import _lib
+
+_lib.load()
+
+__all__ = [
+    "ResidentCalibratedStack",
+    "calibrate_tile_f32",
+    "cuda_available",
+    "get_device_info",
+    "host_pinned_empty_f32",
+    "host_pinned_empty_u8",
+    "list_devices",
+    "resident_dq_map_count_maps_i16",
+]
+
+
+# ---------------------------------------------------------------------------
+# module functions
+# ---------------------------------------------------------------------------
+def cuda_available() -> bool:
+    flag = ctypes.c_int(0)
+    _lib.call("gg_cuda_available", ctypes.byref(flag))
+    return bool(flag.value)
+
+
+def get_device_info(device_id: int = 0) -> dict[str, Any]:
+    info = _lib.DeviceInfo()
+    _lib.call("gg_device_info", int(device_id), ctypes.byref(info))
+    return {
+        "device_id": int(device_id),
+        "name": info.name.decode("utf-8", "replace"),
+        "compute_capability": f"{info.major}.{info.minor}",
+        "major": int(info.major),
+        "minor": int(info.minor),
+        "multiprocessor_count": int(info.multiprocessor_count),
+        "total_memory_bytes": int(info.total_global_mem),
+        "l2_cache_bytes": int(info.l2_cache_bytes),
+        "shared_memory_per_block_optin": int(info.shared_mem_per_block_optin),
+    }
+
+
+def list_devices() -> list[dict[str, Any]]:
+    count = ctypes.c_int(0)
+    _lib.call("gg_device_count", ctypes.byref(count))
+    return [get_device_info(i) for i in range(count.value)]
+
+
+class _PinnedBuffer:
+    """Page-locked host allocation exposed to NumPy (freed with the last view)."""
+
+    def __init__(self, nbytes: int, dtype: np.dtype, shape: tuple[int, ...]):
+        address = ctypes.c_void_p()
+        _lib.call("gg_host_alloc_pinned", ctypes.c_size_t(max(int(nbytes), 1)), ctypes.byref(address))
+        self.address = int(address.value)
+        self.__array_interface__ = {
+            "shape": shape,
+            "typestr": np.dtype(dtype).str,
+            "data": (self.address, False),
+            "version": 3,
+        }
+        weakref.finalize(self, _lib.load().gg_host_free_pinned, ctypes.c_void_p(self.address))
+
+
+def host_pinned_empty_f32(height: int, width: int) -> np.ndarray:
+    h, w = int(height), int(width)
+    if h <= 0 or w <= 0:
+        raise ValueError("height and width must be positive")
+    return np.asarray(_PinnedBuffer(h * w * 4, np.float32, (h, w)))
+
+
+def host_pinned_empty_u8(byte_count: int) -> np.ndarray:
+    n = int(byte_count)
+    if n < 0:
+        raise ValueError("byte_count must be non-negative")
+    return np.asarray(_PinnedBuffer(n, np.uint8, (n,)))
+
+
+def _policy_fields(policy: Any | None) -> tuple[bool, bool, float, float]:
+    """Fields of CalibrationPolicy the calibration reads (models.py:67-81)."""
+    p = policy if isinstance(policy, dict) else ({} if policy is None else dict(policy))
+    return (
+        bool(p.get("master_dark_includes_bias", True)),
+        bool(p.get("dark_scaling_enabled", True)),
+        float(p.get("flat_floor", 1.0e-6)),
+        float(p.get("pedestal", 0.0)),
+    )
+
+
+def _calib_params(policy: Any | None, has_dark: bool, light_exposure_s: float,
+                  dark_exposure_s: float | None) -> _lib.CalibParams:
+    """cpu/calibration.py:62-66: scale = t_light / t_dark when scaling applies."""
+    includes_bias, scaling, floor, pedestal = _policy_fields(policy)
+    scale = 1.0
+    if has_dark and scaling and dark_exposure_s not in (None, 0):
+        scale = float(light_exposure_s) / float(dark_exposure_s)
+    return _lib.CalibParams(int(includes_bias), float(scale), float(floor), float(pedestal))
+
+
+def _f32(value: Any, name: str) -> np.ndarray:
+    array = np.ascontiguousarray(np.asarray(value, dtype=np.float32))
+    if array.ndim != 2 and name != "frame":
+        raise ValueError(f"{name} must be a 2-D array")
+    return array
+
+
+def calibrate_tile_f32(light: Any, bias: Any | None, dark: Any | None, flat: Any | None,
+                       light_exposure_s: float, dark_exposure_s: float | None,
+                       policy: Any | None = None) -> np.ndarray:
+    """Module `calibrate_tile_f32` (glass_cuda.py:477-508)."""
+    light_a = np.ascontiguousarray(np.asarray(light, dtype=np.float32))
+    masters = []
+    for name, m in (("bias", bias), ("dark", dark), ("flat", flat)):
+        if m is None:
+            masters.append(None)
+            continue
+        arr = np.ascontiguousarray(np.asarray(m, dtype=np.float32))
+        if arr.shape != light_a.shape:
+            raise ValueError(f"{name} shape {arr.shape} does not match light shape {light_a.shape}")
+        masters.append(arr)
+    params = _calib_params(policy, dark is not None, light_exposure_s, dark_exposure_s)
+    out = np.empty_like(light_a)
+    _lib.call(
+        "gg_calibrate_tile_f32",
+        _lib.ptr(light_a), _lib.ptr(masters[0]), _lib.ptr(masters[1]), _lib.ptr(masters[2]),
+        ctypes.c_int64(light_a.size), ctypes.byref(params), _lib.ptr(out),
+    )
+    return out
+
+
+def resident_dq_map_count_maps_i16(master: Any, weight_map: Any, coverage_map: Any | None = None,
+                                   low_rejection_map: Any | None = None,
+                                   high_rejection_map: Any | None = None,
+                                   geometric_warp_coverage_map: Any | None = None,
+                                   active_frame_count: int = 0) -> np.ndarray:
+    """Module `resident_dq_map_count_maps_i16` (glass_cuda.py:270-290)."""
+    m = np.ascontiguousarray(np.asarray(master, dtype=np.float32))
+    w = np.ascontiguousarray(np.asarray(weight_map, dtype=np.float32))
+    if w.shape != m.shape:
+        raise ValueError("weight_map must have the master shape")
+
+    def opt(x):
+        if x is None:
+            return None
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+        if a.shape != m.shape:
+            raise ValueError("count maps must have the master shape")
+        return a
+
+    cov, low, high, geo = (opt(x) for x in (coverage_map, low_rejection_map, high_rejection_map,
+                                             geometric_warp_coverage_map))
+    dq = np.empty(m.shape, dtype=np.int16)
+    _lib.call("gg_dq_map_i16", _lib.ptr(m), _lib.ptr(w), _lib.ptr(cov), _lib.ptr(low), _lib.ptr(high),
+              _lib.ptr(geo), ctypes.c_int64(m.size), ctypes.c_int64(int(active_frame_count)), _lib.ptr(dq))
+    return dq
+
+
+# ---------------------------------------------------------------------------
+# ResidentCalibratedStack
+# ---------------------------------------------------------------------------
+_DOWNLOAD_MODES = {"full", "master_weight", "master_only"}
+
+
+class ResidentCalibratedStack:
+    """VRAM-resident calibrated stack (native_bindings.cpp:2915-2934).
+
+    Frames live in padded slots of one HBM allocation; the device table
+    frame->slot lets warps swap output slots instead of copying frames back.
+    """
+
+    def __init__(self, frame_count: int, height: int, width: int):
+        handle = ctypes.c_void_p()
+        _lib.call("gg_stack_create", ctypes.c_int64(int(frame_count)), ctypes.c_int64(int(height)),
+                  ctypes.c_int64(int(width)), ctypes.byref(handle))
+        self._handle = handle
+        self._finalizer = weakref.finalize(self, _lib.load().gg_stack_destroy, handle)
+        self._last_count_dtype: np.dtype | None = None
+
+    # ---- plumbing ----------------------------------------------------------
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._handle
+
+    def _info(self) -> _lib.StackInfo:
+        info = _lib.StackInfo()
+        _lib.call("gg_stack_info", self._handle, ctypes.byref(info))
+        return info
+
+    def close(self) -> None:
+        self._finalizer()
+
+    def set_stream(self, cuda_stream: int | None) -> None:
+        """Enqueues this stack's work on an external cudaStream_t (None: own stream)."""
+        _lib.call("gg_stack_set_stream", self._handle, ctypes.c_void_p(int(cuda_stream) if cuda_stream else 0))
+
+    def synchronize(self) -> None:
+        _lib.call("gg_stack_synchronize", self._handle)
+
+    def device_pointers(self) -> dict[str, int]:
+        ptrs = _lib.StackDevicePtrs()
+        _lib.call("gg_stack_device_ptrs", self._handle, ctypes.byref(ptrs))
+        return {name: int(getattr(ptrs, name) or 0) for name, _ in _lib.StackDevicePtrs._fields_}
+
+    # ---- properties (native_bindings.cpp:20624-20645) -----------------------
+    @property
+    def frame_count(self) -> int:
+        return int(self._info().frame_count)
+
+    @property
+    def height(self) -> int:
+        return int(self._info().height)
+
+    @property
+    def width(self) -> int:
+        return int(self._info().width)
+
+    @property
+    def pixels_per_frame(self) -> int:
+        return int(self._info().pixels_per_frame)
+
+    @property
+    def loaded_count(self) -> int:
+        return int(self._info().loaded_count)
+
+    @property
+    def bytes_allocated(self) -> int:
+        return int(self._info().bytes_allocated)
+
+    @property
+    def warp_scratch_bytes(self) -> int:
+        return int(self._info().warp_scratch_bytes)
+
+    @property
+    def warp_copy_mode(self) -> str:
+        return "slot_swap_no_copy"
+
+    @property
+    def host_pinned_bytes(self) -> int:
+        return int(self._info().host_pinned_bytes)
+
+    @property
+    def calibration_lane_count(self) -> int:
+        return int(self._info().calibration_lane_count)
+
+    @property
+    def warp_coverage_frame_count(self) -> int:
+        return int(self._info().warp_coverage_frame_count)
+
+    @property
+    def frame_stride(self) -> int:
+        return int(self._info().frame_stride)
+
+    # ---- masters / upload / download ---------------------------------------
+    def _frame_array(self, value: Any, name: str) -> np.ndarray:
+        info = self._info()
+        array = np.ascontiguousarray(np.asarray(value, dtype=np.float32))
+        if array.shape != (info.height, info.width):
+            raise ValueError(f"{name} must have shape ({info.height}, {info.width}), got {array.shape}")
+        return array
+
+    def set_calibration_masters(self, bias: Any | None = None, dark: Any | None = None,
+                                flat: Any | None = None) -> None:
+        arrays = [None if m is None else self._frame_array(m, n)
+                  for m, n in ((bias, "bias"), (dark, "dark"), (flat, "flat"))]
+        _lib.call("gg_stack_set_masters", self._handle, *(_lib.ptr(a) for a in arrays))
+
+    def upload_calibrated_frame(self, index: int, frame: Any) -> None:
+        array = self._frame_array(frame, "frame")
+        _lib.call("gg_stack_upload_frame", self._handle, ctypes.c_int64(int(index)), _lib.ptr(array))
+
+    def download_frame_tile(self, index: int, x0: int, y0: int, x1: int, y1: int) -> np.ndarray:
+        return self.download_frames_tile(np.asarray([index], dtype=np.int64), x0, y0, x1, y1)[0]
+
+    def download_frames_tile(self, indices: Any, x0: int, y0: int, x1: int, y1: int) -> np.ndarray:
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+        if idx.size == 0:
+            raise ValueError("indices must contain at least one frame index")
+        out = np.empty((idx.size, max(int(y1) - int(y0), 0), max(int(x1) - int(x0), 0)), dtype=np.float32)
+        _lib.call("gg_stack_download_frames_tile", self._handle, _lib.ptr(idx), ctypes.c_int64(idx.size),
+                  ctypes.c_int64(int(x0)), ctypes.c_int64(int(y0)), ctypes.c_int64(int(x1)),
+                  ctypes.c_int64(int(y1)), _lib.ptr(out))
+        return out
+
+    def download_frame(self, index: int) -> np.ndarray:
+        info = self._info()
+        return self.download_frame_tile(index, 0, 0, info.width, info.height)
+
+    # ---- calibration ---------------------------------------------------------
+    def _params(self, light_exposure_s: float, dark_exposure_s: float | None, policy: Any | None):
+        return _calib_params(policy, bool(self._info().has_dark), light_exposure_s, dark_exposure_s)
+
+    def calibrate_frame(self, index: int, light: Any, light_exposure_s: float,
+                        dark_exposure_s: float | None, policy: Any | None = None) -> None:
+        array = self._frame_array(light, "light")
+        params = self._params(light_exposure_s, dark_exposure_s, policy)
+        _lib.call("gg_stack_calibrate_f32", self._handle, ctypes.c_int64(int(index)), _lib.ptr(array),
+                  ctypes.byref(params))
+
+    def calibrate_frame_timed(self, index: int, light: Any, light_exposure_s: float,
+                              dark_exposure_s: float | None, policy: Any | None = None) -> dict[str, Any]:
+        start = perf_counter()
+        self.calibrate_frame(index, light, light_exposure_s, dark_exposure_s, policy)
+        total = perf_counter() - start
+        return {"schema_version": 1, "h2d_mode": "pageable", "event_mode": "none", "host_copy_s": 0.0,
+                "h2d_s": 0.0, "calibrate_store_s": total, "total_s": total,
+                "host_pinned_bytes": self.host_pinned_bytes}
+
+    def calibrate_frames_u16(self, indices: Any, raw_lights: Any, light_exposure_s: float,
+                             dark_exposure_s: float | None, policy: Any | None = None,
+                             big_endian_bzero: bool = False) -> None:
+        """Fused uint16 decode + calibrate of a (n, H, W) uint16 block (one H2D pipeline)."""
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+        raw = np.asarray(raw_lights)
+        info = self._info()
+        if raw.dtype not in (np.dtype(np.uint16), np.dtype(">u2"), np.dtype(np.int16)):
+            raise ValueError("raw lights must be uint16")
+        raw = np.ascontiguousarray(raw.view(np.uint16) if raw.dtype != np.uint16 else raw)
+        if raw.shape != (idx.size, info.height, info.width):
+            raise ValueError(f"raw lights must have shape ({idx.size}, {info.height}, {info.width})")
+        params = self._params(light_exposure_s, dark_exposure_s, policy)
+        _lib.call("gg_stack_calibrate_u16", self._handle, _lib.ptr(idx), ctypes.c_int64(idx.size),
+                  _lib.ptr(raw), int(bool(big_endian_bzero)), ctypes.byref(params))
+        self.synchronize()
+
+    def calibrate_frames_fits_u16be_bzero_host_async_multistream_callback_release_timed(
+        self, indices: Any, raw_lights: Any, light_exposures_s: Any, dark_exposures_s: Any,
+        stream_count: int, wave_frames: int, release_callback: Any, policy: Any | None = None,
+    ) -> dict[str, Any]:
+        """FITS BITPIX=16 big-endian raw bytes (BZERO 32768) per frame (native_bindings.cpp:7422-8094)."""
+        idx = np.asarray(indices, dtype=np.int64).reshape(-1)
+        raws = list(raw_lights)
+        t_l = np.asarray(light_exposures_s, dtype=np.float32).reshape(-1)
+        t_d = np.asarray(dark_exposures_s, dtype=np.float32).reshape(-1)
+        if not (len(raws) == idx.size == t_l.size == t_d.size):
+            raise ValueError("indices, raw_lights and exposures must have the same length")
+        info = self._info()
+        frame_bytes = info.height * info.width * 2
+        start = perf_counter()
+        for k in range(idx.size):
+            buf = np.ascontiguousarray(np.asarray(raws[k]).view(np.uint8).reshape(-1))
+            if buf.size < frame_bytes:
+                raise ValueError(f"raw light {k} has {buf.size} bytes, expected {frame_bytes}")
+            dark_t = None if not np.isfinite(t_d[k]) or t_d[k] == 0 else float(t_d[k])
+            params = self._params(float(t_l[k]), dark_t, policy)
+            one = np.asarray([idx[k]], dtype=np.int64)
+            _lib.call("gg_stack_calibrate_u16", self._handle, _lib.ptr(one), ctypes.c_int64(1), _lib.ptr(buf),
+                      1, ctypes.byref(params))
+        self.synchronize()
+        if release_callback is not None:
+            for k in range(idx.size):
+                release_callback(int(k))
+        total = perf_counter() - start
+        return {"schema_version": 1, "h2d_mode": "pinned_lanes", "frames": int(idx.size),
+                "stream_count": int(stream_count), "wave_frames": int(wave_frames), "total_s": total,
+                "host_pinned_bytes": self.host_pinned_bytes}
+
+    # ---- statistics ------------------------------------------------------------
+    def frame_global_stats(self, index: int) -> dict[str, Any]:
+        return self.frames_global_stats([index])[0]
+
+    def frames_global_stats(self, indices: Any) -> list[dict[str, Any]]:
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+        out = (_lib.FrameStats * idx.size)()
+        _lib.call("gg_stack_frame_stats", self._handle, _lib.ptr(idx), ctypes.c_int64(idx.size), out)
+        return [
+            {"mean": float(s.mean), "std": float(s.std), "valid_pixels": int(s.valid_pixels),
+             "total_pixels": int(s.total_pixels), "nonfinite_pixels": int(s.total_pixels - s.valid_pixels),
+             "model": "float_float_device_sum"}
+            for s in out
+        ]
+
+    # ---- integration -------------------------------------------------------------
+    def _weights(self, weights: Any | None) -> np.ndarray | None:
+        if weights is None:
+            return None
+        w = np.ascontiguousarray(np.asarray(weights, dtype=np.float32).reshape(-1))
+        if w.shape != (self.frame_count,):
+            raise ValueError("weights must have shape (frame_count,)")
+        return w
+
+    def compute_frame_weights(self, mode: str = "simple_snr", prior: Any | None = None, eps: float = 1.0e-6,
+                              download: bool = True) -> np.ndarray | None:
+        """Frame weights on the device (simple_snr: resident_cuda.py:1948-1956).
+
+        The weights stay in the stack for ``integrate_async(weights="device")``;
+        with download=True they are also returned (one sync).
+        """
+        modes = {"unit": 0, "prior": 0, "simple_snr": 1}
+        if mode not in modes:
+            raise ValueError("weighting mode must be unit, prior or simple_snr")
+        p = self._weights(prior)
+        out = np.empty(self.frame_count, np.float32) if download else None
+        _lib.call("gg_stack_compute_weights", self._handle, modes[mode], _lib.ptr(p), ctypes.c_float(eps),
+                  _lib.ptr(out))
+        return out
+
+    def integrate_async(self, weights: Any | None = None, rejection: int = _lib.GG_REJECT_WINSORIZED,
+                        low_sigma: float = 3.0, high_sigma: float = 3.0, min_samples: int = 3,
+                        max_reject_fraction: float = 0.5, count_map_dtype: str = "uint16",
+                        linear_fit_iterations: int = 5) -> None:
+        """Enqueues the integration; maps stay on the device (see download_maps).
+
+        ``weights="device"`` uses the weights of the last compute_frame_weights
+        without a host round trip.
+        """
+        if count_map_dtype not in {"float32", "uint16"}:
+            raise ValueError("count_map_dtype must be float32 or uint16")
+        params = _lib.IntegrateParams(
+            int(rejection), float(low_sigma), float(high_sigma), int(min_samples), float(max_reject_fraction),
+            _lib.GG_COUNT_U16 if count_map_dtype == "uint16" else _lib.GG_COUNT_F32, int(linear_fit_iterations),
+        )
+        if isinstance(weights, str):
+            if weights != "device":
+                raise ValueError("weights must be an array, None or 'device'")
+            _lib.call("gg_stack_integrate_device_weights", self._handle, None, ctypes.byref(params))
+        else:
+            w = self._weights(weights)
+            _lib.call("gg_stack_integrate", self._handle, _lib.ptr(w), ctypes.byref(params))
+        self._last_count_dtype = np.dtype(np.uint16 if count_map_dtype == "uint16" else np.float32)
+
+    def download_maps(self, download_mode: str = "full", include_dq: bool = True):
+        """(master, weight, coverage, low, high, dq) of the last integration."""
+        if download_mode not in _DOWNLOAD_MODES:
+            raise ValueError("download_mode must be full, master_weight, or master_only")
+        if self._last_count_dtype is None:
+            raise RuntimeError("no integration has been run")
+        info = self._info()
+        shape = (info.height, info.width)
+        master = np.empty(shape, np.float32)
+        weight = np.empty(shape, np.float32) if download_mode != "master_only" else None
+        full = download_mode == "full"
+        cov = np.empty(shape, self._last_count_dtype) if full else None
+        low = np.empty(shape, self._last_count_dtype) if full else None
+        high = np.empty(shape, self._last_count_dtype) if full else None
+        dq = np.empty(shape, np.int16) if (full and include_dq) else None
+        _lib.call("gg_stack_download_maps", self._handle, _lib.ptr(master), _lib.ptr(weight), _lib.ptr(cov),
+                  _lib.ptr(low), _lib.ptr(high), _lib.ptr(dq))
+        return master, weight, cov, low, high, dq
+
+    def integrate_mean(self, weights: Any | None = None) -> tuple[np.ndarray, np.ndarray]:
+        """Weighted mean (cpu/integration.py:106-118; reference kernel integration_kernels.cu:1610)."""
+        self.integrate_async(weights, _lib.GG_REJECT_NONE, count_map_dtype="float32")
+        master, weight, *_ = self.download_maps("master_weight")
+        return master, weight
+
+    def integrate_sigma_clip(self, weights: Any | None = None, low_sigma: float = 3.0, high_sigma: float = 3.0,
+                             winsorize: bool = True, download_mode: str = "full"):
+        """integrate_sigma_clip (native_bindings.cpp:13227) with the CPU semantics.
+
+        winsorize=False is the CPU "sigma_clip" (median centre, std scale);
+        winsorize=True is the CPU "winsorized_sigma" estimator.
+        """
+        if low_sigma <= 0.0 or high_sigma <= 0.0:
+            raise ValueError("sigma thresholds must be positive")
+        if download_mode not in _DOWNLOAD_MODES:
+            raise ValueError("download_mode must be full, master_weight, or master_only")
+        mode = _lib.GG_REJECT_WINSORIZED if winsorize else _lib.GG_REJECT_SIGMA_CLIP
+        self.integrate_async(weights, mode, low_sigma, high_sigma, count_map_dtype="float32")
+        master, weight, cov, low, high, _ = self.download_maps(download_mode, include_dq=False)
+        return master, weight, cov, low, high
+
+    def integrate_hardened_winsorized_sigma(self, weights: Any | None = None, low_sigma: float = 3.0,
+                                            high_sigma: float = 3.0, min_samples: int = 3,
+                                            max_reject_fraction: float = 0.5, count_map_dtype: str = "float32",
+                                            profile: bool = False, download_mode: str = "full"):
+        """native_bindings.cpp:13395 (integration_kernels.cu:2292) with CPU parity."""
+        if low_sigma <= 0.0 or high_sigma <= 0.0:
+            raise ValueError("sigma thresholds must be positive")
+        if int(min_samples) < 1:
+            raise ValueError("min_samples must be at least 1")
+        if not 0.0 <= float(max_reject_fraction) <= 1.0:
+            raise ValueError("max_reject_fraction must be between 0 and 1")
+        if download_mode not in _DOWNLOAD_MODES:
+            raise ValueError("download_mode must be full, master_weight, or master_only")
+        start = perf_counter()
+        self.integrate_async(weights, _lib.GG_REJECT_WINSORIZED, low_sigma, high_sigma, min_samples,
+                             max_reject_fraction, count_map_dtype)
+        enqueue = perf_counter()
+        master, weight, cov, low, high, _ = self.download_maps(download_mode, include_dq=False)
+        done = perf_counter()
+        if profile:
+            info = {"native_kernel_frame_capacity": 64 if self.frame_count <= 64 else 512,
+                    "native_kernel_capacity_selector": "register_column" if self.frame_count <= 64
+                    else "shared_memory_column",
+                    "enqueue_s": enqueue - start, "sync_download_s": done - enqueue}
+            return master, weight, cov, low, high, info
+        return master, weight, cov, low, high
+
+    def integrate_linear_fit_clip(self, weights: Any | None = None, low_sigma: float = 3.0,
+                                  high_sigma: float = 3.0, min_samples: int = 3,
+                                  max_reject_fraction: float = 0.5, iterations: int = 5,
+                                  count_map_dtype: str = "float32", download_mode: str = "full"):
+        """Linear-fit clipping (no counterpart in the reference)."""
+        if low_sigma <= 0.0 or high_sigma <= 0.0:
+            raise ValueError("sigma thresholds must be positive")
+        self.integrate_async(weights, _lib.GG_REJECT_LINEAR_FIT, low_sigma, high_sigma, min_samples,
+                             max_reject_fraction, count_map_dtype, iterations)
+        master, weight, cov, low, high, _ = self.download_maps(download_mode, include_dq=False)
+        return master, weight, cov, low, high
+
+    def dq_map(self) -> np.ndarray:
+        """DQ int16 map fused into the last integration (resident_cuda.py:3110-3297 rules)."""
+        return self.download_maps("full", include_dq=True)[5]

@@ -1,0 +1,233 @@
+"""ctypes binding of libglass_gb300.so (the C ABI in include/glass_gb300.h).
+
+This module only loads the library and declares its prototypes; the
+reference-facing Python surface lives in ``_glass_cuda_native``.  Loading
+fails loudly: there is no CPU fallback behind these names.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+PACKAGE_DIR = Path(__file__).resolve().parent
+LIBRARY_PATH = PACKAGE_DIR / "libglass_gb300.so"
+
+GG_OK = 0
+GG_ERR_INVALID_ARGUMENT = -1
+GG_ERR_OUT_OF_RANGE = -2
+GG_ERR_RUNTIME = -3
+GG_ERR_CUDA = -4
+GG_ERR_NO_DEVICE = -5
+GG_ERR_OUT_OF_MEMORY = -6
+GG_ERR_TIMEOUT = -7
+
+GG_REJECT_NONE = 0
+GG_REJECT_SIGMA_CLIP = 1
+GG_REJECT_WINSORIZED = 2
+GG_REJECT_LINEAR_FIT = 3
+
+GG_COUNT_F32 = 0
+GG_COUNT_U16 = 1
+
+GG_INTERP_BILINEAR = 1
+GG_INTERP_LANCZOS3 = 3
+
+c_int64_p = ctypes.POINTER(ctypes.c_int64)
+c_float_p = ctypes.POINTER(ctypes.c_float)
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int16_p = ctypes.POINTER(ctypes.c_int16)
+
+
+class DeviceInfo(ctypes.Structure):
+    _fields_ = [
+        ("name", ctypes.c_char * 256),
+        ("major", ctypes.c_int),
+        ("minor", ctypes.c_int),
+        ("multiprocessor_count", ctypes.c_int),
+        ("total_global_mem", ctypes.c_int64),
+        ("l2_cache_bytes", ctypes.c_int64),
+        ("shared_mem_per_block_optin", ctypes.c_int64),
+    ]
+
+
+class CalibParams(ctypes.Structure):
+    _fields_ = [
+        ("master_dark_includes_bias", ctypes.c_int),
+        ("dark_scale", ctypes.c_float),
+        ("flat_floor", ctypes.c_float),
+        ("pedestal", ctypes.c_float),
+    ]
+
+
+class StackInfo(ctypes.Structure):
+    _fields_ = [
+        ("frame_count", ctypes.c_int64),
+        ("height", ctypes.c_int64),
+        ("width", ctypes.c_int64),
+        ("pixels_per_frame", ctypes.c_int64),
+        ("frame_stride", ctypes.c_int64),
+        ("slot_count", ctypes.c_int64),
+        ("loaded_count", ctypes.c_int64),
+        ("bytes_allocated", ctypes.c_int64),
+        ("warp_scratch_bytes", ctypes.c_int64),
+        ("host_pinned_bytes", ctypes.c_int64),
+        ("calibration_lane_count", ctypes.c_int64),
+        ("warp_coverage_frame_count", ctypes.c_int64),
+        ("has_bias", ctypes.c_int),
+        ("has_dark", ctypes.c_int),
+        ("has_flat", ctypes.c_int),
+    ]
+
+
+class FrameStats(ctypes.Structure):
+    _fields_ = [
+        ("mean", ctypes.c_double),
+        ("std", ctypes.c_double),
+        ("valid_pixels", ctypes.c_int64),
+        ("total_pixels", ctypes.c_int64),
+    ]
+
+
+class IntegrateParams(ctypes.Structure):
+    _fields_ = [
+        ("rejection", ctypes.c_int),
+        ("low_sigma", ctypes.c_float),
+        ("high_sigma", ctypes.c_float),
+        ("min_samples", ctypes.c_int),
+        ("max_reject_fraction", ctypes.c_float),
+        ("count_dtype", ctypes.c_int),
+        ("linear_fit_iterations", ctypes.c_int),
+    ]
+
+
+class StackDevicePtrs(ctypes.Structure):
+    _fields_ = [
+        ("slots", ctypes.c_void_p),
+        ("slot_of_frame", ctypes.c_void_p),
+        ("master", ctypes.c_void_p),
+        ("weight", ctypes.c_void_p),
+        ("coverage", ctypes.c_void_p),
+        ("low", ctypes.c_void_p),
+        ("high", ctypes.c_void_p),
+        ("dq", ctypes.c_void_p),
+        ("warp_coverage", ctypes.c_void_p),
+    ]
+
+
+# name -> (argtypes); every function returns int status.
+_P = ctypes.c_void_p
+PROTOTYPES: dict[str, list] = {
+    "gg_version": [ctypes.POINTER(ctypes.c_int)],
+    "gg_last_error": [ctypes.c_char_p, ctypes.c_size_t],
+    "gg_kernel_launches": [c_int64_p],
+    "gg_cuda_available": [ctypes.POINTER(ctypes.c_int)],
+    "gg_device_count": [ctypes.POINTER(ctypes.c_int)],
+    "gg_device_info": [ctypes.c_int, ctypes.POINTER(DeviceInfo)],
+    "gg_host_alloc_pinned": [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)],
+    "gg_host_free_pinned": [_P],
+    "gg_calibrate_tile_f32": [_P, _P, _P, _P, ctypes.c_int64, ctypes.POINTER(CalibParams), _P],
+    "gg_stack_create": [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)],
+    "gg_stack_destroy": [_P],
+    "gg_stack_info": [_P, ctypes.POINTER(StackInfo)],
+    "gg_stack_set_stream": [_P, _P],
+    "gg_stack_synchronize": [_P],
+    "gg_stack_set_masters": [_P, _P, _P, _P],
+    "gg_stack_upload_frame": [_P, ctypes.c_int64, _P],
+    "gg_stack_download_frame_tile": [_P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                     ctypes.c_int64, _P],
+    "gg_stack_download_frames_tile": [_P, _P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                      ctypes.c_int64, _P],
+    "gg_stack_calibrate_u16": [_P, _P, ctypes.c_int64, _P, ctypes.c_int, ctypes.POINTER(CalibParams)],
+    "gg_stack_calibrate_u16_device": [_P, _P, ctypes.c_int64, _P, ctypes.c_int, ctypes.POINTER(CalibParams)],
+    "gg_stack_calibrate_f32": [_P, ctypes.c_int64, _P, ctypes.POINTER(CalibParams)],
+    "gg_stack_frame_stats": [_P, _P, ctypes.c_int64, _P],
+    "gg_stack_compute_weights": [_P, ctypes.c_int, _P, ctypes.c_float, _P],
+    "gg_stack_integrate": [_P, _P, ctypes.POINTER(IntegrateParams)],
+    "gg_stack_integrate_device_weights": [_P, _P, ctypes.POINTER(IntegrateParams)],
+    "gg_stack_download_maps": [_P, _P, _P, _P, _P, _P, _P],
+    "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
+    "gg_dq_map_i16": [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P],
+}
+
+_LIB: ctypes.CDLL | None = None
+
+
+class NativeLibraryError(ImportError):
+    """The CUDA library is missing or incomplete; there is no fallback."""
+
+
+def library_path() -> Path:
+    override = os.environ.get("GLASS_GB300_LIBRARY")
+    return Path(override) if override else LIBRARY_PATH
+
+
+def load(required: bool = True) -> ctypes.CDLL | None:
+    """Loads libglass_gb300.so and declares every prototype."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists():
+        if not required:
+            return None
+        raise NativeLibraryError(
+            f"{path} is missing: build it with `python -m glass_gb300.build` (needs nvcc, sm_103a)"
+        )
+    lib = ctypes.CDLL(str(path))
+    for name, argtypes in PROTOTYPES.items():
+        try:
+            fn = getattr(lib, name)
+        except AttributeError as exc:  # pragma: no cover - only on a stale build
+            raise NativeLibraryError(f"{path} does not export {name}; rebuild it") from exc
+        fn.argtypes = argtypes
+        fn.restype = ctypes.c_int
+    _LIB = lib
+    return lib
+
+
+def last_error() -> str:
+    lib = load()
+    buf = ctypes.create_string_buffer(4096)
+    lib.gg_last_error(buf, len(buf))
+    return buf.value.decode("utf-8", "replace")
+
+
+def check(status: int, what: str = "") -> None:
+    """Raises the Python exception that the reference module would raise."""
+    if status == GG_OK:
+        return
+    message = last_error() or f"status {status}"
+    if what:
+        message = f"{what}: {message}"
+    if status == GG_ERR_INVALID_ARGUMENT:
+        raise ValueError(message)
+    if status == GG_ERR_OUT_OF_RANGE:
+        raise IndexError(message)
+    if status == GG_ERR_OUT_OF_MEMORY:
+        raise MemoryError(message)
+    raise RuntimeError(message)
+
+
+def call(name: str, *args) -> None:
+    lib = load()
+    check(getattr(lib, name)(*args), name)
+
+
+def kernel_launches() -> int:
+    """Kernels this library has launched in this process."""
+    count = ctypes.c_int64()
+    call("gg_kernel_launches", ctypes.byref(count))
+    return int(count.value)
+
+
+def ptr(array: np.ndarray | None) -> int | None:
+    """Data pointer of a C-contiguous array (None passes NULL)."""
+    if array is None:
+        return None
+    if not array.flags.c_contiguous:
+        raise ValueError("array must be C-contiguous")
+    return array.ctypes.data

@@ -1,0 +1,667 @@
+// Per-pixel rejection and weighted integration into the six output maps.
+//
+// Semantics are those of the CPU oracle, cpu/integration.py:36-118 with the
+// per-pixel statistics of engine/rejection.py:31-66, 219-366:
+//   valid      = finite(sample) & finite(w) & (w > 0)
+//   winsorized = median / IQR/1.349 (fallback std) -> clip -> mean / std
+//                (fallback first scale) -> reject outside mean -/+ k*std
+//   sigma_clip = median centre, std scale (NumPy nanmedian / nanstd)
+//   guard      = cancel a pixel's rejections when fewer than min_samples
+//                remain or the rejected fraction exceeds max_reject_fraction
+//   master     = sum(w*v) / sum(w) over kept samples; weight = sum(w)
+// NumPy evaluates two formula families depending on whether the *whole* stack
+// is valid (rejection.py:39-44 vs :54-60).  The stack keeps a per-frame count
+// of non-finite samples (maintained by every kernel that writes a frame), so
+// the kernel knows which family applies without another pass over HBM.
+//
+// Arithmetic: float64 sums of the CPU path are reproduced with float-float
+// (TwoSum/TwoProd) accumulators; float32 steps are spelled out with _rn
+// intrinsics so no FMA contraction changes a rounding.  Order statistics come
+// from a sorting network over the pixel's column held in registers.
+//
+// GB300 layout: one thread per output pixel; a warp covers 32 consecutive
+// pixels, so every per-frame load is one coalesced 128 B line and the column
+// lives in registers (N <= 64) or in a [rank][thread] shared-memory tile
+// (N > 64), which is bank-conflict free for any per-thread rank index.
+#include <algorithm>
+#include <cmath>
+
+#include "stack.cuh"
+
+namespace gg {
+
+struct IntegrateArgs {
+  const float* slots;
+  const int* slot_of_frame;
+  int64_t stride;
+  int64_t pixels;
+  int frames;
+  const float* weights;  // device [frames], raw values
+  const unsigned* nonfinite;
+  int rejection;
+  float low_sigma;
+  float high_sigma;
+  int min_samples;
+  float max_frac;
+  int lfc_iterations;
+  float* master;
+  float* weight;
+  void* coverage;
+  void* low;
+  void* high;
+  int16_t* dq;
+  int count_u16;
+  const float* geometric;  // optional warp coverage (float32 per pixel)
+};
+
+constexpr float kInf = __builtin_huge_valf();
+
+// ---- sorting network (Batcher odd-even merge sort, fully unrolled) --------
+// Loop counters are kept additive (log2 of p and k) so that nvcc unrolls the
+// whole network and v[] stays in registers.
+template <int N>
+__device__ __forceinline__ void sort_network(float (&v)[N]) {
+  constexpr int LOG2N = (N <= 1) ? 0 : (N <= 2) ? 1 : (N <= 4) ? 2 : (N <= 8) ? 3 : (N <= 16) ? 4 : (N <= 32) ? 5 : 6;
+  static_assert((1 << LOG2N) == N, "sort_network needs a power-of-two size up to 64");
+#pragma unroll
+  for (int lp = 0; lp < LOG2N; ++lp) {
+#pragma unroll
+    for (int lk = lp; lk >= 0; --lk) {
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        // Comparator (a, a+k) of stage (p, k); all conditions fold at compile time.
+        const int p = 1 << lp, k = 1 << lk, j0 = k % p;
+        if (a >= j0 && a + k < N && ((a - j0) % (2 * k)) < k && (a / (2 * p)) == ((a + k) / (2 * p))) {
+          const float lo = fminf(v[a], v[a + k]);
+          const float hi = fmaxf(v[a], v[a + k]);
+          v[a] = lo;
+          v[a + k] = hi;
+        }
+      }
+    }
+  }
+}
+
+// ---- percentiles ------------------------------------------------------------
+// engine/rejection.py:299-321: per-pixel valid count, lo*(1-t) + hi*t.
+__device__ __forceinline__ float percentile_valid(const float* S, int T, int cnt, float fraction) {
+  if (cnt <= 0) return 0.0f;
+  const float pos = __fmul_rn(static_cast<float>(cnt - 1), fraction);
+  const int lower = static_cast<int>(floorf(pos));
+  const int upper = min(lower + 1, cnt - 1);
+  const float t = __fsub_rn(pos, static_cast<float>(lower));
+  const float lv = S[lower * T];
+  const float uv = S[upper * T];
+  return __fadd_rn(__fmul_rn(lv, __fsub_rn(1.0f, t)), __fmul_rn(uv, t));
+}
+
+// engine/rejection.py:352-366: whole-stack frame count, lo + (hi-lo)*f.
+__device__ __forceinline__ float percentile_all(const float* S, int T, int n, float percent) {
+  if (n == 1) return S[0];
+  const float pos = __fmul_rn(__fdiv_rn(percent, 100.0f), static_cast<float>(n - 1));
+  const int lower = static_cast<int>(floorf(pos));
+  const int upper = static_cast<int>(ceilf(pos));
+  const float f = __fsub_rn(pos, static_cast<float>(lower));
+  const float lv = S[lower * T];
+  if (upper == lower) return lv;
+  const float uv = S[upper * T];
+  return __fadd_rn(lv, __fmul_rn(__fsub_rn(uv, lv), f));
+}
+
+__device__ __forceinline__ float clipf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+
+// ---- output ---------------------------------------------------------------
+// DQ bits: contracts.py:77-88; rules: resident_cuda.py:3110-3297.
+__device__ __forceinline__ void write_outputs(const IntegrateArgs& a, int64_t p, float master, float weight, int cov,
+                                              int nlow, int nhigh, int active_frames) {
+  a.master[p] = master;
+  a.weight[p] = weight;
+  if (a.count_u16) {
+    static_cast<uint16_t*>(a.coverage)[p] = static_cast<uint16_t>(min(cov, 65535));
+    static_cast<uint16_t*>(a.low)[p] = static_cast<uint16_t>(min(nlow, 65535));
+    static_cast<uint16_t*>(a.high)[p] = static_cast<uint16_t>(min(nhigh, 65535));
+  } else {
+    static_cast<float*>(a.coverage)[p] = static_cast<float>(cov);
+    static_cast<float*>(a.low)[p] = static_cast<float>(nlow);
+    static_cast<float*>(a.high)[p] = static_cast<float>(nhigh);
+  }
+  if (a.dq) {
+    int bits = 0;
+    bool invalid = !isfinite(master) || !isfinite(weight) || !(weight > 0.0f);
+    if (cov <= 0) {
+      bits |= 64;
+      invalid = true;
+    }
+    if (a.geometric) {
+      const float g = a.geometric[p];
+      if (!isfinite(g) || g <= 0.5f) {
+        bits |= 64;
+        invalid = true;
+      } else if (active_frames > 0 && g < static_cast<float>(active_frames) - 0.5f) {
+        bits |= 64;
+      }
+    }
+    if (invalid) bits |= 1;
+    if (nlow > 0) bits |= 256;
+    if (nhigh > 0) bits |= 512;
+    a.dq[p] = static_cast<int16_t>(bits);
+  }
+}
+
+// ---- per-pixel statistics over a column ------------------------------------
+// The column is reachable two ways: `sorted` holds the valid samples in
+// ascending order at ranks [0, cnt) with stride T (+inf beyond), and the
+// frame-order view is provided by the caller's RawView.
+struct CenterScale {
+  float center;
+  float scale;
+};
+
+// Fallback scale: std of the valid samples (rejection.py:231 all-valid,
+// rejection.py:323-349 otherwise).
+template <class Sorted>
+__device__ __forceinline__ float std_of_valid(const Sorted& sorted, int cnt, bool allvalid) {
+  FF s1;
+  for (int i = 0; i < cnt; ++i) s1.add(sorted(i));
+  float mh, ml;
+  if (allvalid) {
+    ff_div_pair(s1.hi, s1.lo, static_cast<float>(cnt), mh, ml);
+  } else {
+    mh = ff_div_f32(s1.hi, s1.lo, static_cast<float>(cnt));
+    ml = 0.0f;
+  }
+  FF v;
+  for (int i = 0; i < cnt; ++i) ff_add_sqdev(v, sorted(i), mh, ml);
+  float q, ql;
+  ff_div_pair(v.hi, v.lo, static_cast<float>(cnt), q, ql);
+  return ff_sqrt_f32(q, ql);
+}
+
+// Winsorized sigma centre/scale (rejection.py:219-297).
+template <class Sorted>
+__device__ __forceinline__ CenterScale winsorized_stats(const Sorted& sorted, const float* S, int T, int cnt,
+                                                        int nframes, bool allvalid, float ls, float hs) {
+  CenterScale r{0.0f, 0.0f};
+  if (cnt <= 0) return r;
+  float med, q25, q75;
+  if (allvalid) {
+    med = percentile_all(S, T, nframes, 50.0f);
+    q25 = percentile_all(S, T, nframes, 25.0f);
+    q75 = percentile_all(S, T, nframes, 75.0f);
+  } else {
+    med = percentile_valid(S, T, cnt, 0.5f);
+    q25 = percentile_valid(S, T, cnt, 0.25f);
+    q75 = percentile_valid(S, T, cnt, 0.75f);
+  }
+  float scale1 = __fdiv_rn(__fsub_rn(q75, q25), 1.349f);
+  const bool ok1 = allvalid ? (scale1 > 0.0f) : (scale1 > 0.0f && isfinite(scale1));
+  if (!ok1) scale1 = std_of_valid(sorted, cnt, allvalid);
+  const float lo1 = __fsub_rn(med, __fmul_rn(ls, scale1));
+  const float hi1 = __fadd_rn(med, __fmul_rn(hs, scale1));
+  FF sw;
+  for (int i = 0; i < cnt; ++i) sw.add(clipf(sorted(i), lo1, hi1));
+  float mh, ml;
+  if (allvalid) {
+    ff_div_pair(sw.hi, sw.lo, static_cast<float>(cnt), mh, ml);
+    r.center = __fadd_rn(mh, ml);
+  } else {
+    r.center = ff_div_f32(sw.hi, sw.lo, static_cast<float>(cnt));
+    mh = r.center;
+    ml = 0.0f;
+  }
+  FF sv;
+  for (int i = 0; i < cnt; ++i) ff_add_sqdev(sv, clipf(sorted(i), lo1, hi1), mh, ml);
+  float q, ql;
+  ff_div_pair(sv.hi, sv.lo, static_cast<float>(cnt), q, ql);
+  float scale = ff_sqrt_f32(q, ql);
+  const bool ok2 = allvalid ? (scale > 0.0f) : (scale > 0.0f && isfinite(scale));
+  r.scale = ok2 ? scale : scale1;
+  return r;
+}
+
+// Sigma-clip centre/scale: nanmedian + nanstd in float32, frame order
+// (rejection.py:46-49; NumPy masked median and _nanvar).
+template <class Raw>
+__device__ __forceinline__ CenterScale sigma_stats(const Raw& raw, const float* S, int T, int cnt, int nframes) {
+  CenterScale r{0.0f, 0.0f};
+  if (cnt <= 0) return r;
+  const int h = cnt / 2;
+  const int l = (cnt & 1) ? h : h - 1;
+  r.center = __fmul_rn(__fadd_rn(S[l * T], S[h * T]), 0.5f);
+  float sum = 0.0f;
+  for (int f = 0; f < nframes; ++f) {
+    float x;
+    if (raw(f, x)) sum = __fadd_rn(sum, x);
+  }
+  const float mean = __fdiv_rn(sum, static_cast<float>(cnt));
+  float v = 0.0f;
+  for (int f = 0; f < nframes; ++f) {
+    float x;
+    if (raw(f, x)) {
+      const float d = __fsub_rn(x, mean);
+      v = __fadd_rn(v, __fmul_rn(d, d));
+    }
+  }
+  r.scale = __fsqrt_rn(__fdiv_rn(v, static_cast<float>(cnt)));
+  return r;
+}
+
+// Linear-fit clipping.  The reference has no implementation of it; this
+// library defines it (and oracle/integration.py restates it in float64):
+//   1. fit v = a + b*(r - c) by least squares to the kept sorted samples,
+//      r = rank within the kept range, c = (n-1)/2;
+//   2. sigma = mean |v - fit|;
+//   3. walk up from the lowest kept rank while v < fit - k_lo*sigma and down
+//      from the highest while v > fit + k_hi*sigma; samples equal in value to
+//      the first kept one are kept too, so the kept set is a value interval;
+//   4. repeat on the kept range until it stops changing or `iterations` runs.
+// On return [keep_lo, keep_hi) is the kept rank range.
+template <class Sorted>
+__device__ __forceinline__ void linear_fit_clip(const Sorted& sorted, int cnt, float ls, float hs, int iterations,
+                                                int& keep_lo, int& keep_hi) {
+  keep_lo = 0;
+  keep_hi = cnt;  // exclusive
+  for (int it = 0; it < iterations; ++it) {
+    const int n = keep_hi - keep_lo;
+    if (n < 3) break;
+    const float fn = static_cast<float>(n);
+    const float c = 0.5f * static_cast<float>(n - 1);
+    FF sy, sry;
+    for (int i = keep_lo; i < keep_hi; ++i) {
+      const float y = sorted(i);
+      sy.add(y);
+      sry.add_prod(__fsub_rn(static_cast<float>(i - keep_lo), c), y);
+    }
+    // sum of squared centred ranks n(n^2-1)/12, exact in float for n <= 512.
+    const float srr = fn * (fn * fn - 1.0f) / 12.0f;
+    const float a0 = ff_div_f32(sy.hi, sy.lo, fn);
+    const float b = __fdiv_rn(sry.value_f32(), srr);
+    FF sad;
+    for (int i = keep_lo; i < keep_hi; ++i) {
+      const float fit = __fmaf_rn(b, __fsub_rn(static_cast<float>(i - keep_lo), c), a0);
+      sad.add(fabsf(__fsub_rn(sorted(i), fit)));
+    }
+    const float sigma = ff_div_f32(sad.hi, sad.lo, fn);
+    int new_lo = keep_lo, new_hi = keep_hi;
+    while (new_lo < keep_hi) {
+      const float fit = __fmaf_rn(b, __fsub_rn(static_cast<float>(new_lo - keep_lo), c), a0);
+      if (sorted(new_lo) < __fsub_rn(fit, __fmul_rn(ls, sigma))) ++new_lo; else break;
+    }
+    while (new_hi > new_lo) {
+      const float fit = __fmaf_rn(b, __fsub_rn(static_cast<float>(new_hi - 1 - keep_lo), c), a0);
+      if (sorted(new_hi - 1) > __fadd_rn(fit, __fmul_rn(hs, sigma))) --new_hi; else break;
+    }
+    if (new_hi <= new_lo) break;  // never reject everything
+    while (new_lo > keep_lo && sorted(new_lo - 1) == sorted(new_lo)) --new_lo;
+    while (new_hi < keep_hi && sorted(new_hi) == sorted(new_hi - 1)) ++new_hi;
+    if (new_lo == keep_lo && new_hi == keep_hi) break;
+    keep_lo = new_lo;
+    keep_hi = new_hi;
+  }
+}
+
+// Rejection, guard and final weighted sums for one pixel.  `sorted` gives the
+// valid samples in ascending order, `raw(f, x)` the frame-order view.
+template <class Sorted, class Raw>
+__device__ __forceinline__ void finish_pixel(const IntegrateArgs& a, int64_t p, const Sorted& sorted, const float* S,
+                                             int T, const Raw& raw, const float* s_w, int cnt, bool allvalid,
+                                             bool unit_weights, int active) {
+  const float ls = a.low_sigma, hs = a.high_sigma;
+  int nl = 0, nh = 0;
+  float lt = -kInf, ht = kInf;
+  bool use_thresholds = false;
+  if (a.rejection == GG_REJECT_WINSORIZED || a.rejection == GG_REJECT_SIGMA_CLIP) {
+    const CenterScale cs = (a.rejection == GG_REJECT_WINSORIZED)
+                               ? winsorized_stats(sorted, S, T, cnt, a.frames, allvalid, ls, hs)
+                               : sigma_stats(raw, S, T, cnt, a.frames);
+    lt = __fsub_rn(cs.center, __fmul_rn(ls, cs.scale));
+    ht = __fadd_rn(cs.center, __fmul_rn(hs, cs.scale));
+    for (int i = 0; i < cnt; ++i) {
+      const float x = sorted(i);
+      nl += (x < lt);
+      nh += (x > ht);
+    }
+    use_thresholds = true;
+  } else if (a.rejection == GG_REJECT_LINEAR_FIT && cnt > 0) {
+    int lfc_lo = 0, lfc_hi = cnt;
+    linear_fit_clip(sorted, cnt, ls, hs, a.lfc_iterations, lfc_lo, lfc_hi);
+    nl = lfc_lo;
+    nh = cnt - lfc_hi;
+    // The kept set is the value interval [sorted(lo), sorted(hi-1)].
+    lt = sorted(lfc_lo);
+    ht = sorted(lfc_hi - 1);
+    use_thresholds = true;
+  }
+  if (nl + nh > 0) {
+    // cpu/integration.py:85-99
+    const int rej = nl + nh;
+    const float frac = __fdiv_rn(static_cast<float>(rej), static_cast<float>(cnt));
+    const bool allowed = (cnt - rej >= a.min_samples) && (frac <= a.max_frac);
+    if (!allowed) {
+      nl = nh = 0;
+      use_thresholds = false;
+    }
+  }
+  float master = 0.0f, weight = 0.0f;
+  int kept = 0;
+  if (unit_weights) {
+    // Unit weights: sum the kept samples straight from the sorted column.
+    FF ws;
+    for (int i = 0; i < cnt; ++i) {
+      const float x = sorted(i);
+      if (use_thresholds && (x < lt || x > ht)) continue;
+      ws.add(x);
+      ++kept;
+    }
+    if (kept > 0) {
+      master = ff_div_f32(ws.hi, ws.lo, static_cast<float>(kept));
+      weight = static_cast<float>(kept);
+    }
+  } else {
+    FF ws, wsum;
+    for (int f = 0; f < a.frames; ++f) {
+      float x;
+      if (!raw(f, x)) continue;
+      if (use_thresholds && (x < lt || x > ht)) continue;
+      ws.add_prod(x, s_w[f]);
+      wsum.add(s_w[f]);
+      ++kept;
+    }
+    if (kept > 0 && wsum.hi > 0.0f) {
+      master = ff_div_ff(ws.hi, ws.lo, wsum.hi, wsum.lo);
+      weight = wsum.value_f32();
+    }
+  }
+  write_outputs(a, p, master, weight, kept, nl, nh, active);
+}
+
+// ---- CTA prologue: weights, frame bases, all-valid flag --------------------
+// Both flags are derived here from the device weights, so weights computed on
+// the GPU (frame statistics) feed the integrator without a host round trip.
+template <int MAXF>
+struct FrameTable {
+  float w[MAXF];
+  const float* base[MAXF];
+  int allvalid;  // every weight valid and no non-finite sample anywhere
+  int unit;      // every valid weight is exactly 1
+  int active;    // frames with a valid weight
+};
+
+template <int MAXF>
+__device__ __forceinline__ void load_frame_table(const IntegrateArgs& a, FrameTable<MAXF>& t) {
+  for (int f = threadIdx.x; f < a.frames; f += blockDim.x) {
+    const float w = a.weights ? a.weights[f] : 1.0f;
+    t.w[f] = (isfinite(w) && w > 0.0f) ? w : 0.0f;
+    t.base[f] = a.slots + static_cast<int64_t>(a.slot_of_frame[f]) * a.stride;
+  }
+  if (threadIdx.x < 32) {
+    unsigned bad = 0, invalid_w = 0, non_unit = 0, active = 0;
+    for (int f = threadIdx.x; f < a.frames; f += 32) {
+      bad |= a.nonfinite[f];
+      const float w = a.weights ? a.weights[f] : 1.0f;
+      const bool ok = isfinite(w) && w > 0.0f;
+      invalid_w |= ok ? 0u : 1u;
+      non_unit |= (ok && w != 1.0f) ? 1u : 0u;
+      active += ok ? 1u : 0u;
+    }
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    invalid_w = __reduce_or_sync(0xffffffffu, invalid_w);
+    non_unit = __reduce_or_sync(0xffffffffu, non_unit);
+    active = __reduce_add_sync(0xffffffffu, active);
+    if (threadIdx.x == 0) {
+      t.allvalid = (invalid_w == 0u && bad == 0u) ? 1 : 0;
+      t.unit = non_unit == 0u ? 1 : 0;
+      t.active = static_cast<int>(active);
+    }
+  }
+  __syncthreads();
+}
+
+// ---- kernel A: N <= NB <= 64, column in registers ----------------------------
+template <int NB, int T>
+__global__ void __launch_bounds__(T) integrate_reg_kernel(IntegrateArgs a) {
+  extern __shared__ float smem[];
+  float* R = smem;            // [NB][T] frame order (raw)
+  float* S = smem + NB * T;   // [NB][T] ascending valid samples
+  __shared__ FrameTable<NB> tab;
+  load_frame_table<NB>(a, tab);
+  const bool allvalid = tab.allvalid != 0;
+  const int tid = threadIdx.x;
+  const int N = a.frames;
+  const int64_t P = a.pixels;
+  for (int64_t p = static_cast<int64_t>(blockIdx.x) * T + tid; p < P; p += static_cast<int64_t>(gridDim.x) * T) {
+    float s[NB];
+    int cnt = 0;
+#pragma unroll
+    for (int f = 0; f < NB; ++f) {
+      float x = kInf;
+      if (f < N) {
+        x = __ldcs(tab.base[f] + p);
+        R[f * T + tid] = x;
+      }
+      const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(x);
+      s[f] = ok ? x : kInf;
+      cnt += ok ? 1 : 0;
+    }
+    auto raw = [&](int f, float& x) -> bool {
+      x = R[f * T + tid];
+      return tab.w[f] > 0.0f && isfinite(x);
+    };
+    if (a.rejection != GG_REJECT_NONE) {
+      sort_network<NB>(s);
+#pragma unroll
+      for (int f = 0; f < NB; ++f) S[f * T + tid] = s[f];
+    }
+    auto sorted = [&](int i) -> float { return S[i * T + tid]; };
+    finish_pixel(a, p, sorted, S + tid, T, raw, tab.w, cnt, allvalid, tab.unit != 0, tab.active);
+  }
+}
+
+// ---- kernel B: N > 64, chunk-sorted column in shared memory ------------------
+// Each thread sorts its column in chunks of 32 (registers), then streams a
+// k-way merge of the chunks (k <= MR heads in registers) into the sorted
+// buffer.  Frame-order values are re-read from global memory (the CTA's tile
+// is L2 resident) by the raw view.
+template <int MR, int T>
+__global__ void __launch_bounds__(T) integrate_smem_kernel(IntegrateArgs a) {
+  constexpr int MAXF = MR * 32;
+  extern __shared__ float smem[];
+  float* A = smem;               // [MAXF][T] chunk-sorted
+  float* S = smem + MAXF * T;    // [MAXF][T] merged
+  __shared__ FrameTable<MAXF> tab;
+  load_frame_table<MAXF>(a, tab);
+  const bool allvalid = tab.allvalid != 0;
+  const int tid = threadIdx.x;
+  const int N = a.frames;
+  const int chunks = (N + 31) / 32;
+  const int64_t P = a.pixels;
+  for (int64_t p = static_cast<int64_t>(blockIdx.x) * T + tid; p < P; p += static_cast<int64_t>(gridDim.x) * T) {
+    int cnt = 0;
+    for (int c = 0; c < chunks; ++c) {
+      float v[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const int f = c * 32 + k;
+        float x = kInf;
+        if (f < N) x = __ldcs(tab.base[f] + p);
+        const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(x);
+        v[k] = ok ? x : kInf;
+        cnt += ok ? 1 : 0;
+      }
+      if (a.rejection != GG_REJECT_NONE) sort_network<32>(v);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) A[(c * 32 + k) * T + tid] = v[k];
+    }
+    auto raw = [&](int f, float& x) -> bool {
+      x = tab.base[f][p];
+      return tab.w[f] > 0.0f && isfinite(x);
+    };
+    if (a.rejection != GG_REJECT_NONE) {
+      // k-way merge of the sorted chunks: heads in registers.
+      float head[MR];
+      int pos[MR];
+#pragma unroll
+      for (int r = 0; r < MR; ++r) {
+        pos[r] = 0;
+        head[r] = (r < chunks) ? A[(r * 32) * T + tid] : kInf;
+      }
+      for (int out = 0; out < cnt; ++out) {
+        float best = head[0];
+        int br = 0;
+#pragma unroll
+        for (int r = 1; r < MR; ++r) {
+          if (head[r] < best) {
+            best = head[r];
+            br = r;
+          }
+        }
+        S[out * T + tid] = best;
+#pragma unroll
+        for (int r = 0; r < MR; ++r) {
+          if (r == br) {
+            const int np = pos[r] + 1;
+            pos[r] = np;
+            head[r] = (np < 32) ? A[(r * 32 + np) * T + tid] : kInf;
+          }
+        }
+      }
+    } else {
+      for (int i = 0; i < chunks * 32; ++i) S[i * T + tid] = A[i * T + tid];
+    }
+    auto sorted = [&](int i) -> float { return S[i * T + tid]; };
+    finish_pixel(a, p, sorted, S + tid, T, raw, tab.w, cnt, allvalid, tab.unit != 0, tab.active);
+  }
+}
+
+template <int NB>
+static void launch_reg(const IntegrateArgs& args, cudaStream_t stream) {
+  constexpr int T = 128;
+  const size_t smem = size_t(2) * NB * T * sizeof(float);
+  auto kern = integrate_reg_kernel<NB, T>;
+  check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+             "cudaFuncSetAttribute(integrate)");
+  int per_sm = 0;
+  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem), "occupancy");
+  const unsigned grid = grid_for(static_cast<size_t>(args.pixels), T, std::max(per_sm, 1));
+  note_launch();
+  kern<<<grid, T, smem, stream>>>(args);
+  check_cuda(cudaGetLastError(), "integrate kernel launch");
+}
+
+template <int MR>
+static void launch_smem(const IntegrateArgs& args, cudaStream_t stream) {
+  constexpr int T = 32;
+  const size_t smem = size_t(2) * MR * 32 * T * sizeof(float);
+  auto kern = integrate_smem_kernel<MR, T>;
+  check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+             "cudaFuncSetAttribute(integrate)");
+  int per_sm = 0;
+  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem), "occupancy");
+  const unsigned grid = grid_for(static_cast<size_t>(args.pixels), T, std::max(per_sm, 1));
+  note_launch();
+  kern<<<grid, T, smem, stream>>>(args);
+  check_cuda(cudaGetLastError(), "integrate kernel launch");
+}
+
+static void validate_integrate(const gg_integrate_params_t& p) {
+  require(p.rejection >= GG_REJECT_NONE && p.rejection <= GG_REJECT_LINEAR_FIT, "unsupported rejection mode");
+  require(p.count_dtype == GG_COUNT_F32 || p.count_dtype == GG_COUNT_U16, "count_map_dtype must be float32 or uint16");
+  if (p.rejection != GG_REJECT_NONE) {
+    require(p.low_sigma > 0.0f && p.high_sigma > 0.0f, "sigma thresholds must be positive");
+    require(p.min_samples >= 1, "min_samples must be at least 1");
+    require(p.max_reject_fraction >= 0.0f && p.max_reject_fraction <= 1.0f,
+            "max_reject_fraction must be between 0 and 1");
+  }
+}
+
+void launch_integrate(gg_stack* s, const float* d_weights, const gg_integrate_params_t& p) {
+  stack_ensure_maps(s);
+  IntegrateArgs a{};
+  a.slots = s->d_slots;
+  a.slot_of_frame = s->d_slot_of_frame;
+  a.stride = s->stride;
+  a.pixels = s->pixels;
+  a.frames = static_cast<int>(s->frames);
+  a.weights = d_weights;
+  a.nonfinite = s->d_frame_nonfinite;
+  a.rejection = p.rejection;
+  a.low_sigma = p.low_sigma;
+  a.high_sigma = p.high_sigma;
+  a.min_samples = p.min_samples;
+  a.max_frac = p.max_reject_fraction;
+  a.lfc_iterations = p.linear_fit_iterations > 0 ? p.linear_fit_iterations : 5;
+  a.master = s->d_master;
+  a.weight = s->d_weight;
+  a.coverage = s->d_coverage;
+  a.low = s->d_low;
+  a.high = s->d_high;
+  a.dq = s->d_dq;
+  a.count_u16 = p.count_dtype == GG_COUNT_U16;
+  a.geometric = (s->d_warp_coverage && s->warp_coverage_frames > 0) ? s->d_warp_coverage : nullptr;
+  const int n = a.frames;
+  if (n <= 8) launch_reg<8>(a, s->stream);
+  else if (n <= 16) launch_reg<16>(a, s->stream);
+  else if (n <= 32) launch_reg<32>(a, s->stream);
+  else if (n <= 64) launch_reg<64>(a, s->stream);
+  else if (n <= 128) launch_smem<4>(a, s->stream);
+  else if (n <= 256) launch_smem<8>(a, s->stream);
+  else if (n <= 512) launch_smem<16>(a, s->stream);
+  else fail(GG_ERR_INVALID_ARGUMENT, "frame_count above 512 is not supported by the resident integrator");
+  s->last_count_dtype = p.count_dtype;
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_stack_integrate(gg_stack* s, const float* host_weights, const gg_integrate_params_t* params) {
+  GG_API_BEGIN
+  require(s != nullptr && params != nullptr, "null argument");
+  validate_integrate(*params);
+  stack_require_all_loaded(s, "integration");
+  stack_activate(s);
+  for (int64_t f = 0; f < s->frames; ++f) s->h_weights_pinned[f] = host_weights ? host_weights[f] : 1.0f;
+  check_cuda(cudaMemcpyAsync(s->d_weights, s->h_weights_pinned, sizeof(float) * s->frames, cudaMemcpyHostToDevice,
+                             s->stream),
+             "cudaMemcpyAsync(weights)");
+  launch_integrate(s, s->d_weights, *params);
+  GG_API_END
+}
+
+int gg_stack_integrate_device_weights(gg_stack* s, const void* dev_weights, const gg_integrate_params_t* params) {
+  GG_API_BEGIN
+  require(s != nullptr && params != nullptr, "null argument");
+  validate_integrate(*params);
+  stack_require_all_loaded(s, "integration");
+  stack_activate(s);
+  launch_integrate(s, dev_weights ? static_cast<const float*>(dev_weights) : s->d_weights, *params);
+  GG_API_END
+}
+
+int gg_stack_download_maps(gg_stack* s, float* host_master, float* host_weight, void* host_coverage, void* host_low,
+                           void* host_high, int16_t* host_dq) {
+  GG_API_BEGIN
+  require(s != nullptr, "stack is null");
+  if (s->d_master == nullptr || s->last_count_dtype < 0) fail(GG_ERR_RUNTIME, "no integration has been run");
+  stack_activate(s);
+  const size_t p = static_cast<size_t>(s->pixels);
+  const size_t cb = s->last_count_dtype == GG_COUNT_U16 ? 2 : 4;
+  struct Item {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  } items[] = {{host_master, s->d_master, p * 4}, {host_weight, s->d_weight, p * 4},
+               {host_coverage, s->d_coverage, p * cb}, {host_low, s->d_low, p * cb},
+               {host_high, s->d_high, p * cb}, {host_dq, s->d_dq, p * 2}};
+  for (auto& it : items) {
+    if (!it.dst) continue;
+    check_cuda(cudaMemcpyAsync(it.dst, it.src, it.bytes, cudaMemcpyDeviceToHost, s->stream),
+               "cudaMemcpyAsync(download maps)");
+  }
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(download maps)");
+  GG_API_END
+}
+
+}  // extern "C"

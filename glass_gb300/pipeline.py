@@ -1,0 +1,143 @@
+"""Host orchestration of the resident hot path on one GPU.
+
+Mirrors the order of the resident run (src/glass/engine/resident_cuda.py:
+ResidentCalibratedStack at :7667, set_calibration_masters :8542, calibrate
+:8974-9280, star catalogs :10798-10950, triangle match :11220-11400, warp
+:11466/12505, weights :12762-12785, integrate :13294-13460) for a stack whose
+raw frames are already in memory.  Every stage is a call into
+libglass_gb300.so; all work is enqueued on the stack's stream, so a whole
+step can run without a host synchronisation (and be captured in a CUDA
+graph) until the maps are downloaded.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from glass_gb300 import _lib
+from glass_gb300._glass_cuda_native import ResidentCalibratedStack
+
+
+@dataclass
+class Masters:
+    bias: np.ndarray | None
+    dark: np.ndarray | None
+    flat: np.ndarray | None
+
+
+def build_masters(bias_frames: np.ndarray | None, dark_frames: np.ndarray | None,
+                  flat_frames: np.ndarray | None, flat_floor: float = 1.0e-6) -> Masters:
+    """Master bias / dark / flat on the GPU (cpu/master_frames.py:97-165).
+
+    Each master is the mean of its frames (the stack integrator with no
+    rejection, float64-exact sums); the dark has the master bias subtracted
+    and the flat is bias-subtracted, divided by its median and floored.
+    """
+
+    def combine(frames: np.ndarray) -> np.ndarray:
+        n, h, w = frames.shape
+        stack = ResidentCalibratedStack(n, h, w)
+        raw = np.ascontiguousarray(frames.astype(np.uint16, copy=False))
+        params = _lib.CalibParams(1, 1.0, 1.0e-6, 0.0)
+        idx = np.arange(n, dtype=np.int64)
+        _lib.call("gg_stack_calibrate_u16", stack.handle, _lib.ptr(idx), ctypes.c_int64(n), _lib.ptr(raw), 0,
+                  ctypes.byref(params))
+        master, _ = stack.integrate_mean()
+        stack.close()
+        return master
+
+    bias = combine(bias_frames) if bias_frames is not None else None
+    dark = None
+    if dark_frames is not None:
+        dark = combine(dark_frames)
+        if bias is not None:
+            dark = (dark - bias).astype(np.float32)
+    flat = None
+    if flat_frames is not None:
+        flat = combine(flat_frames)
+        if bias is not None:
+            flat = (flat - bias).astype(np.float32)
+        norm = float(np.median(flat))
+        if abs(norm) < flat_floor:
+            raise ValueError("flat normalization is below flat_floor")
+        flat = np.maximum(flat / norm, flat_floor).astype(np.float32)
+    return Masters(bias, dark, flat)
+
+
+@dataclass
+class StepConfig:
+    rejection: int = _lib.GG_REJECT_WINSORIZED
+    low_sigma: float = 3.0
+    high_sigma: float = 3.0
+    min_samples: int = 3
+    max_reject_fraction: float = 0.5
+    weighting: str = "simple_snr"
+    count_map_dtype: str = "uint16"
+    light_exposure_s: float = 300.0
+    dark_exposure_s: float | None = 300.0
+
+
+class ResidentPipeline:
+    """One resident stack plus the per-step stage sequence."""
+
+    def __init__(self, frames: int, height: int, width: int, masters: Masters, config: StepConfig | None = None):
+        self.stack = ResidentCalibratedStack(frames, height, width)
+        self.stack.set_calibration_masters(masters.bias, masters.dark, masters.flat)
+        self.config = config or StepConfig()
+        self.frames = frames
+        self.height = height
+        self.width = width
+        self._indices = np.arange(frames, dtype=np.int64)
+        self._params = None
+
+    def set_stream(self, cuda_stream: int | None) -> None:
+        self.stack.set_stream(cuda_stream)
+
+    def _calib_params(self) -> _lib.CalibParams:
+        if self._params is None:
+            cfg = self.config
+            has_dark = bool(self.stack._info().has_dark)
+            scale = 1.0
+            if has_dark and cfg.dark_exposure_s not in (None, 0):
+                scale = float(cfg.light_exposure_s) / float(cfg.dark_exposure_s)
+            # build_masters subtracts the bias from the dark, so the bias is
+            # removed separately (master_dark_includes_bias = False).
+            self._params = _lib.CalibParams(0, scale, 1.0e-6, 0.0)
+        return self._params
+
+    # ---- stages (all asynchronous on the stack stream) ------------------------
+    def calibrate_device(self, dev_raw_ptr: int) -> None:
+        """uint16 frames already in device memory -> calibrated stack."""
+        _lib.call("gg_stack_calibrate_u16_device", self.stack.handle, _lib.ptr(self._indices),
+                  ctypes.c_int64(self.frames), ctypes.c_void_p(dev_raw_ptr), 0, ctypes.byref(self._calib_params()))
+
+    def calibrate_host(self, host_raw: np.ndarray) -> None:
+        """uint16 frames in host memory (pinned for full-speed copies)."""
+        _lib.call("gg_stack_calibrate_u16", self.stack.handle, _lib.ptr(self._indices),
+                  ctypes.c_int64(self.frames), _lib.ptr(host_raw), 0, ctypes.byref(self._calib_params()))
+
+    def weights(self) -> None:
+        self.stack.compute_frame_weights(self.config.weighting, None, 1.0e-6, download=False)
+
+    def integrate(self) -> None:
+        cfg = self.config
+        self.stack.integrate_async("device", cfg.rejection, cfg.low_sigma, cfg.high_sigma, cfg.min_samples,
+                                   cfg.max_reject_fraction, cfg.count_map_dtype)
+
+    def step_device(self, dev_raw_ptr: int) -> None:
+        self.calibrate_device(dev_raw_ptr)
+        self.weights()
+        self.integrate()
+
+    def step_host(self, host_raw: np.ndarray):
+        """Public-API step from host memory to host maps (end to end)."""
+        self.calibrate_host(host_raw)
+        self.weights()
+        self.integrate()
+        return self.stack.download_maps("full", include_dq=True)
+
+    def close(self) -> None:
+        self.stack.close()

@@ -1,0 +1,229 @@
+/*
+ * glass_gb300.h - C ABI of the GB300-native resident light-stack library.
+ *
+ * This header is the drop-in boundary.  GLASS reaches its CUDA backend through
+ * one Python module name, `_glass_cuda_native`, imported lazily by
+ * src/glass_cuda.py:31-44 and exercised through the pybind11 module defined in
+ * cpp/src/native_bindings.cpp:20383-21200.  This library replaces that module
+ * with a plain C ABI; glass_gb300/_glass_cuda_native.py is the ctypes shim that
+ * presents the same Python names on top of it.  Each declaration below names
+ * the reference entry point it replaces.
+ *
+ * Conventions (all functions):
+ *   - return int status: GG_OK (0) or a negative GG_ERR_* code; the message of
+ *     the last failure on the calling thread is available from gg_last_error();
+ *   - all pointers named host_* are caller-owned host buffers (pinned or
+ *     pageable), all pointers named dev_* are device pointers;
+ *   - float32 / uint16 / int16 / uint8 / int64 / float64 only, C-contiguous;
+ *   - a gg_stack is not thread-safe; distinct stacks may be used from distinct
+ *     threads.  Work is enqueued on the stack's stream; functions that return
+ *     host data synchronise that stream before returning.
+ */
+#ifndef GLASS_GB300_H
+#define GLASS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (mapped by the shim onto Python exceptions) ----------- */
+#define GG_OK 0
+#define GG_ERR_INVALID_ARGUMENT (-1) /* ValueError  (std::invalid_argument in the reference) */
+#define GG_ERR_OUT_OF_RANGE (-2)     /* IndexError  (std::out_of_range)                      */
+#define GG_ERR_RUNTIME (-3)          /* RuntimeError (state errors, e.g. frames not loaded)  */
+#define GG_ERR_CUDA (-4)             /* RuntimeError (check_cuda, native_bindings.cpp:1011)  */
+#define GG_ERR_NO_DEVICE (-5)        /* RuntimeError: no CUDA device                          */
+#define GG_ERR_OUT_OF_MEMORY (-6)    /* MemoryError                                           */
+#define GG_ERR_TIMEOUT (-7)          /* a bounded device-side wait ran out                    */
+
+/* ---- enumerations -------------------------------------------------------- */
+#define GG_REJECT_NONE 0        /* weighted mean, cpu/integration.py:106-118                 */
+#define GG_REJECT_SIGMA_CLIP 1  /* median centre / std scale, engine/rejection.py:47-49      */
+#define GG_REJECT_WINSORIZED 2  /* engine/rejection.py:39-44, 54-60, 219-297                */
+#define GG_REJECT_LINEAR_FIT 3  /* linear-fit clipping; no counterpart in the reference      */
+
+#define GG_COUNT_F32 0 /* count maps as float32 (cpu/integration.py:100-110)          */
+#define GG_COUNT_U16 1 /* count maps as uint16 (count_map_dtype="uint16")              */
+
+#define GG_INTERP_BILINEAR 1
+#define GG_INTERP_LANCZOS3 3
+
+/* ---- library / device ---------------------------------------------------- */
+/* Library ABI version (major*10000 + minor*100 + patch). */
+int gg_version(int* version);
+/* Copies the last error message of the calling thread (NUL-terminated). */
+int gg_last_error(char* buf, size_t cap);
+/* Number of CUDA kernels this library has launched in this process
+ * (instrumentation; no reference counterpart). */
+int gg_kernel_launches(int64_t* count);
+/* Replaces `cuda_available()` (native_bindings.cpp module def; glass_cuda.py:62). */
+int gg_cuda_available(int* available);
+/* Replaces `list_devices()` / `get_device_info(i)` (glass_cuda.py:184-212). */
+typedef struct {
+  char name[256];
+  int major;
+  int minor;
+  int multiprocessor_count;
+  int64_t total_global_mem;
+  int64_t l2_cache_bytes;
+  int64_t shared_mem_per_block_optin;
+} gg_device_info_t;
+int gg_device_count(int* count);
+int gg_device_info(int device, gg_device_info_t* info);
+/* Replaces `host_pinned_empty_{f32,u8}` (glass_cuda.py:215-226). */
+int gg_host_alloc_pinned(size_t bytes, void** host_ptr);
+int gg_host_free_pinned(void* host_ptr);
+
+/* ---- calibration parameters --------------------------------------------- */
+/* Mirrors CalibrationParameters (native_bindings.cpp:15138-15158) and the CPU
+ * policy fields read by cpu/calibration.py:51-76.  dark_scale is the already
+ * resolved light/dark exposure ratio (1 when scaling is off). */
+typedef struct {
+  int master_dark_includes_bias;
+  float dark_scale;
+  float flat_floor;
+  float pedestal;
+} gg_calib_params_t;
+
+/* Standalone calibrate (replaces module `calibrate_tile_f32`,
+ * glass_cuda.py:477-508 → calibration_kernels.cu:5-43).  Any master may be NULL. */
+int gg_calibrate_tile_f32(const float* host_light, const float* host_bias, const float* host_dark,
+                          const float* host_flat, int64_t n, const gg_calib_params_t* params,
+                          float* host_out);
+
+/* ---- resident stack ------------------------------------------------------ */
+typedef struct gg_stack gg_stack;
+
+typedef struct {
+  int64_t frame_count;
+  int64_t height;
+  int64_t width;
+  int64_t pixels_per_frame;
+  int64_t frame_stride;   /* elements between frame slots (padded to 64) */
+  int64_t slot_count;     /* frame slots incl. spare warp targets        */
+  int64_t loaded_count;
+  int64_t bytes_allocated;
+  int64_t warp_scratch_bytes;
+  int64_t host_pinned_bytes;
+  int64_t calibration_lane_count;
+  int64_t warp_coverage_frame_count;
+  int has_bias;
+  int has_dark;
+  int has_flat;
+} gg_stack_info_t;
+
+/* Replaces ResidentCalibratedStack(frame_count, height, width)
+ * (native_bindings.cpp:2917-2934; glass_cuda.py:2661). */
+int gg_stack_create(int64_t frame_count, int64_t height, int64_t width, gg_stack** out);
+int gg_stack_destroy(gg_stack* stack);
+/* Replaces the read-only properties (native_bindings.cpp:20624-20645). */
+int gg_stack_info(const gg_stack* stack, gg_stack_info_t* info);
+/* Runs the stack's work on the given cudaStream_t (NULL: the stack's own stream). */
+int gg_stack_set_stream(gg_stack* stack, void* cuda_stream);
+int gg_stack_synchronize(gg_stack* stack);
+
+/* Replaces set_calibration_masters(bias, dark, flat); NULL clears a master. */
+int gg_stack_set_masters(gg_stack* stack, const float* host_bias, const float* host_dark,
+                         const float* host_flat);
+/* Replaces upload_calibrated_frame(i, frame). */
+int gg_stack_upload_frame(gg_stack* stack, int64_t index, const float* host_frame);
+/* Replaces download_frame_tile(i, x0, y0, x1, y1) (row-major (y1-y0, x1-x0)). */
+int gg_stack_download_frame_tile(gg_stack* stack, int64_t index, int64_t x0, int64_t y0, int64_t x1,
+                                 int64_t y1, float* host_out);
+/* Replaces download_frames_tile(indices, x0, y0, x1, y1). */
+int gg_stack_download_frames_tile(gg_stack* stack, const int64_t* indices, int64_t count, int64_t x0,
+                                  int64_t y0, int64_t x1, int64_t y1, float* host_out);
+
+/* Fused uint16 decode + calibrate of `count` frames from host memory
+ * (replaces calibrate_frames_fits_u16be_bzero_* native_bindings.cpp:7422-8094 and
+ * calibration_kernels.cu:110-153).  host_raw holds count*H*W uint16 samples;
+ * big_endian_bzero=1 means FITS BITPIX=16 big-endian bytes with BZERO 32768,
+ * 0 means native-endian unsigned values.  Copies overlap the decode kernels. */
+int gg_stack_calibrate_u16(gg_stack* stack, const int64_t* indices, int64_t count, const void* host_raw,
+                           int big_endian_bzero, const gg_calib_params_t* params);
+/* Same with the raw frames already in device memory (count*H*W uint16). */
+int gg_stack_calibrate_u16_device(gg_stack* stack, const int64_t* indices, int64_t count,
+                                  const void* dev_raw, int big_endian_bzero,
+                                  const gg_calib_params_t* params);
+/* Replaces calibrate_frame(i, light_f32, t_L, t_D, policy) (native_bindings.cpp:5979). */
+int gg_stack_calibrate_f32(gg_stack* stack, int64_t index, const float* host_light,
+                           const gg_calib_params_t* params);
+
+/* Replaces frame_global_stats(i) (native_bindings.cpp:10569-10640). */
+typedef struct {
+  double mean;
+  double std;
+  int64_t valid_pixels;
+  int64_t total_pixels;
+} gg_frame_stats_t;
+int gg_stack_frame_stats(gg_stack* stack, const int64_t* indices, int64_t count, gg_frame_stats_t* out);
+
+/* Frame weights computed on the device into the stack's weight vector
+ * (used by gg_stack_integrate_device_weights with dev_weights = NULL).
+ * GG_WEIGHTS_SIMPLE_SNR: w = max(|mean|/std, eps) (1/eps when std <= eps, 0
+ * without valid pixels) - resident_cuda.py:1948-1956 with the statistics of
+ * frame_global_stats; GG_WEIGHTS_PRIOR: w = prior.  A frame whose prior is not
+ * finite and positive gets weight 0.  host_prior (frame_count) may be NULL;
+ * host_weights_out (frame_count) may be NULL to stay asynchronous. */
+#define GG_WEIGHTS_PRIOR 0
+#define GG_WEIGHTS_SIMPLE_SNR 1
+int gg_stack_compute_weights(gg_stack* stack, int mode, const float* host_prior, float eps,
+                             float* host_weights_out);
+
+/* ---- integration --------------------------------------------------------- */
+typedef struct {
+  int rejection;             /* GG_REJECT_*                                  */
+  float low_sigma;
+  float high_sigma;
+  int min_samples;           /* guard, cpu/integration.py:85-99              */
+  float max_reject_fraction;
+  int count_dtype;           /* GG_COUNT_*                                   */
+  int linear_fit_iterations; /* GG_REJECT_LINEAR_FIT only                    */
+} gg_integrate_params_t;
+
+/* Rejection + weighted integration of all frames into the stack's six output
+ * maps (master f32, weight f32, coverage, low, high count maps, DQ int16).
+ * Replaces integrate_mean / integrate_sigma_clip /
+ * integrate_hardened_winsorized_sigma (native_bindings.cpp:13227, 13395-14337;
+ * integration_kernels.cu:1610-1638, 1743-1902, 2292-2836) with the CPU
+ * semantics of cpu/integration.py:36-118.  host_weights may be NULL (unit).
+ * Asynchronous: results stay on the device until gg_stack_download_maps. */
+int gg_stack_integrate(gg_stack* stack, const float* host_weights, const gg_integrate_params_t* params);
+/* Same with the weights already on the device (float32[frame_count]); NULL
+ * uses the weights of the last gg_stack_compute_weights. */
+int gg_stack_integrate_device_weights(gg_stack* stack, const void* dev_weights,
+                                      const gg_integrate_params_t* params);
+/* Downloads the maps of the last integration; any pointer may be NULL.  Count
+ * maps are float32 or uint16 per the count_dtype used. */
+int gg_stack_download_maps(gg_stack* stack, float* host_master, float* host_weight, void* host_coverage,
+                           void* host_low, void* host_high, int16_t* host_dq);
+
+/* Device pointers of the stack's buffers, for zero-copy consumers. */
+typedef struct {
+  void* slots;          /* float32 frame slots                                   */
+  void* slot_of_frame;  /* int32[frame_count] device table frame -> slot          */
+  void* master;
+  void* weight;
+  void* coverage;
+  void* low;
+  void* high;
+  void* dq;
+  void* warp_coverage;  /* float32 coverage accumulator                           */
+} gg_stack_device_ptrs_t;
+int gg_stack_device_ptrs(gg_stack* stack, gg_stack_device_ptrs_t* out);
+
+/* Replaces module `resident_dq_map_count_maps_i16` (glass_cuda.py:270-290;
+ * resident_cuda.py:3110-3297): DQ bits from the output maps.  Any count map
+ * pointer may be NULL; geometric may be NULL. */
+int gg_dq_map_i16(const float* host_master, const float* host_weight, const float* host_coverage,
+                  const float* host_low, const float* host_high, const float* host_geometric,
+                  int64_t n, int64_t active_frame_count, int16_t* host_dq);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLASS_GB300_H */
