@@ -344,8 +344,9 @@ __device__ __forceinline__ void finish_pixel(const IntegrateArgs& a, int64_t p, 
   }
   float master = 0.0f, weight = 0.0f;
   int kept = 0;
-  if (unit_weights) {
-    // Unit weights: sum the kept samples straight from the sorted column.
+  if (unit_weights && a.rejection != GG_REJECT_NONE) {
+    // Unit weights: sum the kept samples straight from the sorted column
+    // (without rejection the column is not sorted and the frame loop runs).
     FF ws;
     for (int i = 0; i < cnt; ++i) {
       const float x = sorted(i);
@@ -415,6 +416,253 @@ __device__ __forceinline__ void load_frame_table(const IntegrateArgs& a, FrameTa
     }
   }
   __syncthreads();
+}
+
+// ---- kernel F: N <= NB <= 32, everything in registers -----------------------
+// Frame-order samples x[] and the sorted copy s[] both live in registers; the
+// statistics passes are unrolled over s[] with two independent float-float
+// accumulators (the TwoSum chain is the latency bottleneck), and the final
+// weighted sum takes the cheap branch for the common pixel: every frame
+// valid and nothing rejected -> sum(w*x) over all frames, weight = sum(w)
+// precomputed once per CTA.
+
+__device__ __forceinline__ void ff_merge2(FF& a, const FF& b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  a.hi = s;
+  a.lo = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+}
+
+// True when every value in [lo, hi] lies within a factor of two of c (same
+// sign), so x - c is exact in float32 (Sterbenz).
+__device__ __forceinline__ bool sterbenz_interval(float lo, float hi, float c) {
+  if (c > 0.0f) return lo >= 0.5f * c && hi <= 2.0f * c;
+  if (c < 0.0f) return hi <= 0.5f * c && lo >= 2.0f * c;
+  return false;
+}
+
+template <int NB>
+__device__ __forceinline__ CenterScale winsorized_stats_reg(const float (&s)[NB], const float* S, int T, int cnt,
+                                                            int nframes, bool allvalid, float ls, float hs) {
+  CenterScale r{0.0f, 0.0f};
+  if (cnt <= 0) return r;
+  float med, q25, q75;
+  if (allvalid) {
+    med = percentile_all(S, T, nframes, 50.0f);
+    q25 = percentile_all(S, T, nframes, 25.0f);
+    q75 = percentile_all(S, T, nframes, 75.0f);
+  } else {
+    med = percentile_valid(S, T, cnt, 0.5f);
+    q25 = percentile_valid(S, T, cnt, 0.25f);
+    q75 = percentile_valid(S, T, cnt, 0.75f);
+  }
+  float scale1 = __fdiv_rn(__fsub_rn(q75, q25), 1.349f);
+  const bool ok1 = allvalid ? (scale1 > 0.0f) : (scale1 > 0.0f && isfinite(scale1));
+  if (!ok1) {
+    auto sorted = [&](int i) -> float { return S[i * T]; };
+    scale1 = std_of_valid(sorted, cnt, allvalid);
+  }
+  const float lo1 = __fsub_rn(med, __fmul_rn(ls, scale1));
+  const float hi1 = __fadd_rn(med, __fmul_rn(hs, scale1));
+  FF a0, a1;
+#pragma unroll
+  for (int i = 0; i < NB; i += 2) {
+    if (i < cnt) a0.add(clipf(s[i], lo1, hi1));
+    if (i + 1 < cnt) a1.add(clipf(s[i + 1], lo1, hi1));
+  }
+  ff_merge2(a0, a1);
+  float mh, ml;
+  if (allvalid) {
+    ff_div_pair(a0.hi, a0.lo, static_cast<float>(cnt), mh, ml);
+    r.center = __fadd_rn(mh, ml);
+  } else {
+    r.center = ff_div_f32(a0.hi, a0.lo, static_cast<float>(cnt));
+    mh = r.center;
+    ml = 0.0f;
+  }
+  // Clipped values lie in [max(lo1, s0), min(hi1, s_last)].
+  const float vlo = fmaxf(lo1, s[0]);
+  float vmax = s[0];
+#pragma unroll
+  for (int i = 1; i < NB; ++i) vmax = (i < cnt) ? s[i] : vmax;
+  const float vhi = fminf(hi1, vmax);
+  FF v0, v1;
+  if (sterbenz_interval(vlo, vhi, mh)) {
+    const float m2 = __fmul_rn(-2.0f, ml);
+#pragma unroll
+    for (int i = 0; i < NB; i += 2) {
+      if (i < cnt) {
+        const float d = __fsub_rn(clipf(s[i], lo1, hi1), mh);
+        const float p = __fmul_rn(d, d);
+        v0.add(p);
+        v0.lo = __fadd_rn(v0.lo, __fmaf_rn(m2, d, __fmaf_rn(d, d, -p)));
+      }
+      if (i + 1 < cnt) {
+        const float d = __fsub_rn(clipf(s[i + 1], lo1, hi1), mh);
+        const float p = __fmul_rn(d, d);
+        v1.add(p);
+        v1.lo = __fadd_rn(v1.lo, __fmaf_rn(m2, d, __fmaf_rn(d, d, -p)));
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < NB; i += 2) {
+      if (i < cnt) ff_add_sqdev(v0, clipf(s[i], lo1, hi1), mh, ml);
+      if (i + 1 < cnt) ff_add_sqdev(v1, clipf(s[i + 1], lo1, hi1), mh, ml);
+    }
+  }
+  ff_merge2(v0, v1);
+  float q, ql;
+  ff_div_pair(v0.hi, v0.lo, static_cast<float>(cnt), q, ql);
+  const float scale = ff_sqrt_f32(q, ql);
+  const bool ok2 = allvalid ? (scale > 0.0f) : (scale > 0.0f && isfinite(scale));
+  r.scale = ok2 ? scale : scale1;
+  return r;
+}
+
+template <int NB, int T>
+__global__ void __launch_bounds__(T) integrate_regfast_kernel(IntegrateArgs a) {
+  extern __shared__ float smem[];
+  float* S = smem;  // [NB][T] ascending valid samples (percentile lookups)
+  __shared__ FrameTable<NB> tab;
+  __shared__ float s_wtot[2];
+  load_frame_table<NB>(a, tab);
+  if (threadIdx.x == 0) {
+    FF wt;
+    for (int f = 0; f < a.frames; ++f)
+      if (tab.w[f] > 0.0f) wt.add(tab.w[f]);
+    s_wtot[0] = wt.hi;
+    s_wtot[1] = wt.lo;
+  }
+  __syncthreads();
+  const bool allvalid = tab.allvalid != 0;
+  const bool unit = tab.unit != 0;
+  const int tid = threadIdx.x;
+  const int N = a.frames;
+  const int64_t P = a.pixels;
+  const float ls = a.low_sigma, hs = a.high_sigma;
+  for (int64_t p = static_cast<int64_t>(blockIdx.x) * T + tid; p < P; p += static_cast<int64_t>(gridDim.x) * T) {
+    float x[NB];
+#pragma unroll
+    for (int f = 0; f < NB; ++f) x[f] = (f < N) ? __ldcs(tab.base[f] + p) : kInf;
+    float s[NB];
+    int cnt = 0;
+#pragma unroll
+    for (int f = 0; f < NB; ++f) {
+      const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(x[f]);
+      s[f] = ok ? x[f] : kInf;
+      cnt += ok ? 1 : 0;
+    }
+    int nl = 0, nh = 0;
+    float lt = -kInf, ht = kInf;
+    bool thresholds = false;
+    if (a.rejection != GG_REJECT_NONE) {
+      sort_network<NB>(s);
+#pragma unroll
+      for (int f = 0; f < NB; ++f) S[f * T + tid] = s[f];
+      CenterScale cs{0.0f, 0.0f};
+      if (a.rejection == GG_REJECT_WINSORIZED) {
+        cs = winsorized_stats_reg<NB>(s, S + tid, T, cnt, N, allvalid, ls, hs);
+      } else if (a.rejection == GG_REJECT_SIGMA_CLIP && cnt > 0) {
+        // NumPy nanmedian + float32 nanstd in frame order (see sigma_stats).
+        const int h = cnt / 2;
+        const int l = (cnt & 1) ? h : h - 1;
+        cs.center = __fmul_rn(__fadd_rn(S[l * T + tid], S[h * T + tid]), 0.5f);
+        float sum = 0.0f;
+#pragma unroll
+        for (int f = 0; f < NB; ++f)
+          if (f < N && tab.w[f] > 0.0f && isfinite(x[f])) sum = __fadd_rn(sum, x[f]);
+        const float mean = __fdiv_rn(sum, static_cast<float>(cnt));
+        float v = 0.0f;
+#pragma unroll
+        for (int f = 0; f < NB; ++f) {
+          if (f < N && tab.w[f] > 0.0f && isfinite(x[f])) {
+            const float d = __fsub_rn(x[f], mean);
+            v = __fadd_rn(v, __fmul_rn(d, d));
+          }
+        }
+        cs.scale = __fsqrt_rn(__fdiv_rn(v, static_cast<float>(cnt)));
+      }
+      if (a.rejection == GG_REJECT_LINEAR_FIT) {
+        if (cnt > 0) {
+          auto sorted = [&](int i) -> float { return S[i * T + tid]; };
+          int lo = 0, hi = cnt;
+          linear_fit_clip(sorted, cnt, ls, hs, a.lfc_iterations, lo, hi);
+          nl = lo;
+          nh = cnt - hi;
+          lt = sorted(lo);
+          ht = sorted(hi - 1);
+        }
+      } else {
+        lt = __fsub_rn(cs.center, __fmul_rn(ls, cs.scale));
+        ht = __fadd_rn(cs.center, __fmul_rn(hs, cs.scale));
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+          nl += (i < cnt && s[i] < lt) ? 1 : 0;
+          nh += (i < cnt && s[i] > ht) ? 1 : 0;
+        }
+      }
+      thresholds = true;
+      if (nl + nh > 0) {
+        const int rej = nl + nh;
+        const float frac = __fdiv_rn(static_cast<float>(rej), static_cast<float>(cnt));
+        if (!((cnt - rej >= a.min_samples) && (frac <= a.max_frac))) {
+          nl = nh = 0;
+          thresholds = false;
+        }
+      } else {
+        thresholds = false;
+      }
+    }
+    float master = 0.0f, weight = 0.0f;
+    int kept = 0;
+    if (unit && a.rejection != GG_REJECT_NONE) {
+      // Kept samples are the contiguous sorted range [nl, cnt - nh).
+      FF w0, w1;
+#pragma unroll
+      for (int i = 0; i < NB; i += 2) {
+        if (i >= nl && i < cnt - nh) w0.add(s[i]);
+        if (i + 1 >= nl && i + 1 < cnt - nh) w1.add(s[i + 1]);
+      }
+      ff_merge2(w0, w1);
+      kept = cnt - nl - nh;
+      if (kept > 0) {
+        master = ff_div_f32(w0.hi, w0.lo, static_cast<float>(kept));
+        weight = static_cast<float>(kept);
+      }
+    } else if (cnt == N && !thresholds) {
+      // Every frame valid, nothing rejected: sum(w*x) over all frames.
+      FF w0, w1;
+#pragma unroll
+      for (int f = 0; f < NB; f += 2) {
+        if (f < N) w0.add_prod(x[f], tab.w[f]);
+        if (f + 1 < N) w1.add_prod(x[f + 1], tab.w[f + 1]);
+      }
+      ff_merge2(w0, w1);
+      kept = N;
+      if (s_wtot[0] > 0.0f) {
+        master = ff_div_ff(w0.hi, w0.lo, s_wtot[0], s_wtot[1]);
+        weight = __fadd_rn(s_wtot[0], s_wtot[1]);
+      }
+    } else {
+      FF ws, wsum;
+#pragma unroll
+      for (int f = 0; f < NB; ++f) {
+        const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(x[f]) &&
+                        !(thresholds && (x[f] < lt || x[f] > ht));
+        if (ok) {
+          ws.add_prod(x[f], tab.w[f]);
+          wsum.add(tab.w[f]);
+          ++kept;
+        }
+      }
+      if (kept > 0 && wsum.hi > 0.0f) {
+        master = ff_div_ff(ws.hi, ws.lo, wsum.hi, wsum.lo);
+        weight = wsum.value_f32();
+      }
+    }
+    write_outputs(a, p, master, weight, kept, nl, nh, tab.active);
+  }
 }
 
 // ---- kernel A: N <= NB <= 64, column in registers ----------------------------
@@ -548,6 +796,21 @@ static void launch_reg(const IntegrateArgs& args, cudaStream_t stream) {
   check_cuda(cudaGetLastError(), "integrate kernel launch");
 }
 
+template <int NB>
+static void launch_regfast(const IntegrateArgs& args, cudaStream_t stream) {
+  constexpr int T = 128;
+  const size_t smem = size_t(NB) * T * sizeof(float);
+  auto kern = integrate_regfast_kernel<NB, T>;
+  check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+             "cudaFuncSetAttribute(integrate)");
+  int per_sm = 0;
+  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem), "occupancy");
+  const unsigned grid = grid_for(static_cast<size_t>(args.pixels), T, std::max(per_sm, 1));
+  note_launch();
+  kern<<<grid, T, smem, stream>>>(args);
+  check_cuda(cudaGetLastError(), "integrate kernel launch");
+}
+
 template <int MR>
 static void launch_smem(const IntegrateArgs& args, cudaStream_t stream) {
   constexpr int T = 32;
@@ -599,9 +862,9 @@ void launch_integrate(gg_stack* s, const float* d_weights, const gg_integrate_pa
   a.count_u16 = p.count_dtype == GG_COUNT_U16;
   a.geometric = (s->d_warp_coverage && s->warp_coverage_frames > 0) ? s->d_warp_coverage : nullptr;
   const int n = a.frames;
-  if (n <= 8) launch_reg<8>(a, s->stream);
-  else if (n <= 16) launch_reg<16>(a, s->stream);
-  else if (n <= 32) launch_reg<32>(a, s->stream);
+  if (n <= 8) launch_regfast<8>(a, s->stream);
+  else if (n <= 16) launch_regfast<16>(a, s->stream);
+  else if (n <= 32) launch_regfast<32>(a, s->stream);
   else if (n <= 64) launch_reg<64>(a, s->stream);
   else if (n <= 128) launch_smem<4>(a, s->stream);
   else if (n <= 256) launch_smem<8>(a, s->stream);

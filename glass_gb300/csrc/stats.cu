@@ -26,16 +26,26 @@ __global__ void __launch_bounds__(256) frame_stats_kernel(const float* slots, co
                                                           int64_t pixels, const int* frames, double* partials) {
   const int frame = frames[blockIdx.y];
   const float* src = slots + static_cast<int64_t>(slot_of_frame[frame]) * stride;
-  FF s1, s2;
+  // Two independent accumulator pairs over float4 loads (slots are 256 B
+  // aligned), then the scalar tail.
+  FF s1, s2, t1, t2;
   unsigned count = 0;
-  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < pixels; p += int64_t(gridDim.x) * blockDim.x) {
-    const float v = __ldcs(src + p);
-    if (isfinite(v)) {
-      s1.add(v);
-      s2.add_prod(v, v);
-      ++count;
-    }
+  const int64_t quads = pixels / 4;
+  const float4* src4 = reinterpret_cast<const float4*>(src);
+  for (int64_t q = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; q < quads; q += int64_t(gridDim.x) * blockDim.x) {
+    const float4 v = __ldcs(src4 + q);
+    if (isfinite(v.x)) { s1.add(v.x); s2.add_prod(v.x, v.x); ++count; }
+    if (isfinite(v.y)) { t1.add(v.y); t2.add_prod(v.y, v.y); ++count; }
+    if (isfinite(v.z)) { s1.add(v.z); s2.add_prod(v.z, v.z); ++count; }
+    if (isfinite(v.w)) { t1.add(v.w); t2.add_prod(v.w, v.w); ++count; }
   }
+  for (int64_t p = quads * 4 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < pixels;
+       p += int64_t(gridDim.x) * blockDim.x) {
+    const float v = src[p];
+    if (isfinite(v)) { s1.add(v); s2.add_prod(v, v); ++count; }
+  }
+  ff_merge(s1, t1);
+  ff_merge(s2, t2);
   for (int off = 16; off > 0; off >>= 1) {
     FF o1, o2;
     o1.hi = __shfl_xor_sync(0xffffffffu, s1.hi, off);
@@ -65,27 +75,31 @@ __global__ void __launch_bounds__(256) frame_stats_kernel(const float* slots, co
 //   valid == 0 -> 0;  std <= eps -> 1/eps;  else max(|mean|/std, eps)
 // A frame whose prior weight is not finite and positive keeps weight 0
 // (zero-weight frames are skipped, resident_cuda.py:12766-12770).
+// One warp per frame: lanes fold the CTA partials, then a shuffle reduction.
 __global__ void snr_weights_kernel(const double* partials, int blocks, const int* frames, int count,
                                    const float* prior, float eps, int mode, float* weights) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
   if (k >= count) return;
   const int f = frames[k];
   const float pw = prior ? prior[k] : 1.0f;
-  if (!(isfinite(pw) && pw > 0.0f)) {
-    weights[f] = 0.0f;
-    return;
-  }
-  if (mode == 0) {
-    weights[f] = pw;
+  if (!(isfinite(pw) && pw > 0.0f) || mode == 0) {
+    if (lane == 0) weights[f] = (isfinite(pw) && pw > 0.0f) ? pw : 0.0f;
     return;
   }
   double sum = 0.0, sum2 = 0.0, n = 0.0;
-  for (int b = 0; b < blocks; ++b) {
+  for (int b = lane; b < blocks; b += 32) {
     const double* q = partials + (static_cast<int64_t>(k) * blocks + b) * 3;
     sum += q[0];
     sum2 += q[1];
     n += q[2];
   }
+  for (int off = 16; off > 0; off >>= 1) {
+    sum += __shfl_xor_sync(0xffffffffu, sum, off);
+    sum2 += __shfl_xor_sync(0xffffffffu, sum2, off);
+    n += __shfl_xor_sync(0xffffffffu, n, off);
+  }
+  if (lane != 0) return;
   if (n <= 0.0) {
     weights[f] = 0.0f;
     return;
@@ -134,7 +148,7 @@ int gg_stack_compute_weights(gg_stack* s, int mode, const float* host_prior, flo
     check_cuda(cudaGetLastError(), "frame_stats kernel launch");
   }
   note_launch();
-  snr_weights_kernel<<<static_cast<unsigned>((count + 127) / 128), 128, 0, s->stream>>>(
+  snr_weights_kernel<<<static_cast<unsigned>((count + 3) / 4), 128, 0, s->stream>>>(
       s->d_partials, blocks, d_frames, static_cast<int>(count), d_prior, eps, mode, s->d_weights);
   check_cuda(cudaGetLastError(), "snr_weights kernel launch");
   if (host_weights_out) {
