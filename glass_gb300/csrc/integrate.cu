@@ -418,19 +418,29 @@ __device__ __forceinline__ void load_frame_table(const IntegrateArgs& a, FrameTa
   __syncthreads();
 }
 
-// ---- kernel F: N <= NB <= 32, everything in registers -----------------------
-// Frame-order samples x[] and the sorted copy s[] both live in registers; the
-// statistics passes are unrolled over s[] with two independent float-float
-// accumulators (the TwoSum chain is the latency bottleneck), and the final
-// weighted sum takes the cheap branch for the common pixel: every frame
-// valid and nothing rejected -> sum(w*x) over all frames, weight = sum(w)
-// precomputed once per CTA.
+// ---- kernel F: N <= NB <= 32, specialised per rejection mode ----------------
+// The frame-order column x[] stays in registers (for the weighted sum); a
+// sorted copy goes through a register sorting network into shared memory
+// S[rank][thread] (conflict-free for any per-thread rank).  The statistics
+// passes are compact rolled loops over S, so the code fits the instruction
+// cache, and they use the magnitude order the sort provides: summing
+// same-sign values from the largest magnitude down makes Fast2Sum (3 flops)
+// error-free, and squared deviations are summed from both ends of the sorted
+// column inwards for the same reason.  Rejection counts are binary searches.
 
 __device__ __forceinline__ void ff_merge2(FF& a, const FF& b) {
   float s, e;
   two_sum(a.hi, b.hi, s, e);
   a.hi = s;
   a.lo = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+}
+
+// Fast2Sum: error-free when |a.hi| >= |x| (or a.hi == 0).
+__device__ __forceinline__ void ff_add_fast(FF& a, float x) {
+  const float s = __fadd_rn(a.hi, x);
+  const float e = __fsub_rn(x, __fsub_rn(s, a.hi));
+  a.hi = s;
+  a.lo = __fadd_rn(a.lo, e);
 }
 
 // True when every value in [lo, hi] lies within a factor of two of c (same
@@ -441,9 +451,82 @@ __device__ __forceinline__ bool sterbenz_interval(float lo, float hi, float c) {
   return false;
 }
 
-template <int NB>
-__device__ __forceinline__ CenterScale winsorized_stats_reg(const float (&s)[NB], const float* S, int T, int cnt,
-                                                            int nframes, bool allvalid, float ls, float hs) {
+// Number of sorted valid values < t (strict) or <= t.
+__device__ __forceinline__ int count_below(const float* S, int T, int cnt, float t, bool inclusive) {
+  int lo = 0, hi = cnt;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    const float v = S[mid * T];
+    if (inclusive ? (v <= t) : (v < t)) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Sum of S[i0..i1) (clipped to [lo, hi]) without rounding error loss.
+__device__ __forceinline__ FF sum_sorted(const float* S, int T, int i0, int i1, float lo, float hi) {
+  FF acc;
+  if (i1 <= i0) return acc;
+  const float first = clipf(S[i0 * T], lo, hi);
+  const float last = clipf(S[(i1 - 1) * T], lo, hi);
+  if (first >= 0.0f) {
+#pragma unroll 4
+    for (int i = i1 - 1; i >= i0; --i) ff_add_fast(acc, clipf(S[i * T], lo, hi));
+  } else if (last <= 0.0f) {
+#pragma unroll 4
+    for (int i = i0; i < i1; ++i) ff_add_fast(acc, clipf(S[i * T], lo, hi));
+  } else {
+    FF b;
+#pragma unroll 2
+    for (int i = i0; i < i1; i += 2) {
+      acc.add(clipf(S[i * T], lo, hi));
+      if (i + 1 < i1) b.add(clipf(S[(i + 1) * T], lo, hi));
+    }
+    ff_merge2(acc, b);
+  }
+  return acc;
+}
+
+// Sum of squared deviations of clip(S[0..cnt)) from (mh + ml).
+__device__ __forceinline__ FF sqdev_sorted(const float* S, int T, int cnt, float lo, float hi, float mh, float ml) {
+  FF left, right;
+  const float vlo = clipf(S[0], lo, hi);
+  const float vhi = clipf(S[(cnt - 1) * T], lo, hi);
+  if (sterbenz_interval(vlo, vhi, mh)) {
+    // Values <= mh from the bottom up and values > mh from the top down:
+    // both sequences have non-increasing |deviation|, so Fast2Sum is exact.
+    const int nl = count_below(S, T, cnt, mh, true);
+    const int nr = cnt - nl;
+    const int steps = max(nl, nr);
+    const float m2 = __fmul_rn(-2.0f, ml);
+#pragma unroll 2
+    for (int k = 0; k < steps; ++k) {
+      if (k < nl) {
+        const float d = __fsub_rn(clipf(S[k * T], lo, hi), mh);
+        const float p = __fmul_rn(d, d);
+        ff_add_fast(left, p);
+        left.lo = __fadd_rn(left.lo, __fmaf_rn(m2, d, __fmaf_rn(d, d, -p)));
+      }
+      if (k < nr) {
+        const float d = __fsub_rn(clipf(S[(cnt - 1 - k) * T], lo, hi), mh);
+        const float p = __fmul_rn(d, d);
+        ff_add_fast(right, p);
+        right.lo = __fadd_rn(right.lo, __fmaf_rn(m2, d, __fmaf_rn(d, d, -p)));
+      }
+    }
+  } else {
+#pragma unroll 2
+    for (int i = 0; i < cnt; i += 2) {
+      ff_add_sqdev(left, clipf(S[i * T], lo, hi), mh, ml);
+      if (i + 1 < cnt) ff_add_sqdev(right, clipf(S[(i + 1) * T], lo, hi), mh, ml);
+    }
+  }
+  ff_merge2(left, right);
+  return left;
+}
+
+// Winsorized centre/scale over the sorted column (rejection.py:219-297).
+__device__ __forceinline__ CenterScale winsorized_sorted(const float* S, int T, int cnt, int nframes, bool allvalid,
+                                                         float ls, float hs) {
   CenterScale r{0.0f, 0.0f};
   if (cnt <= 0) return r;
   float med, q25, q75;
@@ -459,71 +542,45 @@ __device__ __forceinline__ CenterScale winsorized_stats_reg(const float (&s)[NB]
   float scale1 = __fdiv_rn(__fsub_rn(q75, q25), 1.349f);
   const bool ok1 = allvalid ? (scale1 > 0.0f) : (scale1 > 0.0f && isfinite(scale1));
   if (!ok1) {
-    auto sorted = [&](int i) -> float { return S[i * T]; };
-    scale1 = std_of_valid(sorted, cnt, allvalid);
+    // Fallback std of the valid samples (rejection.py:231 / :323-349).
+    const FF s1 = sum_sorted(S, T, 0, cnt, -kInf, kInf);
+    float mh, ml;
+    if (allvalid) {
+      ff_div_pair(s1.hi, s1.lo, static_cast<float>(cnt), mh, ml);
+    } else {
+      mh = ff_div_f32(s1.hi, s1.lo, static_cast<float>(cnt));
+      ml = 0.0f;
+    }
+    const FF v = sqdev_sorted(S, T, cnt, -kInf, kInf, mh, ml);
+    float q, ql;
+    ff_div_pair(v.hi, v.lo, static_cast<float>(cnt), q, ql);
+    scale1 = ff_sqrt_f32(q, ql);
   }
   const float lo1 = __fsub_rn(med, __fmul_rn(ls, scale1));
   const float hi1 = __fadd_rn(med, __fmul_rn(hs, scale1));
-  FF a0, a1;
-#pragma unroll
-  for (int i = 0; i < NB; i += 2) {
-    if (i < cnt) a0.add(clipf(s[i], lo1, hi1));
-    if (i + 1 < cnt) a1.add(clipf(s[i + 1], lo1, hi1));
-  }
-  ff_merge2(a0, a1);
+  const FF sw = sum_sorted(S, T, 0, cnt, lo1, hi1);
   float mh, ml;
   if (allvalid) {
-    ff_div_pair(a0.hi, a0.lo, static_cast<float>(cnt), mh, ml);
+    ff_div_pair(sw.hi, sw.lo, static_cast<float>(cnt), mh, ml);
     r.center = __fadd_rn(mh, ml);
   } else {
-    r.center = ff_div_f32(a0.hi, a0.lo, static_cast<float>(cnt));
+    r.center = ff_div_f32(sw.hi, sw.lo, static_cast<float>(cnt));
     mh = r.center;
     ml = 0.0f;
   }
-  // Clipped values lie in [max(lo1, s0), min(hi1, s_last)].
-  const float vlo = fmaxf(lo1, s[0]);
-  float vmax = s[0];
-#pragma unroll
-  for (int i = 1; i < NB; ++i) vmax = (i < cnt) ? s[i] : vmax;
-  const float vhi = fminf(hi1, vmax);
-  FF v0, v1;
-  if (sterbenz_interval(vlo, vhi, mh)) {
-    const float m2 = __fmul_rn(-2.0f, ml);
-#pragma unroll
-    for (int i = 0; i < NB; i += 2) {
-      if (i < cnt) {
-        const float d = __fsub_rn(clipf(s[i], lo1, hi1), mh);
-        const float p = __fmul_rn(d, d);
-        v0.add(p);
-        v0.lo = __fadd_rn(v0.lo, __fmaf_rn(m2, d, __fmaf_rn(d, d, -p)));
-      }
-      if (i + 1 < cnt) {
-        const float d = __fsub_rn(clipf(s[i + 1], lo1, hi1), mh);
-        const float p = __fmul_rn(d, d);
-        v1.add(p);
-        v1.lo = __fadd_rn(v1.lo, __fmaf_rn(m2, d, __fmaf_rn(d, d, -p)));
-      }
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < NB; i += 2) {
-      if (i < cnt) ff_add_sqdev(v0, clipf(s[i], lo1, hi1), mh, ml);
-      if (i + 1 < cnt) ff_add_sqdev(v1, clipf(s[i + 1], lo1, hi1), mh, ml);
-    }
-  }
-  ff_merge2(v0, v1);
+  const FF sv = sqdev_sorted(S, T, cnt, lo1, hi1, mh, ml);
   float q, ql;
-  ff_div_pair(v0.hi, v0.lo, static_cast<float>(cnt), q, ql);
+  ff_div_pair(sv.hi, sv.lo, static_cast<float>(cnt), q, ql);
   const float scale = ff_sqrt_f32(q, ql);
   const bool ok2 = allvalid ? (scale > 0.0f) : (scale > 0.0f && isfinite(scale));
   r.scale = ok2 ? scale : scale1;
   return r;
 }
 
-template <int NB, int T>
-__global__ void __launch_bounds__(T) integrate_regfast_kernel(IntegrateArgs a) {
+template <int NB, int T, int MODE>
+__global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
   extern __shared__ float smem[];
-  float* S = smem;  // [NB][T] ascending valid samples (percentile lookups)
+  float* S = smem;  // [NB][T] ascending valid samples
   __shared__ FrameTable<NB> tab;
   __shared__ float s_wtot[2];
   load_frame_table<NB>(a, tab);
@@ -541,97 +598,88 @@ __global__ void __launch_bounds__(T) integrate_regfast_kernel(IntegrateArgs a) {
   const int N = a.frames;
   const int64_t P = a.pixels;
   const float ls = a.low_sigma, hs = a.high_sigma;
+  float* St = S + tid;
   for (int64_t p = static_cast<int64_t>(blockIdx.x) * T + tid; p < P; p += static_cast<int64_t>(gridDim.x) * T) {
     float x[NB];
 #pragma unroll
     for (int f = 0; f < NB; ++f) x[f] = (f < N) ? __ldcs(tab.base[f] + p) : kInf;
-    float s[NB];
     int cnt = 0;
-#pragma unroll
-    for (int f = 0; f < NB; ++f) {
-      const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(x[f]);
-      s[f] = ok ? x[f] : kInf;
-      cnt += ok ? 1 : 0;
-    }
     int nl = 0, nh = 0;
     float lt = -kInf, ht = kInf;
     bool thresholds = false;
-    if (a.rejection != GG_REJECT_NONE) {
+    if (MODE != GG_REJECT_NONE) {
+      float s[NB];
+#pragma unroll
+      for (int f = 0; f < NB; ++f) {
+        const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(x[f]);
+        s[f] = ok ? x[f] : kInf;
+        cnt += ok ? 1 : 0;
+      }
       sort_network<NB>(s);
 #pragma unroll
-      for (int f = 0; f < NB; ++f) S[f * T + tid] = s[f];
-      CenterScale cs{0.0f, 0.0f};
-      if (a.rejection == GG_REJECT_WINSORIZED) {
-        cs = winsorized_stats_reg<NB>(s, S + tid, T, cnt, N, allvalid, ls, hs);
-      } else if (a.rejection == GG_REJECT_SIGMA_CLIP && cnt > 0) {
-        // NumPy nanmedian + float32 nanstd in frame order (see sigma_stats).
-        const int h = cnt / 2;
-        const int l = (cnt & 1) ? h : h - 1;
-        cs.center = __fmul_rn(__fadd_rn(S[l * T + tid], S[h * T + tid]), 0.5f);
-        float sum = 0.0f;
-#pragma unroll
-        for (int f = 0; f < NB; ++f)
-          if (f < N && tab.w[f] > 0.0f && isfinite(x[f])) sum = __fadd_rn(sum, x[f]);
-        const float mean = __fdiv_rn(sum, static_cast<float>(cnt));
-        float v = 0.0f;
-#pragma unroll
-        for (int f = 0; f < NB; ++f) {
-          if (f < N && tab.w[f] > 0.0f && isfinite(x[f])) {
-            const float d = __fsub_rn(x[f], mean);
-            v = __fadd_rn(v, __fmul_rn(d, d));
-          }
-        }
-        cs.scale = __fsqrt_rn(__fdiv_rn(v, static_cast<float>(cnt)));
-      }
-      if (a.rejection == GG_REJECT_LINEAR_FIT) {
-        if (cnt > 0) {
-          auto sorted = [&](int i) -> float { return S[i * T + tid]; };
+      for (int f = 0; f < NB; ++f) St[f * T] = s[f];
+      if (cnt > 0) {
+        if (MODE == GG_REJECT_LINEAR_FIT) {
+          auto sorted = [&](int i) -> float { return St[i * T]; };
           int lo = 0, hi = cnt;
           linear_fit_clip(sorted, cnt, ls, hs, a.lfc_iterations, lo, hi);
           nl = lo;
           nh = cnt - hi;
           lt = sorted(lo);
           ht = sorted(hi - 1);
-        }
-      } else {
-        lt = __fsub_rn(cs.center, __fmul_rn(ls, cs.scale));
-        ht = __fadd_rn(cs.center, __fmul_rn(hs, cs.scale));
+        } else {
+          CenterScale cs{0.0f, 0.0f};
+          if (MODE == GG_REJECT_WINSORIZED) {
+            cs = winsorized_sorted(St, T, cnt, N, allvalid, ls, hs);
+          } else {
+            // NumPy nanmedian + float32 nanstd in frame order (sigma_stats).
+            const int h = cnt / 2;
+            const int l = (cnt & 1) ? h : h - 1;
+            cs.center = __fmul_rn(__fadd_rn(St[l * T], St[h * T]), 0.5f);
+            float sum = 0.0f;
 #pragma unroll
-        for (int i = 0; i < NB; ++i) {
-          nl += (i < cnt && s[i] < lt) ? 1 : 0;
-          nh += (i < cnt && s[i] > ht) ? 1 : 0;
+            for (int f = 0; f < NB; ++f)
+              if (f < N && tab.w[f] > 0.0f && isfinite(x[f])) sum = __fadd_rn(sum, x[f]);
+            const float mean = __fdiv_rn(sum, static_cast<float>(cnt));
+            float v = 0.0f;
+#pragma unroll
+            for (int f = 0; f < NB; ++f) {
+              if (f < N && tab.w[f] > 0.0f && isfinite(x[f])) {
+                const float d = __fsub_rn(x[f], mean);
+                v = __fadd_rn(v, __fmul_rn(d, d));
+              }
+            }
+            cs.scale = __fsqrt_rn(__fdiv_rn(v, static_cast<float>(cnt)));
+          }
+          lt = __fsub_rn(cs.center, __fmul_rn(ls, cs.scale));
+          ht = __fadd_rn(cs.center, __fmul_rn(hs, cs.scale));
+          nl = count_below(St, T, cnt, lt, false);
+          nh = cnt - count_below(St, T, cnt, ht, true);
+        }
+        if (nl + nh > 0) {
+          const int rej = nl + nh;
+          const float frac = __fdiv_rn(static_cast<float>(rej), static_cast<float>(cnt));
+          thresholds = (cnt - rej >= a.min_samples) && (frac <= a.max_frac);
+          if (!thresholds) nl = nh = 0;
         }
       }
-      thresholds = true;
-      if (nl + nh > 0) {
-        const int rej = nl + nh;
-        const float frac = __fdiv_rn(static_cast<float>(rej), static_cast<float>(cnt));
-        if (!((cnt - rej >= a.min_samples) && (frac <= a.max_frac))) {
-          nl = nh = 0;
-          thresholds = false;
-        }
-      } else {
-        thresholds = false;
-      }
+    } else {
+#pragma unroll
+      for (int f = 0; f < NB; ++f) cnt += ((f < N) && tab.w[f] > 0.0f && isfinite(x[f])) ? 1 : 0;
     }
     float master = 0.0f, weight = 0.0f;
     int kept = 0;
-    if (unit && a.rejection != GG_REJECT_NONE) {
+    if (MODE != GG_REJECT_NONE && unit) {
       // Kept samples are the contiguous sorted range [nl, cnt - nh).
-      FF w0, w1;
-#pragma unroll
-      for (int i = 0; i < NB; i += 2) {
-        if (i >= nl && i < cnt - nh) w0.add(s[i]);
-        if (i + 1 >= nl && i + 1 < cnt - nh) w1.add(s[i + 1]);
-      }
-      ff_merge2(w0, w1);
       kept = cnt - nl - nh;
       if (kept > 0) {
-        master = ff_div_f32(w0.hi, w0.lo, static_cast<float>(kept));
+        const FF ws = sum_sorted(St, T, nl, cnt - nh, -kInf, kInf);
+        master = ff_div_f32(ws.hi, ws.lo, static_cast<float>(kept));
         weight = static_cast<float>(kept);
       }
     } else if (cnt == N && !thresholds) {
-      // Every frame valid, nothing rejected: sum(w*x) over all frames.
+      // Every frame valid, nothing rejected: sum(w*x) over all frames and the
+      // CTA-wide weight total.
       FF w0, w1;
 #pragma unroll
       for (int f = 0; f < NB; f += 2) {
@@ -648,8 +696,7 @@ __global__ void __launch_bounds__(T) integrate_regfast_kernel(IntegrateArgs a) {
       FF ws, wsum;
 #pragma unroll
       for (int f = 0; f < NB; ++f) {
-        const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(x[f]) &&
-                        !(thresholds && (x[f] < lt || x[f] > ht));
+        const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(x[f]) && !(thresholds && (x[f] < lt || x[f] > ht));
         if (ok) {
           ws.add_prod(x[f], tab.w[f]);
           wsum.add(tab.w[f]);
@@ -796,11 +843,11 @@ static void launch_reg(const IntegrateArgs& args, cudaStream_t stream) {
   check_cuda(cudaGetLastError(), "integrate kernel launch");
 }
 
-template <int NB>
-static void launch_regfast(const IntegrateArgs& args, cudaStream_t stream) {
+template <int NB, int MODE>
+static void launch_col(const IntegrateArgs& args, cudaStream_t stream) {
   constexpr int T = 128;
   const size_t smem = size_t(NB) * T * sizeof(float);
-  auto kern = integrate_regfast_kernel<NB, T>;
+  auto kern = integrate_col_kernel<NB, T, MODE>;
   check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
              "cudaFuncSetAttribute(integrate)");
   int per_sm = 0;
@@ -862,9 +909,29 @@ void launch_integrate(gg_stack* s, const float* d_weights, const gg_integrate_pa
   a.count_u16 = p.count_dtype == GG_COUNT_U16;
   a.geometric = (s->d_warp_coverage && s->warp_coverage_frames > 0) ? s->d_warp_coverage : nullptr;
   const int n = a.frames;
-  if (n <= 8) launch_regfast<8>(a, s->stream);
-  else if (n <= 16) launch_regfast<16>(a, s->stream);
-  else if (n <= 32) launch_regfast<32>(a, s->stream);
+  if (n <= 32) {
+    switch (p.rejection) {
+      case GG_REJECT_NONE:
+        n <= 8 ? launch_col<8, GG_REJECT_NONE>(a, s->stream)
+               : n <= 16 ? launch_col<16, GG_REJECT_NONE>(a, s->stream) : launch_col<32, GG_REJECT_NONE>(a, s->stream);
+        break;
+      case GG_REJECT_SIGMA_CLIP:
+        n <= 8 ? launch_col<8, GG_REJECT_SIGMA_CLIP>(a, s->stream)
+               : n <= 16 ? launch_col<16, GG_REJECT_SIGMA_CLIP>(a, s->stream)
+                         : launch_col<32, GG_REJECT_SIGMA_CLIP>(a, s->stream);
+        break;
+      case GG_REJECT_WINSORIZED:
+        n <= 8 ? launch_col<8, GG_REJECT_WINSORIZED>(a, s->stream)
+               : n <= 16 ? launch_col<16, GG_REJECT_WINSORIZED>(a, s->stream)
+                         : launch_col<32, GG_REJECT_WINSORIZED>(a, s->stream);
+        break;
+      default:
+        n <= 8 ? launch_col<8, GG_REJECT_LINEAR_FIT>(a, s->stream)
+               : n <= 16 ? launch_col<16, GG_REJECT_LINEAR_FIT>(a, s->stream)
+                         : launch_col<32, GG_REJECT_LINEAR_FIT>(a, s->stream);
+        break;
+    }
+  }
   else if (n <= 64) launch_reg<64>(a, s->stream);
   else if (n <= 128) launch_smem<4>(a, s->stream);
   else if (n <= 256) launch_smem<8>(a, s->stream);
