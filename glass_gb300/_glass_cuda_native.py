@@ -153,6 +153,53 @@ def calibrate_tile_f32(light: Any, bias: Any | None, dark: Any | None, flat: Any
     return out
 
 
+def _matrix64(matrix: Any) -> np.ndarray:
+    """The reference takes float32 matrices (np.asarray(m, np.float32)) and
+    inverts them in float64 (native_bindings.cpp:1423-1457)."""
+    m = np.asarray(np.asarray(matrix, dtype=np.float32), dtype=np.float64)
+    if m.shape != (3, 3):
+        raise ValueError(f"warp matrix must be 3x3, got {m.shape}")
+    return np.ascontiguousarray(m)
+
+
+def _warp_image(data: Any, matrix: np.ndarray, interpolation: int, fill: float, clamp: float):
+    image = np.ascontiguousarray(np.asarray(data, dtype=np.float32))
+    if image.ndim != 2:
+        raise ValueError("data must be a 2-D array")
+    h, w = image.shape
+    out = np.empty_like(image)
+    cov = np.empty_like(image)
+    _lib.call("gg_warp_matrix_f32", _lib.ptr(image), ctypes.c_int64(h), ctypes.c_int64(w),
+              _lib.ptr(np.ascontiguousarray(matrix, dtype=np.float64)), int(interpolation), ctypes.c_float(fill),
+              ctypes.c_float(clamp), _lib.ptr(out), _lib.ptr(cov))
+    return out, cov
+
+
+def _translation_matrix(dx: float, dy: float) -> np.ndarray:
+    return np.array([[1.0, 0.0, dx], [0.0, 1.0, dy], [0.0, 0.0, 1.0]], dtype=np.float64)
+
+
+def warp_translation_f32(data: Any, dx: float, dy: float, fill: float = 0.0):
+    """Integer translation (cpu/warp.py:6-22): shifts by round(dx), round(dy)."""
+    return _warp_image(data, _translation_matrix(float(int(round(dx))), float(int(round(dy)))),
+                       _lib.GG_INTERP_NEAREST, fill, -1.0)
+
+
+def warp_translation_bilinear_f32(data: Any, dx: float, dy: float, fill: float = 0.0):
+    """Sub-pixel bilinear translation (glass_cuda.py:564-593)."""
+    return _warp_image(data, _translation_matrix(float(dx), float(dy)), _lib.GG_INTERP_BILINEAR, fill, -1.0)
+
+
+def warp_matrix_bilinear_f32(data: Any, matrix: Any, fill: float = 0.0):
+    """glass_cuda.py:595-629 -> (warped, coverage)."""
+    return _warp_image(data, _matrix64(matrix), _lib.GG_INTERP_BILINEAR, fill, -1.0)
+
+
+def warp_matrix_lanczos3_f32(data: Any, matrix: Any, fill: float = 0.0, clamping_threshold: float = -1.0):
+    """glass_cuda.py:644-706 -> (warped, coverage)."""
+    return _warp_image(data, _matrix64(matrix), _lib.GG_INTERP_LANCZOS3, fill, clamping_threshold)
+
+
 def resident_dq_map_count_maps_i16(master: Any, weight_map: Any, coverage_map: Any | None = None,
                                    low_rejection_map: Any | None = None,
                                    high_rejection_map: Any | None = None,
@@ -378,6 +425,84 @@ class ResidentCalibratedStack:
         return {"schema_version": 1, "h2d_mode": "pinned_lanes", "frames": int(idx.size),
                 "stream_count": int(stream_count), "wave_frames": int(wave_frames), "total_s": total,
                 "host_pinned_bytes": self.host_pinned_bytes}
+
+    # ---- warps (native_bindings.cpp:8900-9924) ------------------------------------
+    @property
+    def tma_enabled(self) -> bool:
+        flag = ctypes.c_int()
+        _lib.call("gg_stack_tma_enabled", self._handle, ctypes.byref(flag))
+        return bool(flag.value)
+
+    def warp_frames_async(self, indices: Any, matrices: Any, interpolation: int, fill: float = np.nan,
+                          clamping_threshold: float = -1.0, track_coverage: bool = False) -> None:
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+        mats = np.asarray(matrices)
+        if mats.dtype != np.float64:
+            mats = np.asarray(np.asarray(mats, dtype=np.float32), dtype=np.float64)
+        mats = np.ascontiguousarray(mats.reshape(-1, 3, 3))
+        if mats.shape[0] != idx.size:
+            raise ValueError("matrices must have shape (len(indices), 3, 3)")
+        if idx.size == 0:
+            return
+        _lib.call("gg_stack_warp_frames", self._handle, _lib.ptr(idx), ctypes.c_int64(idx.size), _lib.ptr(mats),
+                  int(interpolation), ctypes.c_float(fill), ctypes.c_float(clamping_threshold),
+                  int(bool(track_coverage)))
+
+    def _warp_timed(self, indices, matrices, interpolation, fill, clamp, track_coverage, name) -> dict[str, Any]:
+        start = perf_counter()
+        self.warp_frames_async(indices, matrices, interpolation, fill, clamp, track_coverage)
+        enqueue = perf_counter()
+        self.synchronize()
+        done = perf_counter()
+        n = int(np.asarray(indices).size)
+        return {"schema_version": 1, "method": name, "frames": n, "dispatch": "slot_swap_batches",
+                "interpolation": {0: "nearest", 1: "bilinear", 3: "lanczos3"}[interpolation],
+                "track_coverage": bool(track_coverage), "tma_staged": self.tma_enabled,
+                "enqueue_s": enqueue - start, "sync_s": done - enqueue, "total_s": done - start}
+
+    def apply_translation_frame(self, index: int, dx: int, dy: int, fill: float = np.nan) -> None:
+        self.warp_frames_async([index], _translation_matrix(float(int(dx)), float(int(dy)))[None],
+                               _lib.GG_INTERP_NEAREST, fill)
+        self.synchronize()
+
+    def apply_translation_bilinear_frame(self, index: int, dx: float, dy: float, fill: float = np.nan) -> None:
+        self.warp_frames_async([index], _translation_matrix(float(dx), float(dy))[None], _lib.GG_INTERP_BILINEAR,
+                               fill)
+        self.synchronize()
+
+    def apply_matrix_bilinear_frame(self, index: int, matrix: Any, fill: float = np.nan) -> None:
+        self.warp_frames_async([index], _matrix64(matrix)[None], _lib.GG_INTERP_BILINEAR, fill)
+        self.synchronize()
+
+    def apply_matrix_lanczos3_frame(self, index: int, matrix: Any, fill: float = np.nan,
+                                    clamping_threshold: float = -1.0) -> None:
+        self.warp_frames_async([index], _matrix64(matrix)[None], _lib.GG_INTERP_LANCZOS3, fill, clamping_threshold)
+        self.synchronize()
+
+    def apply_matrix_bilinear_frames(self, indices: Any, matrices: Any, fill: float = np.nan, *rest) -> dict:
+        """(indices, matrices, fill, track_coverage) or (..., max_chunk_capacity_frames, track_coverage)."""
+        track = bool(rest[-1]) if rest else True
+        return self._warp_timed(indices, matrices, _lib.GG_INTERP_BILINEAR, fill, -1.0, track,
+                                "apply_matrix_bilinear_frames")
+
+    def apply_matrix_lanczos3_frames(self, indices: Any, matrices: Any, fill: float = np.nan,
+                                     clamping_threshold: float = -1.0, *rest) -> dict:
+        """(..., clamping_threshold, track_coverage) or (..., max_chunk_capacity_frames, track_coverage)."""
+        track = bool(rest[-1]) if rest else True
+        return self._warp_timed(indices, matrices, _lib.GG_INTERP_LANCZOS3, fill, clamping_threshold, track,
+                                "apply_matrix_lanczos3_frames")
+
+    def reset_warp_coverage(self) -> None:
+        _lib.call("gg_stack_reset_warp_coverage", self._handle)
+
+    def accumulate_full_warp_coverage_frame(self) -> None:
+        _lib.call("gg_stack_accumulate_full_warp_coverage_frame", self._handle)
+
+    def warp_coverage_map(self) -> np.ndarray:
+        info = self._info()
+        out = np.empty((info.height, info.width), np.float32)
+        _lib.call("gg_stack_download_warp_coverage", self._handle, _lib.ptr(out))
+        return out
 
     # ---- statistics ------------------------------------------------------------
     def frame_global_stats(self, index: int) -> dict[str, Any]:

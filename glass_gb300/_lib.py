@@ -33,6 +33,7 @@ GG_REJECT_LINEAR_FIT = 3
 GG_COUNT_F32 = 0
 GG_COUNT_U16 = 1
 
+GG_INTERP_NEAREST = 0
 GG_INTERP_BILINEAR = 1
 GG_INTERP_LANCZOS3 = 3
 
@@ -151,6 +152,13 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_download_maps": [_P, _P, _P, _P, _P, _P, _P],
     "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
     "gg_dq_map_i16": [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P],
+    "gg_stack_warp_frames": [_P, _P, ctypes.c_int64, _P, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int],
+    "gg_stack_reset_warp_coverage": [_P],
+    "gg_stack_accumulate_full_warp_coverage_frame": [_P],
+    "gg_stack_download_warp_coverage": [_P, _P],
+    "gg_stack_tma_enabled": [_P, ctypes.POINTER(ctypes.c_int)],
+    "gg_warp_matrix_f32": [_P, ctypes.c_int64, ctypes.c_int64, _P, ctypes.c_int, ctypes.c_float, ctypes.c_float, _P,
+                           _P],
 }
 
 _LIB: ctypes.CDLL | None = None

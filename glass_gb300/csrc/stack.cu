@@ -104,6 +104,18 @@ void stack_ensure_maps(gg_stack* s) {
   s->d_dq = static_cast<int16_t*>(device_alloc(s, p * 2, "dq map"));
 }
 
+void stack_check_device_error(gg_stack* s) {
+  int err = 0;
+  check_cuda(cudaMemcpyAsync(&err, s->d_error, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+             "cudaMemcpyAsync(device error)");
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(device error)");
+  if (err != 0) {
+    check_cuda(cudaMemsetAsync(s->d_error, 0, sizeof(int), s->stream), "cudaMemsetAsync(device error)");
+    check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(device error)");
+    fail(GG_ERR_TIMEOUT, "a device-side wait ran out of its iteration limit (result of the last batch is invalid)");
+  }
+}
+
 void stack_ensure_partials(gg_stack* s, size_t doubles) {
   if (s->partial_capacity >= doubles) return;
   check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(partials)");
@@ -132,12 +144,13 @@ static void stack_free(gg_stack* s) {
                       s->d_bias,     s->d_dark,          s->d_flat,       s->d_master,
                       s->d_weight,   s->d_coverage,      s->d_low,        s->d_high,
                       s->d_dq,       s->d_warp_coverage, s->d_weights,    s->d_partials,
-                      s->d_raw_lane[0], s->d_raw_lane[1]};
+                      s->d_raw_lane[0], s->d_raw_lane[1], s->d_warp_items, s->d_error};
   for (void* p : dev_ptrs) {
     if (p) cudaFree(p);
   }
+  if (s->warp_items_free) cudaEventDestroy(s->warp_items_free);
   void* host_ptrs[] = {s->h_pinned_lane[0], s->h_pinned_lane[1], s->h_weights_pinned, s->h_partials_pinned,
-                       s->h_slot_table_pinned};
+                       s->h_slot_table_pinned, s->h_warp_items};
   for (void* p : host_ptrs) {
     if (p) cudaFreeHost(p);
   }
@@ -289,6 +302,10 @@ int gg_stack_create(int64_t frame_count, int64_t height, int64_t width, gg_stack
     s->d_weights = static_cast<float*>(device_alloc(s, sizeof(float) * frame_count, "weights"));
     s->h_weights_pinned = static_cast<float*>(pinned_alloc(s, sizeof(float) * frame_count, "cudaHostAlloc(weights)"));
     s->h_slot_table_pinned = static_cast<int*>(pinned_alloc(s, sizeof(int) * frame_count, "cudaHostAlloc(slots)"));
+    s->d_error = static_cast<int*>(device_alloc(s, sizeof(int), "device error word"));
+    check_cuda(cudaMemsetAsync(s->d_error, 0, sizeof(int), s->stream), "cudaMemsetAsync(error)");
+    check_cuda(cudaEventCreateWithFlags(&s->warp_items_free, cudaEventDisableTiming), "cudaEventCreate");
+    s->has_slot_tmap = (s->width % 4 == 0) && make_slot_tensor_map(s, 80, 32);
 
     check_cuda(cudaMemsetAsync(s->d_slots, 0, slot_bytes, s->stream), "cudaMemsetAsync(stack)");
     check_cuda(cudaMemsetAsync(s->d_frame_nonfinite, 0, sizeof(unsigned) * frame_count, s->stream),
@@ -358,6 +375,7 @@ int gg_stack_synchronize(gg_stack* s) {
   require(s != nullptr, "stack is null");
   stack_activate(s);
   check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+  stack_check_device_error(s);
   GG_API_END
 }
 

@@ -13,6 +13,8 @@
 // and the host reads it back only for downloads.
 #pragma once
 
+#include <cuda.h>
+
 #include <vector>
 
 #include "common.cuh"
@@ -78,6 +80,18 @@ struct gg_stack {
   size_t partial_capacity = 0;         // doubles
   int* h_slot_table_pinned = nullptr;  // [frames]
 
+  // Warp batches: per-item descriptors (device + pinned staging) and the TMA
+  // descriptor of the slot pool viewed as a [slot][H][W] float32 tensor.
+  void* d_warp_items = nullptr;
+  void* h_warp_items = nullptr;
+  int64_t warp_item_capacity = 0;
+  cudaEvent_t warp_items_free = nullptr;
+  CUtensorMap slot_tmap{};
+  bool has_slot_tmap = false;
+
+  // Device error word set by kernels whose bounded waits run out.
+  int* d_error = nullptr;
+
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaStream_t copy_stream = nullptr;
@@ -98,6 +112,11 @@ void stack_mark_loaded(gg_stack* s, int64_t index);
 void stack_read_slots(gg_stack* s, std::vector<int>& out);
 void stack_ensure_maps(gg_stack* s);
 void stack_ensure_partials(gg_stack* s, size_t doubles);
+// Raises GG_ERR_TIMEOUT if a kernel reported a bounded wait running out
+// (synchronises the stream), then clears the flag.
+void stack_check_device_error(gg_stack* s);
+// Encodes a TMA tensor map over the slot pool ([slot][H][W] float32).
+bool make_slot_tensor_map(gg_stack* s, int box_w, int box_h);
 
 // Kernel launchers (defined in the per-kernel translation units).
 struct CalibLaunch {

@@ -1,0 +1,717 @@
+// Matrix warps of resident frames: bilinear and Lanczos3, TMA-staged.
+//
+// Semantics (CPU oracle): output pixel (x, y) samples the source at
+// M^-1 (x, y, 1) (float64 in the reference: engine/warp.py:155-227,
+// tests/test_gpu_warp_vs_cpu.py:34-128; reference kernels
+// warp_kernels.cu:206-777).
+//   bilinear: valid iff 0 <= sx <= W-1 and 0 <= sy <= H-1; x1 = min(x0+1, W-1);
+//             tx = float32(sx - x0); top/bottom/result in float32 arithmetic.
+//   lanczos3: valid iff 2 <= sx < W-3 and 2 <= sy < H-3; 6x6 taps from
+//             (x0-2, y0-2); w = sinc(d) sinc(d/3); non-finite taps are skipped
+//             and the sum is renormalised; |sum w| <= 1e-12 -> invalid; an
+//             optional clamp to [min - c*range, max + c*range] of the taps.
+//   invalid pixels get `fill` and coverage 0.
+//
+// GB300 design
+//   - source coordinates are evaluated in float-float (TwoProd/TwoSum) from
+//     the float64 inverse, so floor/validity decisions agree with the float64
+//     reference without float64 arithmetic on the device;
+//   - each CTA owns a 64x16 output tile; its source footprint (an 80x32 box
+//     for the small rotations registration produces) is copied to shared
+//     memory by one cp.async.bulk.tensor (TMA) load, double-buffered against
+//     the previous tile's compute.  Footprints that do not fit the box (large
+//     rotation/scale) and image widths that TMA cannot describe (W % 4 != 0)
+//     read the taps straight from global memory instead;
+//   - output goes to a spare slot; a follow-up kernel swaps the frame->slot
+//     table, so nothing is copied back (8 B/pixel instead of 16 B);
+//   - Lanczos weights use sin(pi d) = (-1)^k sin(pi t) and the angle-sum form
+//     of sin(pi d / 3), i.e. one sinpif and one sincospif per axis.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include <cudaTypedefs.h>
+
+#include "stack.cuh"
+
+namespace gg {
+
+constexpr float kInfF = __builtin_huge_valf();
+constexpr int kTileW = 64;
+constexpr int kTileH = 16;
+constexpr int kBoxW = 80;
+constexpr int kBoxH = 32;
+constexpr int kWarpThreads = 256;  // 64 x 4; each thread covers 4 rows
+
+struct WarpItem {
+  int frame;
+  int src_slot;     // filled on the device
+  int dst_slot;     // filled on the device
+  unsigned src_nonfinite;
+  int affine;
+  int pad[3];
+  float m[9][2];  // inverse matrix, float-float (hi, lo), row-major
+};
+
+struct WarpArgs {
+  float* slots;
+  int* slot_of_frame;
+  int* spare_slot;
+  unsigned* nonfinite;
+  WarpItem* items;
+  int item_count;
+  int64_t stride;
+  int width;
+  int height;
+  int tiles_x;
+  int tiles_y;
+  int interp;
+  float fill;
+  float clamp;
+  float* coverage;  // optional accumulator (+1 per covered pixel)
+  int* error;
+};
+
+// ---- PTX helpers -------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: gives up after `limit` polls (each poll may suspend briefly).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, int limit) {
+  for (int i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// ---- float-float coordinates ---------------------------------------------------
+struct FFv {
+  float hi, lo;
+};
+
+// a*x + b*y + c with (hi, lo) coefficients; x, y exact small integers.
+__device__ __forceinline__ FFv ff_lin(const float (*r)[2], float x, float y) {
+  const float p1 = __fmul_rn(r[0][0], x);
+  const float e1 = __fmaf_rn(r[0][0], x, -p1);
+  const float p2 = __fmul_rn(r[1][0], y);
+  const float e2 = __fmaf_rn(r[1][0], y, -p2);
+  float s, t, s2, t2;
+  two_sum(p1, p2, s, t);
+  two_sum(s, r[2][0], s2, t2);
+  float lo = __fadd_rn(t, t2);
+  lo = __fadd_rn(lo, __fadd_rn(e1, e2));
+  lo = __fmaf_rn(r[0][1], x, lo);
+  lo = __fmaf_rn(r[1][1], y, lo);
+  lo = __fadd_rn(lo, r[2][1]);
+  const float h = __fadd_rn(s2, lo);
+  return {h, __fsub_rn(lo, __fsub_rn(h, s2))};
+}
+
+__device__ __forceinline__ FFv ff_div(FFv n, FFv d) {
+  const float q = __fdiv_rn(n.hi, d.hi);
+  float r = __fmaf_rn(-q, d.hi, n.hi);
+  r = __fadd_rn(r, n.lo);
+  r = __fmaf_rn(-q, d.lo, r);
+  const float ql = __fdiv_rn(r, d.hi);
+  const float h = __fadd_rn(q, ql);
+  return {h, __fsub_rn(ql, __fsub_rn(h, q))};
+}
+
+__device__ __forceinline__ bool ff_ge(FFv v, float b) { return v.hi > b || (v.hi == b && v.lo >= 0.0f); }
+__device__ __forceinline__ bool ff_le(FFv v, float b) { return v.hi < b || (v.hi == b && v.lo <= 0.0f); }
+__device__ __forceinline__ bool ff_lt(FFv v, float b) { return v.hi < b || (v.hi == b && v.lo < 0.0f); }
+
+// floor and float32(v - floor(v)) of a float-float value.
+__device__ __forceinline__ void ff_floor_frac(FFv v, int& i, float& frac) {
+  float f = floorf(v.hi);
+  if (v.hi == f && v.lo < 0.0f) f -= 1.0f;
+  i = static_cast<int>(f);
+  frac = __fadd_rn(__fsub_rn(v.hi, f), v.lo);
+}
+
+// Source coordinate of output pixel (x, y); returns false when the
+// projective denominator vanishes (|w| <= 1e-12, engine/warp.py:178-191).
+__device__ __forceinline__ bool source_coord(const WarpItem& it, float x, float y, FFv& sx, FFv& sy) {
+  const float (*m)[2] = it.m;
+  const float rx[3][2] = {{m[0][0], m[0][1]}, {m[1][0], m[1][1]}, {m[2][0], m[2][1]}};
+  const float ry[3][2] = {{m[3][0], m[3][1]}, {m[4][0], m[4][1]}, {m[5][0], m[5][1]}};
+  sx = ff_lin(rx, x, y);
+  sy = ff_lin(ry, x, y);
+  if (it.affine) return true;
+  const float rw[3][2] = {{m[6][0], m[6][1]}, {m[7][0], m[7][1]}, {m[8][0], m[8][1]}};
+  const FFv w = ff_lin(rw, x, y);
+  if (!(fabsf(w.hi) > 1.0e-12f)) return false;
+  sx = ff_div(sx, w);
+  sy = ff_div(sy, w);
+  return true;
+}
+
+// Lanczos3 weights of taps k = -2..3 at fractional offset t (d = t - k).
+__device__ __forceinline__ void lanczos3_weights(float t, float (&w)[6]) {
+  const float s = sinpif(t);
+  float s3, c3;
+  sincospif(__fdiv_rn(t, 3.0f), &s3, &c3);
+  const float ck[6] = {-0.5f, 0.5f, 1.0f, 0.5f, -0.5f, -1.0f};
+  const float sk[6] = {-0.86602540378443865f, -0.86602540378443865f, 0.0f, 0.86602540378443865f,
+                       0.86602540378443865f, 0.0f};
+  constexpr float k3_over_pi2 = 0.30396355092701331f;  // 3 / pi^2
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const float k = static_cast<float>(j - 2);
+    const float d = __fsub_rn(t, k);
+    if (fabsf(d) < 1.0e-6f) {
+      w[j] = 1.0f;
+    } else if (fabsf(d) >= 3.0f) {
+      w[j] = 0.0f;
+    } else {
+      const float s1 = ((j - 2) & 1) ? -s : s;           // sin(pi d)
+      const float s3d = __fmaf_rn(s3, ck[j], -c3 * sk[j]);  // sin(pi d / 3)
+      w[j] = k3_over_pi2 * s1 * s3d / (d * d);
+    }
+  }
+}
+
+// Tap reader: shared-memory tile (origin bx, by) or global frame.
+struct TapSource {
+  const float* tile;  // nullptr -> global
+  const float* src;
+  int bx, by, width;
+  __device__ __forceinline__ float at(int x, int y) const {
+    return tile ? tile[(y - by) * kBoxW + (x - bx)] : __ldg(src + static_cast<int64_t>(y) * width + x);
+  }
+};
+
+__device__ __forceinline__ float sample_bilinear(const TapSource& ts, int x0, int y0, float tx, float ty, int W,
+                                                 int H) {
+  const int x1 = min(x0 + 1, W - 1);
+  const int y1 = min(y0 + 1, H - 1);
+  const float v00 = ts.at(x0, y0), v01 = ts.at(x1, y0), v10 = ts.at(x0, y1), v11 = ts.at(x1, y1);
+  const float ox = __fsub_rn(1.0f, tx), oy = __fsub_rn(1.0f, ty);
+  const float top = __fadd_rn(__fmul_rn(v00, ox), __fmul_rn(v01, tx));
+  const float bottom = __fadd_rn(__fmul_rn(v10, ox), __fmul_rn(v11, tx));
+  return __fadd_rn(__fmul_rn(top, oy), __fmul_rn(bottom, ty));
+}
+
+// Returns false when the tap weights sum to (almost) zero.
+__device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int y0, float tx, float ty,
+                                                bool all_finite, float clamp, float& out) {
+  float wx[6], wy[6];
+  lanczos3_weights(tx, wx);
+  lanczos3_weights(ty, wy);
+  float acc = 0.0f, wsum = 0.0f;
+  float vmin = kInfF, vmax = -kInfF;
+  if (all_finite) {
+    float sx = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) sx += wx[i];
+    float sy = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      float row = 0.0f;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        const float v = ts.at(x0 - 2 + i, y0 - 2 + j);
+        row = __fmaf_rn(wx[i], v, row);
+        if (clamp >= 0.0f) {
+          vmin = fminf(vmin, v);
+          vmax = fmaxf(vmax, v);
+        }
+      }
+      acc = __fmaf_rn(wy[j], row, acc);
+      sy += wy[j];
+    }
+    wsum = sx * sy;
+  } else {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        const float v = ts.at(x0 - 2 + i, y0 - 2 + j);
+        if (isfinite(v)) {
+          const float w = wy[j] * wx[i];
+          acc = __fmaf_rn(w, v, acc);
+          wsum += w;
+          vmin = fminf(vmin, v);
+          vmax = fmaxf(vmax, v);
+        }
+      }
+    }
+  }
+  if (!(fabsf(wsum) > 1.0e-12f)) return false;
+  float value = acc / wsum;
+  if (clamp >= 0.0f && vmin <= vmax) {
+    const float range = vmax - vmin;
+    value = fminf(vmax + clamp * range, fmaxf(vmin - clamp * range, value));
+  }
+  out = value;
+  return true;
+}
+
+// Tile plan: box origin for the source footprint of output tile (tx, ty).
+struct TilePlan {
+  int bx, by, fits;
+};
+
+__device__ __forceinline__ TilePlan plan_tile(const WarpItem& it, int tile_x, int tile_y, int radius) {
+  const float x0 = static_cast<float>(tile_x * kTileW), y0 = static_cast<float>(tile_y * kTileH);
+  const float cx[4] = {x0, x0 + kTileW - 1, x0, x0 + kTileW - 1};
+  const float cy[4] = {y0, y0, y0 + kTileH - 1, y0 + kTileH - 1};
+  float minx = kInfF, maxx = -kInfF, miny = kInfF, maxy = -kInfF;
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    FFv sx, sy;
+    ok &= source_coord(it, cx[c], cy[c], sx, sy);
+    minx = fminf(minx, sx.hi);
+    maxx = fmaxf(maxx, sx.hi);
+    miny = fminf(miny, sy.hi);
+    maxy = fmaxf(maxy, sy.hi);
+  }
+  TilePlan p{0, 0, 0};
+  if (!ok || !(maxx - minx < 1.0e6f) || !(maxy - miny < 1.0e6f) || fabsf(minx) > 1.0e8f || fabsf(miny) > 1.0e8f)
+    return p;
+  // taps span [floor(s) - (radius-1), floor(s) + radius]; one pixel of margin.
+  const int lo_x = static_cast<int>(floorf(minx)) - radius;
+  const int hi_x = static_cast<int>(floorf(maxx)) + radius + 1;  // inclusive
+  const int lo_y = static_cast<int>(floorf(miny)) - radius;
+  const int hi_y = static_cast<int>(floorf(maxy)) + radius + 1;
+  p.bx = lo_x >= 0 ? (lo_x & ~3) : -((-lo_x + 3) & ~3);  // 16-byte aligned x (TMA rule)
+  p.by = lo_y;
+  p.fits = (hi_x - p.bx < kBoxW) && (hi_y - p.by < kBoxH);
+  return p;
+}
+
+template <int INTERP, bool USE_TMA>
+__global__ void __launch_bounds__(kWarpThreads) warp_tiles_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                                  WarpArgs a) {
+  __shared__ alignas(128) float tile[2][kBoxH * kBoxW];
+  __shared__ alignas(8) uint64_t bar[2];
+  __shared__ int s_bx[2], s_by[2], s_fit[2];
+  __shared__ int s_abort;
+  constexpr int radius = (INTERP == GG_INTERP_LANCZOS3) ? 3 : 1;
+  const int tid = threadIdx.x;
+  const int lx = tid & 63, ly = tid >> 6;
+  const int tiles = a.tiles_x * a.tiles_y;
+  const int items = a.item_count * tiles;
+  if (tid == 0) {
+    s_abort = 0;
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  auto issue = [&](int item, int buf) {
+    // thread 0 only
+    const WarpItem& it = a.items[item / tiles];
+    const int t = item % tiles;
+    TilePlan p = plan_tile(it, t % a.tiles_x, t / a.tiles_x, radius);
+    if (!USE_TMA) p.fits = 0;
+    s_bx[buf] = p.bx;
+    s_by[buf] = p.by;
+    s_fit[buf] = p.fits;
+    if (p.fits) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&bar[buf], kBoxW * kBoxH * 4);
+      tma_load_3d(tile[buf], &tmap, p.bx, p.by, it.src_slot, &bar[buf]);
+    }
+  };
+
+  unsigned phase[2] = {0u, 0u};
+  int item = blockIdx.x;
+  if (tid == 0 && item < items) issue(item, 0);
+  __syncthreads();
+  for (int i = 0; item < items; ++i, item += gridDim.x) {
+    const int buf = i & 1;
+    const int next = item + gridDim.x;
+    if (tid == 0 && next < items) issue(next, buf ^ 1);
+    const WarpItem& it = a.items[item / tiles];
+    const int t = item % tiles;
+    const int tile_x = t % a.tiles_x, tile_y = t / a.tiles_x;
+    const bool fit = s_fit[buf] != 0;
+    if (fit) {
+      // Bounded wait: on expiry flag the error, give the copy one more
+      // bounded wait to land, finish this item (its output is discarded by
+      // the host) and leave the loop with the whole CTA.
+      if (!mbar_wait_bounded(&bar[buf], phase[buf], 1 << 24)) {
+        atomicExch(a.error, 1);
+        s_abort = 1;
+        mbar_wait_bounded(&bar[buf], phase[buf], 1 << 24);
+      }
+      phase[buf] ^= 1u;
+    }
+    {
+      TapSource ts;
+      ts.tile = fit ? tile[buf] : nullptr;
+      ts.src = a.slots + static_cast<int64_t>(it.src_slot) * a.stride;
+      ts.bx = s_bx[buf];
+      ts.by = s_by[buf];
+      ts.width = a.width;
+      float* dst = a.slots + static_cast<int64_t>(it.dst_slot) * a.stride;
+      const int ox = tile_x * kTileW + lx;
+      const bool all_finite = it.src_nonfinite == 0u;
+      unsigned bad = 0;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int oy = tile_y * kTileH + ly + 4 * r;
+        const bool inside = ox < a.width && oy < a.height;
+        bool valid = false;
+        float value = a.fill;
+        if (inside) {
+          FFv sx, sy;
+          if (source_coord(it, static_cast<float>(ox), static_cast<float>(oy), sx, sy)) {
+            const float W = static_cast<float>(a.width), H = static_cast<float>(a.height);
+            if (INTERP != GG_INTERP_LANCZOS3)
+              valid = ff_ge(sx, 0.0f) && ff_le(sx, W - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, H - 1.0f);
+            else
+              valid = ff_ge(sx, 2.0f) && ff_lt(sx, W - 3.0f) && ff_ge(sy, 2.0f) && ff_lt(sy, H - 3.0f);
+            if (valid) {
+              int x0, y0;
+              float tx, ty;
+              ff_floor_frac(sx, x0, tx);
+              ff_floor_frac(sy, y0, ty);
+              if (INTERP == GG_INTERP_NEAREST) {
+                // np.rint: round half to even (engine/warp.py:87-96).
+                if (tx > 0.5f || (tx == 0.5f && (x0 & 1))) ++x0;
+                if (ty > 0.5f || (ty == 0.5f && (y0 & 1))) ++y0;
+              }
+              TapSource src = ts;
+              // Any tap outside the staged box reads global memory instead.
+              if (src.tile && (x0 - (radius - 1) < src.bx || x0 + radius >= src.bx + kBoxW ||
+                               y0 - (radius - 1) < src.by || y0 + radius >= src.by + kBoxH))
+                src.tile = nullptr;
+              if (INTERP == GG_INTERP_NEAREST) {
+                value = src.at(x0, y0);
+              } else if (INTERP == GG_INTERP_BILINEAR) {
+                value = sample_bilinear(src, x0, y0, tx, ty, a.width, a.height);
+              } else {
+                valid = sample_lanczos3(src, x0, y0, tx, ty, all_finite, a.clamp, value);
+                if (!valid) value = a.fill;
+              }
+            }
+          }
+          dst[static_cast<int64_t>(oy) * a.width + ox] = value;
+          if (a.coverage && valid) atomicAdd(a.coverage + static_cast<int64_t>(oy) * a.width + ox, 1.0f);
+          bad += isfinite(value) ? 0u : 1u;
+        }
+      }
+      const unsigned warp_bad = __reduce_add_sync(0xffffffffu, bad);
+      if ((tid & 31) == 0 && warp_bad) atomicAdd(a.nonfinite + it.frame, warp_bad);
+    }
+    __syncthreads();
+    if (s_abort) {
+      // Let the prefetch already issued for the next item land before exit.
+      if (next < items && s_fit[buf ^ 1]) mbar_wait_bounded(&bar[buf ^ 1], phase[buf ^ 1], 1 << 24);
+      break;
+    }
+  }
+}
+
+// Resolve slots for the batch and move the source non-finite counts aside.
+__global__ void warp_prepare_kernel(WarpItem* items, int count, const int* slot_of_frame, const int* spare,
+                                    unsigned* nonfinite) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const int f = items[k].frame;
+  items[k].src_slot = slot_of_frame[f];
+  items[k].dst_slot = spare[k];
+  items[k].src_nonfinite = nonfinite[f];
+  nonfinite[f] = 0u;
+}
+
+// The warped frame now lives in the spare slot; the old slot becomes spare.
+__global__ void warp_finish_kernel(const WarpItem* items, int count, int* slot_of_frame, int* spare) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  slot_of_frame[items[k].frame] = items[k].dst_slot;
+  spare[k] = items[k].src_slot;
+}
+
+__global__ void fill_kernel(float* p, int64_t n, float v) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    p[i] = v;
+}
+
+__global__ void add_scalar_kernel(float* p, int64_t n, float v) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    p[i] += v;
+}
+
+// ---- host side -------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+bool make_slot_tensor_map(gg_stack* s, int box_w, int box_h) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  if ((s->width * 4) % 16 != 0 || (s->stride * 4) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {static_cast<cuuint64_t>(s->width), static_cast<cuuint64_t>(s->height),
+                              static_cast<cuuint64_t>(s->slots)};
+  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(s->width) * 4, static_cast<cuuint64_t>(s->stride) * 4};
+  const cuuint32_t box[3] = {static_cast<cuuint32_t>(box_w), static_cast<cuuint32_t>(box_h), 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  std::memset(&s->slot_tmap, 0, sizeof(s->slot_tmap));
+  const CUresult r = fn(&s->slot_tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, s->d_slots, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// float64 3x3 inverse (np.linalg.inv of the float32 matrix promoted to float64).
+static bool invert3(const double* m, double* inv) {
+  const double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5], g = m[6], h = m[7], i = m[8];
+  const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+  const double det = a * A + b * B + c * C;
+  if (!(std::fabs(det) > 0.0) || !std::isfinite(det)) return false;
+  const double r = 1.0 / det;
+  inv[0] = A * r;
+  inv[1] = -(b * i - c * h) * r;
+  inv[2] = (b * f - c * e) * r;
+  inv[3] = B * r;
+  inv[4] = (a * i - c * g) * r;
+  inv[5] = -(a * f - c * d) * r;
+  inv[6] = C * r;
+  inv[7] = -(a * h - b * g) * r;
+  inv[8] = (a * e - b * d) * r;
+  for (int k = 0; k < 9; ++k)
+    if (!std::isfinite(inv[k])) return false;
+  return true;
+}
+
+static void ensure_warp_items(gg_stack* s, int64_t count) {
+  if (s->warp_item_capacity >= count) return;
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(warp items)");
+  if (s->d_warp_items) cudaFree(s->d_warp_items);
+  if (s->h_warp_items) cudaFreeHost(s->h_warp_items);
+  s->d_warp_items = nullptr;
+  s->h_warp_items = nullptr;
+  const size_t bytes = sizeof(WarpItem) * static_cast<size_t>(count);
+  check_cuda(cudaMalloc(&s->d_warp_items, bytes), "cudaMalloc(warp items)");
+  check_cuda(cudaHostAlloc(&s->h_warp_items, bytes, cudaHostAllocPortable), "cudaHostAlloc(warp items)");
+  s->warp_item_capacity = count;
+}
+
+static void ensure_warp_coverage(gg_stack* s) {
+  if (s->d_warp_coverage) return;
+  check_cuda(cudaMalloc(reinterpret_cast<void**>(&s->d_warp_coverage), sizeof(float) * s->pixels),
+             "cudaMalloc(warp coverage)");
+  s->bytes_allocated += static_cast<int64_t>(sizeof(float) * s->pixels);
+  check_cuda(cudaMemsetAsync(s->d_warp_coverage, 0, sizeof(float) * s->pixels, s->stream), "cudaMemsetAsync");
+}
+
+template <int INTERP>
+static void launch_warp_tiles(gg_stack* s, const WarpArgs& args, bool use_tma) {
+  int per_sm = 0;
+  auto kern = use_tma ? warp_tiles_kernel<INTERP, true> : warp_tiles_kernel<INTERP, false>;
+  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpThreads, 0), "occupancy(warp)");
+  const int64_t items = static_cast<int64_t>(args.item_count) * args.tiles_x * args.tiles_y;
+  const unsigned grid =
+      static_cast<unsigned>(std::min<int64_t>(items, static_cast<int64_t>(sm_count()) * std::max(per_sm, 1)));
+  note_launch();
+  kern<<<grid, kWarpThreads, 0, s->stream>>>(s->slot_tmap, args);
+  check_cuda(cudaGetLastError(), "warp kernel launch");
+}
+
+void warp_frames(gg_stack* s, const int64_t* indices, int64_t count, const double* fwd, int interp, float fill,
+                 float clamp, bool track_coverage) {
+  std::vector<WarpItem> items(static_cast<size_t>(count));
+  for (int64_t k = 0; k < count; ++k) {
+    stack_require_loaded(s, indices[k], "warp");
+    for (int64_t j = 0; j < k; ++j)
+      if (indices[j] == indices[k]) fail(GG_ERR_INVALID_ARGUMENT, "frame indices of a warp batch must be unique");
+    double inv[9];
+    const double* m = fwd + 9 * k;
+    for (int q = 0; q < 9; ++q)
+      if (!std::isfinite(m[q])) fail(GG_ERR_INVALID_ARGUMENT, "warp matrix must be finite");
+    if (!invert3(m, inv)) fail(GG_ERR_INVALID_ARGUMENT, "warp matrix is singular");
+    WarpItem& it = items[static_cast<size_t>(k)];
+    std::memset(&it, 0, sizeof(it));
+    it.frame = static_cast<int>(indices[k]);
+    it.affine = (inv[6] == 0.0 && inv[7] == 0.0 && inv[8] == 1.0) ? 1 : 0;
+    for (int q = 0; q < 9; ++q) {
+      const float hi = static_cast<float>(inv[q]);
+      it.m[q][0] = hi;
+      it.m[q][1] = static_cast<float>(inv[q] - static_cast<double>(hi));
+    }
+  }
+  ensure_warp_items(s, std::max<int64_t>(count, s->spares));
+  if (track_coverage) ensure_warp_coverage(s);
+  // The staging buffer may still feed the previous call's copy.
+  check_cuda(cudaEventSynchronize(s->warp_items_free), "cudaEventSynchronize(warp items)");
+  std::memcpy(s->h_warp_items, items.data(), sizeof(WarpItem) * items.size());
+  check_cuda(cudaMemcpyAsync(s->d_warp_items, s->h_warp_items, sizeof(WarpItem) * items.size(),
+                             cudaMemcpyHostToDevice, s->stream),
+             "cudaMemcpyAsync(warp items)");
+  check_cuda(cudaEventRecord(s->warp_items_free, s->stream), "cudaEventRecord(warp items)");
+  auto* d_items = static_cast<WarpItem*>(s->d_warp_items);
+  const bool use_tma = s->has_slot_tmap;
+  for (int64_t k0 = 0; k0 < count; k0 += s->spares) {
+    const int nb = static_cast<int>(std::min<int64_t>(s->spares, count - k0));
+    note_launch();
+    warp_prepare_kernel<<<(nb + 127) / 128, 128, 0, s->stream>>>(d_items + k0, nb, s->d_slot_of_frame,
+                                                                 s->d_spare_slot, s->d_frame_nonfinite);
+    check_cuda(cudaGetLastError(), "warp_prepare launch");
+    WarpArgs a{};
+    a.slots = s->d_slots;
+    a.slot_of_frame = s->d_slot_of_frame;
+    a.spare_slot = s->d_spare_slot;
+    a.nonfinite = s->d_frame_nonfinite;
+    a.items = d_items + k0;
+    a.item_count = nb;
+    a.stride = s->stride;
+    a.width = static_cast<int>(s->width);
+    a.height = static_cast<int>(s->height);
+    a.tiles_x = static_cast<int>((s->width + kTileW - 1) / kTileW);
+    a.tiles_y = static_cast<int>((s->height + kTileH - 1) / kTileH);
+    a.interp = interp;
+    a.fill = fill;
+    a.clamp = clamp;
+    a.coverage = track_coverage ? s->d_warp_coverage : nullptr;
+    a.error = s->d_error;
+    if (interp == GG_INTERP_NEAREST)
+      launch_warp_tiles<GG_INTERP_NEAREST>(s, a, use_tma);
+    else if (interp == GG_INTERP_BILINEAR)
+      launch_warp_tiles<GG_INTERP_BILINEAR>(s, a, use_tma);
+    else
+      launch_warp_tiles<GG_INTERP_LANCZOS3>(s, a, use_tma);
+    note_launch();
+    warp_finish_kernel<<<(nb + 127) / 128, 128, 0, s->stream>>>(d_items + k0, nb, s->d_slot_of_frame,
+                                                                s->d_spare_slot);
+    check_cuda(cudaGetLastError(), "warp_finish launch");
+  }
+  if (track_coverage) s->warp_coverage_frames += count;
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_stack_warp_frames(gg_stack* s, const int64_t* indices, int64_t count, const double* host_matrices,
+                         int interpolation, float fill, float clamping_threshold, int track_coverage) {
+  GG_API_BEGIN
+  require(s != nullptr && indices != nullptr && host_matrices != nullptr, "null argument");
+  require(count > 0, "indices must contain at least one frame index");
+  require(interpolation == GG_INTERP_NEAREST || interpolation == GG_INTERP_BILINEAR ||
+              interpolation == GG_INTERP_LANCZOS3,
+          "interpolation must be nearest, bilinear or lanczos3");
+  require(s->width < (1 << 24) && s->height < (1 << 24), "frame too large for float coordinates");
+  stack_activate(s);
+  warp_frames(s, indices, count, host_matrices, interpolation, fill, clamping_threshold, track_coverage != 0);
+  GG_API_END
+}
+
+int gg_stack_reset_warp_coverage(gg_stack* s) {
+  GG_API_BEGIN
+  require(s != nullptr, "stack is null");
+  stack_activate(s);
+  ensure_warp_coverage(s);
+  check_cuda(cudaMemsetAsync(s->d_warp_coverage, 0, sizeof(float) * s->pixels, s->stream), "cudaMemsetAsync");
+  s->warp_coverage_frames = 0;
+  GG_API_END
+}
+
+int gg_stack_accumulate_full_warp_coverage_frame(gg_stack* s) {
+  GG_API_BEGIN
+  require(s != nullptr, "stack is null");
+  stack_activate(s);
+  ensure_warp_coverage(s);
+  note_launch();
+  add_scalar_kernel<<<grid_for(static_cast<size_t>(s->pixels), 256, 4), 256, 0, s->stream>>>(s->d_warp_coverage,
+                                                                                            s->pixels, 1.0f);
+  check_cuda(cudaGetLastError(), "add_scalar launch");
+  s->warp_coverage_frames += 1;
+  GG_API_END
+}
+
+int gg_stack_download_warp_coverage(gg_stack* s, float* host_out) {
+  GG_API_BEGIN
+  require(s != nullptr && host_out != nullptr, "null argument");
+  stack_activate(s);
+  ensure_warp_coverage(s);
+  check_cuda(cudaMemcpyAsync(host_out, s->d_warp_coverage, sizeof(float) * s->pixels, cudaMemcpyDeviceToHost,
+                             s->stream),
+             "cudaMemcpyAsync(warp coverage)");
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(warp coverage)");
+  stack_check_device_error(s);
+  GG_API_END
+}
+
+int gg_stack_tma_enabled(gg_stack* s, int* enabled) {
+  GG_API_BEGIN
+  require(s != nullptr && enabled != nullptr, "null argument");
+  *enabled = s->has_slot_tmap ? 1 : 0;
+  GG_API_END
+}
+
+int gg_warp_matrix_f32(const float* host_in, int64_t height, int64_t width, const double* host_matrix,
+                       int interpolation, float fill, float clamping_threshold, float* host_out,
+                       float* host_coverage) {
+  GG_API_BEGIN
+  require(host_in != nullptr && host_matrix != nullptr && host_out != nullptr, "null argument");
+  gg_stack* s = nullptr;
+  int rc = gg_stack_create(1, height, width, &s);
+  if (rc != GG_OK) fail(rc, "temporary stack: create failed");
+  struct Guard {
+    gg_stack* s;
+    ~Guard() { gg_stack_destroy(s); }
+  } guard{s};
+  rc = gg_stack_upload_frame(s, 0, host_in);
+  if (rc != GG_OK) fail(rc, "temporary stack: upload failed");
+  const int64_t idx = 0;
+  if (host_coverage) {
+    rc = gg_stack_reset_warp_coverage(s);
+    if (rc != GG_OK) fail(rc, "temporary stack: coverage reset failed");
+  }
+  warp_frames(s, &idx, 1, host_matrix, interpolation, fill, clamping_threshold, host_coverage != nullptr);
+  rc = gg_stack_download_frame_tile(s, 0, 0, 0, width, height, host_out);
+  if (rc != GG_OK) fail(rc, "temporary stack: download failed");
+  if (host_coverage) {
+    rc = gg_stack_download_warp_coverage(s, host_coverage);
+    if (rc != GG_OK) fail(rc, "temporary stack: coverage download failed");
+  }
+  GG_API_END
+}
+
+}  // extern "C"

@@ -48,6 +48,7 @@ extern "C" {
 #define GG_COUNT_F32 0 /* count maps as float32 (cpu/integration.py:100-110)          */
 #define GG_COUNT_U16 1 /* count maps as uint16 (count_map_dtype="uint16")              */
 
+#define GG_INTERP_NEAREST 0 /* integer translations (cpu/warp.py:6-22), engine/warp.py:87-96 */
 #define GG_INTERP_BILINEAR 1
 #define GG_INTERP_LANCZOS3 3
 
@@ -214,6 +215,29 @@ typedef struct {
   void* warp_coverage;  /* float32 coverage accumulator                           */
 } gg_stack_device_ptrs_t;
 int gg_stack_device_ptrs(gg_stack* stack, gg_stack_device_ptrs_t* out);
+
+/* ---- warps --------------------------------------------------------------- */
+/* Warps `count` resident frames in place through their forward matrices
+ * (float64 row-major 3x3, moving -> reference; the kernel samples the source
+ * at the float64 inverse).  Replaces apply_matrix_{bilinear,lanczos3}_frame(s)
+ * (native_bindings.cpp:8900-9924, 9704; warp_kernels.cu:206-777).  Invalid
+ * output pixels get `fill`; clamping_threshold < 0 disables the Lanczos3
+ * overshoot clamp; track_coverage adds 1 to the warp-coverage accumulator for
+ * every covered output pixel.  Asynchronous. */
+int gg_stack_warp_frames(gg_stack* stack, const int64_t* indices, int64_t count, const double* host_matrices,
+                         int interpolation, float fill, float clamping_threshold, int track_coverage);
+/* Warp-coverage accumulator: reset_warp_coverage /
+ * accumulate_full_warp_coverage_frame / warp_coverage_map. */
+int gg_stack_reset_warp_coverage(gg_stack* stack);
+int gg_stack_accumulate_full_warp_coverage_frame(gg_stack* stack);
+int gg_stack_download_warp_coverage(gg_stack* stack, float* host_out);
+/* 1 when the stack's frames are staged by TMA (width % 4 == 0). */
+int gg_stack_tma_enabled(gg_stack* stack, int* enabled);
+/* Standalone warp of one host image (module warp_matrix_{bilinear,lanczos3}_f32,
+ * glass_cuda.py:595-706).  host_coverage (H*W float32) may be NULL. */
+int gg_warp_matrix_f32(const float* host_in, int64_t height, int64_t width, const double* host_matrix,
+                       int interpolation, float fill, float clamping_threshold, float* host_out,
+                       float* host_coverage);
 
 /* Replaces module `resident_dq_map_count_maps_i16` (glass_cuda.py:270-290;
  * resident_cuda.py:3110-3297): DQ bits from the output maps.  Any count map

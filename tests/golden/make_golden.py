@@ -165,6 +165,112 @@ def make_calibration(ref_src: Path) -> None:
     np.savez_compressed(HERE / "calibration.npz", **arrays)
 
 
+# ---------------------------------------------------------------------------
+# warps
+# ---------------------------------------------------------------------------
+def _similarity(theta_deg: float, dx: float, dy: float, scale: float = 1.0) -> np.ndarray:
+    t = np.deg2rad(theta_deg)
+    c, s = scale * np.cos(t), scale * np.sin(t)
+    return np.array([[c, -s, dx], [s, c, dy], [0.0, 0.0, 1.0]], dtype=np.float32)
+
+
+def make_warp(ref_src: Path) -> None:
+    """Reference warp oracles: the per-pixel CPU functions of
+    tests/test_gpu_warp_vs_cpu.py:9-128, the NumPy fallbacks of src/glass_cuda.py
+    (warp_translation_f32 :539, warp_matrix_lanczos3_f32 :644) and the tile
+    warp of src/glass/engine/warp.py:155-227."""
+    sys.path.insert(0, str(ref_src))
+    import glass_cuda  # noqa: E402  (NumPy fallbacks when no native module)
+
+    ns: dict = {"np": np}
+    _load_functions(ref_src.parent / "tests" / "test_gpu_warp_vs_cpu.py",
+                    ["_warp_translation_bilinear_cpu", "_warp_matrix_bilinear_cpu", "_sinc", "_lanczos3_weight",
+                     "_warp_matrix_lanczos3_cpu"], ns)
+    eng: dict = {"np": np}
+    _load_functions(ref_src / "glass" / "engine" / "warp.py",
+                    ["_cubic_weight", "_sinc", "_lanczos3_weight", "_sample_nearest", "_sample_bilinear",
+                     "_sample_windowed", "_warp_tile_matrix"], eng)
+    eng["INTERPOLATOR_KERNEL_RADIUS"] = {"nearest": 0, "bilinear": 1, "bicubic": 2, "lanczos3": 3}
+
+    class Reader:
+        def __init__(self, image):
+            self.image = image
+            self.shape = image.shape
+
+        def read_tile(self, y0, y1, x0, x1):
+            return self.image[y0:y1, x0:x1]
+
+    class Tile:
+        def __init__(self, h, w):
+            self.y0, self.y1, self.x0, self.x1 = 0, h, 0, w
+
+    rng = np.random.default_rng(99)
+    arrays: dict[str, np.ndarray] = {}
+    cases = []
+    # the reference tests' own inputs
+    yy, xx = np.indices((12, 13), dtype=np.float32)
+    ramp = 0.2 * xx + 0.4 * yy
+    ramp[:, 7:] += 5.0
+    cases.append(("reftest_bilinear7", np.arange(49, dtype=np.float32).reshape(7, 7), _similarity(3.0, 1.2, -0.4),
+                  "bilinear", -1.0, -1.0))
+    cases.append(("reftest_lanczos12", ramp, _similarity(1.0, 0.35, -0.25), "lanczos3", -1.0, 0.30))
+    cases.append(("reftest_lanczos_sin", (np.sin(xx * 0.3) + np.cos(yy * 0.2)).astype(np.float32),
+                  _similarity(0.0, 0.4, -0.35), "lanczos3", np.nan, 0.30))
+    for k in range(10):
+        h, w = int(rng.integers(9, 40)), int(rng.integers(9, 44))
+        img = (1000.0 + 50.0 * rng.standard_normal((h, w))).astype(np.float32)
+        img[rng.random((h, w)) < 0.02] += 20000.0
+        m = _similarity(float(rng.uniform(-4, 4)), float(rng.uniform(-6, 6)), float(rng.uniform(-6, 6)),
+                        float(rng.uniform(0.97, 1.03)))
+        for interp in ("bilinear", "lanczos3"):
+            clamp = float(rng.choice([-1.0, 0.0, 0.3])) if interp == "lanczos3" else -1.0
+            cases.append((f"rand{k}_{interp}", img, m, interp, np.nan, clamp))
+        nanimg = img.copy()
+        nanimg[rng.random((h, w)) < 0.05] = np.nan
+        cases.append((f"rand{k}_lanczos3_nan", nanimg, m, "lanczos3", np.nan, 0.3 if k % 2 else -1.0))
+    # projective
+    proj = _similarity(2.0, 1.5, -2.0)
+    proj[2, 0], proj[2, 1] = 1.0e-4, -2.0e-4
+    img = (500.0 + 20.0 * rng.standard_normal((30, 34))).astype(np.float32)
+    cases.append(("projective_bilinear", img, proj, "bilinear", np.nan, -1.0))
+    cases.append(("projective_lanczos3", img, proj, "lanczos3", np.nan, -1.0))
+    names = []
+    for name, image, matrix, interp, fill, clamp in cases:
+        if interp == "bilinear":
+            out, cov = ns["_warp_matrix_bilinear_cpu"](image, matrix, fill)
+        else:
+            out, cov = ns["_warp_matrix_lanczos3_cpu"](image, matrix, fill, clamp)
+        arrays[f"{name}/image"] = image
+        arrays[f"{name}/matrix"] = matrix
+        arrays[f"{name}/out"] = out
+        arrays[f"{name}/coverage"] = cov
+        arrays[f"{name}/params"] = np.array([1.0 if interp == "bilinear" else 3.0, fill, clamp])
+        if np.all(np.isfinite(image)):
+            # engine/warp.py tile warp (no NaN skipping there, so finite inputs only)
+            eout, ecov = eng["_warp_tile_matrix"](Reader(image), Tile(*image.shape), matrix.tolist(), fill,
+                                                  interp)
+            arrays[f"{name}/engine_out"] = eout
+            arrays[f"{name}/engine_coverage"] = ecov
+        if interp == "lanczos3":
+            gout, gcov = glass_cuda.warp_matrix_lanczos3_f32(image, matrix, fill, clamp)
+            arrays[f"{name}/fallback_out"] = gout
+            arrays[f"{name}/fallback_coverage"] = gcov
+        names.append(name)
+    # translations (cpu/warp.py via the glass_cuda fallbacks)
+    img = np.arange(36, dtype=np.float32).reshape(6, 6)
+    for k, (dx, dy) in enumerate([(1, -2), (0.6, 2.5), (-3.4, 0.5), (2.5, -1.5)]):
+        out, cov = glass_cuda.warp_translation_f32(img, dx, dy, -1.0)
+        arrays[f"translation{k}/out"] = out
+        arrays[f"translation{k}/coverage"] = cov
+        arrays[f"translation{k}/shift"] = np.array([dx, dy])
+        bout, bcov = ns["_warp_translation_bilinear_cpu"](img, dx, dy, -1.0)
+        arrays[f"translation{k}/bilinear_out"] = bout
+        arrays[f"translation{k}/bilinear_coverage"] = bcov
+    arrays["translation_image"] = img
+    arrays["_names"] = np.asarray(names)
+    np.savez_compressed(HERE / "warp.npz", **arrays)
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__)
     parser.add_argument("--reference", default="/root/reference", help="GLASS reference checkout")
@@ -172,7 +278,7 @@ def main() -> int:
     args = parser.parse_args()
     ref = Path(args.reference)
     src = ref / "src"
-    jobs = {"integration": make_integration, "calibration": make_calibration}
+    jobs = {"integration": make_integration, "calibration": make_calibration, "warp": make_warp}
     only = [j for j in args.only.split(",") if j] or list(jobs)
     for job in only:
         jobs[job](src)
