@@ -194,8 +194,8 @@ def main():
 
     cfg = CONFIGS[args.config]
     frames = args.frames or cfg.frames
-    workload = f"{args.config}:{frames}x{cfg.height}x{cfg.width} uint16 -> calibrate -> simple_snr weights -> " \
-               f"winsorized 3/3 weighted integration (6 maps)"
+    workload = f"{args.config}:{frames}x{cfg.height}x{cfg.width} uint16 -> calibrate -> Lanczos3 warp " \
+               f"(truth matrices) -> simple_snr weights -> winsorized 3/3 weighted integration (6 maps)"
     metric = "stacked Mpix-frames/s"
 
     if args.impl == "reference":
@@ -262,33 +262,41 @@ def main():
             dist.barrier()
 
     # ---- device-resident throughput ("value") ----
+    matrices = data.truth_matrices
+    P = h * w
+    stages = [
+        ("calibrate", lambda: pipe.calibrate_device(dev_raw.data_ptr()), 6 * n * P + 12 * P),
+        ("warp_lanczos3", lambda: pipe.warp(matrices), 8 * (n - 1) * P),
+        ("weights", pipe.weights, 4 * n * P),
+        ("integrate_winsorized", pipe.integrate, 4 * n * P + 16 * P),
+    ]
     for _ in range(args.warmup):
-        pipe.step_device(dev_raw.data_ptr())
+        for _, fn, _ in stages:
+            fn()
     stream.synchronize()
     barrier()
     torch.cuda.synchronize()
     launches0 = _lib.kernel_launches()
-    ev_int = []
+    events = {name: [] for name, _, _ in stages}
     with ClockSampler(local) as clocks:
         start = torch.cuda.Event(enable_timing=True)
         stop = torch.cuda.Event(enable_timing=True)
         start.record(stream)
         for _ in range(args.steps):
-            pipe.calibrate_device(dev_raw.data_ptr())
-            pipe.weights()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            pipe.integrate()
-            e1.record(stream)
-            ev_int.append((e0, e1))
+            for name, fn, _ in stages:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                events[name].append((e0, e1))
         stop.record(stream)
         stream.synchronize()
     torch.cuda.synchronize()
     barrier()
     launches = _lib.kernel_launches() - launches0
     elapsed_ms = start.elapsed_time(stop)
-    int_ms = [a.elapsed_time(b) for a, b in ev_int]
+    stage_ms = {name: statistics.mean(a.elapsed_time(b) for a, b in ev) for name, ev in events.items()}
     if world > 1:
         import torch.distributed as dist
 
@@ -302,12 +310,12 @@ def main():
     pinned = torch.from_numpy(data.lights.view(np.int16)).pin_memory().numpy().view(np.uint16)
     e2e_steps = max(3, min(args.steps, 10))
     for _ in range(2):
-        maps = pipe.step_host(pinned)
+        maps = pipe.step_host(pinned, matrices)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        maps = pipe.step_host(pinned)
+        maps = pipe.step_host(pinned, matrices)
     t1 = time.perf_counter()
     e2e_s = t1 - t0
     if world > 1:
@@ -323,9 +331,12 @@ def main():
     if rank != 0:
         return 0
     peak, peak_kind = measured_peak()
-    int_avg_s = statistics.mean(int_ms) / 1e3
-    alg_bytes = 4 * n * h * w + 16 * h * w
-    achieved = alg_bytes / int_avg_s / 1e9
+    kernels = {}
+    for name, _, nbytes in stages:
+        ms = stage_ms[name]
+        gbs = nbytes / (ms / 1e3) / 1e9
+        kernels[name] = {"ms": ms, "algorithmic_bytes": nbytes, "achieved_gbs": gbs, "frac": gbs / peak}
+    top = max(kernels, key=lambda k: kernels[k]["ms"])
     cpu = None
     if not args.no_cpu_baseline:
         rate, elapsed, px = cpu_baseline(data, masters, args.cpu_seconds, 1)
@@ -348,10 +359,12 @@ def main():
         "config": {"workload": workload, "frames": n, "height": h, "width": w,
                    "l2": "inputs larger than L2 (stack %.0f MB > 129 MB)" % (4 * n * h * w / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "kernel": "integrate (winsorized)", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": profile_traffic("integrate_winsorized_c2.md"),
-                     "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": int_avg_s * 1e3},
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": kernels[top]["achieved_gbs"], "peak": peak,
+                     "unit": "GB/s", "frac": kernels[top]["frac"], "peak_source": peak_kind,
+                     "traffic": profile_traffic(f"{top}_c2.md"),
+                     "algorithmic_bytes_per_launch": kernels[top]["algorithmic_bytes"],
+                     "launch_ms": kernels[top]["ms"]},
+        "stages": kernels,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mpix-frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * e2e_s / e2e_steps},

@@ -76,6 +76,8 @@ class StepConfig:
     max_reject_fraction: float = 0.5
     weighting: str = "simple_snr"
     count_map_dtype: str = "uint16"
+    interpolation: str = "lanczos3"
+    clamping_threshold: float = -1.0
     light_exposure_s: float = 300.0
     dark_exposure_s: float | None = 300.0
 
@@ -119,6 +121,15 @@ class ResidentPipeline:
         _lib.call("gg_stack_calibrate_u16", self.stack.handle, _lib.ptr(self._indices),
                   ctypes.c_int64(self.frames), _lib.ptr(host_raw), 0, ctypes.byref(self._calib_params()))
 
+    def warp(self, matrices: np.ndarray, reference_index: int = 0) -> None:
+        """Warps every frame but the reference through its moving->reference matrix."""
+        idx = np.array([i for i in range(self.frames) if i != reference_index], dtype=np.int64)
+        if idx.size == 0:
+            return
+        mats = np.ascontiguousarray(np.asarray(matrices, dtype=np.float64)[idx])
+        interp = _lib.GG_INTERP_LANCZOS3 if self.config.interpolation == "lanczos3" else _lib.GG_INTERP_BILINEAR
+        self.stack.warp_frames_async(idx, mats, interp, np.nan, self.config.clamping_threshold, False)
+
     def weights(self) -> None:
         self.stack.compute_frame_weights(self.config.weighting, None, 1.0e-6, download=False)
 
@@ -127,14 +138,18 @@ class ResidentPipeline:
         self.stack.integrate_async("device", cfg.rejection, cfg.low_sigma, cfg.high_sigma, cfg.min_samples,
                                    cfg.max_reject_fraction, cfg.count_map_dtype)
 
-    def step_device(self, dev_raw_ptr: int) -> None:
+    def step_device(self, dev_raw_ptr: int, matrices: np.ndarray | None = None) -> None:
         self.calibrate_device(dev_raw_ptr)
+        if matrices is not None:
+            self.warp(matrices)
         self.weights()
         self.integrate()
 
-    def step_host(self, host_raw: np.ndarray):
+    def step_host(self, host_raw: np.ndarray, matrices: np.ndarray | None = None):
         """Public-API step from host memory to host maps (end to end)."""
         self.calibrate_host(host_raw)
+        if matrices is not None:
+            self.warp(matrices)
         self.weights()
         self.integrate()
         return self.stack.download_maps("full", include_dq=True)
