@@ -248,6 +248,9 @@ __device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int
     }
     wsum = sx * sy;
   } else {
+    // Skipping non-finite taps can leave a small weight sum (lobes cancel),
+    // which amplifies rounding: accumulate in float-float here.
+    FF facc, fw;
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
 #pragma unroll
@@ -255,13 +258,17 @@ __device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int
         const float v = ts.at(x0 - 2 + i, y0 - 2 + j);
         if (isfinite(v)) {
           const float w = wy[j] * wx[i];
-          acc = __fmaf_rn(w, v, acc);
-          wsum += w;
+          facc.add_prod(w, v);
+          fw.add(w);
           vmin = fminf(vmin, v);
           vmax = fmaxf(vmax, v);
         }
       }
     }
+    wsum = __fadd_rn(fw.hi, fw.lo);
+    if (!(fabsf(wsum) > 1.0e-12f)) return false;
+    acc = ff_div_ff(facc.hi, facc.lo, fw.hi, fw.lo);
+    wsum = 1.0f;
   }
   if (!(fabsf(wsum) > 1.0e-12f)) return false;
   float value = acc / wsum;

@@ -3,8 +3,9 @@
 Tolerances: coverage bit-exact; bilinear and nearest within one float32 ulp
 (the kernel replays the float32 arithmetic of the reference; the float64
 source coordinate is evaluated in float-float); Lanczos3 within
-3e-6 x max|image| (float32 weights vs the reference's float64 weights; the
-reference's own CUDA test allows 3e-5 on O(10) data, tests/test_gpu_warp_vs_cpu.py:176-234).
+3e-6 x max|image| + 1e-5 x |value| (float32 weights vs the reference's float64
+weights; the reference's own CUDA test allows 3e-5 on O(10) data,
+tests/test_gpu_warp_vs_cpu.py:176-234).
 """
 
 from __future__ import annotations
@@ -33,7 +34,9 @@ def check_warp(out, cov, exp_out, exp_cov, image, interp, tag):
     np.testing.assert_array_equal(cov, exp_cov, err_msg=tag + " coverage")
     ok = exp_cov > 0
     if interp == "lanczos3":
-        np.testing.assert_allclose(out[ok], exp_out[ok], rtol=0, atol=lanczos_tol(image), err_msg=tag)
+        # rtol covers pixels where dropping non-finite taps leaves nearly
+        # cancelling weights, which amplifies the float32 weight rounding.
+        np.testing.assert_allclose(out[ok], exp_out[ok], rtol=1e-5, atol=lanczos_tol(image), err_msg=tag)
     else:
         a, b = out[ok].astype(np.float64), exp_out[ok].astype(np.float64)
         tol = np.spacing(np.maximum(np.abs(a), np.abs(b)).astype(np.float32)).astype(np.float64)
