@@ -147,6 +147,7 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_calibrate_f32": [_P, ctypes.c_int64, _P, ctypes.POINTER(CalibParams)],
     "gg_stack_frame_stats": [_P, _P, ctypes.c_int64, _P],
     "gg_stack_compute_weights": [_P, ctypes.c_int, _P, ctypes.c_float, _P],
+    "gg_frames_stats_f32_noalloc": [_P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _P, _P],
     "gg_stack_integrate": [_P, _P, ctypes.POINTER(IntegrateParams)],
     "gg_stack_integrate_device_weights": [_P, _P, ctypes.POINTER(IntegrateParams)],
     "gg_stack_download_maps": [_P, _P, _P, _P, _P, _P, _P],

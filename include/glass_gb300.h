@@ -174,6 +174,20 @@ int gg_stack_frame_stats(gg_stack* stack, const int64_t* indices, int64_t count,
 int gg_stack_compute_weights(gg_stack* stack, int mode, const float* host_prior, float eps,
                              float* host_weights_out);
 
+/* Frame statistics (same results as gg_stack_frame_stats) for callers that
+ * cannot allocate device memory: graph-capturing code, plugins whose host owns
+ * every allocation, real-time loops.  No counterpart in the reference.  It
+ * allocates nothing: the reduction scratch is a fixed 192 KiB __device__ array
+ * that every GPU loading this library reserves until exit.  `frame_count`
+ * frames of `pixels` float32 samples start `frame_stride` elements apart at
+ * dev_frames (device memory).  At most 64 frames per call (larger counts are
+ * rejected with GG_ERR_INVALID_ARGUMENT).  The first call on a device resolves
+ * the scratch address and must come before any stream capture.  Calls share
+ * the scratch, so calls that overlap on the GPU race.  Synchronises
+ * cuda_stream (NULL: legacy default stream) before returning. */
+int gg_frames_stats_f32_noalloc(const float* dev_frames, int64_t frame_count, int64_t pixels,
+                                int64_t frame_stride, void* cuda_stream, gg_frame_stats_t* out);
+
 /* ---- integration --------------------------------------------------------- */
 typedef struct {
   int rejection;             /* GG_REJECT_*                                  */
