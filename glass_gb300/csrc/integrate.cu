@@ -585,7 +585,7 @@ __device__ __forceinline__ CenterScale winsorized_sorted(const float* S, int T, 
 }
 
 template <int NB, int T, int MODE>
-__global__ void __launch_bounds__(T, 4) integrate_col_kernel(IntegrateArgs a) {
+__global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
   extern __shared__ float smem[];
   float* S = smem;            // [NB][T] ascending valid samples
   float* R = smem + NB * T;   // [NB][T] frame-order samples

@@ -155,9 +155,28 @@ __device__ __forceinline__ void ff_floor_frac(FFv v, int& i, float& frac) {
   frac = __fadd_rn(__fsub_rn(v.hi, f), v.lo);
 }
 
+// Register copy of one item's inverse matrix (loaded once per work item so
+// that output stores cannot force re-reads of the descriptor).
+struct Coef {
+  float m[9][2];
+  int affine;
+};
+
+__device__ __forceinline__ Coef load_coef(const WarpItem* p) {
+  Coef c;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    c.m[q][0] = __ldg(&p->m[q][0]);
+    c.m[q][1] = __ldg(&p->m[q][1]);
+  }
+  c.affine = __ldg(&p->affine);
+  return c;
+}
+
 // Source coordinate of output pixel (x, y); returns false when the
 // projective denominator vanishes (|w| <= 1e-12, engine/warp.py:178-191).
-__device__ __forceinline__ bool source_coord(const WarpItem& it, float x, float y, FFv& sx, FFv& sy) {
+template <class C>
+__device__ __forceinline__ bool source_coord(const C& it, float x, float y, FFv& sx, FFv& sy) {
   const float (*m)[2] = it.m;
   const float rx[3][2] = {{m[0][0], m[0][1]}, {m[1][0], m[1][1]}, {m[2][0], m[2][1]}};
   const float ry[3][2] = {{m[3][0], m[3][1]}, {m[4][0], m[4][1]}, {m[5][0], m[5][1]}};
@@ -218,6 +237,30 @@ __device__ __forceinline__ float sample_bilinear(const TapSource& ts, int x0, in
   return __fadd_rn(__fmul_rn(top, oy), __fmul_rn(bottom, ty));
 }
 
+// Non-finite taps present: skip them and renormalise.  Dropping taps can
+// leave a small weight sum (lobes cancel), which amplifies rounding, so the
+// sums are float-float here.  Kept out of line: it is the rare path.
+__device__ __noinline__ bool lanczos3_nonfinite(const TapSource& ts, int x0, int y0, const float (&wx)[6],
+                                                const float (&wy)[6], float& value, float& vmin, float& vmax) {
+  FF facc, fw;
+  for (int j = 0; j < 6; ++j) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const float v = ts.at(x0 - 2 + i, y0 - 2 + j);
+      if (isfinite(v)) {
+        const float w = wy[j] * wx[i];
+        facc.add_prod(w, v);
+        fw.add(w);
+        vmin = fminf(vmin, v);
+        vmax = fmaxf(vmax, v);
+      }
+    }
+  }
+  if (!(fabsf(__fadd_rn(fw.hi, fw.lo)) > 1.0e-12f)) return false;
+  value = ff_div_ff(facc.hi, facc.lo, fw.hi, fw.lo);
+  return true;
+}
+
 // Returns false when the tap weights sum to (almost) zero.
 __device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int y0, float tx, float ty,
                                                 bool all_finite, float clamp, float& out) {
@@ -248,26 +291,7 @@ __device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int
     }
     wsum = sx * sy;
   } else {
-    // Skipping non-finite taps can leave a small weight sum (lobes cancel),
-    // which amplifies rounding: accumulate in float-float here.
-    FF facc, fw;
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-#pragma unroll
-      for (int i = 0; i < 6; ++i) {
-        const float v = ts.at(x0 - 2 + i, y0 - 2 + j);
-        if (isfinite(v)) {
-          const float w = wy[j] * wx[i];
-          facc.add_prod(w, v);
-          fw.add(w);
-          vmin = fminf(vmin, v);
-          vmax = fmaxf(vmax, v);
-        }
-      }
-    }
-    wsum = __fadd_rn(fw.hi, fw.lo);
-    if (!(fabsf(wsum) > 1.0e-12f)) return false;
-    acc = ff_div_ff(facc.hi, facc.lo, fw.hi, fw.lo);
+    if (!lanczos3_nonfinite(ts, x0, y0, wx, wy, acc, vmin, vmax)) return false;
     wsum = 1.0f;
   }
   if (!(fabsf(wsum) > 1.0e-12f)) return false;
@@ -285,7 +309,7 @@ struct TilePlan {
   int bx, by, fits;
 };
 
-__device__ __forceinline__ TilePlan plan_tile(const WarpItem& it, int tile_x, int tile_y, int radius) {
+__device__ __forceinline__ TilePlan plan_tile(const Coef& it, int tile_x, int tile_y, int radius) {
   const float x0 = static_cast<float>(tile_x * kTileW), y0 = static_cast<float>(tile_y * kTileH);
   const float cx[4] = {x0, x0 + kTileW - 1, x0, x0 + kTileW - 1};
   const float cy[4] = {y0, y0, y0 + kTileH - 1, y0 + kTileH - 1};
@@ -315,7 +339,7 @@ __device__ __forceinline__ TilePlan plan_tile(const WarpItem& it, int tile_x, in
 }
 
 template <int INTERP, bool USE_TMA>
-__global__ void __launch_bounds__(kWarpThreads) warp_tiles_kernel(const __grid_constant__ CUtensorMap tmap,
+__global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                   WarpArgs a) {
   __shared__ alignas(128) float tile[2][kBoxH * kBoxW];
   __shared__ alignas(8) uint64_t bar[2];
@@ -336,9 +360,9 @@ __global__ void __launch_bounds__(kWarpThreads) warp_tiles_kernel(const __grid_c
 
   auto issue = [&](int item, int buf) {
     // thread 0 only
-    const WarpItem& it = a.items[item / tiles];
+    const WarpItem* ip = a.items + item / tiles;
     const int t = item % tiles;
-    TilePlan p = plan_tile(it, t % a.tiles_x, t / a.tiles_x, radius);
+    TilePlan p = plan_tile(load_coef(ip), t % a.tiles_x, t / a.tiles_x, radius);
     if (!USE_TMA) p.fits = 0;
     s_bx[buf] = p.bx;
     s_by[buf] = p.by;
@@ -346,7 +370,7 @@ __global__ void __launch_bounds__(kWarpThreads) warp_tiles_kernel(const __grid_c
     if (p.fits) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_expect_tx(&bar[buf], kBoxW * kBoxH * 4);
-      tma_load_3d(tile[buf], &tmap, p.bx, p.by, it.src_slot, &bar[buf]);
+      tma_load_3d(tile[buf], &tmap, p.bx, p.by, __ldg(&ip->src_slot), &bar[buf]);
     }
   };
 
@@ -358,7 +382,12 @@ __global__ void __launch_bounds__(kWarpThreads) warp_tiles_kernel(const __grid_c
     const int buf = i & 1;
     const int next = item + gridDim.x;
     if (tid == 0 && next < items) issue(next, buf ^ 1);
-    const WarpItem& it = a.items[item / tiles];
+    const WarpItem* ip = a.items + item / tiles;
+    const Coef co = load_coef(ip);
+    const int it_frame = __ldg(&ip->frame);
+    const int it_src = __ldg(&ip->src_slot);
+    const int it_dst = __ldg(&ip->dst_slot);
+    const unsigned it_nonfinite = __ldg(&ip->src_nonfinite);
     const int t = item % tiles;
     const int tile_x = t % a.tiles_x, tile_y = t / a.tiles_x;
     const bool fit = s_fit[buf] != 0;
@@ -376,15 +405,15 @@ __global__ void __launch_bounds__(kWarpThreads) warp_tiles_kernel(const __grid_c
     {
       TapSource ts;
       ts.tile = fit ? tile[buf] : nullptr;
-      ts.src = a.slots + static_cast<int64_t>(it.src_slot) * a.stride;
+      ts.src = a.slots + static_cast<int64_t>(it_src) * a.stride;
       ts.bx = s_bx[buf];
       ts.by = s_by[buf];
       ts.width = a.width;
-      float* dst = a.slots + static_cast<int64_t>(it.dst_slot) * a.stride;
+      float* dst = a.slots + static_cast<int64_t>(it_dst) * a.stride;
       const int ox = tile_x * kTileW + lx;
-      const bool all_finite = it.src_nonfinite == 0u;
+      const bool all_finite = it_nonfinite == 0u;
       unsigned bad = 0;
-#pragma unroll
+#pragma unroll 1
       for (int r = 0; r < 4; ++r) {
         const int oy = tile_y * kTileH + ly + 4 * r;
         const bool inside = ox < a.width && oy < a.height;
@@ -392,7 +421,7 @@ __global__ void __launch_bounds__(kWarpThreads) warp_tiles_kernel(const __grid_c
         float value = a.fill;
         if (inside) {
           FFv sx, sy;
-          if (source_coord(it, static_cast<float>(ox), static_cast<float>(oy), sx, sy)) {
+          if (source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx, sy)) {
             const float W = static_cast<float>(a.width), H = static_cast<float>(a.height);
             if (INTERP != GG_INTERP_LANCZOS3)
               valid = ff_ge(sx, 0.0f) && ff_le(sx, W - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, H - 1.0f);
@@ -429,7 +458,7 @@ __global__ void __launch_bounds__(kWarpThreads) warp_tiles_kernel(const __grid_c
         }
       }
       const unsigned warp_bad = __reduce_add_sync(0xffffffffu, bad);
-      if ((tid & 31) == 0 && warp_bad) atomicAdd(a.nonfinite + it.frame, warp_bad);
+      if ((tid & 31) == 0 && warp_bad) atomicAdd(a.nonfinite + it_frame, warp_bad);
     }
     __syncthreads();
     if (s_abort) {
