@@ -200,6 +200,22 @@ def warp_matrix_lanczos3_f32(data: Any, matrix: Any, fill: float = 0.0, clamping
     return _warp_image(data, _matrix64(matrix), _lib.GG_INTERP_LANCZOS3, fill, clamping_threshold)
 
 
+def detect_stars_f32(data: Any, threshold_sigma: float = 5.0, max_stars: int = 500,
+                     background: float | None = None, noise: float | None = None, window_radius: int = 4,
+                     min_separation_px: float = 2.0) -> np.ndarray:
+    """detect_stars (cpu/star_detect.py:121-168) of one host image on the GPU."""
+    image = np.ascontiguousarray(np.asarray(data, dtype=np.float32))
+    if image.ndim != 2:
+        raise ValueError("data must be a 2-D array")
+    stack = ResidentCalibratedStack(1, image.shape[0], image.shape[1])
+    try:
+        stack.upload_calibrated_frame(0, image)
+        return stack.detect_stars([0], threshold_sigma, max_stars, background, noise, window_radius,
+                                  min_separation_px)[0]
+    finally:
+        stack.close()
+
+
 def resident_dq_map_count_maps_i16(master: Any, weight_map: Any, coverage_map: Any | None = None,
                                    low_rejection_map: Any | None = None,
                                    high_rejection_map: Any | None = None,
@@ -425,6 +441,31 @@ class ResidentCalibratedStack:
         return {"schema_version": 1, "h2d_mode": "pinned_lanes", "frames": int(idx.size),
                 "stream_count": int(stream_count), "wave_frames": int(wave_frames), "total_s": total,
                 "host_pinned_bytes": self.host_pinned_bytes}
+
+    # ---- star catalogs (star_detect.py:121-168) -------------------------------------
+    def detect_stars(self, indices: Any, threshold_sigma: float = 5.0, max_stars: int = 500,
+                     background: float | None = None, noise: float | None = None, window_radius: int = 4,
+                     min_separation_px: float = 2.0, with_info: bool = False):
+        """detect_stars semantics per resident frame -> list of structured arrays
+        (x, y, flux, peak, fwhm, eccentricity, snr, sharpness, npix), brightest first."""
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+        if idx.size == 0:
+            raise ValueError("indices must contain at least one frame index")
+        params = _lib.StarParams(float(threshold_sigma), int(max_stars), int(window_radius), float(min_separation_px),
+                                 np.nan if background is None else float(background),
+                                 np.nan if noise is None else float(noise))
+        stars = np.zeros((idx.size, int(max_stars)), dtype=_lib.STAR_DTYPE)
+        counts = np.zeros(idx.size, dtype=np.int32)
+        info = (_lib.StarFrameInfo * idx.size)()
+        _lib.call("gg_stack_detect_stars", self._handle, _lib.ptr(idx), ctypes.c_int64(idx.size), ctypes.byref(params),
+                  _lib.ptr(stars), _lib.ptr(counts), info)
+        catalogs = [stars[k, : counts[k]].copy() for k in range(idx.size)]
+        if with_info:
+            meta = [{"median": float(i.median), "mad": float(i.mad), "noise": float(i.noise),
+                     "threshold": float(i.threshold), "candidates": int(i.candidates),
+                     "valid_pixels": int(i.valid_pixels)} for i in info]
+            return catalogs, meta
+        return catalogs
 
     # ---- warps (native_bindings.cpp:8900-9924) ------------------------------------
     @property

@@ -93,6 +93,47 @@ class FrameStats(ctypes.Structure):
     ]
 
 
+class StarParams(ctypes.Structure):
+    _fields_ = [
+        ("threshold_sigma", ctypes.c_float),
+        ("max_stars", ctypes.c_int),
+        ("window_radius", ctypes.c_int),
+        ("min_separation_px", ctypes.c_float),
+        ("background", ctypes.c_float),
+        ("noise", ctypes.c_float),
+    ]
+
+
+class Star(ctypes.Structure):
+    _fields_ = [
+        ("x", ctypes.c_double),
+        ("y", ctypes.c_double),
+        ("flux", ctypes.c_double),
+        ("peak", ctypes.c_double),
+        ("fwhm", ctypes.c_double),
+        ("eccentricity", ctypes.c_double),
+        ("snr", ctypes.c_double),
+        ("sharpness", ctypes.c_double),
+        ("npix", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
+STAR_DTYPE = np.dtype([("x", "f8"), ("y", "f8"), ("flux", "f8"), ("peak", "f8"), ("fwhm", "f8"),
+                       ("eccentricity", "f8"), ("snr", "f8"), ("sharpness", "f8"), ("npix", "i4"), ("pad", "i4")])
+
+
+class StarFrameInfo(ctypes.Structure):
+    _fields_ = [
+        ("median", ctypes.c_float),
+        ("mad", ctypes.c_float),
+        ("noise", ctypes.c_double),
+        ("threshold", ctypes.c_double),
+        ("candidates", ctypes.c_int64),
+        ("valid_pixels", ctypes.c_int64),
+    ]
+
+
 class IntegrateParams(ctypes.Structure):
     _fields_ = [
         ("rejection", ctypes.c_int),
@@ -153,6 +194,7 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_download_maps": [_P, _P, _P, _P, _P, _P, _P],
     "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
     "gg_dq_map_i16": [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P],
+    "gg_stack_detect_stars": [_P, _P, ctypes.c_int64, ctypes.POINTER(StarParams), _P, _P, _P],
     "gg_stack_warp_frames": [_P, _P, ctypes.c_int64, _P, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int],
     "gg_stack_reset_warp_coverage": [_P],
     "gg_stack_accumulate_full_warp_coverage_frame": [_P],

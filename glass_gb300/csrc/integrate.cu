@@ -468,19 +468,12 @@ __device__ __forceinline__ FF sum_sorted(const float* S, int T, int i0, int i1, 
   if (i1 <= i0) return acc;
   const float first = clipf(S[i0 * T], lo, hi);
   const float last = clipf(S[(i1 - 1) * T], lo, hi);
-  if (first >= 0.0f || last <= 0.0f) {
-    // Same sign: walk from the largest magnitude down with two interleaved
-    // accumulators (each sees non-increasing terms, so Fast2Sum is exact).
-    const bool down = first >= 0.0f;
-    const int n = i1 - i0;
-    FF b;
-#pragma unroll 2
-    for (int k = 0; k < n; k += 2) {
-      const int i = down ? i1 - 1 - k : i0 + k;
-      ff_add_fast(acc, clipf(S[i * T], lo, hi));
-      if (k + 1 < n) ff_add_fast(b, clipf(S[(down ? i - 1 : i + 1) * T], lo, hi));
-    }
-    ff_merge2(acc, b);
+  if (first >= 0.0f) {
+#pragma unroll 4
+    for (int i = i1 - 1; i >= i0; --i) ff_add_fast(acc, clipf(S[i * T], lo, hi));
+  } else if (last <= 0.0f) {
+#pragma unroll 4
+    for (int i = i0; i < i1; ++i) ff_add_fast(acc, clipf(S[i * T], lo, hi));
   } else {
     FF b;
 #pragma unroll 2
@@ -587,8 +580,7 @@ __device__ __forceinline__ CenterScale winsorized_sorted(const float* S, int T, 
 template <int NB, int T, int MODE>
 __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
   extern __shared__ float smem[];
-  float* S = smem;            // [NB][T] ascending valid samples
-  float* R = smem + NB * T;   // [NB][T] frame-order samples
+  float* S = smem;  // [NB][T] ascending valid samples
   __shared__ FrameTable<NB> tab;
   __shared__ float s_wtot[2];
   load_frame_table<NB>(a, tab);
@@ -607,14 +599,10 @@ __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
   const int64_t P = a.pixels;
   const float ls = a.low_sigma, hs = a.high_sigma;
   float* St = S + tid;
-  float* Rt = R + tid;
   for (int64_t p = static_cast<int64_t>(blockIdx.x) * T + tid; p < P; p += static_cast<int64_t>(gridDim.x) * T) {
     float x[NB];
 #pragma unroll
-    for (int f = 0; f < NB; ++f) {
-      x[f] = (f < N) ? __ldcs(tab.base[f] + p) : kInf;
-      Rt[f * T] = x[f];
-    }
+    for (int f = 0; f < NB; ++f) x[f] = (f < N) ? __ldcs(tab.base[f] + p) : kInf;
     int cnt = 0;
     int nl = 0, nh = 0;
     float lt = -kInf, ht = kInf;
@@ -651,13 +639,13 @@ __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
             float sum = 0.0f;
 #pragma unroll
             for (int f = 0; f < NB; ++f)
-              if (f < N && tab.w[f] > 0.0f && isfinite(Rt[f * T])) sum = __fadd_rn(sum, Rt[f * T]);
+              if (f < N && tab.w[f] > 0.0f && isfinite(x[f])) sum = __fadd_rn(sum, x[f]);
             const float mean = __fdiv_rn(sum, static_cast<float>(cnt));
             float v = 0.0f;
 #pragma unroll
             for (int f = 0; f < NB; ++f) {
-              if (f < N && tab.w[f] > 0.0f && isfinite(Rt[f * T])) {
-                const float d = __fsub_rn(Rt[f * T], mean);
+              if (f < N && tab.w[f] > 0.0f && isfinite(x[f])) {
+                const float d = __fsub_rn(x[f], mean);
                 v = __fadd_rn(v, __fmul_rn(d, d));
               }
             }
@@ -677,7 +665,7 @@ __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
       }
     } else {
 #pragma unroll
-      for (int f = 0; f < NB; ++f) cnt += ((f < N) && tab.w[f] > 0.0f && isfinite(Rt[f * T])) ? 1 : 0;
+      for (int f = 0; f < NB; ++f) cnt += ((f < N) && tab.w[f] > 0.0f && isfinite(x[f])) ? 1 : 0;
     }
     float master = 0.0f, weight = 0.0f;
     int kept = 0;
@@ -695,8 +683,8 @@ __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
       FF w0, w1;
 #pragma unroll
       for (int f = 0; f < NB; f += 2) {
-        if (f < N) w0.add_prod(Rt[f * T], tab.w[f]);
-        if (f + 1 < N) w1.add_prod(Rt[(f + 1) * T], tab.w[f + 1]);
+        if (f < N) w0.add_prod(x[f], tab.w[f]);
+        if (f + 1 < N) w1.add_prod(x[f + 1], tab.w[f + 1]);
       }
       ff_merge2(w0, w1);
       kept = N;
@@ -708,9 +696,9 @@ __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
       FF ws, wsum;
 #pragma unroll
       for (int f = 0; f < NB; ++f) {
-        const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(Rt[f * T]) && !(thresholds && (Rt[f * T] < lt || Rt[f * T] > ht));
+        const bool ok = (f < N) && tab.w[f] > 0.0f && isfinite(x[f]) && !(thresholds && (x[f] < lt || x[f] > ht));
         if (ok) {
-          ws.add_prod(Rt[f * T], tab.w[f]);
+          ws.add_prod(x[f], tab.w[f]);
           wsum.add(tab.w[f]);
           ++kept;
         }
@@ -858,7 +846,7 @@ static void launch_reg(const IntegrateArgs& args, cudaStream_t stream) {
 template <int NB, int MODE>
 static void launch_col(const IntegrateArgs& args, cudaStream_t stream) {
   constexpr int T = 128;
-  const size_t smem = size_t(2) * NB * T * sizeof(float);
+  const size_t smem = size_t(NB) * T * sizeof(float);
   auto kern = integrate_col_kernel<NB, T, MODE>;
   check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
              "cudaFuncSetAttribute(integrate)");

@@ -92,6 +92,13 @@ struct gg_stack {
   // Device error word set by kernels whose bounded waits run out.
   int* d_error = nullptr;
 
+  // Lazily created per-feature scratch (star detection, registration), freed
+  // with the stack through their own release hooks.
+  void* star_scratch = nullptr;
+  void (*star_scratch_free)(void*) = nullptr;
+  void* reg_scratch = nullptr;
+  void (*reg_scratch_free)(void*) = nullptr;
+
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaStream_t copy_stream = nullptr;

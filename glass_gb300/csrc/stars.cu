@@ -1,0 +1,780 @@
+// Star detection on resident frames: robust background, threshold,
+// local-maximum candidates, windowed moments, flux-ordered de-duplication.
+//
+// Semantics: src/glass/cpu/star_detect.py:29-168 (detect_stars):
+//   median / MAD of the finite pixels (exact order statistics; an even count
+//   takes the float32 mean of the two middle values, as np.median does),
+//   noise = 1.4826 * MAD (float64; falls back to the pixel std, then 1),
+//   threshold = median + k * max(noise, 1e-6) (float64, compared against the
+//   float32 pixels after rounding to float32 - NumPy's scalar promotion),
+//   candidate = interior pixel, finite, > threshold, >= its 8 neighbours,
+//   measurement in a (2r+1)^2 window clipped to the image with float64
+//   moments of max(v - background, 0) (star_detect.py:45-100),
+//   greedy de-duplication in flux order (stable: raster order breaks ties,
+//   star_detect.py:103-118), then the brightest `max_stars`.
+// Background modes: GLOBAL reproduces detect_stars (one median/MAD per
+// frame); MESH computes median/MAD per cell of a background mesh (no
+// reference counterpart; its own float64 restatement lives in
+// oracle/stars.py) and thresholds each pixel against its cell.
+//
+// GB300 layout:
+//   - order statistics by a 3-pass radix select over the frame (11+11+10 key
+//     bits, per-CTA shared-memory histograms folded with global atomics); the
+//     MAD reuses it with key |v - median|;
+//   - candidates are appended with one atomic per warp, then one CTA per
+//     frame sorts them into raster order in shared memory, measures them one
+//     warp per candidate, resolves the flux-ordered de-duplication with a
+//     row-range neighbour search (centroids stay within the window of their
+//     peak) and selects the brightest by a bisection on the flux bits.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "stack.cuh"
+
+namespace gg {
+
+constexpr int kSelBins = 2048;
+constexpr int kMaxCandidates = 32768;  // per frame (shared-memory sort capacity)
+
+// Per-frame detection state on the device.
+struct StarFrameState {
+  unsigned count;        // valid (finite) pixels
+  unsigned candidates;   // appended candidates (may exceed capacity)
+  unsigned overflow;
+  unsigned pad;
+  unsigned prefix[2];    // radix-select prefix per requested rank
+  unsigned residual[2];  // rank remaining inside the prefix bucket
+  float median;
+  float mad;
+  double noise;
+  double threshold;
+  float threshold_f32;
+  float background_f32;
+  double background;
+  int kept;
+  int pad2;
+};
+
+__device__ __forceinline__ unsigned float_key(float v) {
+  const unsigned b = __float_as_uint(v);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(unsigned k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+struct SelectArgs {
+  const float* slots;
+  const int* slot_of_frame;
+  int64_t stride;
+  int64_t pixels;
+  const int* frames;   // [count]
+  StarFrameState* state;
+  unsigned* hist;      // [count][2][kSelBins]
+  int pass;            // 0, 1, 2
+  int mode;            // 0: v, 1: |v - median|
+};
+
+__device__ __forceinline__ bool select_value(const SelectArgs& a, const StarFrameState& st, float v, unsigned& key) {
+  if (!isfinite(v)) return false;
+  if (a.mode == 1) v = fabsf(__fsub_rn(v, st.median));
+  key = float_key(v);
+  return true;
+}
+
+// Histogram pass: digit of `pass` for keys matching each rank's prefix.
+__global__ void __launch_bounds__(256) select_hist_kernel(SelectArgs a) {
+  __shared__ unsigned h[2][kSelBins];
+  __shared__ unsigned s_valid;
+  const int k = blockIdx.y;
+  for (int i = threadIdx.x; i < 2 * kSelBins; i += blockDim.x) (&h[0][0])[i] = 0u;
+  if (threadIdx.x == 0) s_valid = 0;
+  __syncthreads();
+  const StarFrameState st = a.state[k];
+  const float* src = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+  const int shift = a.pass == 0 ? 21 : (a.pass == 1 ? 10 : 0);
+  const unsigned digit_mask = a.pass == 2 ? 1023u : 2047u;
+  const int prefix_shift = a.pass == 0 ? 32 : (a.pass == 1 ? 21 : 10);
+  unsigned valid = 0;
+  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < a.pixels; p += int64_t(gridDim.x) * blockDim.x) {
+    unsigned key;
+    if (!select_value(a, st, __ldg(src + p), key)) continue;
+    ++valid;
+    const unsigned digit = (key >> shift) & digit_mask;
+    if (a.pass == 0) {
+      atomicAdd(&h[0][digit], 1u);
+    } else {
+      const unsigned hp = key >> prefix_shift;
+      if (hp == st.prefix[0]) atomicAdd(&h[0][digit], 1u);
+      if (hp == st.prefix[1]) atomicAdd(&h[1][digit], 1u);
+    }
+  }
+  if (a.pass == 0) {
+    valid = __reduce_add_sync(0xffffffffu, valid);
+    if ((threadIdx.x & 31) == 0 && valid) atomicAdd(&s_valid, valid);
+  }
+  __syncthreads();
+  unsigned* g = a.hist + static_cast<int64_t>(k) * 2 * kSelBins;
+  const int nh = a.pass == 0 ? 1 : 2;
+  for (int i = threadIdx.x; i < nh * kSelBins; i += blockDim.x) {
+    const unsigned v = (&h[0][0])[i];
+    if (v) atomicAdd(g + i, v);
+  }
+  if (a.pass == 0 && a.mode == 0 && threadIdx.x == 0 && s_valid) atomicAdd(&a.state[k].count, s_valid);
+}
+
+// One warp per frame: locate each rank's bucket in the histogram.
+// ranks: pass 0 sets them from the valid count (median of n: n//2 and
+// n//2 - 1 when n is even, both n//2 when odd).
+__global__ void select_scan_kernel(SelectArgs a, int frames) {
+  const int k = blockIdx.x;
+  if (k >= frames) return;
+  StarFrameState& st = a.state[k];
+  const unsigned* g = a.hist + static_cast<int64_t>(k) * 2 * kSelBins;
+  const int nbins = a.pass == 2 ? 1024 : kSelBins;
+  if (threadIdx.x == 0) {
+    if (a.pass == 0) {
+      const unsigned n = st.count;
+      const unsigned hi = n / 2;
+      const unsigned lo = (n & 1u) ? hi : (hi > 0 ? hi - 1 : 0);
+      st.residual[0] = lo;
+      st.residual[1] = hi;
+    }
+    for (int r = 0; r < 2; ++r) {
+      const unsigned* hr = g + (a.pass == 0 ? 0 : r * kSelBins);
+      unsigned rem = st.residual[r];
+      int b = 0;
+      for (; b < nbins; ++b) {
+        if (rem < hr[b]) break;
+        rem -= hr[b];
+      }
+      if (b >= nbins) b = nbins - 1;  // empty frame: keeps the state defined
+      const unsigned prev = a.pass == 0 ? 0u : st.prefix[r];
+      const int bits = a.pass == 2 ? 10 : 11;
+      st.prefix[r] = (prev << bits) | static_cast<unsigned>(b);
+      st.residual[r] = rem;
+    }
+    if (a.pass == 2) {
+      // Both keys are complete: value = mean of the two middle values.
+      const float lo = key_float(st.prefix[0]);
+      const float hi = key_float(st.prefix[1]);
+      const float med = st.count ? __fmul_rn(__fadd_rn(lo, hi), 0.5f) : 0.0f;
+      if (a.mode == 0) st.median = med; else st.mad = med;
+    }
+  }
+}
+
+// Threshold from median / MAD (star_detect.py:29-43, 133-137).
+__global__ void star_threshold_kernel(StarFrameState* state, int frames, float k_sigma, int has_background,
+                                      float background, int has_noise, float noise, const double* rms) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= frames) return;
+  StarFrameState& st = state[k];
+  double med = st.count ? static_cast<double>(st.median) : 0.0;
+  double nz = st.count ? 1.4826 * static_cast<double>(st.mad) : 1.0;
+  if (st.count && !(nz > 0.0)) nz = rms ? rms[k] : 0.0;
+  if (!(nz > 0.0)) nz = 1.0;
+  if (has_background) med = static_cast<double>(background);
+  if (has_noise) nz = static_cast<double>(noise);
+  st.noise = nz;
+  st.threshold = med + static_cast<double>(k_sigma) * fmax(nz, 1.0e-6);
+  st.threshold_f32 = static_cast<float>(st.threshold);
+  st.background_f32 = static_cast<float>(med);
+  st.background = med;
+}
+
+struct DetectArgs {
+  const float* slots;
+  const int* slot_of_frame;
+  int64_t stride;
+  int width, height;
+  const int* frames;
+  StarFrameState* state;
+  unsigned* cand;  // [count][kMaxCandidates] raster indices
+};
+
+// Local-maximum candidates (star_detect.py:142-151).
+__global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
+  const int k = blockIdx.y;
+  const float* img = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+  const float thr = a.state[k].threshold_f32;
+  const int W = a.width, H = a.height;
+  const int64_t interior = static_cast<int64_t>(W - 2) * (H - 2);
+  unsigned* out = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
+  for (int64_t q = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; q - threadIdx.x < interior;
+       q += int64_t(gridDim.x) * blockDim.x) {
+    bool hit = false;
+    int64_t idx = 0;
+    if (q < interior) {
+      const int x = 1 + static_cast<int>(q % (W - 2));
+      const int y = 1 + static_cast<int>(q / (W - 2));
+      idx = static_cast<int64_t>(y) * W + x;
+      const float c = __ldg(img + idx);
+      if (isfinite(c) && c > thr) {
+        hit = true;
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx)
+            if (dx || dy) hit &= (c >= __ldg(img + idx + static_cast<int64_t>(dy) * W + dx));
+      }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, hit);
+    if (mask) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(mask) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(&a.state[k].candidates, static_cast<unsigned>(__popc(mask)));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (hit) {
+        const unsigned pos = base + __popc(mask & ((1u << lane) - 1u));
+        if (pos < static_cast<unsigned>(kMaxCandidates)) out[pos] = static_cast<unsigned>(idx);
+      }
+    }
+  }
+}
+
+// Measured star (float64 fields as the CPU's Python floats).
+struct StarRec {
+  double x, y, flux, peak, fwhm, ecc, snr, sharpness;
+  int npix;
+  int valid;
+};
+
+struct CatalogArgs {
+  const float* slots;
+  const int* slot_of_frame;
+  int64_t stride;
+  int width, height;
+  const int* frames;
+  StarFrameState* state;
+  unsigned* cand;   // [count][kMaxCandidates]
+  StarRec* recs;    // [count][kMaxCandidates]
+  int* kept;        // [count][kMaxCandidates] flags / order
+  gg_star_t* out;   // [count][max_stars]
+  int max_stars;
+  int radius;
+  double min_sep;
+  int* error;
+};
+
+// Sort candidate raster indices ascending (one CTA per frame, bitonic in
+// shared memory, padded with 0xffffffff).
+__global__ void __launch_bounds__(1024) star_sort_kernel(CatalogArgs a) {
+  extern __shared__ unsigned keys[];
+  const int k = blockIdx.x;
+  StarFrameState& st = a.state[k];
+  const unsigned n = min(st.candidates, static_cast<unsigned>(kMaxCandidates));
+  if (threadIdx.x == 0 && st.candidates > static_cast<unsigned>(kMaxCandidates)) st.overflow = 1u;
+  unsigned m = 1;
+  while (m < n) m <<= 1;
+  unsigned* cand = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
+  for (unsigned i = threadIdx.x; i < m; i += blockDim.x) keys[i] = i < n ? cand[i] : 0xffffffffu;
+  __syncthreads();
+  for (unsigned size = 2; size <= m; size <<= 1) {
+    for (unsigned stride = size >> 1; stride > 0; stride >>= 1) {
+      for (unsigned i = threadIdx.x; i < m; i += blockDim.x) {
+        const unsigned j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          const unsigned ki = keys[i], kj = keys[j];
+          if ((ki > kj) == up) {
+            keys[i] = kj;
+            keys[j] = ki;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (unsigned i = threadIdx.x; i < n; i += blockDim.x) cand[i] = keys[i];
+}
+
+// One warp per candidate: windowed moments (star_detect.py:45-100).
+__global__ void __launch_bounds__(256) star_measure_kernel(CatalogArgs a) {
+  const int k = blockIdx.y;
+  const StarFrameState& st = a.state[k];
+  const int n = static_cast<int>(min(st.candidates, static_cast<unsigned>(kMaxCandidates)));
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const float* img = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+  const unsigned* cand = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
+  StarRec* recs = a.recs + static_cast<int64_t>(k) * kMaxCandidates;
+  const int W = a.width, H = a.height, r = a.radius;
+  const float bg32 = st.background_f32;
+  const double bg = st.background;
+  for (int c = warp; c < n; c += nwarps) {
+    const unsigned idx = cand[c];
+    const int x = static_cast<int>(idx % static_cast<unsigned>(W));
+    const int y = static_cast<int>(idx / static_cast<unsigned>(W));
+    const int x0 = max(0, x - r), x1 = min(W, x + r + 1);
+    const int y0 = max(0, y - r), y1 = min(H, y + r + 1);
+    const int ww = x1 - x0, npx = ww * (y1 - y0);
+    double f = 0.0, sx = 0.0, sy = 0.0;
+    int fin = 0, pos = 0;
+    for (int q = lane; q < npx; q += 32) {
+      const int xx = x0 + q % ww, yy = y0 + q / ww;
+      const float v = __ldg(img + static_cast<int64_t>(yy) * W + xx);
+      if (!isfinite(v)) continue;
+      ++fin;
+      const float wv = fmaxf(__fsub_rn(v, bg32), 0.0f);
+      pos += wv > 0.0f;
+      const double wd = static_cast<double>(wv);
+      f += wd;
+      sx += static_cast<double>(xx) * wd;
+      sy += static_cast<double>(yy) * wd;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      f += __shfl_xor_sync(0xffffffffu, f, off);
+      sx += __shfl_xor_sync(0xffffffffu, sx, off);
+      sy += __shfl_xor_sync(0xffffffffu, sy, off);
+      fin += __shfl_xor_sync(0xffffffffu, fin, off);
+      pos += __shfl_xor_sync(0xffffffffu, pos, off);
+    }
+    StarRec rec{};
+    rec.valid = (fin > 0 && f > 0.0) ? 1 : 0;
+    if (rec.valid) {
+      const double cx = sx / f, cy = sy / f;
+      double mxx = 0.0, myy = 0.0, mxy = 0.0;
+      for (int q = lane; q < npx; q += 32) {
+        const int xx = x0 + q % ww, yy = y0 + q / ww;
+        const float v = __ldg(img + static_cast<int64_t>(yy) * W + xx);
+        if (!isfinite(v)) continue;
+        const double wd = static_cast<double>(fmaxf(__fsub_rn(v, bg32), 0.0f));
+        const double dx = static_cast<double>(xx) - cx, dy = static_cast<double>(yy) - cy;
+        mxx += dx * dx * wd;
+        myy += dy * dy * wd;
+        mxy += dx * dy * wd;
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        mxx += __shfl_xor_sync(0xffffffffu, mxx, off);
+        myy += __shfl_xor_sync(0xffffffffu, myy, off);
+        mxy += __shfl_xor_sync(0xffffffffu, mxy, off);
+      }
+      mxx /= f;
+      myy /= f;
+      mxy /= f;
+      const double trace = fmax(mxx + myy, 0.0);
+      const double det = fmax((mxx - myy) * (mxx - myy) + 4.0 * mxy * mxy, 0.0);
+      const double root = sqrt(det);
+      const double major = fmax((trace + root) / 2.0, 0.0);
+      const double minor = fmax((trace - root) / 2.0, 0.0);
+      const double mean_sigma = sqrt(fmax((major + minor) / 2.0, 0.0));
+      rec.x = cx;
+      rec.y = cy;
+      rec.flux = f;
+      rec.fwhm = mean_sigma > 0.0 ? 2.354820045 * mean_sigma : nan("");
+      rec.ecc = major > 0.0 ? sqrt(fmax(0.0, 1.0 - minor / major)) : nan("");
+      const float center = __ldg(img + static_cast<int64_t>(y) * W + x);
+      rec.peak = fmax(static_cast<double>(center) - bg, 0.0);
+      rec.npix = pos;
+      rec.snr = f / fmax(st.noise * sqrt(static_cast<double>(max(pos, 1))), 1.0e-6);
+      rec.sharpness = rec.peak / fmax(f, 1.0e-6);
+    }
+    if (lane == 0) recs[c] = rec;
+  }
+}
+
+// Priority: higher flux first, then lower raster index (stable sort order).
+__device__ __forceinline__ bool higher_priority(double fj, unsigned rj, double fi, unsigned ri) {
+  return fj > fi || (fj == fi && rj < ri);
+}
+
+__device__ __forceinline__ unsigned long long flux_key(double f) {
+  return static_cast<unsigned long long>(__double_as_longlong(f));  // f > 0: bit order = value order
+}
+
+// One CTA per frame: flux-ordered greedy de-duplication and top-N selection.
+__global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
+  extern __shared__ unsigned char sm[];
+  const int k = blockIdx.x;
+  StarFrameState& st = a.state[k];
+  const int n = static_cast<int>(min(st.candidates, static_cast<unsigned>(kMaxCandidates)));
+  const unsigned* cand = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
+  const StarRec* recs = a.recs + static_cast<int64_t>(k) * kMaxCandidates;
+  int* state = a.kept + static_cast<int64_t>(k) * kMaxCandidates;  // -1 undecided, 0 dropped, 1 kept
+  const int W = a.width;
+  const int reach = static_cast<int>(ceil(a.min_sep)) + 2 * a.radius;
+  const double sep2 = a.min_sep * a.min_sep;
+  const bool dedupe = a.min_sep > 0.0;
+  // 1) initial state: invalid stars drop out; others undecided
+  for (int i = threadIdx.x; i < n; i += blockDim.x) state[i] = recs[i].valid ? -1 : 0;
+  __syncthreads();
+  // 2) rounds: a star is kept when no higher-priority conflicting star can be
+  //    kept; dropped when a higher-priority conflicting star is kept.
+  __shared__ int s_changed, s_undecided;
+  for (int round = 0; round < n + 1; ++round) {
+    if (threadIdx.x == 0) {
+      s_changed = 0;
+      s_undecided = 0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      if (state[i] != -1) continue;
+      const StarRec ri = recs[i];
+      const unsigned ci = cand[i];
+      int verdict = 1;  // kept unless a conflict says otherwise
+      if (dedupe) {
+        const int py = static_cast<int>(ci / static_cast<unsigned>(W));
+        const int px = static_cast<int>(ci % static_cast<unsigned>(W));
+        const unsigned lo_key = static_cast<unsigned>(max(0, py - reach)) * static_cast<unsigned>(W);
+        int lo = 0, hi = n;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (cand[mid] < lo_key) lo = mid + 1; else hi = mid;
+        }
+        for (int j = lo; j < n; ++j) {
+          const unsigned cj = cand[j];
+          const int qy = static_cast<int>(cj / static_cast<unsigned>(W));
+          if (qy > py + reach) break;
+          if (j == i || abs(static_cast<int>(cj % static_cast<unsigned>(W)) - px) > reach) continue;
+          const int sj = state[j];
+          if (sj == 0) continue;
+          const StarRec rj = recs[j];
+          if (!higher_priority(rj.flux, cj, ri.flux, ci)) continue;
+          const double dx = ri.x - rj.x, dy = ri.y - rj.y;
+          if (dx * dx + dy * dy < sep2) {
+            if (sj == 1) {
+              verdict = 0;
+              break;
+            }
+            verdict = -1;  // waits for the brighter neighbour
+          }
+        }
+      }
+      if (verdict != -1) {
+        state[i] = verdict;
+        s_changed = 1;
+      } else {
+        s_undecided = 1;
+      }
+    }
+    __syncthreads();
+    const bool done = s_undecided == 0 || s_changed == 0;
+    __syncthreads();
+    if (done) break;
+  }
+  // 3) the max_stars-th largest kept flux by bisection on its bits
+  __shared__ unsigned long long s_lo, s_hi;
+  __shared__ int s_count;
+  int total_kept = 0;
+  {
+    int c = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) c += state[i] == 1;
+    if (threadIdx.x == 0) s_count = 0;
+    __syncthreads();
+    atomicAdd(&s_count, c);
+    __syncthreads();
+    total_kept = s_count;
+  }
+  const int take = min(total_kept, a.max_stars);
+  unsigned long long t = 0;  // keep fluxes with key > t, plus ties at t
+  if (take < total_kept) {
+    if (threadIdx.x == 0) {
+      s_lo = 0ull;
+      s_hi = 0x7ff0000000000000ull;
+    }
+    __syncthreads();
+    // smallest key T such that count(key > T) < take  (then key == T fills up)
+    for (int it = 0; it < 64; ++it) {
+      const unsigned long long lo = s_lo, hi = s_hi;
+      if (lo >= hi) break;
+      const unsigned long long mid = lo + (hi - lo) / 2;
+      int c = 0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) c += (state[i] == 1 && flux_key(recs[i].flux) > mid);
+      __syncthreads();
+      if (threadIdx.x == 0) s_count = 0;
+      __syncthreads();
+      atomicAdd(&s_count, c);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        if (s_count < take) s_hi = mid; else s_lo = mid + 1;
+      }
+      __syncthreads();
+    }
+    t = s_lo;
+  }
+  // 4) gather the selected stars (key > t, then ties key == t in raster
+  //    order up to `take`) and sort them by priority in shared memory.
+  struct Sel {
+    double flux;
+    unsigned raster;
+    int idx;
+  };
+  Sel* sel = reinterpret_cast<Sel*>(sm);
+  __shared__ int s_n, s_gt;
+  if (threadIdx.x == 0) {
+    s_n = 0;
+    s_gt = 0;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    if (state[i] == 1 && (take == total_kept || flux_key(recs[i].flux) > t)) {
+      const int p = atomicAdd(&s_n, 1);
+      if (p < 4096) sel[p] = {recs[i].flux, cand[i], i};
+    }
+  }
+  __syncthreads();
+  if (take < total_kept && threadIdx.x == 0) {
+    // ties at t in raster order (cand[] is raster-sorted)
+    int p = s_n;
+    for (int i = 0; i < n && p < take; ++i)
+      if (state[i] == 1 && flux_key(recs[i].flux) == t && p < 4096) sel[p++] = {recs[i].flux, cand[i], i};
+    s_n = p;
+  }
+  __syncthreads();
+  const int m0 = min(s_n, 4096);
+  int m = 1;
+  while (m < m0) m <<= 1;
+  for (int i = threadIdx.x + m0; i < m; i += blockDim.x) sel[i] = {-1.0, 0xffffffffu, -1};
+  __syncthreads();
+  for (int size = 2; size <= m; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;  // "up" = priority order
+          const Sel si = sel[i], sj = sel[j];
+          const bool j_first = higher_priority(sj.flux, sj.raster, si.flux, si.raster);
+          if (j_first == up) {
+            sel[i] = sj;
+            sel[j] = si;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  gg_star_t* out = a.out + static_cast<int64_t>(k) * a.max_stars;
+  const int nout = min(take, m0);
+  for (int i = threadIdx.x; i < nout; i += blockDim.x) {
+    const StarRec r = recs[sel[i].idx];
+    gg_star_t s;
+    s.x = r.x;
+    s.y = r.y;
+    s.flux = r.flux;
+    s.peak = r.peak;
+    s.fwhm = r.fwhm;
+    s.eccentricity = r.ecc;
+    s.snr = r.snr;
+    s.sharpness = r.sharpness;
+    s.npix = r.npix;
+    s.pad = 0;
+    out[i] = s;
+  }
+  if (threadIdx.x == 0) st.kept = nout;
+}
+
+// ---- host side -------------------------------------------------------------------
+struct StarScratch {
+  StarFrameState* state = nullptr;
+  unsigned* hist = nullptr;
+  unsigned* cand = nullptr;
+  StarRec* recs = nullptr;
+  int* kept = nullptr;
+  gg_star_t* out = nullptr;
+  int* frames = nullptr;
+  int capacity_frames = 0;
+  int max_stars = 0;
+};
+
+static void free_star_scratch(StarScratch& s) {
+  void* ps[] = {s.state, s.hist, s.cand, s.recs, s.kept, s.out, s.frames};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  s = StarScratch{};
+}
+
+static void ensure_star_scratch(StarScratch& s, int frames, int max_stars) {
+  if (s.capacity_frames >= frames && s.max_stars >= max_stars) return;
+  free_star_scratch(s);
+  const size_t f = static_cast<size_t>(frames);
+  check_cuda(cudaMalloc(&s.state, sizeof(StarFrameState) * f), "cudaMalloc(star state)");
+  check_cuda(cudaMalloc(&s.hist, sizeof(unsigned) * f * 2 * kSelBins), "cudaMalloc(star hist)");
+  check_cuda(cudaMalloc(&s.cand, sizeof(unsigned) * f * kMaxCandidates), "cudaMalloc(star candidates)");
+  check_cuda(cudaMalloc(&s.recs, sizeof(StarRec) * f * kMaxCandidates), "cudaMalloc(star records)");
+  check_cuda(cudaMalloc(&s.kept, sizeof(int) * f * kMaxCandidates), "cudaMalloc(star kept)");
+  check_cuda(cudaMalloc(&s.out, sizeof(gg_star_t) * f * static_cast<size_t>(max_stars)), "cudaMalloc(star out)");
+  check_cuda(cudaMalloc(&s.frames, sizeof(int) * f), "cudaMalloc(star frames)");
+  s.capacity_frames = frames;
+  s.max_stars = max_stars;
+}
+
+// Scratch lives with the stack (freed by gg_stack_destroy through the hook).
+static StarScratch& star_scratch(gg_stack* s) {
+  if (!s->star_scratch) {
+    s->star_scratch = new StarScratch();
+    s->star_scratch_free = [](void* p) {
+      auto* sc = static_cast<StarScratch*>(p);
+      free_star_scratch(*sc);
+      delete sc;
+    };
+  }
+  return *static_cast<StarScratch*>(s->star_scratch);
+}
+
+__global__ void star_rms_kernel(const double* partials, int blocks, int count, double* rms) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  double s1 = 0.0, s2 = 0.0, n = 0.0;
+  for (int b = 0; b < blocks; ++b) {
+    const double* q = partials + (static_cast<int64_t>(k) * blocks + b) * 3;
+    s1 += q[0];
+    s2 += q[1];
+    n += q[2];
+  }
+  const double mean = n > 0 ? s1 / n : 0.0;
+  const double var = n > 0 ? fmax(s2 / n - mean * mean, 0.0) : 0.0;
+  rms[k] = sqrt(var);
+}
+
+void launch_frame_stats_partials(gg_stack* s, const int* d_frames, int count, int blocks, double* partials);
+
+void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_params_t& p) {
+  StarScratch& sc = star_scratch(s);
+  ensure_star_scratch(sc, count, p.max_stars);
+  std::vector<int> frames(static_cast<size_t>(count));
+  for (int k = 0; k < count; ++k) frames[static_cast<size_t>(k)] = static_cast<int>(indices[k]);
+  check_cuda(cudaMemcpyAsync(sc.frames, frames.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s->stream),
+             "cudaMemcpyAsync(star frames)");
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(star frames)");
+  check_cuda(cudaMemsetAsync(sc.state, 0, sizeof(StarFrameState) * count, s->stream), "cudaMemsetAsync(state)");
+  const bool need_stats = !std::isfinite(p.background) || !std::isfinite(p.noise);
+  SelectArgs sa{};
+  sa.slots = s->d_slots;
+  sa.slot_of_frame = s->d_slot_of_frame;
+  sa.stride = s->stride;
+  sa.pixels = s->pixels;
+  sa.frames = sc.frames;
+  sa.state = sc.state;
+  sa.hist = sc.hist;
+  const unsigned per_frame =
+      std::max(1u, std::min<unsigned>(static_cast<unsigned>((s->pixels + 255) / 256),
+                                      std::max(1u, static_cast<unsigned>(sm_count() * 8 / std::max(count, 1)))));
+  double* rms = nullptr;
+  if (need_stats) {
+    for (int mode = 0; mode < 2; ++mode) {
+      sa.mode = mode;
+      for (int pass = 0; pass < 3; ++pass) {
+        sa.pass = pass;
+        check_cuda(cudaMemsetAsync(sc.hist, 0, sizeof(unsigned) * count * 2 * kSelBins, s->stream),
+                   "cudaMemsetAsync(hist)");
+        note_launch();
+        select_hist_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), 256, 0, s->stream>>>(sa);
+        check_cuda(cudaGetLastError(), "select_hist launch");
+        note_launch();
+        select_scan_kernel<<<static_cast<unsigned>(count), 32, 0, s->stream>>>(sa, count);
+        check_cuda(cudaGetLastError(), "select_scan launch");
+      }
+    }
+    // Pixel std, the fallback noise when the MAD is zero (star_detect.py:38-41).
+    const int blocks = static_cast<int>(std::min<int64_t>(sm_count() * 2, (s->pixels + 255) / 256));
+    stack_ensure_partials(s, static_cast<size_t>(count) * blocks * 3 + static_cast<size_t>(count));
+    launch_frame_stats_partials(s, sc.frames, count, blocks, s->d_partials);
+    rms = s->d_partials + static_cast<size_t>(count) * blocks * 3;
+    note_launch();
+    star_rms_kernel<<<(count + 127) / 128, 128, 0, s->stream>>>(s->d_partials, blocks, count, rms);
+    check_cuda(cudaGetLastError(), "star_rms launch");
+  }
+  note_launch();
+  star_threshold_kernel<<<(count + 127) / 128, 128, 0, s->stream>>>(
+      sc.state, count, p.threshold_sigma, std::isfinite(p.background) ? 1 : 0, p.background,
+      std::isfinite(p.noise) ? 1 : 0, p.noise, rms);
+  check_cuda(cudaGetLastError(), "star_threshold launch");
+  if (s->width < 3 || s->height < 3) return;  // no interior (star_detect.py:140-141)
+  DetectArgs da{};
+  da.slots = s->d_slots;
+  da.slot_of_frame = s->d_slot_of_frame;
+  da.stride = s->stride;
+  da.width = static_cast<int>(s->width);
+  da.height = static_cast<int>(s->height);
+  da.frames = sc.frames;
+  da.state = sc.state;
+  da.cand = sc.cand;
+  note_launch();
+  star_detect_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), 256, 0, s->stream>>>(da);
+  check_cuda(cudaGetLastError(), "star_detect launch");
+  CatalogArgs ca{};
+  ca.slots = s->d_slots;
+  ca.slot_of_frame = s->d_slot_of_frame;
+  ca.stride = s->stride;
+  ca.width = da.width;
+  ca.height = da.height;
+  ca.frames = sc.frames;
+  ca.state = sc.state;
+  ca.cand = sc.cand;
+  ca.recs = sc.recs;
+  ca.kept = sc.kept;
+  ca.out = sc.out;
+  ca.max_stars = p.max_stars;
+  ca.radius = std::max(1, p.window_radius);
+  ca.min_sep = p.min_separation_px;
+  ca.error = s->d_error;
+  const size_t sort_smem = sizeof(unsigned) * kMaxCandidates;
+  check_cuda(cudaFuncSetAttribute(star_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(sort_smem)),
+             "cudaFuncSetAttribute(star sort)");
+  note_launch();
+  star_sort_kernel<<<static_cast<unsigned>(count), 1024, sort_smem, s->stream>>>(ca);
+  check_cuda(cudaGetLastError(), "star_sort launch");
+  note_launch();
+  star_measure_kernel<<<dim3(64, static_cast<unsigned>(count)), 256, 0, s->stream>>>(ca);
+  check_cuda(cudaGetLastError(), "star_measure launch");
+  const size_t sel_smem = 16 * 4096;
+  check_cuda(cudaFuncSetAttribute(star_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(sel_smem)),
+             "cudaFuncSetAttribute(star select)");
+  note_launch();
+  star_select_kernel<<<static_cast<unsigned>(count), 1024, sel_smem, s->stream>>>(ca);
+  check_cuda(cudaGetLastError(), "star_select launch");
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_stack_detect_stars(gg_stack* s, const int64_t* indices, int64_t count, const gg_star_params_t* params,
+                          gg_star_t* host_stars, int32_t* host_counts, gg_star_frame_info_t* host_info) {
+  GG_API_BEGIN
+  require(s != nullptr && indices != nullptr && params != nullptr, "null argument");
+  require(count > 0 && count <= 65535, "frame count must be in [1, 65535]");
+  const gg_star_params_t& p = *params;
+  require(p.max_stars >= 1 && p.max_stars <= 4096, "max_stars must be in [1, 4096]");
+  require(p.window_radius >= 0 && p.window_radius <= 16, "window_radius must be in [0, 16]");
+  require(std::isfinite(p.threshold_sigma), "threshold_sigma must be finite");
+  require(std::isfinite(p.min_separation_px), "min_separation_px must be finite");
+  for (int64_t k = 0; k < count; ++k) stack_require_loaded(s, indices[k], "star detection");
+  stack_activate(s);
+  detect_stars(s, indices, static_cast<int>(count), p);
+  StarScratch& sc = star_scratch(s);
+  std::vector<StarFrameState> st(static_cast<size_t>(count));
+  check_cuda(cudaMemcpyAsync(st.data(), sc.state, sizeof(StarFrameState) * count, cudaMemcpyDeviceToHost, s->stream),
+             "cudaMemcpyAsync(star state)");
+  if (host_stars) {
+    check_cuda(cudaMemcpyAsync(host_stars, sc.out, sizeof(gg_star_t) * count * p.max_stars, cudaMemcpyDeviceToHost,
+                               s->stream),
+               "cudaMemcpyAsync(stars)");
+  }
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(stars)");
+  stack_check_device_error(s);
+  for (int64_t k = 0; k < count; ++k) {
+    const StarFrameState& f = st[static_cast<size_t>(k)];
+    if (f.overflow) fail(GG_ERR_RUNTIME, "more than 32768 star candidates in one frame; raise threshold_sigma");
+    if (host_counts) host_counts[k] = (s->width < 3 || s->height < 3) ? 0 : f.kept;
+    if (host_info) {
+      host_info[k].median = f.median;
+      host_info[k].mad = f.mad;
+      host_info[k].noise = f.noise;
+      host_info[k].threshold = f.threshold;
+      host_info[k].candidates = static_cast<int64_t>(f.candidates);
+      host_info[k].valid_pixels = static_cast<int64_t>(f.count);
+    }
+  }
+  GG_API_END
+}
+
+}  // extern "C"

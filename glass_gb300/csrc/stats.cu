@@ -113,6 +113,14 @@ __global__ void snr_weights_kernel(const double* partials, int blocks, const int
   weights[f] = static_cast<float>(w);
 }
 
+// Per-CTA (sum, sum2, count) partials of the given frames (device frame list).
+void launch_frame_stats_partials(gg_stack* s, const int* d_frames, int count, int blocks, double* partials) {
+  note_launch();
+  frame_stats_kernel<<<dim3(blocks, static_cast<unsigned>(count)), 256, 0, s->stream>>>(
+      s->d_slots, s->d_slot_of_frame, s->stride, s->pixels, d_frames, partials);
+  check_cuda(cudaGetLastError(), "frame_stats kernel launch");
+}
+
 }  // namespace gg
 
 using namespace gg;

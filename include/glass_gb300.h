@@ -230,6 +230,49 @@ typedef struct {
 } gg_stack_device_ptrs_t;
 int gg_stack_device_ptrs(gg_stack* stack, gg_stack_device_ptrs_t* out);
 
+/* ---- star detection ------------------------------------------------------ */
+/* Parameters of detect_stars (cpu/star_detect.py:121-132).  background /
+ * noise: NaN estimates them (median / 1.4826*MAD of the finite pixels). */
+typedef struct {
+  float threshold_sigma;   /* 5.0   */
+  int max_stars;           /* 500, at most 4096 */
+  int window_radius;       /* 4     */
+  float min_separation_px; /* 2.0   */
+  float background;        /* NaN   */
+  float noise;             /* NaN   */
+} gg_star_params_t;
+
+/* One star (cpu/star_detect.py:8-18); fwhm / eccentricity NaN when undefined. */
+typedef struct {
+  double x;
+  double y;
+  double flux;
+  double peak;
+  double fwhm;
+  double eccentricity;
+  double snr;
+  double sharpness;
+  int32_t npix;
+  int32_t pad;
+} gg_star_t;
+
+typedef struct {
+  float median;
+  float mad;
+  double noise;
+  double threshold;
+  int64_t candidates;
+  int64_t valid_pixels;
+} gg_star_frame_info_t;
+
+/* detect_stars for `count` resident frames (star_detect.py:121-168; reference
+ * device path: star_detect_kernels.cu, native_bindings.cpp:12123).  host_stars
+ * receives count * max_stars records (brightest first), host_counts the stars
+ * per frame; host_info (may be NULL) the background statistics.  The
+ * catalogs also stay on the device for registration. */
+int gg_stack_detect_stars(gg_stack* stack, const int64_t* indices, int64_t count, const gg_star_params_t* params,
+                          gg_star_t* host_stars, int32_t* host_counts, gg_star_frame_info_t* host_info);
+
 /* ---- warps --------------------------------------------------------------- */
 /* Warps `count` resident frames in place through their forward matrices
  * (float64 row-major 3x3, moving -> reference; the kernel samples the source

@@ -271,6 +271,73 @@ def make_warp(ref_src: Path) -> None:
     np.savez_compressed(HERE / "warp.npz", **arrays)
 
 
+# ---------------------------------------------------------------------------
+# star detection
+# ---------------------------------------------------------------------------
+STAR_FIELDS = ("x", "y", "flux", "peak", "fwhm_px", "eccentricity", "snr", "sharpness", "npix")
+
+
+def _star_field(rng, h, w, n, background, noise, fwhm=(2.0, 3.5)):
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    img = np.full((h, w), background, dtype=np.float64)
+    for _ in range(n):
+        x0, y0 = rng.uniform(2, w - 3), rng.uniform(2, h - 3)
+        s = rng.uniform(*fwhm) / 2.3548
+        img += rng.uniform(200, 20000) * np.exp(-((xx - x0) ** 2 + (yy - y0) ** 2) / (2 * s * s))
+    img += noise * rng.standard_normal((h, w))
+    return img.astype(np.float32)
+
+
+def make_stars(ref_src: Path) -> None:
+    """detect_stars (src/glass/cpu/star_detect.py:121-168) on seeded fields and
+    on the reference tests' own images (tests/test_cpu_star_detect.py:15-38,
+    rendered by src/glass/synthetic/generator.py:render_star_field)."""
+    sys.path.insert(0, str(ref_src))
+    from glass.cpu.star_detect import detect_stars  # noqa: E402
+
+    gen: dict = {"np": np}
+    _load_functions(ref_src / "glass" / "synthetic" / "generator.py", ["render_star_field"], gen)
+    rng = np.random.default_rng(314)
+    cases = []
+    stars = np.array([[16.0, 16.0, 1000.0], [8.0, 20.0, 800.0]], dtype=np.float32)
+    cases.append(("reftest_two_stars", gen["render_star_field"](32, 32, stars), dict(threshold_sigma=3.0)))
+    yy, xx = np.mgrid[0:64, 0:64]
+    ell = (1000.0 * np.exp(-(((xx - 32.0) / 2.3) ** 2 + ((yy - 32.0) / 1.0) ** 2) / 2.0)).astype(np.float32)
+    cases.append(("reftest_elliptical", ell, dict(threshold_sigma=3.0)))
+    for k in range(6):
+        h, w = int(rng.integers(40, 120)), int(rng.integers(40, 140))
+        img = _star_field(rng, h, w, int(rng.integers(5, 60)), 1000.0, 15.0)
+        if k % 2:
+            img[rng.random((h, w)) < 0.01] = np.nan
+        if k == 2:  # plateau: two equal neighbouring maxima
+            img[20, 20] = img[20, 21] = 30000.0
+        if k == 3:  # close pair (de-duplication)
+            img[30, 30] = 25000.0
+            img[31, 32] = 24000.0
+        params = dict(threshold_sigma=float(rng.choice([3.0, 5.0])), max_stars=int(rng.choice([5, 20, 500])))
+        cases.append((f"field{k}", img, params))
+    cases.append(("field_big", _star_field(rng, 256, 256, 300, 800.0, 10.0), dict(threshold_sigma=5.0)))
+    cases.append(("field_given_bg", _star_field(rng, 64, 64, 10, 500.0, 8.0),
+                  dict(threshold_sigma=4.0, background=480.25, noise=9.5)))
+    cases.append(("field_window2_sep5", _star_field(rng, 80, 90, 40, 1200.0, 20.0),
+                  dict(threshold_sigma=3.0, window_radius=2, min_separation_px=5.0)))
+    flat = np.full((20, 24), 7.0, dtype=np.float32)
+    flat[10, 12] = 50.0
+    cases.append(("constant_background", flat, dict(threshold_sigma=3.0)))
+    arrays: dict[str, np.ndarray] = {}
+    names = []
+    for name, img, params in cases:
+        found = detect_stars(img, **params)
+        arrays[f"{name}/image"] = img
+        arrays[f"{name}/params"] = np.asarray(repr(params))
+        for field in STAR_FIELDS:
+            vals = [getattr(s, field) for s in found]
+            arrays[f"{name}/{field}"] = np.asarray([np.nan if v is None else v for v in vals], dtype=np.float64)
+        names.append(name)
+    arrays["_names"] = np.asarray(names)
+    np.savez_compressed(HERE / "stars.npz", **arrays)
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__)
     parser.add_argument("--reference", default="/root/reference", help="GLASS reference checkout")
@@ -278,7 +345,8 @@ def main() -> int:
     args = parser.parse_args()
     ref = Path(args.reference)
     src = ref / "src"
-    jobs = {"integration": make_integration, "calibration": make_calibration, "warp": make_warp}
+    jobs = {"integration": make_integration, "calibration": make_calibration, "warp": make_warp,
+            "stars": make_stars}
     only = [j for j in args.only.split(",") if j] or list(jobs)
     for job in only:
         jobs[job](src)
