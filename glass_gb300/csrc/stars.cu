@@ -567,6 +567,188 @@ __global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
   if (threadIdx.x == 0) st.kept = nout;
 }
 
+// ---- np.std of the finite pixels, bit-exact (fallback noise, MAD == 0) -----
+// NumPy sums a contiguous float32 array pairwise: blocks of <= 128 use eight
+// interleaved accumulators, longer runs split at n/2 rounded down to a
+// multiple of 8 (verified against np.sum).  np.std(finite) is
+// sqrt(pairwise((x - m)^2) / n) with m = pairwise(x) / n, all float32.  The
+// finite pixels form a compacted sequence; a per-1024-pixel finite-count
+// prefix maps a compacted index back to raster order.  One CTA walks the
+// frames of the batch in turn and only works on frames whose MAD is zero.
+constexpr int kPwBlock = 1024;
+
+struct PwArgs {
+  const float* slots;
+  const int* slot_of_frame;
+  int64_t stride;
+  int64_t pixels;
+  const int* frames;
+  int count;
+  StarFrameState* state;
+  double* rms;     // [count]
+  int* prefix;     // [pixels / kPwBlock + 2]
+  int2* leaves;    // [pixels / 64 + 2]
+  float* leaf_sum; // [pixels / 64 + 2]
+};
+
+// Position of the `c`-th finite pixel (compacted index) in raster order.
+__device__ int64_t finite_position(const float* src, const int* prefix, int nblocks, int64_t pixels, int64_t c,
+                                   bool dense) {
+  if (dense) return c;
+  int lo = 0, hi = nblocks;  // last block with prefix <= c
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= c) lo = mid; else hi = mid;
+  }
+  int64_t p = static_cast<int64_t>(lo) * kPwBlock;
+  int64_t seen = prefix[lo];
+  for (; p < pixels; ++p) {
+    if (isfinite(src[p])) {
+      if (seen == c) return p;
+      ++seen;
+    }
+  }
+  return pixels;
+}
+
+__device__ float pw_leaf(const float* src, const int* prefix, int nblocks, int64_t pixels, bool dense, int64_t off,
+                         int len, bool square, float mean) {
+  int64_t p = finite_position(src, prefix, nblocks, pixels, off, dense);
+  auto next = [&]() -> float {
+    while (!isfinite(src[p])) ++p;
+    float v = src[p++];
+    if (square) {
+      const float d = __fsub_rn(v, mean);
+      v = __fmul_rn(d, d);
+    }
+    return v;
+  };
+  if (len < 8) {
+    float r = 0.0f;
+    for (int i = 0; i < len; ++i) r = __fadd_rn(r, next());
+    return r;
+  }
+  float r[8];
+  for (int j = 0; j < 8; ++j) r[j] = next();
+  int i = 8;
+  for (; i < len - (len % 8); i += 8)
+    for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], next());
+  float res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
+                        __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
+  for (; i < len; ++i) res = __fadd_rn(res, next());
+  return res;
+}
+
+__device__ __forceinline__ int64_t pw_split(int64_t n) {
+  int64_t n2 = n / 2;
+  return n2 - n2 % 8;
+}
+
+// Thread 0: leaves of the pairwise tree in left-to-right order.
+__device__ int pw_leaves(int64_t n, int2* leaves) {
+  int64_t st_off[96], st_n[96];
+  int top = 0, count = 0;
+  st_off[0] = 0;
+  st_n[0] = n;
+  top = 1;
+  while (top > 0) {
+    --top;
+    const int64_t off = st_off[top], m = st_n[top];
+    if (m <= 128) {
+      leaves[count++] = make_int2(static_cast<int>(off), static_cast<int>(m));
+    } else {
+      const int64_t m2 = pw_split(m);
+      st_off[top] = off + m2;
+      st_n[top] = m - m2;
+      ++top;
+      st_off[top] = off;
+      st_n[top] = m2;
+      ++top;
+    }
+  }
+  return count;
+}
+
+// Thread 0: fold the leaf sums in the tree's order (left + right at each node).
+__device__ float pw_fold(int64_t n, const float* leaf_sum) {
+  int64_t node_n[96];
+  int node_state[96];
+  float vals[96];
+  int top = 1, vtop = 0, next = 0;
+  node_n[0] = n;
+  node_state[0] = 0;
+  while (top > 0) {
+    const int64_t m = node_n[top - 1];
+    if (m <= 128) {
+      --top;
+      vals[vtop++] = leaf_sum[next++];
+    } else if (node_state[top - 1] == 0) {
+      node_state[top - 1] = 1;
+      const int64_t m2 = pw_split(m);
+      node_n[top] = m - m2;
+      node_state[top] = 0;
+      ++top;
+      node_n[top] = m2;
+      node_state[top] = 0;
+      ++top;
+    } else {
+      --top;
+      const float b = vals[--vtop];
+      const float a = vals[--vtop];
+      vals[vtop++] = __fadd_rn(a, b);
+    }
+  }
+  return vals[0];
+}
+
+__global__ void __launch_bounds__(1024) pairwise_std_kernel(PwArgs a) {
+  __shared__ int s_leaves;
+  __shared__ float s_mean;
+  const int nblocks = static_cast<int>((a.pixels + kPwBlock - 1) / kPwBlock);
+  for (int k = 0; k < a.count; ++k) {
+    const StarFrameState& st = a.state[k];
+    if (st.count == 0 || !(1.4826 * static_cast<double>(st.mad) <= 0.0)) continue;  // uniform branch
+    const float* src = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+    const bool dense = static_cast<int64_t>(st.count) == a.pixels;
+    if (!dense) {
+      // finite counts per block, then an exclusive prefix (thread 0)
+      for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        int c = 0;
+        const int64_t p1 = min(a.pixels, static_cast<int64_t>(b + 1) * kPwBlock);
+        for (int64_t p = static_cast<int64_t>(b) * kPwBlock; p < p1; ++p) c += isfinite(src[p]) ? 1 : 0;
+        a.prefix[b + 1] = c;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        a.prefix[0] = 0;
+        for (int b = 1; b <= nblocks; ++b) a.prefix[b] += a.prefix[b - 1];
+      }
+    }
+    const int64_t n = st.count;
+    if (threadIdx.x == 0) s_leaves = pw_leaves(n, a.leaves);
+    __syncthreads();
+    const int L = s_leaves;
+    for (int pass = 0; pass < 2; ++pass) {
+      const float mean = pass ? s_mean : 0.0f;
+      for (int l = threadIdx.x; l < L; l += blockDim.x) {
+        const int2 lf = a.leaves[l];
+        a.leaf_sum[l] = pw_leaf(src, a.prefix, nblocks, a.pixels, dense, lf.x, lf.y, pass == 1, mean);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const float total = pw_fold(n, a.leaf_sum);
+        const float fn = static_cast<float>(n);
+        if (pass == 0) {
+          s_mean = __fdiv_rn(total, fn);
+        } else {
+          a.rms[k] = static_cast<double>(__fsqrt_rn(__fdiv_rn(total, fn)));
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // ---- host side -------------------------------------------------------------------
 struct StarScratch {
   StarFrameState* state = nullptr;
@@ -576,12 +758,17 @@ struct StarScratch {
   int* kept = nullptr;
   gg_star_t* out = nullptr;
   int* frames = nullptr;
+  double* rms = nullptr;
+  int* pw_prefix = nullptr;
+  int2* pw_leaves = nullptr;
+  float* pw_sums = nullptr;
+  int64_t pw_pixels = 0;
   int capacity_frames = 0;
   int max_stars = 0;
 };
 
 static void free_star_scratch(StarScratch& s) {
-  void* ps[] = {s.state, s.hist, s.cand, s.recs, s.kept, s.out, s.frames};
+  void* ps[] = {s.state, s.hist, s.cand, s.recs, s.kept, s.out, s.frames, s.rms, s.pw_prefix, s.pw_leaves, s.pw_sums};
   for (void* p : ps)
     if (p) cudaFree(p);
   s = StarScratch{};
@@ -598,6 +785,7 @@ static void ensure_star_scratch(StarScratch& s, int frames, int max_stars) {
   check_cuda(cudaMalloc(&s.kept, sizeof(int) * f * kMaxCandidates), "cudaMalloc(star kept)");
   check_cuda(cudaMalloc(&s.out, sizeof(gg_star_t) * f * static_cast<size_t>(max_stars)), "cudaMalloc(star out)");
   check_cuda(cudaMalloc(&s.frames, sizeof(int) * f), "cudaMalloc(star frames)");
+  check_cuda(cudaMalloc(&s.rms, sizeof(double) * f), "cudaMalloc(star rms)");
   s.capacity_frames = frames;
   s.max_stars = max_stars;
 }
@@ -669,14 +857,36 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
         check_cuda(cudaGetLastError(), "select_scan launch");
       }
     }
-    // Pixel std, the fallback noise when the MAD is zero (star_detect.py:38-41).
-    const int blocks = static_cast<int>(std::min<int64_t>(sm_count() * 2, (s->pixels + 255) / 256));
-    stack_ensure_partials(s, static_cast<size_t>(count) * blocks * 3 + static_cast<size_t>(count));
-    launch_frame_stats_partials(s, sc.frames, count, blocks, s->d_partials);
-    rms = s->d_partials + static_cast<size_t>(count) * blocks * 3;
+    // np.std of the finite pixels, the fallback noise when the MAD is zero
+    // (star_detect.py:35-41); computed only for such frames.
+    if (sc.pw_pixels != s->pixels) {
+      if (sc.pw_prefix) cudaFree(sc.pw_prefix);
+      if (sc.pw_leaves) cudaFree(sc.pw_leaves);
+      if (sc.pw_sums) cudaFree(sc.pw_sums);
+      const size_t nb = static_cast<size_t>(s->pixels / kPwBlock + 2);
+      // leaves hold >= 57 elements once n > 128 (split at n/2 rounded down to 8)
+      const size_t nl = static_cast<size_t>(s->pixels / 32 + 2);
+      check_cuda(cudaMalloc(&sc.pw_prefix, sizeof(int) * nb), "cudaMalloc(pairwise prefix)");
+      check_cuda(cudaMalloc(&sc.pw_leaves, sizeof(int2) * nl), "cudaMalloc(pairwise leaves)");
+      check_cuda(cudaMalloc(&sc.pw_sums, sizeof(float) * nl), "cudaMalloc(pairwise sums)");
+      sc.pw_pixels = s->pixels;
+    }
+    PwArgs pa{};
+    pa.slots = s->d_slots;
+    pa.slot_of_frame = s->d_slot_of_frame;
+    pa.stride = s->stride;
+    pa.pixels = s->pixels;
+    pa.frames = sc.frames;
+    pa.count = count;
+    pa.state = sc.state;
+    pa.rms = sc.rms;
+    pa.prefix = sc.pw_prefix;
+    pa.leaves = sc.pw_leaves;
+    pa.leaf_sum = sc.pw_sums;
+    rms = sc.rms;
     note_launch();
-    star_rms_kernel<<<(count + 127) / 128, 128, 0, s->stream>>>(s->d_partials, blocks, count, rms);
-    check_cuda(cudaGetLastError(), "star_rms launch");
+    pairwise_std_kernel<<<1, 1024, 0, s->stream>>>(pa);
+    check_cuda(cudaGetLastError(), "pairwise_std launch");
   }
   note_launch();
   star_threshold_kernel<<<(count + 127) / 128, 128, 0, s->stream>>>(
