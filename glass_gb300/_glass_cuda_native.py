@@ -216,6 +216,172 @@ def detect_stars_f32(data: Any, threshold_sigma: float = 5.0, max_stars: int = 5
         stack.close()
 
 
+# ---- registration: triangle asterisms (cpu/registration.py:242-475) ----------------
+_REG_MAX_STARS = 80
+
+
+def _catalog_xy(x: Any, y: Any) -> np.ndarray:
+    xa = np.asarray(x, dtype=np.float32).reshape(-1)
+    ya = np.asarray(y, dtype=np.float32).reshape(-1)
+    if xa.shape != ya.shape:
+        raise ValueError("catalog coordinate arrays must have the same shape")
+    return np.ascontiguousarray(np.column_stack([xa, ya]).astype(np.float64))
+
+
+def _points_xy(points: Any) -> np.ndarray:
+    """(n, 2) float64 (x, y) from an array or a list of objects with .x/.y."""
+    if isinstance(points, np.ndarray) and points.dtype.names and "x" in points.dtype.names:
+        xy = np.column_stack([points["x"], points["y"]])
+    elif isinstance(points, (list, tuple)) and points and hasattr(points[0], "x"):
+        xy = [(p.x, p.y) for p in points]
+    else:
+        xy = points
+    arr = np.asarray(xy, dtype=np.float64).reshape(-1, 2)
+    return np.ascontiguousarray(arr)
+
+
+def _register_params(transform_model: str, min_inliers: int, tolerance_px: float, max_stars: int, neighbors: int,
+                     descriptor_radius: float, max_descriptors: int, max_candidates: int) -> _lib.RegisterParams:
+    if transform_model != "similarity":
+        raise ValueError("triangle asterism registration on the GPU supports the similarity model")
+    return _lib.RegisterParams(_lib.GG_TRANSFORM_SIMILARITY, int(min_inliers), float(tolerance_px),
+                               float(descriptor_radius), int(max_stars), int(neighbors), int(max_descriptors),
+                               int(max_candidates))
+
+
+def _registration_dict(r: _lib.Registration, pairs: np.ndarray | None = None) -> dict[str, Any]:
+    out = {
+        "transform_model": "similarity",
+        "matrix": np.asarray(r.matrix, dtype=np.float64).reshape(3, 3),
+        "matched_stars": int(r.inliers),
+        "inliers": int(r.inliers),
+        "rms_px": float(r.rms_px),
+        "status": "ok" if r.status == 1 else "failed",
+        "best_candidate_index": int(r.best_candidate),
+        "reference_descriptor_count": int(r.descriptors_reference),
+        "moving_descriptor_count": int(r.descriptors_moving),
+        "descriptor_matches": int(r.matches),
+    }
+    if pairs is not None:
+        p = pairs.reshape(-1, 2)[: int(r.inliers)]
+        out["pairs"] = [(int(a), int(b)) for a, b in p]
+    return out
+
+
+def triangle_asterism_descriptors_f32(x: Any, y: Any, max_stars: int = 80, neighbors: int = 5,
+                                      max_descriptors: int = 1200) -> dict[str, Any]:
+    """Module triangle_asterism_descriptors_f32 (glass_cuda.py:1835-1902): local
+    triangle descriptors of one catalog, area-descending."""
+    if max_stars < 0:
+        raise ValueError("max_stars must be non-negative")
+    if max_descriptors < 0:
+        raise ValueError("max_descriptors must be non-negative")
+    xy = _catalog_xy(x, y)
+    limited = min(len(xy), int(max_stars))
+    cap = limited * 20
+    desc = np.zeros((max(cap, 1), 2), dtype=np.float64)
+    idx = np.zeros((max(cap, 1), 3), dtype=np.int32)
+    areas = np.zeros(max(cap, 1), dtype=np.float64)
+    count = ctypes.c_int64()
+    _lib.call("gg_triangle_descriptors", _lib.ptr(xy), ctypes.c_int64(len(xy)), ctypes.c_int32(int(max_stars)),
+              ctypes.c_int32(int(neighbors)), ctypes.c_int32(int(max_descriptors)), _lib.ptr(desc), _lib.ptr(idx),
+              _lib.ptr(areas), ctypes.c_int64(desc.shape[0]), ctypes.byref(count))
+    n = int(count.value)
+    k = min(limited, max(3, int(neighbors)))
+    raw = limited * k * (k - 1) * (k - 2) // 6 if limited >= 3 else 0
+    return {"count": n, "raw_count": int(raw), "max_stars": int(max_stars), "neighbors": int(k),
+            "descriptors": desc[:n].astype(np.float32), "indices": idx[:n].copy(),
+            "areas": areas[:n].astype(np.float32), "model": "triangle_asterism_descriptors_cuda"}
+
+
+def triangle_asterism_descriptors_batch_f32(x_list: list[Any], y_list: list[Any], max_stars: int = 80,
+                                            neighbors: int = 5, max_descriptors: int = 1200) -> list[dict[str, Any]]:
+    """Module triangle_asterism_descriptors_batch_f32 (glass_cuda.py:1935-1990)."""
+    if len(x_list) != len(y_list):
+        raise ValueError("catalog x/y batch lists must have the same length")
+    out = []
+    for k, (x, y) in enumerate(zip(x_list, y_list)):
+        r = triangle_asterism_descriptors_f32(x, y, max_stars, neighbors, max_descriptors)
+        r.update(batch_index=k, batch_count=len(x_list), batch_model="triangle_asterism_descriptors_cuda_batch")
+        out.append(r)
+    return out
+
+
+def estimate_similarity_from_triangle_descriptors_f32(reference_x: Any, reference_y: Any, moving_x: Any,
+                                                      moving_y: Any, reference_descriptors: Any,
+                                                      reference_indices: Any, moving_descriptors: Any,
+                                                      moving_indices: Any, tolerance_px: float = 2.0,
+                                                      descriptor_radius: float = 0.1) -> dict[str, Any]:
+    """Module estimate_similarity_from_triangle_descriptors_f32
+    (glass_cuda.py:2054-2140): best similarity over every descriptor pair within
+    the radius (reference-major), both orientations, no refit."""
+    if tolerance_px < 0.0:
+        raise ValueError("tolerance_px must be non-negative")
+    if descriptor_radius < 0.0:
+        raise ValueError("descriptor_radius must be non-negative")
+    ref = _catalog_xy(reference_x, reference_y)
+    mov = _catalog_xy(moving_x, moving_y)
+    rd = np.ascontiguousarray(np.asarray(reference_descriptors, dtype=np.float32).reshape(-1, 2))
+    md = np.ascontiguousarray(np.asarray(moving_descriptors, dtype=np.float32).reshape(-1, 2))
+    ri = np.ascontiguousarray(np.asarray(reference_indices, dtype=np.int32).reshape(-1, 3))
+    mi = np.ascontiguousarray(np.asarray(moving_indices, dtype=np.int32).reshape(-1, 3))
+    if rd.shape[0] != ri.shape[0] or md.shape[0] != mi.shape[0]:
+        raise ValueError("descriptor and index row counts must match")
+    res = _lib.Registration()
+    _lib.call("gg_similarity_from_descriptors", _lib.ptr(ref), ctypes.c_int64(len(ref)), _lib.ptr(mov),
+              ctypes.c_int64(len(mov)), _lib.ptr(rd), _lib.ptr(ri), ctypes.c_int64(rd.shape[0]), _lib.ptr(md),
+              _lib.ptr(mi), ctypes.c_int64(md.shape[0]), ctypes.c_double(float(tolerance_px)),
+              ctypes.c_double(float(descriptor_radius)), ctypes.byref(res), None)
+    m = np.asarray(res.matrix, dtype=np.float64).reshape(3, 3)
+    a, b = float(m[0, 0]), float(m[1, 0])
+    return {"matrix": m.astype(np.float32).tolist(), "scale": float(np.sqrt(a * a + b * b)),
+            "rotation_rad": float(np.arctan2(b, a)), "rms_px": float(res.rms_px), "inliers": int(res.inliers),
+            "best_candidate_index": int(res.best_candidate), "candidate_count": int(rd.shape[0] * md.shape[0] * 2),
+            "reference_count": int(len(ref)), "moving_count": int(len(mov)),
+            "reference_descriptor_count": int(rd.shape[0]), "moving_descriptor_count": int(md.shape[0]),
+            "tolerance_px": float(tolerance_px), "descriptor_radius": float(descriptor_radius),
+            "status": "ok" if res.inliers > 0 else "failed", "model": "triangle_descriptor_similarity_cuda"}
+
+
+def estimate_similarity_from_triangle_descriptors_batch_f32(reference_x: Any, reference_y: Any,
+                                                            reference_descriptors: Any, reference_indices: Any,
+                                                            moving_x_list: list[Any], moving_y_list: list[Any],
+                                                            moving_descriptors_list: list[Any],
+                                                            moving_indices_list: list[Any],
+                                                            tolerance_px: float = 2.0,
+                                                            descriptor_radius: float = 0.1) -> list[dict[str, Any]]:
+    """Module estimate_similarity_from_triangle_descriptors_batch_f32 (glass_cuda.py:2149-2230)."""
+    lists = (moving_x_list, moving_y_list, moving_descriptors_list, moving_indices_list)
+    if len({len(v) for v in lists}) != 1:
+        raise ValueError("moving batch lists must have the same length")
+    out = []
+    for k, (mx, my, md, mi) in enumerate(zip(*lists)):
+        r = estimate_similarity_from_triangle_descriptors_f32(reference_x, reference_y, mx, my,
+                                                              reference_descriptors, reference_indices, md, mi,
+                                                              tolerance_px, descriptor_radius)
+        r.update(batch_index=k, batch_count=len(moving_x_list), batch_model="triangle_descriptor_similarity_cuda")
+        out.append(r)
+    return out
+
+
+def estimate_triangle_asterism_transform(reference: Any, moving: Any, transform_model: str = "similarity",
+                                         min_inliers: int = 6, tolerance_px: float = 3.0, max_stars: int = 80,
+                                         neighbors: int = 5, descriptor_radius: float = 0.1,
+                                         max_descriptors: int = 1200, max_candidates: int = 1500) -> dict[str, Any]:
+    """estimate_triangle_asterism_transform (cpu/registration.py:361-475) on the
+    GPU.  reference / moving: (n, 2) arrays, star records or Star-like objects,
+    brightest first.  Returns the StarRegistration fields as a dict."""
+    params = _register_params(transform_model, min_inliers, tolerance_px, max_stars, neighbors, descriptor_radius,
+                              max_descriptors, max_candidates)
+    ref = _points_xy(reference)
+    mov = _points_xy(moving)
+    res = _lib.Registration()
+    pairs = np.full((_REG_MAX_STARS, 2), -1, dtype=np.int32)
+    _lib.call("gg_register_star_lists", _lib.ptr(ref), ctypes.c_int64(len(ref)), _lib.ptr(mov),
+              ctypes.c_int64(len(mov)), ctypes.byref(params), ctypes.byref(res), _lib.ptr(pairs))
+    return _registration_dict(res, pairs)
+
+
 def resident_dq_map_count_maps_i16(master: Any, weight_map: Any, coverage_map: Any | None = None,
                                    low_rejection_map: Any | None = None,
                                    high_rejection_map: Any | None = None,
@@ -466,6 +632,23 @@ class ResidentCalibratedStack:
                      "valid_pixels": int(i.valid_pixels)} for i in info]
             return catalogs, meta
         return catalogs
+
+    def register_frames_triangle(self, reference_index: int, indices: Any, transform_model: str = "similarity",
+                                 min_inliers: int = 6, tolerance_px: float = 3.0, max_stars: int = 80,
+                                 neighbors: int = 5, descriptor_radius: float = 0.1, max_descriptors: int = 1200,
+                                 max_candidates: int = 1500) -> list[dict[str, Any]]:
+        """estimate_triangle_asterism_transform of each frame's catalog (from its
+        last detect_stars) against the reference frame's catalog, all on the
+        device; returns one StarRegistration-like dict per index."""
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+        if idx.size == 0:
+            raise ValueError("indices must contain at least one frame index")
+        params = _register_params(transform_model, min_inliers, tolerance_px, max_stars, neighbors,
+                                  descriptor_radius, max_descriptors, max_candidates)
+        out = (_lib.Registration * idx.size)()
+        _lib.call("gg_stack_register_frames", self._handle, ctypes.c_int64(int(reference_index)), _lib.ptr(idx),
+                  ctypes.c_int64(idx.size), ctypes.byref(params), out)
+        return [_registration_dict(r) for r in out]
 
     # ---- warps (native_bindings.cpp:8900-9924) ------------------------------------
     @property

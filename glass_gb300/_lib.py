@@ -146,6 +146,36 @@ class IntegrateParams(ctypes.Structure):
     ]
 
 
+GG_TRANSFORM_SIMILARITY = 1
+
+
+class RegisterParams(ctypes.Structure):
+    _fields_ = [
+        ("transform_model", ctypes.c_int32),
+        ("min_inliers", ctypes.c_int32),
+        ("tolerance_px", ctypes.c_double),
+        ("descriptor_radius", ctypes.c_double),
+        ("max_stars", ctypes.c_int32),
+        ("neighbors", ctypes.c_int32),
+        ("max_descriptors", ctypes.c_int32),
+        ("max_candidates", ctypes.c_int32),
+    ]
+
+
+class Registration(ctypes.Structure):
+    _fields_ = [
+        ("matrix", ctypes.c_double * 9),
+        ("rms_px", ctypes.c_double),
+        ("best_candidate", ctypes.c_int64),
+        ("inliers", ctypes.c_int32),
+        ("status", ctypes.c_int32),
+        ("descriptors_reference", ctypes.c_int32),
+        ("descriptors_moving", ctypes.c_int32),
+        ("matches", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
 class StackDevicePtrs(ctypes.Structure):
     _fields_ = [
         ("slots", ctypes.c_void_p),
@@ -195,6 +225,14 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
     "gg_dq_map_i16": [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P],
     "gg_stack_detect_stars": [_P, _P, ctypes.c_int64, ctypes.POINTER(StarParams), _P, _P, _P],
+    "gg_triangle_descriptors": [_P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P,
+                                ctypes.c_int64, c_int64_p],
+    "gg_register_star_lists": [_P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.POINTER(RegisterParams),
+                               ctypes.POINTER(Registration), _P],
+    "gg_similarity_from_descriptors": [_P, ctypes.c_int64, _P, ctypes.c_int64, _P, _P, ctypes.c_int64, _P, _P,
+                                       ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                       ctypes.POINTER(Registration), _P],
+    "gg_stack_register_frames": [_P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.POINTER(RegisterParams), _P],
     "gg_stack_warp_frames": [_P, _P, ctypes.c_int64, _P, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int],
     "gg_stack_reset_warp_coverage": [_P],
     "gg_stack_accumulate_full_warp_coverage_frame": [_P],

@@ -99,6 +99,11 @@ struct gg_stack {
   void* reg_scratch = nullptr;
   void (*reg_scratch_free)(void*) = nullptr;
 
+  // Per-frame registration catalogs: the brightest kCatalogPoints star
+  // centroids of each frame's last detection (x, y float64) and their count.
+  double* d_cat_xy = nullptr;
+  int* d_cat_n = nullptr;
+
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaStream_t copy_stream = nullptr;
@@ -124,6 +129,9 @@ void stack_ensure_partials(gg_stack* s, size_t doubles);
 void stack_check_device_error(gg_stack* s);
 // Encodes a TMA tensor map over the slot pool ([slot][H][W] float32).
 bool make_slot_tensor_map(gg_stack* s, int box_w, int box_h);
+// Registration catalog storage (allocated on first detection).
+constexpr int kCatalogPoints = 80;
+void ensure_catalog_storage(gg_stack* s);
 
 // Kernel launchers (defined in the per-kernel translation units).
 struct CalibLaunch {
@@ -136,7 +144,6 @@ struct CalibLaunch {
 void launch_calibrate(gg_stack* s, const CalibLaunch& job, const gg_calib_params_t& p);
 void launch_count_nonfinite(gg_stack* s, int64_t frame);
 void launch_frame_stats(gg_stack* s, const int64_t* indices, int64_t count, int blocks_per_frame);
-void launch_integrate(gg_stack* s, const float* d_weights, bool weights_all_valid, bool unit_weights,
-                      int active_frames, const gg_integrate_params_t& p);
+void launch_integrate(gg_stack* s, const float* d_weights, const gg_integrate_params_t& p);
 
 }  // namespace gg

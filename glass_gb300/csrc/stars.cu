@@ -257,6 +257,8 @@ struct CatalogArgs {
   int radius;
   double min_sep;
   int* error;
+  double* cat_xy;  // [frames][kCatalogPoints][2]: brightest stars, for registration
+  int* cat_n;      // [frames]
 };
 
 // Sort candidate raster indices ascending (one CTA per frame, bitonic in
@@ -565,6 +567,18 @@ __global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
     out[i] = s;
   }
   if (threadIdx.x == 0) st.kept = nout;
+  if (a.cat_xy) {
+    // registration uses the first (brightest) points of the catalog
+    // (cpu/registration.py:37-39, max_stars = 80)
+    const int frame = a.frames[k];
+    const int np = min(nout, kCatalogPoints);
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+      const StarRec r = recs[sel[i].idx];
+      a.cat_xy[(static_cast<int64_t>(frame) * kCatalogPoints + i) * 2] = r.x;
+      a.cat_xy[(static_cast<int64_t>(frame) * kCatalogPoints + i) * 2 + 1] = r.y;
+    }
+    if (threadIdx.x == 0) a.cat_n[frame] = np;
+  }
 }
 
 // ---- np.std of the finite pixels, bit-exact (fallback noise, MAD == 0) -----
@@ -750,6 +764,14 @@ __global__ void __launch_bounds__(1024) pairwise_std_kernel(PwArgs a) {
 }
 
 // ---- host side -------------------------------------------------------------------
+void ensure_catalog_storage(gg_stack* s) {
+  if (s->d_cat_xy) return;
+  check_cuda(cudaMalloc(&s->d_cat_xy, sizeof(double) * 2 * kCatalogPoints * s->frames), "cudaMalloc(catalogs)");
+  check_cuda(cudaMalloc(&s->d_cat_n, sizeof(int) * s->frames), "cudaMalloc(catalog counts)");
+  check_cuda(cudaMemsetAsync(s->d_cat_n, 0, sizeof(int) * s->frames, s->stream), "cudaMemsetAsync(catalogs)");
+  s->bytes_allocated += static_cast<int64_t>(sizeof(double) * 2 * kCatalogPoints * s->frames + sizeof(int) * s->frames);
+}
+
 struct StarScratch {
   StarFrameState* state = nullptr;
   unsigned* hist = nullptr;
@@ -922,6 +944,9 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
   ca.radius = std::max(1, p.window_radius);
   ca.min_sep = p.min_separation_px;
   ca.error = s->d_error;
+  ensure_catalog_storage(s);
+  ca.cat_xy = s->d_cat_xy;
+  ca.cat_n = s->d_cat_n;
   const size_t sort_smem = sizeof(unsigned) * kMaxCandidates;
   check_cuda(cudaFuncSetAttribute(star_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(sort_smem)),

@@ -80,6 +80,11 @@ class StepConfig:
     clamping_threshold: float = -1.0
     light_exposure_s: float = 300.0
     dark_exposure_s: float | None = 300.0
+    # star catalogs + triangle registration (resident_cuda.py:10790-11400)
+    star_threshold_sigma: float = 5.0
+    star_max_stars: int = 80
+    registration_tolerance_px: float = 3.0
+    registration_min_inliers: int = 6
 
 
 class ResidentPipeline:
@@ -121,9 +126,38 @@ class ResidentPipeline:
         _lib.call("gg_stack_calibrate_u16", self.stack.handle, _lib.ptr(self._indices),
                   ctypes.c_int64(self.frames), _lib.ptr(host_raw), 0, ctypes.byref(self._calib_params()))
 
+    def detect(self) -> None:
+        """Star catalogs of every frame; they stay on the device for register()."""
+        _lib.call("gg_stack_detect_stars", self.stack.handle, _lib.ptr(self._indices), ctypes.c_int64(self.frames),
+                  ctypes.byref(_lib.StarParams(float(self.config.star_threshold_sigma), int(self.config.star_max_stars),
+                                               4, 2.0, np.nan, np.nan)), None, None, None)
+
+    def register(self, reference_index: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        """Triangle registration of every frame to the reference frame from the
+        device catalogs -> (matrices [frames, 3, 3], ok [frames]).  Frames that
+        fail keep the identity matrix and are weighted 0 by weights()."""
+        cfg = self.config
+        params = _lib.RegisterParams(_lib.GG_TRANSFORM_SIMILARITY, int(cfg.registration_min_inliers),
+                                     float(cfg.registration_tolerance_px), 0.1, 80, 5, 1200, 1500)
+        idx = np.array([i for i in range(self.frames) if i != reference_index], dtype=np.int64)
+        matrices = np.tile(np.eye(3), (self.frames, 1, 1))
+        ok = np.ones(self.frames, dtype=bool)
+        if idx.size:
+            out = (_lib.Registration * idx.size)()
+            _lib.call("gg_stack_register_frames", self.stack.handle, ctypes.c_int64(int(reference_index)),
+                      _lib.ptr(idx), ctypes.c_int64(idx.size), ctypes.byref(params), out)
+            for pos, k in enumerate(idx):
+                ok[k] = out[pos].status == 1
+                if ok[k]:
+                    matrices[k] = np.asarray(out[pos].matrix, dtype=np.float64).reshape(3, 3)
+        self._registered = ok
+        return matrices, ok
+
     def warp(self, matrices: np.ndarray, reference_index: int = 0) -> None:
         """Warps every frame but the reference through its moving->reference matrix."""
-        idx = np.array([i for i in range(self.frames) if i != reference_index], dtype=np.int64)
+        ok = getattr(self, "_registered", None)
+        idx = np.array([i for i in range(self.frames) if i != reference_index and (ok is None or ok[i])],
+                       dtype=np.int64)
         if idx.size == 0:
             return
         mats = np.ascontiguousarray(np.asarray(matrices, dtype=np.float64)[idx])
@@ -131,7 +165,9 @@ class ResidentPipeline:
         self.stack.warp_frames_async(idx, mats, interp, np.nan, self.config.clamping_threshold, False)
 
     def weights(self) -> None:
-        self.stack.compute_frame_weights(self.config.weighting, None, 1.0e-6, download=False)
+        ok = getattr(self, "_registered", None)
+        prior = None if ok is None else ok.astype(np.float32)
+        self.stack.compute_frame_weights(self.config.weighting, prior, 1.0e-6, download=False)
 
     def integrate(self) -> None:
         cfg = self.config
@@ -145,9 +181,13 @@ class ResidentPipeline:
         self.weights()
         self.integrate()
 
-    def step_host(self, host_raw: np.ndarray, matrices: np.ndarray | None = None):
-        """Public-API step from host memory to host maps (end to end)."""
+    def step_host(self, host_raw: np.ndarray, matrices: np.ndarray | None = None, register: bool = False):
+        """Public-API step from host memory to host maps (end to end).  With
+        register=True the matrices come from detect() + register()."""
         self.calibrate_host(host_raw)
+        if register:
+            self.detect()
+            matrices, _ok = self.register()
         if matrices is not None:
             self.warp(matrices)
         self.weights()

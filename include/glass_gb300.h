@@ -273,6 +273,64 @@ typedef struct {
 int gg_stack_detect_stars(gg_stack* stack, const int64_t* indices, int64_t count, const gg_star_params_t* params,
                           gg_star_t* host_stars, int32_t* host_counts, gg_star_frame_info_t* host_info);
 
+/* ---- registration (triangle asterisms) ----------------------------------- */
+/* Point lists are (x, y) float64 pairs, brightest star first.  Catalogs hold
+ * at most 80 stars. */
+#define GG_TRANSFORM_SIMILARITY 1
+
+/* Parameters of estimate_triangle_asterism_transform
+ * (cpu/registration.py:361-373). */
+typedef struct {
+  int32_t transform_model;  /* GG_TRANSFORM_SIMILARITY */
+  int32_t min_inliers;      /* 6 */
+  double tolerance_px;      /* 3.0 */
+  double descriptor_radius; /* 0.1 */
+  int32_t max_stars;        /* 80, at most 80 */
+  int32_t neighbors;        /* 5, at most 6 (values below 3 mean 3) */
+  int32_t max_descriptors;  /* 1200 */
+  int32_t max_candidates;   /* 1500, at most 2048 */
+} gg_register_params_t;
+
+/* StarRegistration (cpu/registration.py:11-20) without the warning strings. */
+typedef struct {
+  double matrix[9];         /* row-major 3x3, moving -> reference pixels */
+  double rms_px;            /* NaN without pairs */
+  int64_t best_candidate;   /* winning candidate (2 * match + orientation), -1 if none */
+  int32_t inliers;          /* = matched_stars */
+  int32_t status;           /* 1 "ok", 0 "failed" */
+  int32_t descriptors_reference;
+  int32_t descriptors_moving;
+  int32_t matches;          /* descriptor matches scored */
+  int32_t pad;
+} gg_registration_t;
+
+/* Replaces module triangle_asterism_descriptors_f32 (glass_cuda.py:1835-1902;
+ * cpu/registration.py:273-303): local triangle descriptors of one catalog,
+ * area-descending.  host_descriptors [count][2], host_indices [count][3] and
+ * host_areas [count] may each be NULL; `capacity` rows are available. */
+int gg_triangle_descriptors(const double* host_xy, int64_t n, int32_t max_stars, int32_t neighbors,
+                            int32_t max_descriptors, double* host_descriptors, int32_t* host_indices,
+                            double* host_areas, int64_t capacity, int64_t* count);
+/* estimate_triangle_asterism_transform (cpu/registration.py:361-475) of two
+ * host catalogs.  host_pairs (may be NULL) receives 80 (moving, reference)
+ * index pairs, -1 past the inliers. */
+int gg_register_star_lists(const double* host_ref_xy, int64_t n_ref, const double* host_mov_xy, int64_t n_mov,
+                           const gg_register_params_t* params, gg_registration_t* host_out, int32_t* host_pairs);
+/* Replaces module estimate_similarity_from_triangle_descriptors_f32
+ * (glass_cuda.py:2054-2140): every descriptor pair within the radius, both
+ * reference orientations, best by (pairs, rms), no refit. */
+int gg_similarity_from_descriptors(const double* host_ref_xy, int64_t n_ref, const double* host_mov_xy,
+                                   int64_t n_mov, const float* host_ref_desc, const int32_t* host_ref_idx,
+                                   int64_t n_ref_desc, const float* host_mov_desc, const int32_t* host_mov_idx,
+                                   int64_t n_mov_desc, double tolerance_px, double descriptor_radius,
+                                   gg_registration_t* host_out, int32_t* host_pairs);
+/* Registers resident frames to a resident reference frame from the catalogs
+ * of their last gg_stack_detect_stars (the reference's resident triangle path,
+ * resident_cuda.py:10790-11420).  host_out receives `count` results.
+ * Synchronises the stack stream. */
+int gg_stack_register_frames(gg_stack* stack, int64_t reference_index, const int64_t* indices, int64_t count,
+                             const gg_register_params_t* params, gg_registration_t* host_out);
+
 /* ---- warps --------------------------------------------------------------- */
 /* Warps `count` resident frames in place through their forward matrices
  * (float64 row-major 3x3, moving -> reference; the kernel samples the source

@@ -338,6 +338,160 @@ def make_stars(ref_src: Path) -> None:
     np.savez_compressed(HERE / "stars.npz", **arrays)
 
 
+# ---------------------------------------------------------------------------
+# registration
+# ---------------------------------------------------------------------------
+def _similar_catalog(rng, n, theta_deg, scale, dx, dy, noise, extent=2000.0, drop=0, add=0, swap=0):
+    """Reference catalog (n, 2) and a moving catalog that the similarity
+    (theta, scale, dx, dy) maps back onto it, with centroid noise, dropped and
+    spurious stars and a perturbed brightness order."""
+    ref = rng.uniform(20.0, extent - 20.0, size=(n, 2))
+    t = np.deg2rad(theta_deg)
+    lin = scale * np.array([[np.cos(t), -np.sin(t)], [np.sin(t), np.cos(t)]])
+    mov = (ref - np.array([dx, dy])) @ np.linalg.inv(lin).T + noise * rng.standard_normal((n, 2))
+    keep = np.sort(rng.permutation(n)[: n - drop])
+    mov = mov[keep]
+    if add:
+        mov = np.vstack([mov, rng.uniform(0.0, extent, size=(add, 2))])
+    order = np.arange(len(mov))
+    for _ in range(swap):  # neighbouring brightness swaps
+        i = int(rng.integers(0, len(mov) - 1))
+        order[i], order[i + 1] = order[i + 1], order[i]
+    return ref, mov[order]
+
+
+def make_registration(ref_src: Path) -> None:
+    """estimate_triangle_asterism_transform and _local_triangle_descriptors
+    (src/glass/cpu/registration.py:273-475) on seeded catalogs and on the
+    reference tests' own cases (tests/test_cpu_registration.py:114-149,
+    206-235), plus the descriptor-list similarity fallback of
+    src/glass_cuda.py:2054-2140."""
+    sys.path.insert(0, str(ref_src))
+    from glass.cpu.registration import _local_triangle_descriptors, estimate_triangle_asterism_transform
+    from glass.cpu.star_detect import Star, detect_stars
+    import glass_cuda
+
+    rng = np.random.default_rng(2718)
+    cases = []
+    # reftest: 8 points, similarity (-7 deg, 0.98, (-4, 3)) plus one outlier
+    pts = np.array([(10, 10), (20, 10), (10, 25), (30, 30), (5, 35), (35, 5), (25, 18), (14, 32)], dtype=np.float64)
+    ang = np.deg2rad(-7.0)
+    lin = 0.98 * np.array([[np.cos(ang), -np.sin(ang)], [np.sin(ang), np.cos(ang)]])
+    mov = np.vstack([(pts - np.array([-4.0, 3.0])) @ np.linalg.inv(lin).T, [[100.0, 100.0]]])
+    cases.append(("reftest_outlier", pts, mov, dict(min_inliers=8, tolerance_px=0.5, neighbors=5,
+                                                     descriptor_radius=0.1)))
+    # reftest: detected star field shifted by (4, -3)
+    shape = (96, 112)
+    field = np.full(shape, 10.0, dtype=np.float32)
+    yy, xx = np.indices(shape, dtype=np.float32)
+    for x, y, flux in [(12, 17, 100.0), (30, 42, 220.0), (71, 15, 160.0), (88, 63, 180.0), (45, 79, 250.0),
+                       (19, 86, 130.0), (101, 33, 145.0), (53, 55, 190.0)]:
+        field += flux * np.exp(-(((xx - x) ** 2 + (yy - y) ** 2) / (2.0 * 1.4 ** 2)))
+    field = field.astype(np.float32)
+    shifted = np.zeros_like(field)
+    shifted[0:93, 4:112] = field[3:96, 0:108]
+    rs = detect_stars(field, threshold_sigma=3, max_stars=50)
+    ms = detect_stars(shifted, threshold_sigma=3, max_stars=50)
+    cases.append(("reftest_star_field", np.array([(s.x, s.y) for s in rs]), np.array([(s.x, s.y) for s in ms]),
+                  dict(min_inliers=6, tolerance_px=0.5, neighbors=5, descriptor_radius=0.1)))
+    # seeded catalogs
+    specs = [
+        (80, 0.3, 1.0, 12.5, -7.25, 0.05, 0, 0, 0, {}),
+        (80, -2.0, 1.01, -40.0, 33.0, 0.1, 5, 5, 6, {}),
+        (60, 4.5, 0.99, 3.0, 150.0, 0.2, 8, 10, 10, dict(tolerance_px=2.0)),
+        (40, 0.0, 1.0, 0.5, 0.25, 0.0, 0, 0, 0, dict(neighbors=4)),
+        (80, 1.0, 1.0, -5.0, 5.0, 0.05, 0, 0, 0, dict(neighbors=6, max_candidates=200)),
+        (80, -0.7, 1.0, 8.0, -2.0, 0.05, 2, 3, 4, dict(max_descriptors=100, max_candidates=50)),
+        (50, 10.0, 1.05, 100.0, -80.0, 0.1, 0, 0, 0, dict(max_stars=30)),
+        (25, 0.2, 1.0, 1.0, 1.0, 0.05, 10, 12, 0, dict(min_inliers=10)),
+        (12, 0.0, 1.0, 2.0, 3.0, 0.0, 0, 0, 0, dict(tolerance_px=1.0)),
+        (80, 180.0, 1.0, 2000.0, 2000.0, 0.05, 0, 0, 0, {}),
+        (80, 0.5, 1.0, 3.0, 4.0, 0.05, 0, 0, 0, dict(descriptor_radius=0.02)),
+        (80, 0.5, 1.0, 3.0, 4.0, 0.05, 0, 0, 0, dict(descriptor_radius=0.0)),
+    ]
+    for k, (n, th, sc, dx, dy, noise, drop, add, swap, params) in enumerate(specs):
+        ref, mov = _similar_catalog(rng, n, th, sc, dx, dy, noise, drop=drop, add=add, swap=swap)
+        cases.append((f"seeded{k}", ref, mov, params))
+    # dense field: many point pairs inside the tolerance
+    ref, mov = _similar_catalog(rng, 80, 0.1, 1.0, 1.0, 1.0, 0.3, extent=120.0)
+    cases.append(("dense", ref, mov, dict(tolerance_px=3.0)))
+    # mirrored moving catalog: the SVD reflection branch
+    ref = rng.uniform(0.0, 500.0, size=(30, 2))
+    cases.append(("mirrored", ref, ref * np.array([-1.0, 1.0]) + 600.0, {}))
+    # regular grid: identical descriptors, ties everywhere
+    g = np.stack(np.meshgrid(np.arange(8) * 25.0 + 10.0, np.arange(8) * 25.0 + 10.0), -1).reshape(-1, 2)
+    cases.append(("grid", g, g + np.array([3.0, -2.0]), dict(max_candidates=300)))
+    # degenerate inputs
+    line = np.column_stack([np.arange(10) * 7.0, np.arange(10) * 3.0])
+    cases.append(("collinear", line, line + 1.0, {}))
+    cases.append(("two_stars", np.array([[1.0, 2.0], [30.0, 40.0]]), np.array([[2.0, 2.0], [31.0, 40.0]]), {}))
+    cases.append(("empty_moving", rng.uniform(0, 100, (10, 2)), np.zeros((0, 2)), {}))
+    cases.append(("duplicates", np.repeat(rng.uniform(0, 300, (6, 2)), 2, axis=0),
+                  np.repeat(rng.uniform(0, 300, (6, 2)), 2, axis=0), {}))
+
+    arrays: dict[str, np.ndarray] = {}
+    names = []
+    for name, ref, mov, params in cases:
+        rstars = [Star(float(x), float(y), 1000.0 - i) for i, (x, y) in enumerate(ref)]
+        mstars = [Star(float(x), float(y), 1000.0 - i) for i, (x, y) in enumerate(mov)]
+        res = estimate_triangle_asterism_transform(rstars, mstars, "similarity", **params)
+        arrays[f"{name}/ref"] = np.asarray(ref, dtype=np.float64).reshape(-1, 2)
+        arrays[f"{name}/mov"] = np.asarray(mov, dtype=np.float64).reshape(-1, 2)
+        arrays[f"{name}/params"] = np.asarray(repr(params))
+        arrays[f"{name}/matrix"] = np.asarray(res.matrix, dtype=np.float64)
+        arrays[f"{name}/inliers"] = np.asarray(res.inliers)
+        arrays[f"{name}/rms_px"] = np.asarray(res.rms_px)
+        arrays[f"{name}/status"] = np.asarray(res.status)
+        arrays[f"{name}/pairs"] = np.asarray(res.pairs, dtype=np.int32).reshape(-1, 2)
+        arrays[f"{name}/warnings"] = np.asarray(res.warnings)
+        names.append(name)
+    arrays["_names"] = np.asarray(names)
+
+    # descriptors of single catalogs
+    dnames = []
+    for k, (n, mp, nb, md) in enumerate([(80, 80, 5, 1200), (80, 80, 6, 1200), (50, 40, 4, 1200), (80, 80, 5, 300),
+                                         (10, 80, 2, 1200), (3, 80, 5, 1200), (64, 80, 5, 1200)]):
+        pts = rng.uniform(0.0, 1500.0, size=(n, 2)) if k != 6 else g + 0.0
+        desc = _local_triangle_descriptors(pts, max_points=mp, neighbors=nb, max_descriptors=md)
+        key = f"desc{k}"
+        arrays[f"{key}/points"] = pts
+        arrays[f"{key}/params"] = np.asarray(repr(dict(max_points=mp, neighbors=nb, max_descriptors=md)))
+        arrays[f"{key}/descriptors"] = np.asarray([d[0] for d in desc], dtype=np.float64).reshape(-1, 2)
+        arrays[f"{key}/indices"] = np.asarray([d[1] for d in desc], dtype=np.int32).reshape(-1, 3)
+        arrays[f"{key}/areas"] = np.asarray([d[2] for d in desc], dtype=np.float64)
+        dnames.append(key)
+    arrays["_desc_names"] = np.asarray(dnames)
+
+    # descriptor-list similarity (module fallback; glass_cuda._native() is None here)
+    assert glass_cuda._native() is None
+    lnames = []
+    for k, (n, th, dx, dy, tol) in enumerate([(30, 1.0, 5.0, -3.0, 2.0), (60, -3.0, 20.0, 10.0, 1.0),
+                                              (20, 0.0, 0.5, 0.5, 2.0)]):
+        ref, mov = _similar_catalog(rng, n, th, 1.0, dx, dy, 0.05, extent=1000.0, drop=2, add=2)
+        ref32, mov32 = ref.astype(np.float32), mov.astype(np.float32)
+        rdesc = glass_cuda.triangle_asterism_descriptors_f32(ref32[:, 0], ref32[:, 1], 80, 5, 400)
+        mdesc = glass_cuda.triangle_asterism_descriptors_f32(mov32[:, 0], mov32[:, 1], 80, 5, 400)
+        res = glass_cuda.estimate_similarity_from_triangle_descriptors_f32(
+            ref32[:, 0], ref32[:, 1], mov32[:, 0], mov32[:, 1], rdesc["descriptors"], rdesc["indices"],
+            mdesc["descriptors"], mdesc["indices"], tolerance_px=tol, descriptor_radius=0.1)
+        key = f"list{k}"
+        arrays[f"{key}/ref"] = ref32
+        arrays[f"{key}/mov"] = mov32
+        arrays[f"{key}/ref_desc"] = rdesc["descriptors"]
+        arrays[f"{key}/ref_idx"] = rdesc["indices"]
+        arrays[f"{key}/mov_desc"] = mdesc["descriptors"]
+        arrays[f"{key}/mov_idx"] = mdesc["indices"]
+        arrays[f"{key}/tolerance_px"] = np.asarray(tol)
+        arrays[f"{key}/matrix32"] = np.asarray(res["matrix"], dtype=np.float32)
+        arrays[f"{key}/inliers"] = np.asarray(res["inliers"])
+        arrays[f"{key}/rms_px"] = np.asarray(res["rms_px"])
+        arrays[f"{key}/best_candidate_index"] = np.asarray(res["best_candidate_index"])
+        arrays[f"{key}/status"] = np.asarray(res["status"])
+        lnames.append(key)
+    arrays["_list_names"] = np.asarray(lnames)
+    np.savez_compressed(HERE / "registration.npz", **arrays)
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__)
     parser.add_argument("--reference", default="/root/reference", help="GLASS reference checkout")
@@ -346,7 +500,7 @@ def main() -> int:
     ref = Path(args.reference)
     src = ref / "src"
     jobs = {"integration": make_integration, "calibration": make_calibration, "warp": make_warp,
-            "stars": make_stars}
+            "stars": make_stars, "registration": make_registration}
     only = [j for j in args.only.split(",") if j] or list(jobs)
     for job in only:
         jobs[job](src)
