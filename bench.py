@@ -81,9 +81,11 @@ def profile_traffic(name: str):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling (every 20 ms) during the timed
+    region: samples are time-stamped and only those between mark_start() and
+    mark_stop() are summarised."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -91,16 +93,26 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.file = None
+        self.t0 = None
+        self.t1 = None
 
     def __enter__(self):
         try:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=self.file, stderr=subprocess.DEVNULL)
+                 "-lms", "20"], stdout=self.file, stderr=subprocess.DEVNULL)
+            time.sleep(0.5)  # let the sampler start before the timed region
         except Exception:
             self.proc = None
         return self
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_stop(self):
+        self.t1 = time.time()
+        time.sleep(0.05)
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -111,16 +123,25 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        import datetime as _dt
+
         if self.proc is None or self.file is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.file.flush()
         rows = []
         for line in Path(self.file.name).read_text().splitlines():
             parts = [x.strip() for x in line.split(",")]
-            if len(parts) >= 9:
-                rows.append(parts)
+            if len(parts) < 9:
+                continue
+            try:
+                ts = _dt.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                continue
+            if self.t0 is not None and self.t1 is not None and not (self.t0 - 0.02 <= ts <= self.t1 + 0.02):
+                continue
+            rows.append(parts)
         if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples in the timed region"]}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         reasons = set()
@@ -288,6 +309,7 @@ def main():
     with ClockSampler(local) as clocks:
         start = torch.cuda.Event(enable_timing=True)
         stop = torch.cuda.Event(enable_timing=True)
+        clocks.mark_start()
         start.record(stream)
         for _ in range(args.steps):
             for name, fn, _ in stages:
@@ -299,6 +321,7 @@ def main():
                 events[name].append((e0, e1))
         stop.record(stream)
         stream.synchronize()
+        clocks.mark_stop()
     torch.cuda.synchronize()
     barrier()
     launches = _lib.kernel_launches() - launches0
@@ -320,14 +343,19 @@ def main():
     registration = {"frames_ok": int(reg["ok"].sum()), "frames": n,
                     "max_corner_error_px_vs_truth": reg_err}
     pinned = torch.from_numpy(data.lights.view(np.int16)).pin_memory().numpy().view(np.uint16)
+    # reused pinned destinations for the six maps (master, weight f32; coverage,
+    # low, high uint16; dq int16)
+    map_out = tuple(torch.empty((h, w), dtype=dt).pin_memory().numpy() for dt in (torch.float32, torch.float32))
+    map_out += tuple(torch.empty((h, w), dtype=torch.int16).pin_memory().numpy().view(np.uint16) for _ in range(3))
+    map_out += (torch.empty((h, w), dtype=torch.int16).pin_memory().numpy(),)
     e2e_steps = max(3, min(args.steps, 10))
     for _ in range(2):
-        maps = pipe.step_host(pinned, register=True)
+        maps = pipe.step_host(pinned, register=True, out=map_out)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        maps = pipe.step_host(pinned, register=True)
+        maps = pipe.step_host(pinned, register=True, out=map_out)
     t1 = time.perf_counter()
     e2e_s = t1 - t0
     if world > 1:

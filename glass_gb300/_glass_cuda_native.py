@@ -792,21 +792,38 @@ class ResidentCalibratedStack:
             _lib.call("gg_stack_integrate", self._handle, _lib.ptr(w), ctypes.byref(params))
         self._last_count_dtype = np.dtype(np.uint16 if count_map_dtype == "uint16" else np.float32)
 
-    def download_maps(self, download_mode: str = "full", include_dq: bool = True):
-        """(master, weight, coverage, low, high, dq) of the last integration."""
+    def download_maps(self, download_mode: str = "full", include_dq: bool = True, out: tuple | None = None):
+        """(master, weight, coverage, low, high, dq) of the last integration.
+
+        ``out`` may supply the six destination arrays (e.g. reused pinned
+        buffers from host_pinned_empty_f32); entries the mode does not
+        download may be None.
+        """
         if download_mode not in _DOWNLOAD_MODES:
             raise ValueError("download_mode must be full, master_weight, or master_only")
         if self._last_count_dtype is None:
             raise RuntimeError("no integration has been run")
         info = self._info()
         shape = (info.height, info.width)
-        master = np.empty(shape, np.float32)
-        weight = np.empty(shape, np.float32) if download_mode != "master_only" else None
         full = download_mode == "full"
-        cov = np.empty(shape, self._last_count_dtype) if full else None
-        low = np.empty(shape, self._last_count_dtype) if full else None
-        high = np.empty(shape, self._last_count_dtype) if full else None
-        dq = np.empty(shape, np.int16) if (full and include_dq) else None
+        want = (True, download_mode != "master_only", full, full, full, full and include_dq)
+        dtypes = (np.float32, np.float32, self._last_count_dtype, self._last_count_dtype, self._last_count_dtype,
+                  np.int16)
+        bufs = []
+        for k in range(6):
+            if not want[k]:
+                bufs.append(None)
+                continue
+            given = None if out is None else out[k]
+            if given is None:
+                bufs.append(np.empty(shape, dtypes[k]))
+                continue
+            if (not isinstance(given, np.ndarray) or given.shape != shape or given.dtype != np.dtype(dtypes[k])
+                    or not given.flags.c_contiguous or not given.flags.writeable):
+                raise ValueError(f"out[{k}] must be a writable C-contiguous {np.dtype(dtypes[k])} array of shape "
+                                 f"{shape}")
+            bufs.append(given)
+        master, weight, cov, low, high, dq = bufs
         _lib.call("gg_stack_download_maps", self._handle, _lib.ptr(master), _lib.ptr(weight), _lib.ptr(cov),
                   _lib.ptr(low), _lib.ptr(high), _lib.ptr(dq))
         return master, weight, cov, low, high, dq

@@ -123,6 +123,10 @@ __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a,
 __device__ __forceinline__ double hyp_sum(double dx, double dy) { return sqrt(dadd(dmul(dx, dx), dmul(dy, dy))); }
 // np.linalg.norm of a 2-vector: a dot product whose second term is fused
 __device__ __forceinline__ double hyp_dot(double dx, double dy) { return sqrt(__fma_rn(dy, dy, dmul(dx, dx))); }
+// Order-preserving bits of a non-negative double.
+__device__ __forceinline__ unsigned long long dbits_of(double d) {
+  return static_cast<unsigned long long>(__double_as_longlong(d));
+}
 
 // NumPy's pairwise sum of a contiguous float64 array (eight interleaved
 // accumulators per block of <= 128, longer runs split at n/2 rounded down to
@@ -199,27 +203,87 @@ __device__ bool fit_similarity(const double* mx, const double* my, const double*
 }
 
 // ---- point pairs of a transform (registration.py:177-215) ------------------------
-struct WarpScratch {
-  double tx[kRegPts], ty[kRegPts];
-  float tx32[kRegPts], ty32[kRegPts];
-  double dist[kPairCap];
-  int idx[kPairCap];
-  double res[kRegPts];
-  int count;
-};
+// The reference catalog of a frame pair is bucketed into a uniform grid of at
+// most 8 x 8 cells (at least 2 * (tol + 0.5) px wide), so a transformed
+// moving star only visits the reference stars of <= 2 x 2 cells instead of
+// all of them.
+constexpr int kGrid = 8;
 
 struct JobPoints {
   double mx[kRegPts], my[kRegPts], rx[kRegPts], ry[kRegPts];
-  float rx32[kRegPts], ry32[kRegPts];
+  float mx32[kRegPts], my32[kRegPts], rx32[kRegPts], ry32[kRegPts];
+  unsigned char cell_start[kGrid * kGrid + 1];
+  unsigned char cell_pt[kRegPts];
+  float gx0, gy0, ginv;
+  int gnx, gny;
+  float cmax;  // max |x| + |y| of the moving stars
+  float rmax;  // max |x|, |y| of the reference stars
   int nm, nr;
 };
 
-// Warp-cooperative: every lane returns the pair count and rms; lane 0 writes
-// the greedy pairs (moving, reference) when `pairs` is not null.
-__device__ void warp_score(const double (&m)[6], const JobPoints& jp, double tol, WarpScratch& w, int& npairs,
-                           double& rms, short2* pairs, int* overflow) {
+struct WarpScratch {
+  double tx[kRegPts], ty[kRegPts];
+  float tx32[kRegPts], ty32[kRegPts];
+  unsigned long long key[kPairCap];  // distance bits of the pairs within tolerance
+  int idx[kPairCap];                 // (moving << 8) | reference: row-major order
+  int acc[kRegPts];                  // accepted entries in greedy order
+  double res[kRegPts];
+  unsigned used_r[3];
+  int count;
+};
+
+// Reference stars within `r` of (x, y) in grid order; calls f(j).
+template <class F>
+__device__ __forceinline__ void grid_visit(const JobPoints& jp, float x, float y, float r, F&& f) {
+  if (!(fabsf(x) < 3.0e38f && fabsf(y) < 3.0e38f) || jp.gnx == 0) return;
+  const float fx0 = (x - r - jp.gx0) * jp.ginv, fx1 = (x + r - jp.gx0) * jp.ginv;
+  const float fy0 = (y - r - jp.gy0) * jp.ginv, fy1 = (y + r - jp.gy0) * jp.ginv;
+  if (fx1 < 0.0f || fy1 < 0.0f || fx0 >= static_cast<float>(jp.gnx) || fy0 >= static_cast<float>(jp.gny)) return;
+  const int cx0 = max(0, static_cast<int>(floorf(fmaxf(fx0, -1.0f))));
+  const int cx1 = min(jp.gnx - 1, static_cast<int>(floorf(fminf(fx1, static_cast<float>(jp.gnx)))));
+  const int cy0 = max(0, static_cast<int>(floorf(fmaxf(fy0, -1.0f))));
+  const int cy1 = min(jp.gny - 1, static_cast<int>(floorf(fminf(fy1, static_cast<float>(jp.gny)))));
+  for (int cy = cy0; cy <= cy1; ++cy)
+    for (int cx = cx0; cx <= cx1; ++cx) {
+      const int c = cy * kGrid + cx;
+      for (int k = jp.cell_start[c]; k < jp.cell_start[c + 1]; ++k) f(static_cast<int>(jp.cell_pt[k]));
+    }
+}
+
+// NumPy pairwise sum of v[0..n) (n <= 128) by lanes 0..7 of the warp: lane j
+// runs accumulator j; every lane returns the sum.
+__device__ double warp_pw_sum(const double* v, int n) {
   const int lane = threadIdx.x & 31;
-  const int nm = jp.nm, nr = jp.nr;
+  double r = 0.0;
+  if (n >= 8 && lane < 8) {
+    r = v[lane];
+    for (int i = lane + 8; i < n - (n % 8); i += 8) r = dadd(r, v[i]);
+  }
+  double out = 0.0;
+  const double r1 = __shfl_down_sync(0xffffffffu, r, 1);
+  const double r2 = __shfl_down_sync(0xffffffffu, r, 2);
+  const double r3 = __shfl_down_sync(0xffffffffu, r, 3);
+  const double r4 = __shfl_down_sync(0xffffffffu, r, 4);
+  const double r5 = __shfl_down_sync(0xffffffffu, r, 5);
+  const double r6 = __shfl_down_sync(0xffffffffu, r, 6);
+  const double r7 = __shfl_down_sync(0xffffffffu, r, 7);
+  if (lane == 0) {
+    if (n < 8) {
+      for (int i = 0; i < n; ++i) out = dadd(out, v[i]);
+    } else {
+      out = dadd(dadd(dadd(r, r1), dadd(r2, r3)), dadd(dadd(r4, r5), dadd(r6, r7)));
+      for (int i = n - (n % 8); i < n; ++i) out = dadd(out, v[i]);
+    }
+  }
+  return __shfl_sync(0xffffffffu, out, 0);
+}
+
+// Exact scoring: every lane returns the greedy pair count and rms (+inf
+// without pairs); the pairs (moving, reference) go to `pairs` when not null.
+__device__ void warp_score_exact(const double (&m)[6], const JobPoints& jp, double tol, WarpScratch& w,
+                                 int& npairs, double& rms, short2* pairs, int* overflow) {
+  const int lane = threadIdx.x & 31;
+  const int nm = jp.nm;
   for (int i = lane; i < nm; i += 32) {
     const double x = dadd(dadd(dmul(jp.mx[i], m[0]), dmul(jp.my[i], m[1])), m[2]);
     const double y = dadd(dadd(dmul(jp.mx[i], m[3]), dmul(jp.my[i], m[4])), m[5]);
@@ -230,73 +294,206 @@ __device__ void warp_score(const double (&m)[6], const JobPoints& jp, double tol
   }
   if (lane == 0) w.count = 0;
   __syncwarp();
-  // float32 prefilter: the float64 distance is evaluated only within tol + 0.5
-  const float pre = static_cast<float>((tol + 0.5) * (tol + 0.5));
-  const int total = nm * nr;
-  for (int q0 = 0; q0 < total; q0 += 32) {
-    const int q = q0 + lane;
-    bool hit = false;
-    double d = 0.0;
-    if (q < total) {
-      const int i = q / nr, j = q - (q / nr) * nr;
-      const float fx = w.tx32[i] - jp.rx32[j], fy = w.ty32[i] - jp.ry32[j];
-      if (fx * fx + fy * fy <= pre) {
-        d = hyp_sum(dsub(w.tx[i], jp.rx[j]), dsub(w.ty[i], jp.ry[j]));
-        hit = d <= tol;
+  // pairs within tolerance (float32 prefilter with a 0.5 px margin, then the
+  // float64 distance); any order, sorted below
+  const float r = static_cast<float>(tol + 0.5);
+  const float pre = r * r;
+  for (int i = lane; i < nm; i += 32) {
+    const float x = w.tx32[i], y = w.ty32[i];
+    grid_visit(jp, x, y, r, [&](int j) {
+      const float fx = x - jp.rx32[j], fy = y - jp.ry32[j];
+      if (fx * fx + fy * fy > pre) return;
+      const double d = hyp_sum(dsub(w.tx[i], jp.rx[j]), dsub(w.ty[i], jp.ry[j]));
+      if (!(d <= tol)) return;
+      const int pos = atomicAdd(&w.count, 1);
+      if (pos < kPairCap) {
+        w.key[pos] = dbits_of(d);
+        w.idx[pos] = (i << 8) | j;
       }
-    }
-    const unsigned mask = __ballot_sync(0xffffffffu, hit);
-    if (mask) {
-      const int base = w.count;
-      if (hit) {
-        const int pos = base + __popc(mask & ((1u << lane) - 1u));
-        if (pos < kPairCap) {
-          w.dist[pos] = d;
-          w.idx[pos] = q;
+    });
+  }
+  __syncwarp();
+  int L = w.count;
+  if (L > kPairCap) {
+    if (lane == 0) atomicExch(overflow, 1);
+    L = kPairCap;
+  }
+  // sort by (distance, row-major index): the stable distance sort of the
+  // row-major candidate list
+  int mlen = 1;
+  while (mlen < L) mlen <<= 1;
+  for (int t = L + lane; t < mlen; t += 32) {
+    w.key[t] = ~0ull;
+    w.idx[t] = 0x7fffffff;
+  }
+  __syncwarp();
+  for (int size = 2; size <= mlen; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = lane; t < mlen; t += 32) {
+        const int u = t ^ stride;
+        if (u > t) {
+          const bool up = (t & size) == 0;
+          const unsigned long long kt = w.key[t], ku = w.key[u];
+          const int it = w.idx[t], iu = w.idx[u];
+          const bool gt = kt > ku || (kt == ku && it > iu);
+          if (gt == up) {
+            w.key[t] = ku;
+            w.key[u] = kt;
+            w.idx[t] = iu;
+            w.idx[u] = it;
+          }
         }
       }
       __syncwarp();
-      if (lane == 0) w.count = base + __popc(mask);
-      __syncwarp();
     }
   }
+  // greedy one-to-one pairing in distance order
   int n = 0;
-  double r = __longlong_as_double(0x7ff0000000000000ll);
   if (lane == 0) {
-    int L = w.count;
-    if (L > kPairCap) {
-      atomicExch(overflow, 1);
-      L = kPairCap;
-    }
-    // stable sort by distance of the row-major candidate list
-    for (int a = 1; a < L; ++a) {
-      const double dk = w.dist[a];
-      const int ik = w.idx[a];
-      int b = a - 1;
-      while (b >= 0 && (w.dist[b] > dk || (w.dist[b] == dk && w.idx[b] > ik))) {
-        w.dist[b + 1] = w.dist[b];
-        w.idx[b + 1] = w.idx[b];
-        --b;
-      }
-      w.dist[b + 1] = dk;
-      w.idx[b + 1] = ik;
-    }
     unsigned used_m[3] = {0u, 0u, 0u}, used_r[3] = {0u, 0u, 0u};
     for (int a = 0; a < L; ++a) {
-      const int i = w.idx[a] / nr, j = w.idx[a] - (w.idx[a] / nr) * nr;
+      const int i = w.idx[a] >> 8, j = w.idx[a] & 255;
       if ((used_m[i >> 5] >> (i & 31)) & 1u) continue;
       if ((used_r[j >> 5] >> (j & 31)) & 1u) continue;
       used_m[i >> 5] |= 1u << (i & 31);
       used_r[j >> 5] |= 1u << (j & 31);
-      if (pairs) pairs[n] = make_short2(static_cast<short>(i), static_cast<short>(j));
-      w.res[n] = dmul(w.dist[a], w.dist[a]);
-      ++n;
+      w.acc[n++] = a;
     }
-    if (n > 0) r = sqrt(__ddiv_rn(pw_sum(w.res, n), static_cast<double>(n)));
   }
-  npairs = __shfl_sync(0xffffffffu, n, 0);
-  rms = __shfl_sync(0xffffffffu, r, 0);
+  n = __shfl_sync(0xffffffffu, n, 0);
   __syncwarp();
+  for (int t = lane; t < n; t += 32) {
+    const int a = w.acc[t];
+    const double d = __longlong_as_double(static_cast<long long>(w.key[a]));
+    w.res[t] = dmul(d, d);
+    if (pairs) pairs[t] = make_short2(static_cast<short>(w.idx[a] >> 8), static_cast<short>(w.idx[a] & 255));
+  }
+  __syncwarp();
+  const double s = warp_pw_sum(w.res, n);
+  npairs = n;
+  rms = n > 0 ? sqrt(__ddiv_rn(s, static_cast<double>(n))) : __longlong_as_double(0x7ff0000000000000ll);
+  __syncwarp();
+}
+
+// Fast scoring for ranking: the exact pair count when no moving or reference
+// star has two partners within tolerance (then greedy pairing keeps every
+// pair), and the sum of squared residuals in any order.  Membership is
+// decided in float32 outside a band of +-delta around the tolerance (delta
+// bounds the float32 transform error) and in float64 inside it.  `conflict`
+// reports that the exact scorer is needed.
+__device__ void warp_score_fast(const double (&m)[6], const JobPoints& jp, double tol, WarpScratch& w, int& count,
+                                double& sum_d2, bool& conflict) {
+  const int lane = threadIdx.x & 31;
+  const float m0 = static_cast<float>(m[0]), m1 = static_cast<float>(m[1]), m2 = static_cast<float>(m[2]);
+  const float m3 = static_cast<float>(m[3]), m4 = static_cast<float>(m[4]), m5 = static_cast<float>(m[5]);
+  const double lin = fmax(fmax(fabs(m[0]), fabs(m[1])), fmax(fabs(m[3]), fabs(m[4])));
+  const double trn = fmax(fabs(m[2]), fabs(m[5]));
+  const double eps = 5.9604644775390625e-08;  // 2^-24
+  const double delta = 2.0 * (1.5 * (6.0 * eps * (lin * jp.cmax + trn) + eps * jp.rmax) + 4.0 * eps * (tol + 1.0)) +
+                       1.0e-6;
+  const double lo = tol - delta;
+  const float lo2 = lo > 0.0 ? static_cast<float>(lo * lo) : -1.0f;
+  const float hi2 = static_cast<float>((tol + delta) * (tol + delta));
+  const float r = static_cast<float>(tol + delta);
+  if (lane < 3) w.used_r[lane] = 0u;
+  __syncwarp();
+  int cnt = 0;
+  double acc = 0.0;
+  bool conf = false;
+  for (int i = lane; i < jp.nm; i += 32) {
+    const float x = __fadd_rn(__fadd_rn(__fmul_rn(m0, jp.mx32[i]), __fmul_rn(m1, jp.my32[i])), m2);
+    const float y = __fadd_rn(__fadd_rn(__fmul_rn(m3, jp.mx32[i]), __fmul_rn(m4, jp.my32[i])), m5);
+    int hits = 0;
+    bool have64 = false;
+    double x64 = 0.0, y64 = 0.0;
+    grid_visit(jp, x, y, r, [&](int j) {
+      const float fx = x - jp.rx32[j], fy = y - jp.ry32[j];
+      const float d2 = fx * fx + fy * fy;
+      if (d2 > hi2) return;
+      if (!have64) {
+        x64 = dadd(dadd(dmul(jp.mx[i], m[0]), dmul(jp.my[i], m[1])), m[2]);
+        y64 = dadd(dadd(dmul(jp.mx[i], m[3]), dmul(jp.my[i], m[4])), m[5]);
+        have64 = true;
+      }
+      const double ex = dsub(x64, jp.rx[j]), ey = dsub(y64, jp.ry[j]);
+      const double dd2 = dadd(dmul(ex, ex), dmul(ey, ey));
+      if (!(d2 <= lo2) && !(sqrt(dd2) <= tol)) return;
+      ++hits;
+      acc = dadd(acc, dd2);
+      const unsigned bit = 1u << (j & 31);
+      if (atomicOr(&w.used_r[j >> 5], bit) & bit) conf = true;
+    });
+    if (hits > 1) conf = true;
+    cnt += hits;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+    acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, off));
+  }
+  conflict = __any_sync(0xffffffffu, conf);
+  count = cnt;
+  sum_d2 = acc;
+  __syncwarp();
+}
+
+// Warp-cooperative similarity fit of n <= 80 pairs: the same arithmetic as
+// fit_similarity with the independent sums on separate lanes.  Every lane
+// returns the result.
+__device__ bool warp_fit_similarity(const double* mx, const double* my, const double* rx, const double* ry, int n,
+                                    double* sq, double (&m)[6]) {
+  const int lane = threadIdx.x & 31;
+  if (n < 2) return false;
+  double s = 0.0;
+  if (lane < 4) {
+    const double* v = lane == 0 ? mx : (lane == 1 ? my : (lane == 2 ? rx : ry));
+    for (int i = 0; i < n; ++i) s = dadd(s, v[i]);
+  }
+  const double dn = static_cast<double>(n);
+  const double mmx = __ddiv_rn(__shfl_sync(0xffffffffu, s, 0), dn);
+  const double mmy = __ddiv_rn(__shfl_sync(0xffffffffu, s, 1), dn);
+  const double mrx = __ddiv_rn(__shfl_sync(0xffffffffu, s, 2), dn);
+  const double mry = __ddiv_rn(__shfl_sync(0xffffffffu, s, 3), dn);
+  for (int i = lane; i < n; i += 32) {
+    const double cx = dsub(mx[i], mmx), cy = dsub(my[i], mmy);
+    sq[2 * i] = dmul(cx, cx);
+    sq[2 * i + 1] = dmul(cy, cy);
+  }
+  __syncwarp();
+  double variance;
+  if (2 * n <= 128) {
+    variance = warp_pw_sum(sq, 2 * n);
+  } else {
+    int n2 = n;  // (2n) / 2
+    n2 -= n2 % 8;
+    variance = dadd(warp_pw_sum(sq, n2), warp_pw_sum(sq + n2, 2 * n - n2));
+  }
+  if (!(variance > 1.0e-12)) return false;
+  double c = 0.0;
+  if (lane < 4) {
+    for (int i = 0; i < n; ++i) {
+      const double a = lane < 2 ? dsub(mx[i], mmx) : dsub(my[i], mmy);
+      const double b = (lane & 1) == 0 ? dsub(rx[i], mrx) : dsub(ry[i], mry);
+      c = dadd(c, dmul(a, b));
+    }
+  }
+  const double c00 = __shfl_sync(0xffffffffu, c, 0), c01 = __shfl_sync(0xffffffffu, c, 1);
+  const double c10 = __shfl_sync(0xffffffffu, c, 2), c11 = __shfl_sync(0xffffffffu, c, 3);
+  const double e = hyp_sum(dadd(c00, c11), dsub(c01, c10));
+  const double f = hyp_sum(dsub(c00, c11), dadd(c01, c10));
+  double cs = 1.0, sn = 0.0;
+  if (e > 0.0) {
+    cs = __ddiv_rn(dadd(c00, c11), e);
+    sn = __ddiv_rn(dsub(c01, c10), e);
+  }
+  const double scale = __ddiv_rn(fmax(e, f), variance);
+  const double l00 = dmul(scale, cs), l01 = dmul(scale, -sn), l10 = dmul(scale, sn), l11 = dmul(scale, cs);
+  m[0] = l00;
+  m[1] = l01;
+  m[2] = dsub(mrx, dadd(dmul(mmx, l00), dmul(mmy, l01)));
+  m[3] = l10;
+  m[4] = l11;
+  m[5] = dsub(mry, dadd(dmul(mmx, l10), dmul(mmy, l11)));
+  return true;
 }
 
 // ---- K1: triangle descriptors, one CTA per catalog row ----------------------------------
@@ -454,15 +651,26 @@ __global__ void __launch_bounds__(1024) reg_match_kernel(RegArgs a) {
   double2* rdd = reinterpret_cast<double2*>(smem);              // [kMaxDesc]
   double2* mdd = rdd + kMaxDesc;                                // [kMaxDesc]
   SelEntry* sel = reinterpret_cast<SelEntry*>(mdd + kMaxDesc);  // [kMaxSel]
+  float2* rdf = reinterpret_cast<float2*>(sel + kMaxSel);       // [kMaxDesc]
+  float2* mdf = rdf + kMaxDesc;                                 // [kMaxDesc]
   __shared__ unsigned s_count;
   __shared__ int s_c, s_n;
+  __shared__ unsigned s_hist[256];
+  __shared__ unsigned long long s_prefix;
+  __shared__ int s_rank, s_eq;
   const int j = blockIdx.x;
   const RegJob job = a.jobs[j];
   const Desc* rd = a.desc + static_cast<int64_t>(job.ref_row) * kMaxDesc;
   const Desc* md = a.desc + static_cast<int64_t>(job.mov_row) * kMaxDesc;
   const int nr = a.ndesc[job.ref_row], nm = a.ndesc[job.mov_row];
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) rdd[i] = make_double2(rd[i].d0, rd[i].d1);
-  for (int i = threadIdx.x; i < nm; i += blockDim.x) mdd[i] = make_double2(md[i].d0, md[i].d1);
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    rdd[i] = make_double2(rd[i].d0, rd[i].d1);
+    rdf[i] = make_float2(static_cast<float>(rd[i].d0), static_cast<float>(rd[i].d1));
+  }
+  for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+    mdd[i] = make_double2(md[i].d0, md[i].d1);
+    mdf[i] = make_float2(static_cast<float>(md[i].d0), static_cast<float>(md[i].d1));
+  }
   double* mdist = a.match_dist + static_cast<int64_t>(j) * a.match_cap;
   int* mkey = a.match_key + static_cast<int64_t>(j) * a.match_cap;
   if (threadIdx.x == 0) s_count = 0;
@@ -470,19 +678,25 @@ __global__ void __launch_bounds__(1024) reg_match_kernel(RegArgs a) {
   const int total = nm * nr;
   const double radius = a.radius;
   const double bound = radius * 1.000001 + 1.0e-300;
+  const float radf = static_cast<float>(radius) * 1.000001f + 1.0e-30f;
   const bool list_mode = a.mode == kDescriptorList;
   // descriptor distance of flat index q = moving * nr + reference; false when
   // the pair is outside the radius
   auto match_dist = [&](int q, double& d) -> bool {
     const int mi = q / nr, ri = q - (q / nr) * nr;
-    const double2 r = rdd[ri], m = mdd[mi];
+    const float2 rf = rdf[ri], mf = mdf[mi];
     if (list_mode) {
-      const float e0 = __fsub_rn(static_cast<float>(r.x), static_cast<float>(m.x));
-      const float e1 = __fsub_rn(static_cast<float>(r.y), static_cast<float>(m.y));
+      const float e0 = __fsub_rn(rf.x, mf.x);
+      const float e1 = __fsub_rn(rf.y, mf.y);
       const float df = sqrtf(__fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1)));
       d = static_cast<double>(df);
       return d <= radius;
     }
+    // float32 bounds per component (conversion error <= 2^-24 relative),
+    // then the float64 distance
+    if (fabsf(rf.x - mf.x) > radf + 3.0e-7f * (fabsf(rf.x) + fabsf(mf.x))) return false;
+    if (fabsf(rf.y - mf.y) > radf + 3.0e-7f * (fabsf(rf.y) + fabsf(mf.y))) return false;
+    const double2 r = rdd[ri], m = mdd[mi];
     const double e0 = dsub(r.x, m.x);
     if (fabs(e0) > bound) return false;
     const double e1 = dsub(r.y, m.y);
@@ -554,22 +768,73 @@ __global__ void __launch_bounds__(1024) reg_match_kernel(RegArgs a) {
     t = 0ull;
     K = -1;  // keeps nothing: distances are never below +0
   } else if (take < n) {
-    unsigned long long lo = 0ull, hi = dbits(radius);
-    while (lo < hi) {
-      const unsigned long long mid = lo + (hi - lo) / 2;
-      if (block_count([&](unsigned long long b, int) { return b <= mid; }) >= take) hi = mid;
-      else lo = mid + 1;
+    int need = 0, equal = 0;
+    if (stored_all) {
+      // radix select (8-bit digits, most significant first) of the
+      // (take - 1)-th smallest distance among the stored matches
+      unsigned long long prefix = 0ull, mask = 0ull;
+      int rank = take - 1;
+      for (int shift = 56; shift >= 0; shift -= 8) {
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) s_hist[i] = 0u;
+        __syncthreads();
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+          const unsigned long long k = dbits(mdist[q]);
+          if ((k & mask) == prefix) atomicAdd(&s_hist[(k >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+          const int lane = threadIdx.x;
+          unsigned loc = 0;
+          for (int b = 0; b < 8; ++b) loc += s_hist[lane * 8 + b];
+          unsigned incl = loc;
+          for (int off = 1; off < 32; off <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += v;
+          }
+          const unsigned excl = incl - loc;
+          const bool here = excl <= static_cast<unsigned>(rank) && static_cast<unsigned>(rank) < incl;
+          if (here) {
+            unsigned r = static_cast<unsigned>(rank) - excl;
+            int b = lane * 8;
+            while (r >= s_hist[b]) {
+              r -= s_hist[b];
+              ++b;
+            }
+            s_prefix = prefix | (static_cast<unsigned long long>(b) << shift);
+            s_rank = static_cast<int>(r);
+            s_eq = static_cast<int>(s_hist[b]);
+          }
+        }
+        __syncthreads();
+        prefix = s_prefix;
+        rank = s_rank;
+        mask |= 0xffull << shift;
+        __syncthreads();
+      }
+      t = prefix;
+      need = rank + 1;  // entries at exactly distance t to keep
+      equal = s_eq;     // entries at exactly distance t
+    } else {
+      unsigned long long lo = 0ull, hi = dbits(radius);
+      while (lo < hi) {
+        const unsigned long long mid = lo + (hi - lo) / 2;
+        if (block_count([&](unsigned long long b, int) { return b <= mid; }) >= take) hi = mid;
+        else lo = mid + 1;
+      }
+      t = lo;
+      const int below = t == 0 ? 0 : block_count([&](unsigned long long b, int) { return b < t; });
+      need = take - below;
+      equal = block_count([&](unsigned long long b, int) { return b == t; });
     }
-    t = lo;
-    const int below = t == 0 ? 0 : block_count([&](unsigned long long b, int) { return b < t; });
-    const int need = take - below;
-    int klo = 0, khi = total - 1;
-    while (klo < khi) {
-      const int mid = klo + (khi - klo) / 2;
-      if (block_count([&](unsigned long long b, int q) { return b == t && q <= mid; }) >= need) khi = mid;
-      else klo = mid + 1;
+    if (need < equal) {  // ties at the cut: the smallest flat indices win
+      int klo = 0, khi = total - 1;
+      while (klo < khi) {
+        const int mid = klo + (khi - klo) / 2;
+        if (block_count([&](unsigned long long b, int q) { return b == t && q <= mid; }) >= need) khi = mid;
+        else klo = mid + 1;
+      }
+      K = klo;
     }
-    K = klo;
   }
   if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
@@ -627,14 +892,18 @@ __global__ void __launch_bounds__(1024) reg_match_kernel(RegArgs a) {
   }
 }
 
-// ---- K3: candidate transforms, one warp per candidate ------------------------------
-__device__ void load_job_points(const RegArgs& a, const RegJob& job, JobPoints& jp) {
+// ---- K3: candidate transforms ---------------------------------------------------------
+// Loads the two catalogs of a job and buckets the reference stars (block-wide;
+// the caller synchronises afterwards).
+__device__ void load_job_points(const RegArgs& a, const RegJob& job, JobPoints& jp, double tol) {
   const int nm = min(a.npts[job.mov_row], a.max_stars);
   const int nr = min(a.npts[job.ref_row], a.max_stars);
   for (int i = threadIdx.x; i < kRegPts; i += blockDim.x) {
     if (i < nm) {
       jp.mx[i] = row_x(a, job.mov_row, i);
       jp.my[i] = row_y(a, job.mov_row, i);
+      jp.mx32[i] = static_cast<float>(jp.mx[i]);
+      jp.my32[i] = static_cast<float>(jp.my[i]);
     }
     if (i < nr) {
       jp.rx[i] = row_x(a, job.ref_row, i);
@@ -643,20 +912,75 @@ __device__ void load_job_points(const RegArgs& a, const RegJob& job, JobPoints& 
       jp.ry32[i] = static_cast<float>(jp.ry[i]);
     }
   }
+  __syncthreads();
   if (threadIdx.x == 0) {
     jp.nm = nm;
     jp.nr = nr;
+    float cmax = 0.0f, rmax = 0.0f;
+    for (int i = 0; i < nm; ++i) cmax = fmaxf(cmax, fabsf(jp.mx32[i]) + fabsf(jp.my32[i]));
+    float x0 = 3.0e38f, x1 = -3.0e38f, y0 = 3.0e38f, y1 = -3.0e38f;
+    for (int i = 0; i < nr; ++i) {
+      x0 = fminf(x0, jp.rx32[i]);
+      x1 = fmaxf(x1, jp.rx32[i]);
+      y0 = fminf(y0, jp.ry32[i]);
+      y1 = fmaxf(y1, jp.ry32[i]);
+      rmax = fmaxf(rmax, fmaxf(fabsf(jp.rx32[i]), fabsf(jp.ry32[i])));
+    }
+    jp.cmax = cmax * 1.0001f + 1.0f;
+    jp.rmax = rmax * 1.0001f + 1.0f;
+    for (int c = 0; c <= kGrid * kGrid; ++c) jp.cell_start[c] = 0;
+    if (nr == 0) {
+      jp.gnx = jp.gny = 0;
+      jp.gx0 = jp.gy0 = 0.0f;
+      jp.ginv = 1.0f;
+    } else {
+      // cells at least 2 * (tol + 0.5) wide (> the widest search radius) so
+      // a search touches <= 2 x 2 cells
+      const float reach = static_cast<float>(2.0 * (tol + 0.5)) + 1.0f;
+      const float cell = fmaxf(fmaxf(x1 - x0, y1 - y0) / static_cast<float>(kGrid), reach);
+      jp.gx0 = x0;
+      jp.gy0 = y0;
+      if (cell < 1.0e30f) {
+        jp.ginv = 1.0f / cell;
+        jp.gnx = min(kGrid, static_cast<int>((x1 - x0) * jp.ginv) + 1);
+        jp.gny = min(kGrid, static_cast<int>((y1 - y0) * jp.ginv) + 1);
+      } else {  // one cell holding every star
+        jp.ginv = 0.0f;
+        jp.gnx = jp.gny = 1;
+      }
+      unsigned char cnt[kGrid * kGrid];
+      for (int c = 0; c < kGrid * kGrid; ++c) cnt[c] = 0;
+      int cellof[kRegPts];
+      for (int i = 0; i < nr; ++i) {
+        const int cx = min(jp.gnx - 1, max(0, static_cast<int>((jp.rx32[i] - x0) * jp.ginv)));
+        const int cy = min(jp.gny - 1, max(0, static_cast<int>((jp.ry32[i] - y0) * jp.ginv)));
+        cellof[i] = cy * kGrid + cx;
+        ++cnt[cellof[i]];
+      }
+      int run = 0;
+      for (int c = 0; c < kGrid * kGrid; ++c) {
+        jp.cell_start[c] = static_cast<unsigned char>(run);
+        run += cnt[c];
+      }
+      jp.cell_start[kGrid * kGrid] = static_cast<unsigned char>(run);
+      for (int c = 0; c < kGrid * kGrid; ++c) cnt[c] = jp.cell_start[c];
+      for (int i = 0; i < nr; ++i) jp.cell_pt[cnt[cellof[i]]++] = static_cast<unsigned char>(i);
+    }
   }
 }
 
 constexpr int kScoreWarps = 4;
 
+// Cand::valid bits: 1 = fit succeeded, 2 = count and rms are exact.
 __global__ void __launch_bounds__(32 * kScoreWarps) reg_score_kernel(RegArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  WarpScratch* ws = reinterpret_cast<WarpScratch*>(smem);
   __shared__ JobPoints jp;
-  __shared__ WarpScratch ws[kScoreWarps];
+  __shared__ double cm[kScoreWarps][32][6];
+  __shared__ int cok[kScoreWarps][32];
   const int j = blockIdx.y;
   const RegJob job = a.jobs[j];
-  load_job_points(a, job, jp);
+  load_job_points(a, job, jp, a.tol);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncand = 2 * a.nsel[j];
@@ -665,87 +989,144 @@ __global__ void __launch_bounds__(32 * kScoreWarps) reg_score_kernel(RegArgs a) 
   const int2* sel = a.sel + static_cast<int64_t>(j) * a.sel_cap;
   const long long* order = a.sel_order + static_cast<int64_t>(j) * a.sel_cap;
   Cand* cands = a.cands + static_cast<int64_t>(j) * 2 * a.sel_cap;
-  for (int c = blockIdx.x * kScoreWarps + warp; c < ncand; c += gridDim.x * kScoreWarps) {
-    const int2 s = sel[c >> 1];
-    const Desc dm = md[s.x], dr = rd[s.y];
-    int rv0 = dr.v[0], rv1 = dr.v[1];
-    if (c & 1) {  // reference triangle in the order [1, 0, 2]
-      const int q = rv0;
-      rv0 = rv1;
-      rv1 = q;
+  for (int base = (blockIdx.x * kScoreWarps + warp) * 32; base < ncand; base += gridDim.x * kScoreWarps * 32) {
+    // one 3-point fit per lane
+    const int c = base + lane;
+    int ok = 0;
+    if (c < ncand) {
+      const int2 s = sel[c >> 1];
+      const Desc dm = md[s.x], dr = rd[s.y];
+      int rv0 = dr.v[0], rv1 = dr.v[1];
+      if (c & 1) {  // reference triangle in the order [1, 0, 2]
+        const int q = rv0;
+        rv0 = rv1;
+        rv1 = q;
+      }
+      const double tmx[3] = {jp.mx[dm.v[0]], jp.mx[dm.v[1]], jp.mx[dm.v[2]]};
+      const double tmy[3] = {jp.my[dm.v[0]], jp.my[dm.v[1]], jp.my[dm.v[2]]};
+      const double trx[3] = {jp.rx[rv0], jp.rx[rv1], jp.rx[dr.v[2]]};
+      const double try_[3] = {jp.ry[rv0], jp.ry[rv1], jp.ry[dr.v[2]]};
+      double scratch[6];
+      double m[6];
+      ok = fit_similarity(tmx, tmy, trx, try_, 3, scratch, m) ? 1 : 0;
+      Cand& cd = cands[c];
+      for (int q = 0; q < 6; ++q) {
+        cm[warp][lane][q] = ok ? m[q] : 0.0;
+        cd.m[q] = ok ? m[q] : 0.0;
+      }
+      cd.order = 2 * order[c >> 1] + (c & 1);
     }
-    const double tmx[3] = {jp.mx[dm.v[0]], jp.mx[dm.v[1]], jp.mx[dm.v[2]]};
-    const double tmy[3] = {jp.my[dm.v[0]], jp.my[dm.v[1]], jp.my[dm.v[2]]};
-    const double trx[3] = {jp.rx[rv0], jp.rx[rv1], jp.rx[dr.v[2]]};
-    const double try_[3] = {jp.ry[rv0], jp.ry[rv1], jp.ry[dr.v[2]]};
-    double scratch[6];
-    double m[6];
-    const bool ok = fit_similarity(tmx, tmy, trx, try_, 3, scratch, m);
-    Cand cd;
-    cd.valid = ok ? 1 : 0;
-    cd.count = 0;
-    cd.rms = __longlong_as_double(0x7ff0000000000000ll);
-    cd.order = 2 * order[c >> 1] + (c & 1);
-    for (int q = 0; q < 6; ++q) cd.m[q] = ok ? m[q] : 0.0;
-    if (ok) warp_score(m, jp, a.tol, ws[warp], cd.count, cd.rms, nullptr, a.overflow);
-    if (lane == 0) cands[c] = cd;
+    cok[warp][lane] = ok;
+    __syncwarp();
+    // score the chunk one candidate at a time with the whole warp
+    const int nb = min(32, ncand - base);
+    for (int t = 0; t < nb; ++t) {
+      int count = 0, exact = 0;
+      double rms = __longlong_as_double(0x7ff0000000000000ll);
+      if (cok[warp][t]) {
+        double m[6];
+        for (int q = 0; q < 6; ++q) m[q] = cm[warp][t][q];
+        double sum_d2;
+        bool conflict;
+        warp_score_fast(m, jp, a.tol, ws[warp], count, sum_d2, conflict);
+        if (conflict) {
+          warp_score_exact(m, jp, a.tol, ws[warp], count, rms, nullptr, a.overflow);
+          exact = 1;
+        } else if (count > 0) {
+          rms = sqrt(__ddiv_rn(sum_d2, static_cast<double>(count)));
+        }
+      }
+      if (lane == 0) {
+        Cand& cd = cands[base + t];
+        cd.count = count;
+        cd.rms = rms;
+        cd.valid = cok[warp][t] ? (1 | (exact << 1)) : 0;
+      }
+    }
     __syncwarp();
   }
 }
 
 // ---- K4: best candidate and guarded refits, one warp per frame pair --------------------
-// Is (n1, r1, o1) preferred over (n2, r2, o2)?  An order below zero marks "none".
-__device__ __forceinline__ bool cand_better(int n1, double r1, long long o1, int n2, double r2, long long o2) {
-  if (o1 < 0) return false;
-  if (o2 < 0) return true;
-  if (n1 != n2) return n1 > n2;
-  if (r1 != r2) return r1 < r2;
-  return o1 < o2;
-}
+// The reference keeps the first candidate with the most pairs and, among
+// those, the smallest rms.  Counts are exact for every candidate; the fast
+// rms differs from the exact one by < 1e-13 relative, so every candidate that
+// can win lies in the window rms <= min * (1 + 1e-12) and only those are
+// re-scored exactly (usually one).
+constexpr int kWindowCap = 1024;
 
 __global__ void __launch_bounds__(32) reg_best_kernel(RegArgs a) {
   __shared__ JobPoints jp;
   __shared__ WarpScratch ws;
   __shared__ double fx[kRegPts], fy[kRegPts], gx[kRegPts], gy[kRegPts], buf[2 * kRegPts];
   __shared__ short2 prs[kRegPts], prs2[kRegPts];
+  __shared__ int window[kWindowCap];
   const int j = blockIdx.x;
   const int lane = threadIdx.x;
   const RegJob job = a.jobs[j];
-  load_job_points(a, job, jp);
-  __syncwarp();
+  load_job_points(a, job, jp, a.tol);
+  __syncthreads();
   const int ncand = 2 * a.nsel[j];
   const Cand* cs = a.cands + static_cast<int64_t>(j) * 2 * a.sel_cap;
-  int bn = 0, bc = -1;
-  double br = __longlong_as_double(0x7ff0000000000000ll);
-  long long bo = -1;
-  for (int c = lane; c < ncand; c += 32) {
-    const Cand& cd = cs[c];
-    if (!cd.valid || cd.count <= 0) continue;  // never accepted by the reference
-    if (cand_better(cd.count, cd.rms, cd.order, bn, br, bo)) {
-      bn = cd.count;
-      br = cd.rms;
-      bo = cd.order;
-      bc = c;
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  // most pairs
+  int bn = 0;
+  for (int c = lane; c < ncand; c += 32)
+    if ((cs[c].valid & 1) && cs[c].count > bn) bn = cs[c].count;
+  for (int off = 16; off > 0; off >>= 1) bn = max(bn, __shfl_xor_sync(0xffffffffu, bn, off));
+  // smallest (fast) rms among them
+  double rmin = inf;
+  if (bn > 0) {
+    for (int c = lane; c < ncand; c += 32)
+      if ((cs[c].valid & 1) && cs[c].count == bn) rmin = fmin(rmin, cs[c].rms);
+    for (int off = 16; off > 0; off >>= 1) rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, off));
+  }
+  const double thr = rmin + rmin * 1.0e-12;
+  // window members in candidate order
+  int nw = 0;
+  if (bn > 0) {
+    for (int base = 0; base < ncand; base += 32) {
+      const int c = base + lane;
+      const bool in = c < ncand && (cs[c].valid & 1) && cs[c].count == bn && cs[c].rms <= thr;
+      const unsigned mask = __ballot_sync(0xffffffffu, in);
+      if (in) {
+        const int pos = nw + __popc(mask & ((1u << lane) - 1u));
+        if (pos < kWindowCap) window[pos] = c;
+      }
+      nw += __popc(mask);
     }
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    const int on = __shfl_xor_sync(0xffffffffu, bn, off);
-    const double orr = __shfl_xor_sync(0xffffffffu, br, off);
-    const long long oo = __shfl_xor_sync(0xffffffffu, bo, off);
-    const int oc = __shfl_xor_sync(0xffffffffu, bc, off);
-    if (cand_better(on, orr, oo, bn, br, bo)) {
-      bn = on;
-      br = orr;
-      bo = oo;
-      bc = oc;
+  if (nw > kWindowCap) {
+    if (lane == 0) atomicExch(a.overflow, 1);
+    nw = kWindowCap;
+  }
+  __syncwarp();
+  // exact rms of the window members: smallest wins, earliest order on ties
+  int bc = -1;
+  double br = inf;
+  long long bo = -1;
+  for (int w = 0; w < nw; ++w) {
+    const int c = window[w];
+    double r = cs[c].rms;
+    if (!(cs[c].valid & 2)) {
+      double m[6];
+      for (int q = 0; q < 6; ++q) m[q] = cs[c].m[q];
+      int n;
+      warp_score_exact(m, jp, a.tol, ws, n, r, nullptr, a.overflow);
+    }
+    const long long o = cs[c].order;
+    if (bc < 0 || r < br || (r == br && o < bo)) {
+      bc = c;
+      br = r;
+      bo = o;
     }
   }
   double best[6] = {1.0, 0.0, 0.0, 0.0, 1.0, 0.0};
   int best_n = 0;
-  double best_rms = __longlong_as_double(0x7ff0000000000000ll);
+  double best_rms = inf;
   if (bc >= 0) {
     for (int q = 0; q < 6; ++q) best[q] = cs[bc].m[q];
-    warp_score(best, jp, a.tol, ws, best_n, best_rms, prs, a.overflow);
+    warp_score_exact(best, jp, a.tol, ws, best_n, best_rms, prs, a.overflow);
   }
   __syncwarp();
   const int iterations = a.mode == kEstimator ? 3 : 0;
@@ -759,14 +1140,10 @@ __global__ void __launch_bounds__(32) reg_best_kernel(RegArgs a) {
     }
     __syncwarp();
     double m[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    int ok = 0;
-    if (lane == 0) ok = fit_similarity(fx, fy, gx, gy, best_n, buf, m) ? 1 : 0;
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) break;
-    for (int q = 0; q < 6; ++q) m[q] = __shfl_sync(0xffffffffu, m[q], 0);
+    if (!warp_fit_similarity(fx, fy, gx, gy, best_n, buf, m)) break;
     int n2;
     double r2;
-    warp_score(m, jp, a.tol, ws, n2, r2, prs2, a.overflow);
+    warp_score_exact(m, jp, a.tol, ws, n2, r2, prs2, a.overflow);
     if (n2 > best_n || (n2 == best_n && r2 <= best_rms)) {
       for (int q = 0; q < 6; ++q) best[q] = m[q];
       for (int q = lane; q < n2; q += 32) prs[q] = prs2[q];
@@ -936,17 +1313,21 @@ static void launch_desc(const RegArgs& a, int rows, cudaStream_t stream) {
 }
 
 static void launch_match_score_best(const RegArgs& a, int njobs, int64_t max_sel, cudaStream_t stream) {
-  const size_t smem = sizeof(double2) * 2 * kMaxDesc + sizeof(SelEntry) * kMaxSel;
+  const size_t smem = (sizeof(double2) + sizeof(float2)) * 2 * kMaxDesc + sizeof(SelEntry) * kMaxSel;
   check_cuda(cudaFuncSetAttribute(reg_match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(smem)),
              "cudaFuncSetAttribute(reg_match)");
   note_launch();
   reg_match_kernel<<<njobs, 1024, smem, stream>>>(a);
   check_cuda(cudaGetLastError(), "reg_match launch");
-  const int64_t per_job = (2 * max_sel + kScoreWarps - 1) / kScoreWarps;
+  const int64_t per_job = (2 * max_sel + 32 * kScoreWarps - 1) / (32 * kScoreWarps);
   const unsigned gx = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(per_job, 1024)));
+  const size_t score_smem = sizeof(WarpScratch) * kScoreWarps;
+  check_cuda(cudaFuncSetAttribute(reg_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(score_smem)),
+             "cudaFuncSetAttribute(reg_score)");
   note_launch();
-  reg_score_kernel<<<dim3(gx, static_cast<unsigned>(njobs)), 32 * kScoreWarps, 0, stream>>>(a);
+  reg_score_kernel<<<dim3(gx, static_cast<unsigned>(njobs)), 32 * kScoreWarps, score_smem, stream>>>(a);
   check_cuda(cudaGetLastError(), "reg_score launch");
   note_launch();
   reg_best_kernel<<<njobs, 32, 0, stream>>>(a);
@@ -1005,8 +1386,11 @@ static void check_overflow(const RegScratch& r, cudaStream_t stream) {
   if (overflow) fail(GG_ERR_RUNTIME, "registration buffers overflowed (too many descriptor matches or point pairs)");
 }
 
+// Pixel coordinates: finite and within +-1e15 (float32-representable with
+// room for the transform error bound).
 static void require_finite_points(const double* xy, int64_t n) {
-  for (int64_t i = 0; i < 2 * n; ++i) require(std::isfinite(xy[i]), "star coordinates must be finite");
+  for (int64_t i = 0; i < 2 * n; ++i)
+    require(std::isfinite(xy[i]) && std::fabs(xy[i]) <= 1.0e15, "star coordinates must be finite and within 1e15");
 }
 
 }  // namespace gg

@@ -76,14 +76,11 @@ struct SelectArgs {
   int mode;            // 0: v, 1: |v - median|
 };
 
-__device__ __forceinline__ bool select_value(const SelectArgs& a, const StarFrameState& st, float v, unsigned& key) {
-  if (!isfinite(v)) return false;
-  if (a.mode == 1) v = fabsf(__fsub_rn(v, st.median));
-  key = float_key(v);
-  return true;
-}
-
 // Histogram pass: digit of `pass` for keys matching each rank's prefix.
+// Sky pixels share their leading digits, so each thread keeps a run-length
+// counter per histogram (last digit, count) and only touches shared memory
+// when the digit changes; four pixels per float4 load.
+template <int PASS>
 __global__ void __launch_bounds__(256) select_hist_kernel(SelectArgs a) {
   __shared__ unsigned h[2][kSelBins];
   __shared__ unsigned s_valid;
@@ -91,70 +88,137 @@ __global__ void __launch_bounds__(256) select_hist_kernel(SelectArgs a) {
   for (int i = threadIdx.x; i < 2 * kSelBins; i += blockDim.x) (&h[0][0])[i] = 0u;
   if (threadIdx.x == 0) s_valid = 0;
   __syncthreads();
-  const StarFrameState st = a.state[k];
+  const unsigned p0 = a.state[k].prefix[0], p1 = a.state[k].prefix[1];
+  const float median = a.state[k].median;
+  const bool absdev = a.mode == 1;
   const float* src = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
-  const int shift = a.pass == 0 ? 21 : (a.pass == 1 ? 10 : 0);
-  const unsigned digit_mask = a.pass == 2 ? 1023u : 2047u;
-  const int prefix_shift = a.pass == 0 ? 32 : (a.pass == 1 ? 21 : 10);
+  constexpr int kShift = PASS == 0 ? 21 : (PASS == 1 ? 10 : 0);
+  constexpr unsigned kMask = PASS == 2 ? 1023u : 2047u;
+  constexpr int kPrefixShift = PASS == 1 ? 21 : 10;
   unsigned valid = 0;
-  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < a.pixels; p += int64_t(gridDim.x) * blockDim.x) {
-    unsigned key;
-    if (!select_value(a, st, __ldg(src + p), key)) continue;
+  unsigned d0 = 0xffffffffu, n0 = 0u, d1 = 0xffffffffu, n1 = 0u;
+  auto add = [&](float v) {
+    if (!isfinite(v)) return;
     ++valid;
-    const unsigned digit = (key >> shift) & digit_mask;
-    if (a.pass == 0) {
-      atomicAdd(&h[0][digit], 1u);
-    } else {
-      const unsigned hp = key >> prefix_shift;
-      if (hp == st.prefix[0]) atomicAdd(&h[0][digit], 1u);
-      if (hp == st.prefix[1]) atomicAdd(&h[1][digit], 1u);
+    if (absdev) v = fabsf(__fsub_rn(v, median));
+    const unsigned key = float_key(v);
+    const unsigned digit = (key >> kShift) & kMask;
+    bool in0 = true, in1 = false;
+    if constexpr (PASS != 0) {
+      const unsigned hp = key >> kPrefixShift;
+      in0 = hp == p0;
+      in1 = hp == p1;
     }
+    if (in0) {
+      if (digit == d0) {
+        ++n0;
+      } else {
+        if (n0) atomicAdd(&h[0][d0], n0);
+        d0 = digit;
+        n0 = 1u;
+      }
+    }
+    if (in1) {
+      if (digit == d1) {
+        ++n1;
+      } else {
+        if (n1) atomicAdd(&h[1][d1], n1);
+        d1 = digit;
+        n1 = 1u;
+      }
+    }
+  };
+  const int64_t gtid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  const int64_t gstride = int64_t(gridDim.x) * blockDim.x;
+  const int64_t n4 = a.pixels / 4;  // slots start on 256-byte boundaries
+  const float4* src4 = reinterpret_cast<const float4*>(src);
+  for (int64_t i = gtid; i < n4; i += gstride) {
+    const float4 q = __ldg(src4 + i);
+    add(q.x);
+    add(q.y);
+    add(q.z);
+    add(q.w);
   }
-  if (a.pass == 0) {
+  for (int64_t p = n4 * 4 + gtid; p < a.pixels; p += gstride) add(__ldg(src + p));
+  if (n0) atomicAdd(&h[0][d0], n0);
+  if (n1) atomicAdd(&h[1][d1], n1);
+  if (PASS == 0) {
     valid = __reduce_add_sync(0xffffffffu, valid);
     if ((threadIdx.x & 31) == 0 && valid) atomicAdd(&s_valid, valid);
   }
   __syncthreads();
   unsigned* g = a.hist + static_cast<int64_t>(k) * 2 * kSelBins;
-  const int nh = a.pass == 0 ? 1 : 2;
+  const int nh = PASS == 0 ? 1 : 2;
   for (int i = threadIdx.x; i < nh * kSelBins; i += blockDim.x) {
     const unsigned v = (&h[0][0])[i];
     if (v) atomicAdd(g + i, v);
   }
-  if (a.pass == 0 && a.mode == 0 && threadIdx.x == 0 && s_valid) atomicAdd(&a.state[k].count, s_valid);
+  if (PASS == 0 && a.mode == 0 && threadIdx.x == 0 && s_valid) atomicAdd(&a.state[k].count, s_valid);
 }
 
-// One warp per frame: locate each rank's bucket in the histogram.
+// One block per frame: locate each rank's bucket in the histogram (copied to
+// shared memory, then a warp prefix scan over 32 runs of bins).
 // ranks: pass 0 sets them from the valid count (median of n: n//2 and
 // n//2 - 1 when n is even, both n//2 when odd).
-__global__ void select_scan_kernel(SelectArgs a, int frames) {
+__global__ void __launch_bounds__(256) select_scan_kernel(SelectArgs a, int frames) {
+  __shared__ unsigned hs[2][kSelBins];
+  __shared__ unsigned s_bucket[2], s_rem[2];
   const int k = blockIdx.x;
   if (k >= frames) return;
   StarFrameState& st = a.state[k];
   const unsigned* g = a.hist + static_cast<int64_t>(k) * 2 * kSelBins;
   const int nbins = a.pass == 2 ? 1024 : kSelBins;
-  if (threadIdx.x == 0) {
-    if (a.pass == 0) {
-      const unsigned n = st.count;
-      const unsigned hi = n / 2;
-      const unsigned lo = (n & 1u) ? hi : (hi > 0 ? hi - 1 : 0);
-      st.residual[0] = lo;
-      st.residual[1] = hi;
-    }
+  const int nh = a.pass == 0 ? 1 : 2;
+  for (int i = threadIdx.x; i < nh * kSelBins; i += blockDim.x) (&hs[0][0])[i] = g[i];
+  if (threadIdx.x == 0 && a.pass == 0) {
+    const unsigned n = st.count;
+    const unsigned hi = n / 2;
+    const unsigned lo = (n & 1u) ? hi : (hi > 0 ? hi - 1 : 0);
+    st.residual[0] = lo;
+    st.residual[1] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int per = nbins / 32;
     for (int r = 0; r < 2; ++r) {
-      const unsigned* hr = g + (a.pass == 0 ? 0 : r * kSelBins);
-      unsigned rem = st.residual[r];
-      int b = 0;
-      for (; b < nbins; ++b) {
-        if (rem < hr[b]) break;
-        rem -= hr[b];
+      const unsigned* hr = hs[a.pass == 0 ? 0 : r];
+      const unsigned rem = st.residual[r];
+      unsigned loc = 0;
+      for (int b = 0; b < per; ++b) loc += hr[lane * per + b];
+      unsigned incl = loc;
+      for (int off = 1; off < 32; off <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += v;
       }
-      if (b >= nbins) b = nbins - 1;  // empty frame: keeps the state defined
-      const unsigned prev = a.pass == 0 ? 0u : st.prefix[r];
-      const int bits = a.pass == 2 ? 10 : 11;
-      st.prefix[r] = (prev << bits) | static_cast<unsigned>(b);
-      st.residual[r] = rem;
+      const unsigned excl = incl - loc;
+      if (lane == 0) {  // empty frame (rank past the end): keeps the state defined
+        s_bucket[r] = static_cast<unsigned>(nbins - 1);
+        s_rem[r] = 0u;
+      }
+      __syncwarp();
+      if (excl <= rem && rem < incl) {
+        unsigned left = rem - excl;
+        int b = lane * per;
+        while (left >= hr[b]) {
+          left -= hr[b];
+          ++b;
+        }
+        s_bucket[r] = static_cast<unsigned>(b);
+        s_rem[r] = left;
+      }
+      __syncwarp();
     }
+    if (lane == 0) {
+      const int bits = a.pass == 2 ? 10 : 11;
+      for (int r = 0; r < 2; ++r) {
+        const unsigned prev = a.pass == 0 ? 0u : st.prefix[r];
+        st.prefix[r] = (prev << bits) | s_bucket[r];
+        st.residual[r] = s_rem[r];
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
     if (a.pass == 2) {
       // Both keys are complete: value = mean of the two middle values.
       const float lo = key_float(st.prefix[0]);
@@ -202,14 +266,17 @@ __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
   const int W = a.width, H = a.height;
   const int64_t interior = static_cast<int64_t>(W - 2) * (H - 2);
   unsigned* out = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
-  for (int64_t q = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; q - threadIdx.x < interior;
-       q += int64_t(gridDim.x) * blockDim.x) {
+  // rows are dealt to blocks, columns to threads (coalesced, no division)
+  const int cols = W - 2;
+  const int64_t per_row = (cols + blockDim.x - 1) / blockDim.x;  // thread slots per row
+  const int64_t slots = per_row * (H - 2);
+  for (int64_t s = blockIdx.x; s < slots; s += gridDim.x) {
+    const int y = 1 + static_cast<int>(s / per_row);
+    const int x = 1 + static_cast<int>(s - (s / per_row) * per_row) * static_cast<int>(blockDim.x) +
+                  static_cast<int>(threadIdx.x);
     bool hit = false;
-    int64_t idx = 0;
-    if (q < interior) {
-      const int x = 1 + static_cast<int>(q % (W - 2));
-      const int y = 1 + static_cast<int>(q / (W - 2));
-      idx = static_cast<int64_t>(y) * W + x;
+    const int64_t idx = static_cast<int64_t>(y) * W + x;
+    if (interior > 0 && x <= cols) {
       const float c = __ldg(img + idx);
       if (isfinite(c) && c > thr) {
         hit = true;
@@ -338,37 +405,11 @@ __global__ void __launch_bounds__(256) star_measure_kernel(CatalogArgs a) {
     StarRec rec{};
     rec.valid = (fin > 0 && f > 0.0) ? 1 : 0;
     if (rec.valid) {
-      const double cx = sx / f, cy = sy / f;
-      double mxx = 0.0, myy = 0.0, mxy = 0.0;
-      for (int q = lane; q < npx; q += 32) {
-        const int xx = x0 + q % ww, yy = y0 + q / ww;
-        const float v = __ldg(img + static_cast<int64_t>(yy) * W + xx);
-        if (!isfinite(v)) continue;
-        const double wd = static_cast<double>(fmaxf(__fsub_rn(v, bg32), 0.0f));
-        const double dx = static_cast<double>(xx) - cx, dy = static_cast<double>(yy) - cy;
-        mxx += dx * dx * wd;
-        myy += dy * dy * wd;
-        mxy += dx * dy * wd;
-      }
-      for (int off = 16; off > 0; off >>= 1) {
-        mxx += __shfl_xor_sync(0xffffffffu, mxx, off);
-        myy += __shfl_xor_sync(0xffffffffu, myy, off);
-        mxy += __shfl_xor_sync(0xffffffffu, mxy, off);
-      }
-      mxx /= f;
-      myy /= f;
-      mxy /= f;
-      const double trace = fmax(mxx + myy, 0.0);
-      const double det = fmax((mxx - myy) * (mxx - myy) + 4.0 * mxy * mxy, 0.0);
-      const double root = sqrt(det);
-      const double major = fmax((trace + root) / 2.0, 0.0);
-      const double minor = fmax((trace - root) / 2.0, 0.0);
-      const double mean_sigma = sqrt(fmax((major + minor) / 2.0, 0.0));
-      rec.x = cx;
-      rec.y = cy;
+      // second moments (fwhm, eccentricity) are measured later, only for the
+      // stars that survive selection (star_moments_kernel)
+      rec.x = sx / f;
+      rec.y = sy / f;
       rec.flux = f;
-      rec.fwhm = mean_sigma > 0.0 ? 2.354820045 * mean_sigma : nan("");
-      rec.ecc = major > 0.0 ? sqrt(fmax(0.0, 1.0 - minor / major)) : nan("");
       const float center = __ldg(img + static_cast<int64_t>(y) * W + x);
       rec.peak = fmax(static_cast<double>(center) - bg, 0.0);
       rec.npix = pos;
@@ -458,9 +499,12 @@ __global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
     __syncthreads();
     if (done) break;
   }
-  // 3) the max_stars-th largest kept flux by bisection on its bits
-  __shared__ unsigned long long s_lo, s_hi;
+  // 3) the max_stars-th largest kept flux: radix select (8-bit digits, most
+  //    significant first) of rank total_kept - take in ascending key order
   __shared__ int s_count;
+  __shared__ unsigned s_hist[256];
+  __shared__ unsigned long long s_prefix;
+  __shared__ int s_rank;
   int total_kept = 0;
   {
     int c = 0;
@@ -474,57 +518,63 @@ __global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
   const int take = min(total_kept, a.max_stars);
   unsigned long long t = 0;  // keep fluxes with key > t, plus ties at t
   if (take < total_kept) {
-    if (threadIdx.x == 0) {
-      s_lo = 0ull;
-      s_hi = 0x7ff0000000000000ull;
-    }
-    __syncthreads();
-    // smallest key T such that count(key > T) < take  (then key == T fills up)
-    for (int it = 0; it < 64; ++it) {
-      const unsigned long long lo = s_lo, hi = s_hi;
-      if (lo >= hi) break;
-      const unsigned long long mid = lo + (hi - lo) / 2;
-      int c = 0;
-      for (int i = threadIdx.x; i < n; i += blockDim.x) c += (state[i] == 1 && flux_key(recs[i].flux) > mid);
+    unsigned long long prefix = 0ull, mask = 0ull;
+    int rank = total_kept - take;
+    for (int shift = 56; shift >= 0; shift -= 8) {
+      for (int i = threadIdx.x; i < 256; i += blockDim.x) s_hist[i] = 0u;
       __syncthreads();
-      if (threadIdx.x == 0) s_count = 0;
-      __syncthreads();
-      atomicAdd(&s_count, c);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        if (s_count < take) s_hi = mid; else s_lo = mid + 1;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        if (state[i] != 1) continue;
+        const unsigned long long key = flux_key(recs[i].flux);
+        if ((key & mask) == prefix) atomicAdd(&s_hist[(key >> shift) & 255u], 1u);
       }
       __syncthreads();
+      if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        unsigned loc = 0;
+        for (int b = 0; b < 8; ++b) loc += s_hist[lane * 8 + b];
+        unsigned incl = loc;
+        for (int off = 1; off < 32; off <<= 1) {
+          const unsigned v = __shfl_up_sync(0xffffffffu, incl, off);
+          if (lane >= off) incl += v;
+        }
+        const unsigned excl = incl - loc;
+        if (excl <= static_cast<unsigned>(rank) && static_cast<unsigned>(rank) < incl) {
+          unsigned r = static_cast<unsigned>(rank) - excl;
+          int b = lane * 8;
+          while (r >= s_hist[b]) {
+            r -= s_hist[b];
+            ++b;
+          }
+          s_prefix = prefix | (static_cast<unsigned long long>(b) << shift);
+          s_rank = static_cast<int>(r);
+        }
+      }
+      __syncthreads();
+      prefix = s_prefix;
+      rank = s_rank;
+      mask |= 0xffull << shift;
+      __syncthreads();
     }
-    t = s_lo;
+    t = prefix;
   }
-  // 4) gather the selected stars (key > t, then ties key == t in raster
-  //    order up to `take`) and sort them by priority in shared memory.
+  // 4) gather the selected stars (key > t and all ties key == t) and sort
+  //    them by priority in shared memory: the first `take` are the answer
+  //    (ties at t come out in raster order).
   struct Sel {
     double flux;
     unsigned raster;
     int idx;
   };
   Sel* sel = reinterpret_cast<Sel*>(sm);
-  __shared__ int s_n, s_gt;
-  if (threadIdx.x == 0) {
-    s_n = 0;
-    s_gt = 0;
-  }
+  __shared__ int s_n;
+  if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    if (state[i] == 1 && (take == total_kept || flux_key(recs[i].flux) > t)) {
+    if (state[i] == 1 && (take == total_kept || flux_key(recs[i].flux) >= t)) {
       const int p = atomicAdd(&s_n, 1);
       if (p < 4096) sel[p] = {recs[i].flux, cand[i], i};
     }
-  }
-  __syncthreads();
-  if (take < total_kept && threadIdx.x == 0) {
-    // ties at t in raster order (cand[] is raster-sorted)
-    int p = s_n;
-    for (int i = 0; i < n && p < take; ++i)
-      if (state[i] == 1 && flux_key(recs[i].flux) == t && p < 4096) sel[p++] = {recs[i].flux, cand[i], i};
-    s_n = p;
   }
   __syncthreads();
   const int m0 = min(s_n, 4096);
@@ -551,6 +601,7 @@ __global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
   }
   gg_star_t* out = a.out + static_cast<int64_t>(k) * a.max_stars;
   const int nout = min(take, m0);
+  int* chosen = a.kept + static_cast<int64_t>(k) * kMaxCandidates;  // dedupe states are no longer read
   for (int i = threadIdx.x; i < nout; i += blockDim.x) {
     const StarRec r = recs[sel[i].idx];
     gg_star_t s;
@@ -558,13 +609,14 @@ __global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
     s.y = r.y;
     s.flux = r.flux;
     s.peak = r.peak;
-    s.fwhm = r.fwhm;
-    s.eccentricity = r.ecc;
+    s.fwhm = nan("");  // star_moments_kernel
+    s.eccentricity = nan("");
     s.snr = r.snr;
     s.sharpness = r.sharpness;
     s.npix = r.npix;
     s.pad = 0;
     out[i] = s;
+    chosen[i] = sel[i].idx;
   }
   if (threadIdx.x == 0) st.kept = nout;
   if (a.cat_xy) {
@@ -578,6 +630,65 @@ __global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
       a.cat_xy[(static_cast<int64_t>(frame) * kCatalogPoints + i) * 2 + 1] = r.y;
     }
     if (threadIdx.x == 0) a.cat_n[frame] = np;
+  }
+}
+
+// Second moments of the selected stars (star_detect.py:83-99): intensity
+// weighted about the centroid, fwhm from the mean of the principal
+// variances, eccentricity from their ratio.  One warp per star.
+__global__ void __launch_bounds__(256) star_moments_kernel(CatalogArgs a) {
+  const int k = blockIdx.y;
+  const StarFrameState& st = a.state[k];
+  const int nout = st.kept;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const float* img = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+  const unsigned* cand = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
+  const StarRec* recs = a.recs + static_cast<int64_t>(k) * kMaxCandidates;
+  const int* chosen = a.kept + static_cast<int64_t>(k) * kMaxCandidates;
+  gg_star_t* out = a.out + static_cast<int64_t>(k) * a.max_stars;
+  const int W = a.width, H = a.height, r = a.radius;
+  const float bg32 = st.background_f32;
+  for (int i = warp; i < nout; i += nwarps) {
+    const int c = chosen[i];
+    const StarRec rec = recs[c];
+    const unsigned idx = cand[c];
+    const int x = static_cast<int>(idx % static_cast<unsigned>(W));
+    const int y = static_cast<int>(idx / static_cast<unsigned>(W));
+    const int x0 = max(0, x - r), x1 = min(W, x + r + 1);
+    const int y0 = max(0, y - r), y1 = min(H, y + r + 1);
+    const int ww = x1 - x0, npx = ww * (y1 - y0);
+    const double cx = rec.x, cy = rec.y, f = rec.flux;
+    double mxx = 0.0, myy = 0.0, mxy = 0.0;
+    for (int q = lane; q < npx; q += 32) {
+      const int xx = x0 + q % ww, yy = y0 + q / ww;
+      const float v = __ldg(img + static_cast<int64_t>(yy) * W + xx);
+      if (!isfinite(v)) continue;
+      const double wd = static_cast<double>(fmaxf(__fsub_rn(v, bg32), 0.0f));
+      const double dx = static_cast<double>(xx) - cx, dy = static_cast<double>(yy) - cy;
+      mxx += dx * dx * wd;
+      myy += dy * dy * wd;
+      mxy += dx * dy * wd;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      mxx += __shfl_xor_sync(0xffffffffu, mxx, off);
+      myy += __shfl_xor_sync(0xffffffffu, myy, off);
+      mxy += __shfl_xor_sync(0xffffffffu, mxy, off);
+    }
+    mxx /= f;
+    myy /= f;
+    mxy /= f;
+    const double trace = fmax(mxx + myy, 0.0);
+    const double det = fmax((mxx - myy) * (mxx - myy) + 4.0 * mxy * mxy, 0.0);
+    const double root = sqrt(det);
+    const double major = fmax((trace + root) / 2.0, 0.0);
+    const double minor = fmax((trace - root) / 2.0, 0.0);
+    const double mean_sigma = sqrt(fmax((major + minor) / 2.0, 0.0));
+    if (lane == 0) {
+      out[i].fwhm = mean_sigma > 0.0 ? 2.354820045 * mean_sigma : nan("");
+      out[i].eccentricity = major > 0.0 ? sqrt(fmax(0.0, 1.0 - minor / major)) : nan("");
+    }
   }
 }
 
@@ -872,10 +983,13 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
         check_cuda(cudaMemsetAsync(sc.hist, 0, sizeof(unsigned) * count * 2 * kSelBins, s->stream),
                    "cudaMemsetAsync(hist)");
         note_launch();
-        select_hist_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), 256, 0, s->stream>>>(sa);
+        const dim3 hist_grid(per_frame, static_cast<unsigned>(count));
+        if (pass == 0) select_hist_kernel<0><<<hist_grid, 256, 0, s->stream>>>(sa);
+        else if (pass == 1) select_hist_kernel<1><<<hist_grid, 256, 0, s->stream>>>(sa);
+        else select_hist_kernel<2><<<hist_grid, 256, 0, s->stream>>>(sa);
         check_cuda(cudaGetLastError(), "select_hist launch");
         note_launch();
-        select_scan_kernel<<<static_cast<unsigned>(count), 32, 0, s->stream>>>(sa, count);
+        select_scan_kernel<<<static_cast<unsigned>(count), 256, 0, s->stream>>>(sa, count);
         check_cuda(cudaGetLastError(), "select_scan launch");
       }
     }
@@ -964,6 +1078,10 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
   note_launch();
   star_select_kernel<<<static_cast<unsigned>(count), 1024, sel_smem, s->stream>>>(ca);
   check_cuda(cudaGetLastError(), "star_select launch");
+  const unsigned mom_blocks = static_cast<unsigned>(std::max(1, std::min(64, (p.max_stars * 32 + 255) / 256)));
+  note_launch();
+  star_moments_kernel<<<dim3(mom_blocks, static_cast<unsigned>(count)), 256, 0, s->stream>>>(ca);
+  check_cuda(cudaGetLastError(), "star_moments launch");
 }
 
 }  // namespace gg

@@ -181,9 +181,11 @@ class ResidentPipeline:
         self.weights()
         self.integrate()
 
-    def step_host(self, host_raw: np.ndarray, matrices: np.ndarray | None = None, register: bool = False):
+    def step_host(self, host_raw: np.ndarray, matrices: np.ndarray | None = None, register: bool = False,
+                  out: tuple | None = None):
         """Public-API step from host memory to host maps (end to end).  With
-        register=True the matrices come from detect() + register()."""
+        register=True the matrices come from detect() + register(); `out`
+        optionally supplies the six map buffers (see download_maps)."""
         self.calibrate_host(host_raw)
         if register:
             self.detect()
@@ -192,7 +194,7 @@ class ResidentPipeline:
             self.warp(matrices)
         self.weights()
         self.integrate()
-        return self.stack.download_maps("full", include_dq=True)
+        return self.stack.download_maps("full", include_dq=True, out=out)
 
     def close(self) -> None:
         self.stack.close()
