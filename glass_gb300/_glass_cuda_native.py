@@ -382,6 +382,80 @@ def estimate_triangle_asterism_transform(reference: Any, moving: Any, transform_
     return _registration_dict(res, pairs)
 
 
+# ---- alignment metrics / sub-pixel refinement (glass_cuda.py:706-1245) -------------
+def _metrics_dict(m: _lib.AlignmentMetrics, model: str) -> dict[str, Any]:
+    return {"valid_pixels": int(m.valid_pixels), "sampled_pixels": int(m.sampled_pixels),
+            "sample_stride": int(m.sample_stride), "rms": float(m.rms), "mean_abs_diff": float(m.mean_abs_diff),
+            "ncc": float(m.ncc), "model": model}
+
+
+def _pair_stack(reference: Any, moving: Any) -> "ResidentCalibratedStack":
+    ref = np.ascontiguousarray(np.asarray(reference, dtype=np.float32))
+    mov = np.ascontiguousarray(np.asarray(moving, dtype=np.float32))
+    if ref.shape != mov.shape:
+        raise ValueError(f"shape mismatch for registration: {ref.shape} != {mov.shape}")
+    if ref.ndim != 2:
+        raise ValueError("reference and moving must be 2-D arrays")
+    stack = ResidentCalibratedStack(2, ref.shape[0], ref.shape[1])
+    stack.upload_calibrated_frame(0, ref)
+    stack.upload_calibrated_frame(1, mov)
+    return stack
+
+
+def matrix_alignment_metrics_f32(reference: Any, moving: Any, matrix: Any, sample_stride: int = 1) -> dict[str, Any]:
+    """Module matrix_alignment_metrics_f32 (glass_cuda.py:706-768)."""
+    if sample_stride <= 0:
+        raise ValueError("sample_stride must be positive")
+    stack = _pair_stack(reference, moving)
+    try:
+        return stack.matrix_alignment_metrics(0, [1], [matrix], sample_stride)[0]
+    finally:
+        stack.close()
+
+
+def refine_matrix_translation_with_metrics_f32(reference: Any, moving: Any, matrix: Any,
+                                               search_radius_px: float = 1.0, coarse_step_px: float = 0.25,
+                                               fine_radius_px: float = 0.25, fine_step_px: float = 0.0625,
+                                               coarse_sample_stride: int = 4,
+                                               final_sample_stride: int = 1) -> dict[str, Any]:
+    """Module refine_matrix_translation_with_metrics_f32 (glass_cuda.py:771-900)."""
+    stack = _pair_stack(reference, moving)
+    try:
+        res = stack.refine_matrix_translation_candidates_batch_to_reference(
+            0, [1], [matrix], search_radius_px, coarse_step_px, fine_radius_px, fine_step_px, coarse_sample_stride,
+            final_sample_stride)[0]
+    finally:
+        stack.close()
+    for key in ("reference_index", "moving_index", "batch_index", "batch_count", "batch_model"):
+        res.pop(key, None)
+    res["model"] = "cuda_matrix_metric_translation_refine_grid"
+    return res
+
+
+def estimate_translation_subpixel_ncc_f32(reference: Any, moving: Any, center_dx: float, center_dy: float,
+                                          radius_steps: int, step: float, sample_stride: int = 1) -> dict[str, Any]:
+    """Module estimate_translation_subpixel_ncc_f32 (glass_cuda.py:1175-1245)."""
+    if sample_stride <= 0:
+        raise ValueError("sample_stride must be positive")
+    if radius_steps < 0:
+        raise ValueError("radius_steps must be non-negative")
+    if step <= 0.0:
+        raise ValueError("step must be positive")
+    stack = _pair_stack(reference, moving)
+    out = _lib.TranslationNcc()
+    try:
+        _lib.call("gg_stack_translation_ncc", stack.handle, ctypes.c_int64(0), ctypes.c_int64(1),
+                  ctypes.c_double(float(center_dx)), ctypes.c_double(float(center_dy)),
+                  ctypes.c_int32(int(radius_steps)), ctypes.c_double(float(step)), ctypes.c_int32(int(sample_stride)),
+                  ctypes.byref(out))
+    finally:
+        stack.close()
+    return {"dx": float(out.dx), "dy": float(out.dy), "score": float(out.score),
+            "candidate_count": int(out.candidate_count), "center_dx": float(center_dx),
+            "center_dy": float(center_dy), "radius_steps": int(radius_steps), "step": float(step),
+            "sample_stride": int(sample_stride), "model": "translation_subpixel_ncc_cuda"}
+
+
 def resident_dq_map_count_maps_i16(master: Any, weight_map: Any, coverage_map: Any | None = None,
                                    low_rejection_map: Any | None = None,
                                    high_rejection_map: Any | None = None,
@@ -649,6 +723,60 @@ class ResidentCalibratedStack:
         _lib.call("gg_stack_register_frames", self._handle, ctypes.c_int64(int(reference_index)), _lib.ptr(idx),
                   ctypes.c_int64(idx.size), ctypes.byref(params), out)
         return [_registration_dict(r) for r in out]
+
+    # ---- alignment metrics / refinement (native_bindings.cpp:10186-10417) ------------
+    def _matrices(self, matrices: Any, count: int) -> np.ndarray:
+        mats = np.ascontiguousarray(np.asarray(matrices, dtype=np.float64).reshape(-1, 3, 3))
+        if mats.shape[0] != count:
+            raise ValueError("batch refine requires one seed matrix per moving frame")
+        return mats
+
+    def matrix_alignment_metrics(self, reference_index: int, moving_indices: Any, matrices: Any,
+                                 sample_stride: int = 1) -> list[dict[str, Any]]:
+        """matrix_alignment_metrics_f32 of each moving frame against the reference frame."""
+        idx = np.ascontiguousarray(np.asarray(moving_indices, dtype=np.int64).reshape(-1))
+        if idx.size == 0:
+            return []
+        mats = self._matrices(matrices, idx.size)
+        out = (_lib.AlignmentMetrics * idx.size)()
+        _lib.call("gg_stack_alignment_metrics", self._handle, ctypes.c_int64(int(reference_index)), _lib.ptr(idx),
+                  ctypes.c_int64(idx.size), _lib.ptr(mats), ctypes.c_int32(int(sample_stride)), out)
+        return [_metrics_dict(m, "matrix_alignment_metrics_cuda") for m in out]
+
+    def refine_matrix_translation_candidates_batch_to_reference(
+            self, reference_index: int, moving_indices: Any, matrices: Any, search_radius_px: float = 1.0,
+            coarse_step_px: float = 0.25, fine_radius_px: float = 0.25, fine_step_px: float = 0.0625,
+            coarse_sample_stride: int = 4, final_sample_stride: int = 1) -> list[dict[str, Any]]:
+        """Coarse-to-fine translation refinement of each moving frame's matrix
+        against the reference frame (native_bindings.cpp:10186-10417)."""
+        if search_radius_px < 0.0 or fine_radius_px < 0.0:
+            raise ValueError("search radii must be non-negative")
+        if coarse_step_px <= 0.0 or fine_step_px <= 0.0:
+            raise ValueError("search steps must be positive")
+        if coarse_sample_stride <= 0 or final_sample_stride <= 0:
+            raise ValueError("sample strides must be positive")
+        idx = np.ascontiguousarray(np.asarray(moving_indices, dtype=np.int64).reshape(-1))
+        if idx.size == 0:
+            return []
+        mats = self._matrices(matrices, idx.size)
+        params = _lib.RefineParams(float(search_radius_px), float(coarse_step_px), float(fine_radius_px),
+                                   float(fine_step_px), int(coarse_sample_stride), int(final_sample_stride))
+        out = (_lib.RefineResult * idx.size)()
+        _lib.call("gg_stack_refine_translation", self._handle, ctypes.c_int64(int(reference_index)), _lib.ptr(idx),
+                  ctypes.c_int64(idx.size), _lib.ptr(mats), ctypes.byref(params), out)
+        results = []
+        for k, r in enumerate(out):
+            results.append({
+                "matrix": np.asarray(r.matrix, dtype=np.float32).reshape(3, 3).tolist(),
+                "dx_correction": float(r.dx_correction), "dy_correction": float(r.dy_correction),
+                "metrics": _metrics_dict(r.metrics, "matrix_alignment_metrics_cuda_candidate_grid"),
+                "coarse_candidates": int(r.coarse_candidates), "fine_candidates": int(r.fine_candidates),
+                "search_radius_px": float(search_radius_px), "coarse_step_px": float(coarse_step_px),
+                "fine_radius_px": float(fine_radius_px), "fine_step_px": float(fine_step_px),
+                "coarse_sample_stride": int(coarse_sample_stride), "final_sample_stride": int(final_sample_stride),
+                "reference_index": int(reference_index), "moving_index": int(idx[k]), "batch_index": k,
+                "batch_count": int(idx.size), "batch_model": "gb300_candidate_grid_batch_refine"})
+        return results
 
     # ---- warps (native_bindings.cpp:8900-9924) ------------------------------------
     @property

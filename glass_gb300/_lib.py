@@ -176,6 +176,49 @@ class Registration(ctypes.Structure):
     ]
 
 
+class AlignmentMetrics(ctypes.Structure):
+    _fields_ = [
+        ("valid_pixels", ctypes.c_int64),
+        ("sampled_pixels", ctypes.c_int64),
+        ("sample_stride", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+        ("rms", ctypes.c_double),
+        ("mean_abs_diff", ctypes.c_double),
+        ("ncc", ctypes.c_double),
+    ]
+
+
+class RefineParams(ctypes.Structure):
+    _fields_ = [
+        ("search_radius_px", ctypes.c_double),
+        ("coarse_step_px", ctypes.c_double),
+        ("fine_radius_px", ctypes.c_double),
+        ("fine_step_px", ctypes.c_double),
+        ("coarse_sample_stride", ctypes.c_int32),
+        ("final_sample_stride", ctypes.c_int32),
+    ]
+
+
+class RefineResult(ctypes.Structure):
+    _fields_ = [
+        ("matrix", ctypes.c_double * 9),
+        ("dx_correction", ctypes.c_double),
+        ("dy_correction", ctypes.c_double),
+        ("metrics", AlignmentMetrics),
+        ("coarse_candidates", ctypes.c_int32),
+        ("fine_candidates", ctypes.c_int32),
+    ]
+
+
+class TranslationNcc(ctypes.Structure):
+    _fields_ = [
+        ("dx", ctypes.c_double),
+        ("dy", ctypes.c_double),
+        ("score", ctypes.c_double),
+        ("candidate_count", ctypes.c_int64),
+    ]
+
+
 class StackDevicePtrs(ctypes.Structure):
     _fields_ = [
         ("slots", ctypes.c_void_p),
@@ -233,6 +276,10 @@ PROTOTYPES: dict[str, list] = {
                                        ctypes.c_int64, ctypes.c_double, ctypes.c_double,
                                        ctypes.POINTER(Registration), _P],
     "gg_stack_register_frames": [_P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.POINTER(RegisterParams), _P],
+    "gg_stack_alignment_metrics": [_P, ctypes.c_int64, _P, ctypes.c_int64, _P, ctypes.c_int32, _P],
+    "gg_stack_refine_translation": [_P, ctypes.c_int64, _P, ctypes.c_int64, _P, ctypes.POINTER(RefineParams), _P],
+    "gg_stack_translation_ncc": [_P, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(TranslationNcc)],
     "gg_stack_warp_frames": [_P, _P, ctypes.c_int64, _P, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int],
     "gg_stack_reset_warp_coverage": [_P],
     "gg_stack_accumulate_full_warp_coverage_frame": [_P],

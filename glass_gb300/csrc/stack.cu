@@ -142,6 +142,7 @@ static void stack_free(gg_stack* s) {
   if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
   if (s->star_scratch && s->star_scratch_free) s->star_scratch_free(s->star_scratch);
   if (s->reg_scratch && s->reg_scratch_free) s->reg_scratch_free(s->reg_scratch);
+  if (s->metric_scratch && s->metric_scratch_free) s->metric_scratch_free(s->metric_scratch);
   void* dev_ptrs[] = {s->d_slots,    s->d_slot_of_frame, s->d_spare_slot, s->d_frame_nonfinite,
                       s->d_bias,     s->d_dark,          s->d_flat,       s->d_master,
                       s->d_weight,   s->d_coverage,      s->d_low,        s->d_high,

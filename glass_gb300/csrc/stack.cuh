@@ -98,6 +98,8 @@ struct gg_stack {
   void (*star_scratch_free)(void*) = nullptr;
   void* reg_scratch = nullptr;
   void (*reg_scratch_free)(void*) = nullptr;
+  void* metric_scratch = nullptr;
+  void (*metric_scratch_free)(void*) = nullptr;
 
   // Per-frame registration catalogs: the brightest kCatalogPoints star
   // centroids of each frame's last detection (x, y float64) and their count.

@@ -32,6 +32,7 @@
 
 #include <cudaTypedefs.h>
 
+#include "geometry.cuh"
 #include "stack.cuh"
 
 namespace gg {
@@ -110,51 +111,6 @@ __device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, 
       : "memory");
 }
 
-// ---- float-float coordinates ---------------------------------------------------
-struct FFv {
-  float hi, lo;
-};
-
-// a*x + b*y + c with (hi, lo) coefficients; x, y exact small integers.
-__device__ __forceinline__ FFv ff_lin(const float (*r)[2], float x, float y) {
-  const float p1 = __fmul_rn(r[0][0], x);
-  const float e1 = __fmaf_rn(r[0][0], x, -p1);
-  const float p2 = __fmul_rn(r[1][0], y);
-  const float e2 = __fmaf_rn(r[1][0], y, -p2);
-  float s, t, s2, t2;
-  two_sum(p1, p2, s, t);
-  two_sum(s, r[2][0], s2, t2);
-  float lo = __fadd_rn(t, t2);
-  lo = __fadd_rn(lo, __fadd_rn(e1, e2));
-  lo = __fmaf_rn(r[0][1], x, lo);
-  lo = __fmaf_rn(r[1][1], y, lo);
-  lo = __fadd_rn(lo, r[2][1]);
-  const float h = __fadd_rn(s2, lo);
-  return {h, __fsub_rn(lo, __fsub_rn(h, s2))};
-}
-
-__device__ __forceinline__ FFv ff_div(FFv n, FFv d) {
-  const float q = __fdiv_rn(n.hi, d.hi);
-  float r = __fmaf_rn(-q, d.hi, n.hi);
-  r = __fadd_rn(r, n.lo);
-  r = __fmaf_rn(-q, d.lo, r);
-  const float ql = __fdiv_rn(r, d.hi);
-  const float h = __fadd_rn(q, ql);
-  return {h, __fsub_rn(ql, __fsub_rn(h, q))};
-}
-
-__device__ __forceinline__ bool ff_ge(FFv v, float b) { return v.hi > b || (v.hi == b && v.lo >= 0.0f); }
-__device__ __forceinline__ bool ff_le(FFv v, float b) { return v.hi < b || (v.hi == b && v.lo <= 0.0f); }
-__device__ __forceinline__ bool ff_lt(FFv v, float b) { return v.hi < b || (v.hi == b && v.lo < 0.0f); }
-
-// floor and float32(v - floor(v)) of a float-float value.
-__device__ __forceinline__ void ff_floor_frac(FFv v, int& i, float& frac) {
-  float f = floorf(v.hi);
-  if (v.hi == f && v.lo < 0.0f) f -= 1.0f;
-  i = static_cast<int>(f);
-  frac = __fadd_rn(__fsub_rn(v.hi, f), v.lo);
-}
-
 // Register copy of one item's inverse matrix (loaded once per work item so
 // that output stores cannot force re-reads of the descriptor).
 struct Coef {
@@ -171,24 +127,6 @@ __device__ __forceinline__ Coef load_coef(const WarpItem* p) {
   }
   c.affine = __ldg(&p->affine);
   return c;
-}
-
-// Source coordinate of output pixel (x, y); returns false when the
-// projective denominator vanishes (|w| <= 1e-12, engine/warp.py:178-191).
-template <class C>
-__device__ __forceinline__ bool source_coord(const C& it, float x, float y, FFv& sx, FFv& sy) {
-  const float (*m)[2] = it.m;
-  const float rx[3][2] = {{m[0][0], m[0][1]}, {m[1][0], m[1][1]}, {m[2][0], m[2][1]}};
-  const float ry[3][2] = {{m[3][0], m[3][1]}, {m[4][0], m[4][1]}, {m[5][0], m[5][1]}};
-  sx = ff_lin(rx, x, y);
-  sy = ff_lin(ry, x, y);
-  if (it.affine) return true;
-  const float rw[3][2] = {{m[6][0], m[6][1]}, {m[7][0], m[7][1]}, {m[8][0], m[8][1]}};
-  const FFv w = ff_lin(rw, x, y);
-  if (!(fabsf(w.hi) > 1.0e-12f)) return false;
-  sx = ff_div(sx, w);
-  sy = ff_div(sy, w);
-  return true;
 }
 
 // sin(pi u) for |u| <= 1/2 and sin / cos of |x| <= pi/3 by their Taylor
@@ -583,26 +521,6 @@ bool make_slot_tensor_map(gg_stack* s, int box_w, int box_h) {
 }
 
 // float64 3x3 inverse (np.linalg.inv of the float32 matrix promoted to float64).
-static bool invert3(const double* m, double* inv) {
-  const double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5], g = m[6], h = m[7], i = m[8];
-  const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
-  const double det = a * A + b * B + c * C;
-  if (!(std::fabs(det) > 0.0) || !std::isfinite(det)) return false;
-  const double r = 1.0 / det;
-  inv[0] = A * r;
-  inv[1] = -(b * i - c * h) * r;
-  inv[2] = (b * f - c * e) * r;
-  inv[3] = B * r;
-  inv[4] = (a * i - c * g) * r;
-  inv[5] = -(a * f - c * d) * r;
-  inv[6] = C * r;
-  inv[7] = -(a * h - b * g) * r;
-  inv[8] = (a * e - b * d) * r;
-  for (int k = 0; k < 9; ++k)
-    if (!std::isfinite(inv[k])) return false;
-  return true;
-}
-
 static void ensure_warp_items(gg_stack* s, int64_t count) {
   if (s->warp_item_capacity >= count) return;
   check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(warp items)");
@@ -644,20 +562,13 @@ void warp_frames(gg_stack* s, const int64_t* indices, int64_t count, const doubl
     stack_require_loaded(s, indices[k], "warp");
     for (int64_t j = 0; j < k; ++j)
       if (indices[j] == indices[k]) fail(GG_ERR_INVALID_ARGUMENT, "frame indices of a warp batch must be unique");
-    double inv[9];
     const double* m = fwd + 9 * k;
     for (int q = 0; q < 9; ++q)
       if (!std::isfinite(m[q])) fail(GG_ERR_INVALID_ARGUMENT, "warp matrix must be finite");
-    if (!invert3(m, inv)) fail(GG_ERR_INVALID_ARGUMENT, "warp matrix is singular");
     WarpItem& it = items[static_cast<size_t>(k)];
     std::memset(&it, 0, sizeof(it));
     it.frame = static_cast<int>(indices[k]);
-    it.affine = (inv[6] == 0.0 && inv[7] == 0.0 && inv[8] == 1.0) ? 1 : 0;
-    for (int q = 0; q < 9; ++q) {
-      const float hi = static_cast<float>(inv[q]);
-      it.m[q][0] = hi;
-      it.m[q][1] = static_cast<float>(inv[q] - static_cast<double>(hi));
-    }
+    if (!inverse_coefficients(m, it.m, it.affine)) fail(GG_ERR_INVALID_ARGUMENT, "warp matrix is singular");
   }
   ensure_warp_items(s, std::max<int64_t>(count, s->spares));
   if (track_coverage) ensure_warp_coverage(s);

@@ -331,6 +331,67 @@ int gg_similarity_from_descriptors(const double* host_ref_xy, int64_t n_ref, con
 int gg_stack_register_frames(gg_stack* stack, int64_t reference_index, const int64_t* indices, int64_t count,
                              const gg_register_params_t* params, gg_registration_t* host_out);
 
+/* ---- alignment metrics and sub-pixel refinement ---------------------------- */
+/* matrix_alignment_metrics_f32 (glass_cuda.py:706-768): bilinear warp of the
+ * moving frame (fill 0) compared with the reference on every
+ * sample_stride-th row and column. */
+typedef struct {
+  int64_t valid_pixels;
+  int64_t sampled_pixels;
+  int32_t sample_stride;
+  int32_t pad;
+  double rms;           /* NaN without valid samples */
+  double mean_abs_diff; /* NaN without valid samples */
+  double ncc;           /* NaN with <= 1 valid sample or a zero denominator */
+} gg_alignment_metrics_t;
+
+/* refine_matrix_translation_with_metrics_f32 (glass_cuda.py:771-900). */
+typedef struct {
+  double search_radius_px; /* 1.0    */
+  double coarse_step_px;   /* 0.25   */
+  double fine_radius_px;   /* 0.25   */
+  double fine_step_px;     /* 0.0625 */
+  int32_t coarse_sample_stride; /* 4 */
+  int32_t final_sample_stride;  /* 1 */
+} gg_refine_params_t;
+
+typedef struct {
+  double matrix[9];      /* refined matrix (float32 values), row-major */
+  double dx_correction;  /* float32 value */
+  double dy_correction;
+  gg_alignment_metrics_t metrics; /* of the refined matrix at the last stride */
+  int32_t coarse_candidates;
+  int32_t fine_candidates;
+} gg_refine_result_t;
+
+/* estimate_translation_subpixel_ncc_f32 (glass_cuda.py:1131-1245). */
+typedef struct {
+  double dx;
+  double dy;
+  double score; /* best NCC, -inf when no candidate scored */
+  int64_t candidate_count;
+} gg_translation_ncc_t;
+
+/* Metrics of one forward matrix (moving -> reference, float64 row-major 3x3)
+ * per moving frame against a resident reference frame.  Replaces module
+ * matrix_alignment_metrics_f32 (and its kernel warp_kernels.cu:1198-1323). */
+int gg_stack_alignment_metrics(gg_stack* stack, int64_t reference_index, const int64_t* indices, int64_t count,
+                               const double* host_matrices, int32_t sample_stride, gg_alignment_metrics_t* host_out);
+/* Coarse-to-fine translation refinement of each moving frame's matrix
+ * against the reference frame.  Replaces
+ * refine_matrix_translation_candidates_batch_to_reference
+ * (native_bindings.cpp:10186-10417) and module
+ * refine_matrix_translation_with_metrics_f32 (glass_cuda.py:771-900). */
+int gg_stack_refine_translation(gg_stack* stack, int64_t reference_index, const int64_t* indices, int64_t count,
+                                const double* host_matrices, const gg_refine_params_t* params,
+                                gg_refine_result_t* host_out);
+/* Sub-pixel translation by NCC over a (2r+1)^2 grid of translations around
+ * (center_dx, center_dy).  Replaces estimate_translation_subpixel_ncc_f32
+ * (glass_cuda.py:1175-1245; registration_kernels.cu:127-233). */
+int gg_stack_translation_ncc(gg_stack* stack, int64_t reference_index, int64_t moving_index, double center_dx,
+                             double center_dy, int32_t radius_steps, double step, int32_t sample_stride,
+                             gg_translation_ncc_t* host_out);
+
 /* ---- warps --------------------------------------------------------------- */
 /* Warps `count` resident frames in place through their forward matrices
  * (float64 row-major 3x3, moving -> reference; the kernel samples the source

@@ -492,6 +492,114 @@ def make_registration(ref_src: Path) -> None:
     np.savez_compressed(HERE / "registration.npz", **arrays)
 
 
+# ---------------------------------------------------------------------------
+# alignment metrics / sub-pixel refinement
+# ---------------------------------------------------------------------------
+def _shifted_field(rng, h, w, n, dx, dy, theta_deg=0.0, noise=3.0):
+    """Gaussian stars rendered in the reference frame and in a frame related by
+    moving -> reference = rotation(theta) then translation (dx, dy)."""
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    pts = np.column_stack([rng.uniform(3, w - 4, n), rng.uniform(3, h - 4, n)])
+    flux = rng.uniform(200.0, 3000.0, n)
+    t = np.deg2rad(theta_deg)
+    fwd = np.array([[np.cos(t), -np.sin(t), dx], [np.sin(t), np.cos(t), dy], [0.0, 0.0, 1.0]])
+    inv = np.linalg.inv(fwd)
+    mov_pts = np.column_stack([pts, np.ones(n)]) @ inv.T
+
+    def render(p):
+        img = np.full((h, w), 100.0)
+        for (x0, y0, _), f in zip(np.column_stack([p[:, :2], np.ones(n)]), flux):
+            img += f * np.exp(-((xx - x0) ** 2 + (yy - y0) ** 2) / (2 * 1.3 ** 2))
+        return (img + noise * rng.standard_normal((h, w))).astype(np.float32)
+
+    return render(pts), render(mov_pts), fwd
+
+
+def make_alignment(ref_src: Path) -> None:
+    """matrix_alignment_metrics_f32, refine_matrix_translation_with_metrics_f32
+    and estimate_translation_subpixel_ncc_f32 (src/glass_cuda.py:706-1245) on
+    their NumPy paths (no native module importable here)."""
+    sys.path.insert(0, str(ref_src))
+    import glass_cuda
+
+    assert glass_cuda._native() is None
+    rng = np.random.default_rng(1618)
+    arrays: dict[str, np.ndarray] = {}
+    # metrics
+    ref, mov, _fwd = _shifted_field(rng, 30, 38, 12, 0.37, -0.61)
+    mov_nan = mov.copy()
+    mov_nan[rng.random(mov.shape) < 0.03] = np.nan
+    ref_nan = ref.copy()
+    ref_nan[5, 7] = np.nan
+    mcases = []
+    mats = {"identity": np.eye(3), "shift": np.array([[1.0, 0.0, 0.37], [0.0, 1.0, -0.61], [0.0, 0.0, 1.0]]),
+            "rotate": np.array([[0.9998, -0.0175, 1.2], [0.0175, 0.9998, -0.8], [0.0, 0.0, 1.0]]),
+            "projective": np.array([[1.0, 0.01, 0.5], [-0.01, 1.0, 0.25], [1e-4, -2e-4, 1.0]]),
+            "outside": np.array([[1.0, 0.0, 500.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])}
+    for (rname, r), (mname, m) in [(("ref", ref), ("mov", mov)), (("refnan", ref_nan), ("movnan", mov_nan))]:
+        for key, mat in mats.items():
+            for stride in (1, 2, 3):
+                name = f"metrics_{rname}_{mname}_{key}_s{stride}"
+                res = glass_cuda.matrix_alignment_metrics_f32(r, m, mat, sample_stride=stride)
+                arrays[f"{name}/ref"] = r
+                arrays[f"{name}/mov"] = m
+                arrays[f"{name}/matrix"] = mat
+                arrays[f"{name}/stride"] = np.asarray(stride)
+                for k in ("valid_pixels", "sampled_pixels", "rms", "mean_abs_diff", "ncc"):
+                    arrays[f"{name}/{k}"] = np.asarray(res[k])
+                mcases.append(name)
+    arrays["_metric_names"] = np.asarray(mcases)
+    # refinement
+    rcases = []
+    specs = [
+        ("refine_default", (0.37, -0.61, 0.0), np.array([[1.0, 0.0, 0.25], [0.0, 1.0, -0.5], [0.0, 0.0, 1.0]]), {}),
+        ("refine_rotated", (1.1, 0.4, 0.6),
+         np.array([[0.99995, -0.0105, 1.0], [0.0105, 0.99995, 0.5], [0.0, 0.0, 1.0]]),
+         dict(search_radius_px=0.5, coarse_step_px=0.25, fine_radius_px=0.125, fine_step_px=0.0625,
+              coarse_sample_stride=2, final_sample_stride=1)),
+        ("refine_rescore", (-0.3, 0.2, 0.0), np.eye(3),
+         dict(search_radius_px=0.5, coarse_step_px=0.25, fine_radius_px=0.0, coarse_sample_stride=3,
+              final_sample_stride=1)),
+        ("refine_coarse_only", (0.1, 0.1, 0.0), np.eye(3),
+         dict(search_radius_px=0.25, coarse_step_px=0.125, fine_radius_px=0.0, coarse_sample_stride=2,
+              final_sample_stride=2)),
+    ]
+    for name, (dx, dy, th), seed, params in specs:
+        r, m, _ = _shifted_field(rng, 28, 34, 10, dx, dy, th)
+        if name == "refine_rotated":
+            m[rng.random(m.shape) < 0.02] = np.nan
+        res = glass_cuda.refine_matrix_translation_with_metrics_f32(r, m, seed, **params)
+        arrays[f"{name}/ref"] = r
+        arrays[f"{name}/mov"] = m
+        arrays[f"{name}/seed"] = seed
+        arrays[f"{name}/params"] = np.asarray(repr(params))
+        arrays[f"{name}/matrix"] = np.asarray(res["matrix"], dtype=np.float32)
+        arrays[f"{name}/dx_correction"] = np.asarray(res["dx_correction"])
+        arrays[f"{name}/dy_correction"] = np.asarray(res["dy_correction"])
+        arrays[f"{name}/coarse_candidates"] = np.asarray(res["coarse_candidates"])
+        arrays[f"{name}/fine_candidates"] = np.asarray(res["fine_candidates"])
+        for k in ("valid_pixels", "sampled_pixels", "sample_stride", "rms", "mean_abs_diff", "ncc"):
+            arrays[f"{name}/metrics_{k}"] = np.asarray(res["metrics"][k])
+        rcases.append(name)
+    arrays["_refine_names"] = np.asarray(rcases)
+    # translation NCC
+    ncases = []
+    r, m, _ = _shifted_field(rng, 26, 30, 9, 0.8, -0.45)
+    flat = np.full((12, 14), 5.0, dtype=np.float32)
+    for name, (rr, mm, cdx, cdy, rad, step, stride) in {
+            "ncc_s1": (r, m, 0.75, -0.5, 2, 0.125, 1), "ncc_s2": (r, m, 1.0, 0.0, 3, 0.25, 2),
+            "ncc_flat": (flat, flat, 0.0, 0.0, 1, 0.5, 1)}.items():
+        res = glass_cuda.estimate_translation_subpixel_ncc_f32(rr, mm, cdx, cdy, rad, step, stride)
+        arrays[f"{name}/ref"] = rr
+        arrays[f"{name}/mov"] = mm
+        arrays[f"{name}/args"] = np.asarray([cdx, cdy, rad, step, stride], dtype=np.float64)
+        for k in ("dx", "dy", "score", "candidate_count"):
+            arrays[f"{name}/{k}"] = np.asarray(res[k])
+        ncases.append(name)
+    arrays["_ncc_names"] = np.asarray(ncases)
+    np.savez_compressed(HERE / "alignment.npz", **arrays)
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__)
     parser.add_argument("--reference", default="/root/reference", help="GLASS reference checkout")
@@ -500,7 +608,7 @@ def main() -> int:
     ref = Path(args.reference)
     src = ref / "src"
     jobs = {"integration": make_integration, "calibration": make_calibration, "warp": make_warp,
-            "stars": make_stars, "registration": make_registration}
+            "stars": make_stars, "registration": make_registration, "alignment": make_alignment}
     only = [j for j in args.only.split(",") if j] or list(jobs)
     for job in only:
         jobs[job](src)
