@@ -978,6 +978,63 @@ class ResidentCalibratedStack:
         master, weight, cov, low, high, _ = self.download_maps(download_mode, include_dq=False)
         return master, weight, cov, low, high
 
+    # ---- fused warp + integration (glass_cuda.py:5142-5287) ----------------------
+    def _integrate_warped(self, matrices, weights, interpolation, clamping_threshold, rejection, low_sigma,
+                          high_sigma) -> dict[str, Any]:
+        if interpolation not in {"bilinear", "lanczos3"}:
+            raise ValueError("fused matrix-warped interpolation must be bilinear or lanczos3")
+        mats = np.ascontiguousarray(np.asarray(matrices, dtype=np.float32).astype(np.float64))
+        if mats.shape != (self.frame_count, 3, 3):
+            raise ValueError("matrices must have shape (frame_count, 3, 3)")
+        w = self._weights(weights)
+        params = _lib.IntegrateParams(int(rejection), float(low_sigma), float(high_sigma), 3, 0.5, _lib.GG_COUNT_F32,
+                                      5)
+        interp = _lib.GG_INTERP_BILINEAR if interpolation == "bilinear" else _lib.GG_INTERP_LANCZOS3
+        start = perf_counter()
+        _lib.call("gg_stack_integrate_warped", self._handle, _lib.ptr(mats), interp,
+                  ctypes.c_float(float(clamping_threshold)), _lib.ptr(w), ctypes.byref(params))
+        self._last_count_dtype = np.dtype(np.float32)
+        return {"schema_version": 1, "interpolation": interpolation, "clamping_threshold": float(clamping_threshold),
+                "frame_count": self.frame_count, "enqueue_s": perf_counter() - start, "avoids_stack_scatter": True,
+                "modifies_resident_stack": False}
+
+    def fused_geometric_coverage(self) -> np.ndarray:
+        out = np.empty((self.height, self.width), np.float32)
+        _lib.call("gg_stack_download_fused_coverage", self._handle, _lib.ptr(out))
+        return out
+
+    def integrate_matrix_warped_mean(self, matrices: Any, weights: Any | None = None, interpolation: str = "bilinear",
+                                     clamping_threshold: float = -1.0, download_mode: str = "full"):
+        """Fused warp + weighted mean -> (master, weight, coverage, geometric
+        coverage, timing); the resident frames are not modified."""
+        if download_mode not in _DOWNLOAD_MODES:
+            raise ValueError("download_mode must be full, master_weight, or master_only")
+        timing = self._integrate_warped(matrices, weights, interpolation, clamping_threshold, _lib.GG_REJECT_NONE,
+                                        3.0, 3.0)
+        master, weight, cov, _low, _high, _dq = self.download_maps(download_mode, include_dq=False)
+        geo = self.fused_geometric_coverage() if download_mode == "full" else None
+        timing.update(rejection="none", download_mode=download_mode)
+        return master, weight, cov, geo, timing
+
+    def integrate_matrix_warped_sigma_clip(self, matrices: Any, weights: Any | None = None,
+                                           interpolation: str = "bilinear", clamping_threshold: float = -1.0,
+                                           low_sigma: float = 3.0, high_sigma: float = 3.0, winsorize: bool = True,
+                                           download_mode: str = "full"):
+        """Fused warp + sigma clip (winsorized when winsorize) -> (master,
+        weight, coverage, low, high, geometric coverage, timing)."""
+        if low_sigma <= 0.0 or high_sigma <= 0.0:
+            raise ValueError("sigma thresholds must be positive")
+        if download_mode not in _DOWNLOAD_MODES:
+            raise ValueError("download_mode must be full, master_weight, or master_only")
+        mode = _lib.GG_REJECT_WINSORIZED if winsorize else _lib.GG_REJECT_SIGMA_CLIP
+        timing = self._integrate_warped(matrices, weights, interpolation, clamping_threshold, mode, low_sigma,
+                                        high_sigma)
+        master, weight, cov, low, high, _dq = self.download_maps(download_mode, include_dq=False)
+        geo = self.fused_geometric_coverage() if download_mode == "full" else None
+        timing.update(rejection="winsorized_sigma" if winsorize else "sigma_clip", winsorize=bool(winsorize),
+                      low_sigma=float(low_sigma), high_sigma=float(high_sigma), download_mode=download_mode)
+        return master, weight, cov, low, high, geo, timing
+
     def integrate_hardened_winsorized_sigma(self, weights: Any | None = None, low_sigma: float = 3.0,
                                             high_sigma: float = 3.0, min_samples: int = 3,
                                             max_reject_fraction: float = 0.5, count_map_dtype: str = "float32",

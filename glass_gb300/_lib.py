@@ -265,6 +265,8 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_integrate": [_P, _P, ctypes.POINTER(IntegrateParams)],
     "gg_stack_integrate_device_weights": [_P, _P, ctypes.POINTER(IntegrateParams)],
     "gg_stack_download_maps": [_P, _P, _P, _P, _P, _P, _P],
+    "gg_stack_integrate_warped": [_P, _P, ctypes.c_int, ctypes.c_float, _P, ctypes.POINTER(IntegrateParams)],
+    "gg_stack_download_fused_coverage": [_P, _P],
     "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
     "gg_dq_map_i16": [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P],
     "gg_stack_detect_stars": [_P, _P, ctypes.c_int64, ctypes.POINTER(StarParams), _P, _P, _P],

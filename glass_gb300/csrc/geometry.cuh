@@ -117,6 +117,14 @@ inline bool invert3(const double* m, double* inv) {
 inline bool inverse_coefficients(const double* fwd, float (*m)[2], int& affine) {
   double inv[9];
   if (!invert3(fwd, inv)) return false;
+  // An affine matrix has an affine inverse; the cofactor formula leaves
+  // inv[8] = det * (1 / det), which may round to 1 - 2^-53 and would send
+  // every sample through the projective division for a 1e-16 relative change.
+  if (fwd[6] == 0.0 && fwd[7] == 0.0 && fwd[8] == 1.0) {
+    inv[6] = 0.0;
+    inv[7] = 0.0;
+    inv[8] = 1.0;
+  }
   affine = (inv[6] == 0.0 && inv[7] == 0.0 && inv[8] == 1.0) ? 1 : 0;
   for (int q = 0; q < 9; ++q) {
     const float hi = static_cast<float>(inv[q]);

@@ -25,10 +25,22 @@
 // (N > 64), which is bank-conflict free for any per-thread rank index.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <vector>
 
+#include "sampling.cuh"
 #include "stack.cuh"
 
 namespace gg {
+
+// Fused warp (integrate_matrix_warped_*): a frame's samples come from its
+// source pixels through the inverse of its matrix instead of from the stack.
+struct FusedFrame {
+  float m[9][2];  // inverse, float-float
+  int affine;
+  unsigned src_nonfinite;  // non-finite source pixels of the frame
+  int pad[2];
+};
 
 struct IntegrateArgs {
   const float* slots;
@@ -52,7 +64,45 @@ struct IntegrateArgs {
   int16_t* dq;
   int count_u16;
   const float* geometric;  // optional warp coverage (float32 per pixel)
+  // fused warp only
+  const FusedFrame* fused;
+  int width, height;
+  float clamp;
+  float* geometric_out;  // frames with a geometrically valid sample, per pixel
 };
+
+// One fused sample of frame f at output pixel (x, y): the value the warp
+// kernel would have written (NaN fill when invalid); `geo` counts the
+// samples the warp would have marked covered.
+template <int INTERP>
+__device__ __noinline__ float fused_sample(const IntegrateArgs& a, const float* src, const FusedFrame& fz, int x,
+                                           int y, int& geo) {
+  const float nan = __int_as_float(0x7fc00000);
+  FFv sx, sy;
+  if (!source_coord(fz, static_cast<float>(x), static_cast<float>(y), sx, sy)) return nan;
+  const float W = static_cast<float>(a.width), H = static_cast<float>(a.height);
+  const bool valid = INTERP == GG_INTERP_BILINEAR
+                         ? (ff_ge(sx, 0.0f) && ff_le(sx, W - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, H - 1.0f))
+                         : (ff_ge(sx, 2.0f) && ff_lt(sx, W - 3.0f) && ff_ge(sy, 2.0f) && ff_lt(sy, H - 3.0f));
+  if (!valid) return nan;
+  int x0, y0;
+  float tx, ty;
+  ff_floor_frac(sx, x0, tx);
+  ff_floor_frac(sy, y0, ty);
+  TapSource ts;
+  ts.tile = nullptr;
+  ts.src = src;
+  ts.bx = ts.by = 0;
+  ts.width = a.width;
+  float v;
+  if (INTERP == GG_INTERP_BILINEAR) {
+    v = sample_bilinear(ts, x0, y0, tx, ty, a.width, a.height);
+  } else if (!sample_lanczos3(ts, x0, y0, tx, ty, fz.src_nonfinite == 0u, a.clamp, v)) {
+    return nan;
+  }
+  ++geo;
+  return v;
+}
 
 constexpr float kInf = __builtin_huge_valf();
 
@@ -577,12 +627,17 @@ __device__ __forceinline__ CenterScale winsorized_sorted(const float* S, int T, 
   return r;
 }
 
-template <int NB, int T, int MODE>
+// WARP = 0 reads the stack; GG_INTERP_BILINEAR / GG_INTERP_LANCZOS3 sample
+// every frame through its inverse matrix (fused warp + integration).
+template <int NB, int T, int MODE, int WARP = 0>
 __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
   extern __shared__ float smem[];
   float* S = smem;  // [NB][T] ascending valid samples
   __shared__ FrameTable<NB> tab;
   __shared__ float s_wtot[2];
+  __shared__ FusedFrame fz[WARP ? NB : 1];
+  if constexpr (WARP != 0)
+    for (int f = threadIdx.x; f < a.frames; f += blockDim.x) fz[f] = a.fused[f];
   load_frame_table<NB>(a, tab);
   if (threadIdx.x == 0) {
     FF wt;
@@ -601,8 +656,20 @@ __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
   float* St = S + tid;
   for (int64_t p = static_cast<int64_t>(blockIdx.x) * T + tid; p < P; p += static_cast<int64_t>(gridDim.x) * T) {
     float x[NB];
+    if constexpr (WARP == 0) {
 #pragma unroll
-    for (int f = 0; f < NB; ++f) x[f] = (f < N) ? __ldcs(tab.base[f] + p) : kInf;
+      for (int f = 0; f < NB; ++f) x[f] = (f < N) ? __ldcs(tab.base[f] + p) : kInf;
+    } else {
+      // samples staged through this thread's own shared-memory column (the
+      // sampler stays out of the unrolled register code)
+      const int py = static_cast<int>(p / a.width), px = static_cast<int>(p - static_cast<int64_t>(py) * a.width);
+      int geo = 0;
+#pragma unroll 1
+      for (int f = 0; f < N; ++f) St[f * T] = fused_sample<WARP>(a, tab.base[f], fz[f], px, py, geo);
+#pragma unroll
+      for (int f = 0; f < NB; ++f) x[f] = (f < N) ? St[f * T] : kInf;
+      a.geometric_out[p] = static_cast<float>(geo);
+    }
     int cnt = 0;
     int nl = 0, nh = 0;
     float lt = -kInf, ht = kInf;
@@ -858,6 +925,61 @@ static void launch_col(const IntegrateArgs& args, cudaStream_t stream) {
   check_cuda(cudaGetLastError(), "integrate kernel launch");
 }
 
+// Non-finite warped samples per frame for the fused path: the count the warp
+// kernel would have left in the frame's counter (it selects the integrator's
+// all-valid formulas).  Frames without non-finite source pixels only need
+// the validity test; the others evaluate the sample.
+template <int INTERP>
+__global__ void __launch_bounds__(256) fused_nonfinite_kernel(IntegrateArgs a, unsigned* counts) {
+  const int f = blockIdx.y;
+  __shared__ FusedFrame fz;
+  __shared__ const float* base;
+  if (threadIdx.x == 0) {
+    fz = a.fused[f];
+    base = a.slots + static_cast<int64_t>(a.slot_of_frame[f]) * a.stride;
+  }
+  __syncthreads();
+  const bool src_finite = fz.src_nonfinite == 0u;
+  const float W = static_cast<float>(a.width), H = static_cast<float>(a.height);
+  unsigned bad = 0;
+  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < a.pixels; p += int64_t(gridDim.x) * blockDim.x) {
+    const int py = static_cast<int>(p / a.width), px = static_cast<int>(p - static_cast<int64_t>(py) * a.width);
+    bool nan_out;
+    if (src_finite) {
+      FFv sx, sy;
+      if (!source_coord(fz, static_cast<float>(px), static_cast<float>(py), sx, sy)) {
+        nan_out = true;
+      } else if (INTERP == GG_INTERP_BILINEAR) {
+        nan_out = !(ff_ge(sx, 0.0f) && ff_le(sx, W - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, H - 1.0f));
+      } else if (!(ff_ge(sx, 2.0f) && ff_lt(sx, W - 3.0f) && ff_ge(sy, 2.0f) && ff_lt(sy, H - 3.0f))) {
+        nan_out = true;
+      } else {
+        // all taps finite: the sample is invalid only for a vanishing weight sum
+        int x0, y0;
+        float tx, ty;
+        ff_floor_frac(sx, x0, tx);
+        ff_floor_frac(sy, y0, ty);
+        float wx[6], wy[6];
+        lanczos3_weights(tx, wx);
+        lanczos3_weights(ty, wy);
+        float sxw = 0.0f, syw = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+          sxw += wx[i];
+          syw += wy[i];
+        }
+        nan_out = !(fabsf(sxw * syw) > 1.0e-12f);
+      }
+    } else {
+      int geo = 0;
+      nan_out = !isfinite(fused_sample<INTERP>(a, base, fz, px, py, geo));
+    }
+    bad += nan_out ? 1u : 0u;
+  }
+  bad = __reduce_add_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31) == 0 && bad) atomicAdd(counts + f, bad);
+}
+
 template <int MR>
 static void launch_smem(const IntegrateArgs& args, cudaStream_t stream) {
   constexpr int T = 32;
@@ -940,6 +1062,110 @@ void launch_integrate(gg_stack* s, const float* d_weights, const gg_integrate_pa
   s->last_count_dtype = p.count_dtype;
 }
 
+__global__ void fused_prepare_kernel(FusedFrame* fused, const unsigned* src_nonfinite, unsigned* counts, int frames) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= frames) return;
+  fused[f].src_nonfinite = src_nonfinite[f];
+  counts[f] = 0u;
+}
+
+template <int MODE, int INTERP>
+static void launch_fused(const IntegrateArgs& a, cudaStream_t stream) {
+  constexpr int T = 128;
+  const size_t smem = size_t(32) * T * sizeof(float);
+  auto kern = integrate_col_kernel<32, T, MODE, INTERP>;
+  check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+             "cudaFuncSetAttribute(fused integrate)");
+  int per_sm = 0;
+  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem), "occupancy");
+  const unsigned grid = grid_for(static_cast<size_t>(a.pixels), T, std::max(per_sm, 1));
+  note_launch();
+  kern<<<grid, T, smem, stream>>>(a);
+  check_cuda(cudaGetLastError(), "fused integrate launch");
+}
+
+// integrate_matrix_warped_{mean,sigma_clip} (integration_kernels.cu:3840-4123):
+// the result of warping every frame through its matrix (NaN fill) and
+// integrating, without writing the warped frames.
+static void integrate_warped(gg_stack* s, const double* fwd, int interp, float clamp, const float* d_weights,
+                             const gg_integrate_params_t& p) {
+  require(s->frames <= 32, "fused warp-integration supports at most 32 frames");
+  require(p.rejection == GG_REJECT_NONE || p.rejection == GG_REJECT_SIGMA_CLIP || p.rejection == GG_REJECT_WINSORIZED,
+          "fused warp-integration supports the mean, sigma-clip and winsorized sigma-clip rejections");
+  require(interp == GG_INTERP_BILINEAR || interp == GG_INTERP_LANCZOS3,
+          "fused matrix-warped interpolation must be bilinear or lanczos3");
+  const int n = static_cast<int>(s->frames);
+  std::vector<FusedFrame> frames(static_cast<size_t>(n));
+  for (int f = 0; f < n; ++f) {
+    const double* m = fwd + 9 * f;
+    for (int q = 0; q < 9; ++q)
+      if (!std::isfinite(m[q])) fail(GG_ERR_INVALID_ARGUMENT, "warp matrix must be finite");
+    FusedFrame& ff = frames[static_cast<size_t>(f)];
+    std::memset(&ff, 0, sizeof(ff));
+    if (!inverse_coefficients(m, ff.m, ff.affine)) fail(GG_ERR_INVALID_ARGUMENT, "warp matrix is singular");
+  }
+  stack_ensure_maps(s);
+  if (!s->d_fused_frames) {
+    check_cuda(cudaMalloc(&s->d_fused_frames, sizeof(FusedFrame) * n), "cudaMalloc(fused frames)");
+    check_cuda(cudaMalloc(&s->d_fused_counts, sizeof(unsigned) * n), "cudaMalloc(fused counts)");
+    check_cuda(cudaMalloc(&s->d_fused_geometric, sizeof(float) * s->pixels), "cudaMalloc(fused coverage)");
+    s->bytes_allocated += static_cast<int64_t>(sizeof(FusedFrame) + sizeof(unsigned)) * n + 4 * s->pixels;
+  }
+  auto* d_frames = static_cast<FusedFrame*>(s->d_fused_frames);
+  check_cuda(cudaMemcpyAsync(d_frames, frames.data(), sizeof(FusedFrame) * n, cudaMemcpyHostToDevice, s->stream),
+             "cudaMemcpyAsync(fused frames)");
+  note_launch();
+  fused_prepare_kernel<<<(n + 127) / 128, 128, 0, s->stream>>>(d_frames, s->d_frame_nonfinite, s->d_fused_counts, n);
+  check_cuda(cudaGetLastError(), "fused_prepare launch");
+  IntegrateArgs a{};
+  a.slots = s->d_slots;
+  a.slot_of_frame = s->d_slot_of_frame;
+  a.stride = s->stride;
+  a.pixels = s->pixels;
+  a.frames = n;
+  a.weights = d_weights;
+  a.nonfinite = s->d_fused_counts;
+  a.rejection = p.rejection;
+  a.low_sigma = p.low_sigma;
+  a.high_sigma = p.high_sigma;
+  a.min_samples = p.min_samples;
+  a.max_frac = p.max_reject_fraction;
+  a.lfc_iterations = 5;
+  a.master = s->d_master;
+  a.weight = s->d_weight;
+  a.coverage = s->d_coverage;
+  a.low = s->d_low;
+  a.high = s->d_high;
+  a.dq = s->d_dq;
+  a.count_u16 = p.count_dtype == GG_COUNT_U16;
+  a.fused = d_frames;
+  a.width = static_cast<int>(s->width);
+  a.height = static_cast<int>(s->height);
+  a.clamp = clamp;
+  a.geometric_out = s->d_fused_geometric;
+  a.geometric = s->d_fused_geometric;
+  const dim3 count_grid(static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((s->pixels + 255) / 256,
+                                                                                      sm_count() * 8 / n + 1))),
+                        static_cast<unsigned>(n));
+  note_launch();
+  if (interp == GG_INTERP_BILINEAR)
+    fused_nonfinite_kernel<GG_INTERP_BILINEAR><<<count_grid, 256, 0, s->stream>>>(a, s->d_fused_counts);
+  else
+    fused_nonfinite_kernel<GG_INTERP_LANCZOS3><<<count_grid, 256, 0, s->stream>>>(a, s->d_fused_counts);
+  check_cuda(cudaGetLastError(), "fused_nonfinite launch");
+  if (interp == GG_INTERP_BILINEAR) {
+    if (p.rejection == GG_REJECT_NONE) launch_fused<GG_REJECT_NONE, GG_INTERP_BILINEAR>(a, s->stream);
+    else if (p.rejection == GG_REJECT_SIGMA_CLIP) launch_fused<GG_REJECT_SIGMA_CLIP, GG_INTERP_BILINEAR>(a, s->stream);
+    else launch_fused<GG_REJECT_WINSORIZED, GG_INTERP_BILINEAR>(a, s->stream);
+  } else {
+    if (p.rejection == GG_REJECT_NONE) launch_fused<GG_REJECT_NONE, GG_INTERP_LANCZOS3>(a, s->stream);
+    else if (p.rejection == GG_REJECT_SIGMA_CLIP) launch_fused<GG_REJECT_SIGMA_CLIP, GG_INTERP_LANCZOS3>(a, s->stream);
+    else launch_fused<GG_REJECT_WINSORIZED, GG_INTERP_LANCZOS3>(a, s->stream);
+  }
+  s->last_count_dtype = p.count_dtype;
+  s->has_fused_geometric = true;
+}
+
 }  // namespace gg
 
 using namespace gg;
@@ -967,6 +1193,33 @@ int gg_stack_integrate_device_weights(gg_stack* s, const void* dev_weights, cons
   stack_require_all_loaded(s, "integration");
   stack_activate(s);
   launch_integrate(s, dev_weights ? static_cast<const float*>(dev_weights) : s->d_weights, *params);
+  GG_API_END
+}
+
+int gg_stack_integrate_warped(gg_stack* s, const double* host_matrices, int interpolation, float clamping_threshold,
+                              const float* host_weights, const gg_integrate_params_t* params) {
+  GG_API_BEGIN
+  require(s != nullptr && host_matrices != nullptr && params != nullptr, "null argument");
+  validate_integrate(*params);
+  stack_require_all_loaded(s, "fused warp-integration");
+  stack_activate(s);
+  for (int64_t f = 0; f < s->frames; ++f) s->h_weights_pinned[f] = host_weights ? host_weights[f] : 1.0f;
+  check_cuda(cudaMemcpyAsync(s->d_weights, s->h_weights_pinned, sizeof(float) * s->frames, cudaMemcpyHostToDevice,
+                             s->stream),
+             "cudaMemcpyAsync(weights)");
+  integrate_warped(s, host_matrices, interpolation, clamping_threshold, s->d_weights, *params);
+  GG_API_END
+}
+
+int gg_stack_download_fused_coverage(gg_stack* s, float* host_out) {
+  GG_API_BEGIN
+  require(s != nullptr && host_out != nullptr, "null argument");
+  if (!s->has_fused_geometric) fail(GG_ERR_RUNTIME, "no fused warp-integration has been run");
+  stack_activate(s);
+  check_cuda(cudaMemcpyAsync(host_out, s->d_fused_geometric, sizeof(float) * s->pixels, cudaMemcpyDeviceToHost,
+                             s->stream),
+             "cudaMemcpyAsync(fused coverage)");
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(fused coverage)");
   GG_API_END
 }
 

@@ -148,7 +148,8 @@ static void stack_free(gg_stack* s) {
                       s->d_weight,   s->d_coverage,      s->d_low,        s->d_high,
                       s->d_dq,       s->d_warp_coverage, s->d_weights,    s->d_partials,
                       s->d_raw_lane[0], s->d_raw_lane[1], s->d_warp_items, s->d_error,
-                      s->d_cat_xy,   s->d_cat_n};
+                      s->d_cat_xy,   s->d_cat_n,         s->d_fused_frames, s->d_fused_counts,
+                      s->d_fused_geometric};
   for (void* p : dev_ptrs) {
     if (p) cudaFree(p);
   }

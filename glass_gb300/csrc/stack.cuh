@@ -101,6 +101,14 @@ struct gg_stack {
   void* metric_scratch = nullptr;
   void (*metric_scratch_free)(void*) = nullptr;
 
+  // Fused warp-integration: per-frame inverse matrices, per-frame
+  // non-finite sample counts of the virtual warped stack and the geometric
+  // coverage map of the last fused integration.
+  void* d_fused_frames = nullptr;
+  unsigned* d_fused_counts = nullptr;
+  float* d_fused_geometric = nullptr;
+  bool has_fused_geometric = false;
+
   // Per-frame registration catalogs: the brightest kCatalogPoints star
   // centroids of each frame's last detection (x, y float64) and their count.
   double* d_cat_xy = nullptr;

@@ -32,16 +32,13 @@
 
 #include <cudaTypedefs.h>
 
-#include "geometry.cuh"
+#include "sampling.cuh"
 #include "stack.cuh"
 
 namespace gg {
 
-constexpr float kInfF = __builtin_huge_valf();
 constexpr int kTileW = 64;
 constexpr int kTileH = 16;
-constexpr int kBoxW = 80;
-constexpr int kBoxH = 32;
 constexpr int kWarpThreads = 256;  // 64 x 4; each thread covers 4 rows
 
 struct WarpItem {
@@ -127,168 +124,6 @@ __device__ __forceinline__ Coef load_coef(const WarpItem* p) {
   }
   c.affine = __ldg(&p->affine);
   return c;
-}
-
-// sin(pi u) for |u| <= 1/2 and sin / cos of |x| <= pi/3 by their Taylor
-// series (truncation below 1e-9 on these ranges), evaluated by Horner.
-__device__ __forceinline__ float sin_taylor(float z) {
-  const float z2 = z * z;
-  float p = 1.0f / 6227020800.0f;
-  p = __fmaf_rn(p, z2, -1.0f / 39916800.0f);
-  p = __fmaf_rn(p, z2, 1.0f / 362880.0f);
-  p = __fmaf_rn(p, z2, -1.0f / 5040.0f);
-  p = __fmaf_rn(p, z2, 1.0f / 120.0f);
-  p = __fmaf_rn(p, z2, -1.0f / 6.0f);
-  return __fmaf_rn(p * z2, z, z);
-}
-
-__device__ __forceinline__ float cos_taylor(float z) {
-  const float z2 = z * z;
-  float p = -1.0f / 87178291200.0f;
-  p = __fmaf_rn(p, z2, 1.0f / 479001600.0f);
-  p = __fmaf_rn(p, z2, -1.0f / 3628800.0f);
-  p = __fmaf_rn(p, z2, 1.0f / 40320.0f);
-  p = __fmaf_rn(p, z2, -1.0f / 720.0f);
-  p = __fmaf_rn(p, z2, 1.0f / 24.0f);
-  p = __fmaf_rn(p, z2, -0.5f);
-  return __fmaf_rn(p, z2, 1.0f);
-}
-
-constexpr float kPiF = 3.14159265358979323846f;
-
-// Lanczos3 weights of taps k = -2..3 at fractional offset t in [0, 1)
-// (d = t - k): w = sinc(d) sinc(d/3) = 3 sin(pi d) sin(pi d / 3) / (pi d)^2,
-// with sin(pi d) = (-1)^k sin(pi t) and sin(pi d / 3) from the angle sum, so
-// one sin(pi t) and one sin/cos(pi t / 3) serve all six taps.  |d| < 1e-6
-// gives 1, as the reference's sinc does.
-__device__ __forceinline__ void lanczos3_weights(float t, float (&w)[6]) {
-  const float u = t <= 0.5f ? t : 1.0f - t;
-  const float s = sin_taylor(kPiF * u);
-  const float x3 = t * (kPiF / 3.0f);
-  const float s3 = sin_taylor(x3), c3 = cos_taylor(x3);
-  const float ck[6] = {-0.5f, 0.5f, 1.0f, 0.5f, -0.5f, -1.0f};
-  const float sk[6] = {-0.86602540378443865f, -0.86602540378443865f, 0.0f, 0.86602540378443865f,
-                       0.86602540378443865f, 0.0f};
-  constexpr float k3_over_pi2 = 0.30396355092701331f;  // 3 / pi^2
-  // Tap k = 1 (d = t - 1 in [-1, 0)) would lose its small sin(pi d / 3) to
-  // cancellation in the angle sum near t = 1: evaluate it directly.
-  const float s3_k1 = sin_taylor((kPiF / 3.0f) * (t - 1.0f));
-#pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    const float d = t - static_cast<float>(j - 2);
-    const float s1 = ((j - 2) & 1) ? -s : s;
-    const float s3d = (j == 3) ? s3_k1 : __fmaf_rn(s3, ck[j], -c3 * sk[j]);
-    const float wv = k3_over_pi2 * s1 * s3d * __fdividef(1.0f, d * d);
-    w[j] = fabsf(d) < 1.0e-6f ? 1.0f : wv;
-  }
-}
-
-// Tap reader: shared-memory tile (origin bx, by) or global frame.
-struct TapSource {
-  const float* tile;  // nullptr -> global
-  const float* src;
-  int bx, by, width;
-  __device__ __forceinline__ float at(int x, int y) const {
-    return tile ? tile[(y - by) * kBoxW + (x - bx)] : __ldg(src + static_cast<int64_t>(y) * width + x);
-  }
-};
-
-__device__ __forceinline__ float sample_bilinear(const TapSource& ts, int x0, int y0, float tx, float ty, int W,
-                                                 int H) {
-  const int x1 = min(x0 + 1, W - 1);
-  const int y1 = min(y0 + 1, H - 1);
-  const float v00 = ts.at(x0, y0), v01 = ts.at(x1, y0), v10 = ts.at(x0, y1), v11 = ts.at(x1, y1);
-  const float ox = __fsub_rn(1.0f, tx), oy = __fsub_rn(1.0f, ty);
-  const float top = __fadd_rn(__fmul_rn(v00, ox), __fmul_rn(v01, tx));
-  const float bottom = __fadd_rn(__fmul_rn(v10, ox), __fmul_rn(v11, tx));
-  return __fadd_rn(__fmul_rn(top, oy), __fmul_rn(bottom, ty));
-}
-
-// Non-finite taps present: skip them and renormalise.  Dropping taps can
-// leave a small weight sum (lobes cancel), which amplifies rounding, so the
-// sums are float-float here.  Kept out of line: it is the rare path.
-__device__ __noinline__ bool lanczos3_nonfinite(const TapSource& ts, int x0, int y0, const float (&wx)[6],
-                                                const float (&wy)[6], float& value, float& vmin, float& vmax) {
-  FF facc, fw;
-  for (int j = 0; j < 6; ++j) {
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      const float v = ts.at(x0 - 2 + i, y0 - 2 + j);
-      if (isfinite(v)) {
-        const float w = wy[j] * wx[i];
-        facc.add_prod(w, v);
-        fw.add(w);
-        vmin = fminf(vmin, v);
-        vmax = fmaxf(vmax, v);
-      }
-    }
-  }
-  if (!(fabsf(__fadd_rn(fw.hi, fw.lo)) > 1.0e-12f)) return false;
-  value = ff_div_ff(facc.hi, facc.lo, fw.hi, fw.lo);
-  return true;
-}
-
-// Returns false when the tap weights sum to (almost) zero.
-__device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int y0, float tx, float ty,
-                                                bool all_finite, float clamp, float& out) {
-  float wx[6], wy[6];
-  lanczos3_weights(tx, wx);
-  lanczos3_weights(ty, wy);
-  float acc = 0.0f, wsum = 0.0f;
-  float vmin = kInfF, vmax = -kInfF;
-  if (all_finite) {
-    float sx = 0.0f, sy = 0.0f;
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      sx += wx[i];
-      sy += wy[i];
-    }
-    if (ts.tile) {
-      // 6x6 window at constant offsets from one shared-memory row pointer.
-      const float* r0 = ts.tile + (y0 - 2 - ts.by) * kBoxW + (x0 - 2 - ts.bx);
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        float row = 0.0f;
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-          const float v = r0[j * kBoxW + i];
-          row = __fmaf_rn(wx[i], v, row);
-          if (clamp >= 0.0f) {
-            vmin = fminf(vmin, v);
-            vmax = fmaxf(vmax, v);
-          }
-        }
-        acc = __fmaf_rn(wy[j], row, acc);
-      }
-    } else {
-#pragma unroll 1
-      for (int j = 0; j < 6; ++j) {
-        float row = 0.0f;
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-          const float v = ts.at(x0 - 2 + i, y0 - 2 + j);
-          row = __fmaf_rn(wx[i], v, row);
-          if (clamp >= 0.0f) {
-            vmin = fminf(vmin, v);
-            vmax = fmaxf(vmax, v);
-          }
-        }
-        acc = __fmaf_rn(wy[j], row, acc);
-      }
-    }
-    wsum = sx * sy;
-  } else {
-    if (!lanczos3_nonfinite(ts, x0, y0, wx, wy, acc, vmin, vmax)) return false;
-    wsum = 1.0f;
-  }
-  if (!(fabsf(wsum) > 1.0e-12f)) return false;
-  float value = __fdiv_rn(acc, wsum);
-  if (clamp >= 0.0f && vmin <= vmax) {
-    const float range = vmax - vmin;
-    value = fminf(vmax + clamp * range, fmaxf(vmin - clamp * range, value));
-  }
-  out = value;
-  return true;
 }
 
 // Tile plan: box origin for the source footprint of output tile (tx, ty).

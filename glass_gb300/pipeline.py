@@ -85,6 +85,14 @@ class StepConfig:
     star_max_stars: int = 80
     registration_tolerance_px: float = 3.0
     registration_min_inliers: int = 6
+    # sub-pixel translation refinement of the triangle matrices (a coarse
+    # +-1 px grid of 0.25 px at stride 4, then +-0.25 px of 0.0625 px at
+    # stride 8: the resident run's settings); None skips it
+    refine: dict | None = None
+
+
+DEFAULT_REFINE = {"search_radius_px": 1.0, "coarse_step_px": 0.25, "fine_radius_px": 0.25, "fine_step_px": 0.0625,
+                  "coarse_sample_stride": 4, "final_sample_stride": 8}
 
 
 class ResidentPipeline:
@@ -153,6 +161,28 @@ class ResidentPipeline:
         self._registered = ok
         return matrices, ok
 
+    def refine(self, matrices: np.ndarray, reference_index: int = 0) -> np.ndarray:
+        """Sub-pixel translation refinement (config.refine) of the registered
+        frames' matrices against the reference frame; returns new matrices."""
+        cfg = self.config
+        ok = getattr(self, "_registered", None)
+        out = np.array(matrices, dtype=np.float64, copy=True)
+        good = np.array([k for k in range(self.frames) if k != reference_index and (ok is None or ok[k])],
+                        dtype=np.int64)
+        if not cfg.refine or good.size == 0:
+            return out
+        r = cfg.refine
+        params = _lib.RefineParams(float(r["search_radius_px"]), float(r["coarse_step_px"]), float(r["fine_radius_px"]),
+                                   float(r["fine_step_px"]), int(r["coarse_sample_stride"]),
+                                   int(r["final_sample_stride"]))
+        res = (_lib.RefineResult * good.size)()
+        seeds = np.ascontiguousarray(out[good])
+        _lib.call("gg_stack_refine_translation", self.stack.handle, ctypes.c_int64(int(reference_index)),
+                  _lib.ptr(good), ctypes.c_int64(good.size), _lib.ptr(seeds), ctypes.byref(params), res)
+        for pos, k in enumerate(good):
+            out[k] = np.asarray(res[pos].matrix, dtype=np.float64).reshape(3, 3)
+        return out
+
     def warp(self, matrices: np.ndarray, reference_index: int = 0) -> None:
         """Warps every frame but the reference through its moving->reference matrix."""
         ok = getattr(self, "_registered", None)
@@ -190,6 +220,7 @@ class ResidentPipeline:
         if register:
             self.detect()
             matrices, _ok = self.register()
+            matrices = self.refine(matrices)
         if matrices is not None:
             self.warp(matrices)
         self.weights()

@@ -211,6 +211,19 @@ int gg_stack_integrate(gg_stack* stack, const float* host_weights, const gg_inte
  * uses the weights of the last gg_stack_compute_weights. */
 int gg_stack_integrate_device_weights(gg_stack* stack, const void* dev_weights,
                                       const gg_integrate_params_t* params);
+/* Fused warp + integration: the maps of integrating every frame warped
+ * through its forward matrix (float64 row-major 3x3 per frame, moving ->
+ * reference; invalid samples excluded) without writing warped frames, plus
+ * the geometric coverage (frames with a valid sample per pixel).  Replaces
+ * integrate_matrix_warped_{mean,sigma_clip} (glass_cuda.py:5142-5287;
+ * integration_kernels.cu:3840-4123).  interpolation GG_INTERP_BILINEAR or
+ * GG_INTERP_LANCZOS3; rejection NONE, SIGMA_CLIP or WINSORIZED; at most 32
+ * frames.  host_weights may be NULL (unit).  Asynchronous. */
+int gg_stack_integrate_warped(gg_stack* stack, const double* host_matrices, int interpolation,
+                              float clamping_threshold, const float* host_weights,
+                              const gg_integrate_params_t* params);
+/* Geometric coverage (float32 H*W) of the last fused warp-integration. */
+int gg_stack_download_fused_coverage(gg_stack* stack, float* host_out);
 /* Downloads the maps of the last integration; any pointer may be NULL.  Count
  * maps are float32 or uint16 per the count_dtype used. */
 int gg_stack_download_maps(gg_stack* stack, float* host_master, float* host_weight, void* host_coverage,
