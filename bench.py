@@ -31,6 +31,9 @@ import numpy as np
 REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO))
 
+from glass_gb300 import replicas  # noqa: E402  (no CUDA needed to import)
+from glass_gb300.replicas import dist_env  # noqa: E402
+
 L2_BYTES = 129 * 1024 * 1024
 FALLBACK_HBM_GBS = 6800.0
 
@@ -47,12 +50,6 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     return p.parse_args()
 
-
-def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
 
 
 def measured_peak():
@@ -262,10 +259,7 @@ def main():
     import torch
 
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    replicas.init("nccl", torch.device("cuda", local))
     from glass_gb300 import _lib
     from glass_gb300.pipeline import DEFAULT_REFINE, ResidentPipeline, StepConfig, build_masters
 
@@ -278,11 +272,7 @@ def main():
     dev_raw = torch.from_numpy(data.lights.view(np.int16)).to(f"cuda:{local}")
     torch.cuda.synchronize()
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
+    barrier = replicas.barrier
 
     # ---- device-resident throughput ("value") ----
     P = h * w
@@ -332,14 +322,9 @@ def main():
     launches = _lib.kernel_launches() - launches0
     elapsed_ms = start.elapsed_time(stop)
     stage_ms = {name: statistics.mean(a.elapsed_time(b) for a, b in ev) for name, ev in events.items()}
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([elapsed_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = replicas.max_over_ranks(elapsed_ms, torch.device("cuda", local))
     mpix_frames = n * h * w / 1e6
-    value = world * mpix_frames * args.steps / (elapsed_ms / 1e3)
+    value = replicas.replica_throughput(world, mpix_frames, args.steps, elapsed_ms / 1e3)
 
     # ---- end to end through the public API (host pinned in, host maps out) ----
     truth = np.asarray(data.truth_matrices, dtype=np.float64)
@@ -365,16 +350,10 @@ def main():
     for _ in range(e2e_steps):
         maps = pipe.step_host(pinned, register=True, out=map_out)
     t1 = time.perf_counter()
-    e2e_s = t1 - t0
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replicas.max_over_ranks(t1 - t0, torch.device("cuda", local))
     h2d = int(pinned.nbytes)
     d2h = int(sum(m.nbytes for m in maps if m is not None))
-    e2e_value = world * mpix_frames * e2e_steps / e2e_s
+    e2e_value = replicas.replica_throughput(world, mpix_frames, e2e_steps, e2e_s)
 
     if rank != 0:
         return 0
@@ -425,10 +404,7 @@ def main():
     }
     print(json.dumps(line))
     pipe.close()
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
+    replicas.shutdown()
     return 0
 
 

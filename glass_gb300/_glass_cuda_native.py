@@ -685,15 +685,20 @@ class ResidentCalibratedStack:
     # ---- star catalogs (star_detect.py:121-168) -------------------------------------
     def detect_stars(self, indices: Any, threshold_sigma: float = 5.0, max_stars: int = 500,
                      background: float | None = None, noise: float | None = None, window_radius: int = 4,
-                     min_separation_px: float = 2.0, with_info: bool = False):
+                     min_separation_px: float = 2.0, with_info: bool = False, catalog_min_fwhm: float = 0.0,
+                     catalog_max_eccentricity: float = 1.0):
         """detect_stars semantics per resident frame -> list of structured arrays
-        (x, y, flux, peak, fwhm, eccentricity, snr, sharpness, npix), brightest first."""
+        (x, y, flux, peak, fwhm, eccentricity, snr, sharpness, npix), brightest first.
+
+        The first 80 stars passing the optional catalog shape filter stay on
+        the device as each frame's registration catalog."""
         idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
         if idx.size == 0:
             raise ValueError("indices must contain at least one frame index")
         params = _lib.StarParams(float(threshold_sigma), int(max_stars), int(window_radius), float(min_separation_px),
                                  np.nan if background is None else float(background),
-                                 np.nan if noise is None else float(noise))
+                                 np.nan if noise is None else float(noise), float(catalog_min_fwhm),
+                                 float(catalog_max_eccentricity))
         stars = np.zeros((idx.size, int(max_stars)), dtype=_lib.STAR_DTYPE)
         counts = np.zeros(idx.size, dtype=np.int32)
         info = (_lib.StarFrameInfo * idx.size)()

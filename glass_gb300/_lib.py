@@ -101,6 +101,8 @@ class StarParams(ctypes.Structure):
         ("min_separation_px", ctypes.c_float),
         ("background", ctypes.c_float),
         ("noise", ctypes.c_float),
+        ("catalog_min_fwhm", ctypes.c_float),
+        ("catalog_max_eccentricity", ctypes.c_float),
     ]
 
 

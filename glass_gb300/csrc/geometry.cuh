@@ -17,22 +17,39 @@ struct FFv {
   float hi, lo;
 };
 
-// a*x + b*y + c with (hi, lo) coefficients; x, y exact small integers.
-__device__ __forceinline__ FFv ff_lin(const float (*r)[2], float x, float y) {
-  const float p1 = __fmul_rn(r[0][0], x);
-  const float e1 = __fmaf_rn(r[0][0], x, -p1);
-  const float p2 = __fmul_rn(r[1][0], y);
-  const float e2 = __fmaf_rn(r[1][0], y, -p2);
-  float s, t, s2, t2;
-  two_sum(p1, p2, s, t);
-  two_sum(s, r[2][0], s2, t2);
-  float lo = __fadd_rn(t, t2);
-  lo = __fadd_rn(lo, __fadd_rn(e1, e2));
-  lo = __fmaf_rn(r[0][1], x, lo);
-  lo = __fmaf_rn(r[1][1], y, lo);
-  lo = __fadd_rn(lo, r[2][1]);
+// a*x + b*y + c with (hi, lo) coefficients; x, y exact small integers.  Split
+// into the part that does not depend on c (shared by transforms that differ
+// only in their translation) and the rest; ff_lin is the two in sequence.
+struct FFPre {
+  float s, t, e;
+};
+
+__device__ __forceinline__ FFPre ff_lin_pre(float a_hi, float b_hi, float x, float y) {
+  const float p1 = __fmul_rn(a_hi, x);
+  const float e1 = __fmaf_rn(a_hi, x, -p1);
+  const float p2 = __fmul_rn(b_hi, y);
+  const float e2 = __fmaf_rn(b_hi, y, -p2);
+  FFPre r;
+  two_sum(p1, p2, r.s, r.t);
+  r.e = __fadd_rn(e1, e2);
+  return r;
+}
+
+__device__ __forceinline__ FFv ff_lin_finish(const FFPre& p, float a_lo, float b_lo, float x, float y, float c_hi,
+                                             float c_lo) {
+  float s2, t2;
+  two_sum(p.s, c_hi, s2, t2);
+  float lo = __fadd_rn(p.t, t2);
+  lo = __fadd_rn(lo, p.e);
+  lo = __fmaf_rn(a_lo, x, lo);
+  lo = __fmaf_rn(b_lo, y, lo);
+  lo = __fadd_rn(lo, c_lo);
   const float h = __fadd_rn(s2, lo);
   return {h, __fsub_rn(lo, __fsub_rn(h, s2))};
+}
+
+__device__ __forceinline__ FFv ff_lin(const float (*r)[2], float x, float y) {
+  return ff_lin_finish(ff_lin_pre(r[0][0], r[1][0], x, y), r[0][1], r[1][1], x, y, r[2][0], r[2][1]);
 }
 
 __device__ __forceinline__ FFv ff_div(FFv n, FFv d) {

@@ -19,25 +19,26 @@
 // The resident reference evaluates the same grids with its own kernels
 // (native_bindings.cpp:10186-10417, warp_kernels.cu:1198-1323).
 //
-// GB300 mapping: one CTA per (job, sample band).  Each warp loads a chunk of
-// 32 x 4 reference samples once and evaluates every candidate of the job on
-// it; the moving-frame taps of a chunk stay in L1 across candidates, so HBM
-// sees one pass over the sampled pixels per job instead of one per candidate.
-// Per-chunk sums are float32 (128 samples about a centring constant), folded
-// into per-warp float-float accumulators and combined in float64.
+// GB300 mapping: one CTA per (job, sample band).  A warp takes a chunk of
+// 32 x 4 samples, keeps the reference samples (and the candidate-independent
+// part of the float-float coordinates) in registers and scores every
+// candidate of the job on it; the chunk's moving-frame taps stay in L1 across
+// candidates, so HBM sees one pass over the sampled pixels per job instead of
+// one per candidate.  Per-lane float32 sums about a centring constant, one
+// transposing butterfly reduction (8 statistics, 9 shuffles) per candidate
+// and chunk, float64 across warps and bands.
 #include <array>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
-#include "geometry.cuh"
+#include "sampling.cuh"
 #include "stack.cuh"
 
 namespace gg {
 
 constexpr int kMetricThreads = 256;
 constexpr int kMetricWarps = kMetricThreads / 32;
-constexpr int kMetricK = 4;          // samples per lane per chunk
 constexpr int kMaxJobCands = 128;    // candidates of one job per launch
 constexpr int kMetricStats = 7;      // sum r, sum w, sum d^2, sum |d|, sum r^2, sum w^2, sum r w
 
@@ -66,35 +67,73 @@ struct MetricArgs {
   double* partial;  // [cand][bands][8]: n, 7 sums
 };
 
-__device__ __forceinline__ void ff_accumulate(float& hi, float& lo, float v) {
-  float s, e;
-  two_sum(hi, v, s, e);
-  lo = __fadd_rn(lo, e);
-  two_sum(s, lo, hi, lo);
-}
-
 struct MetricShared {
-  float acc[kMetricWarps][kMaxJobCands][kMetricStats][2];  // per-warp float-float sums
-  int cnt[kMetricWarps][kMaxJobCands];
+  float acc[kMetricWarps][kMaxJobCands][8];  // per-warp sums: n, 7 statistics
   MetricCand sc[kMaxJobCands];
 };
+
+constexpr int kChunkK = 4;  // samples per lane per chunk
+
+// Sums v[0..7] over the warp and leaves the sum of v[(lane >> 2) & 7] in
+// every lane: a transposing butterfly (4 + 2 + 1 + 1 + 1 shuffles instead
+// of 5 per value).
+__device__ __forceinline__ float warp_sum8_transposed(const float (&v)[8], int lane) {
+  const bool b4 = (lane >> 4) & 1, b3 = (lane >> 3) & 1, b2 = (lane >> 2) & 1;
+  float u[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float send = b4 ? v[i] : v[i + 4];
+    const float keep = b4 ? v[i + 4] : v[i];
+    u[i] = __fadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, 16));
+  }
+  float w[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const float send = b3 ? u[i] : u[i + 2];
+    const float keep = b3 ? u[i + 2] : u[i];
+    w[i] = __fadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, 8));
+  }
+  float z = __fadd_rn(b2 ? w[1] : w[0], __shfl_xor_sync(0xffffffffu, b2 ? w[0] : w[1], 4));
+  z = __fadd_rn(z, __shfl_xor_sync(0xffffffffu, z, 2));
+  z = __fadd_rn(z, __shfl_xor_sync(0xffffffffu, z, 1));
+  return z;
+}
 
 __global__ void __launch_bounds__(kMetricThreads) metric_partials_kernel(MetricArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   MetricShared& sh_ = *reinterpret_cast<MetricShared*>(smem);
   auto& acc = sh_.acc;
-  auto& cnt = sh_.cnt;
   auto& sc = sh_.sc;
+  __shared__ int s_shared;
+  __shared__ float s_urange[4];  // min/max translation (hi) over the candidates: x0, x1, y0, y1
   const MetricJob job = a.jobs[blockIdx.y];
   const int nc = job.cand_count;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i < nc; i += blockDim.x) sc[i] = a.cands[job.cand_begin + i];
-  for (int i = threadIdx.x; i < kMetricWarps * kMaxJobCands; i += blockDim.x) {
-    (&cnt[0][0])[i] = 0;
-    for (int s = 0; s < kMetricStats; ++s) {
-      (&acc[0][0][0][0])[(i * kMetricStats + s) * 2] = 0.0f;
-      (&acc[0][0][0][0])[(i * kMetricStats + s) * 2 + 1] = 0.0f;
+  for (int i = threadIdx.x; i < kMetricWarps * kMaxJobCands * 8; i += blockDim.x) (&acc[0][0][0])[i] = 0.0f;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // Candidates that differ only in their translation (a translation grid
+    // around one matrix) share the x/y products of the source coordinate.
+    int shared = 1;
+    for (int c = 0; c < nc && shared; ++c) {
+      const MetricCand& q = sc[c];
+      shared = q.affine && q.m[0][0] == sc[0].m[0][0] && q.m[0][1] == sc[0].m[0][1] &&
+               q.m[1][0] == sc[0].m[1][0] && q.m[1][1] == sc[0].m[1][1] && q.m[3][0] == sc[0].m[3][0] &&
+               q.m[3][1] == sc[0].m[3][1] && q.m[4][0] == sc[0].m[4][0] && q.m[4][1] == sc[0].m[4][1];
     }
+    s_shared = shared;
+    float ux0 = kInfF, ux1 = -kInfF, uy0 = kInfF, uy1 = -kInfF;
+    for (int c = 0; c < nc; ++c) {
+      ux0 = fminf(ux0, sc[c].m[2][0]);
+      ux1 = fmaxf(ux1, sc[c].m[2][0]);
+      uy0 = fminf(uy0, sc[c].m[5][0]);
+      uy1 = fmaxf(uy1, sc[c].m[5][0]);
+    }
+    s_urange[0] = ux0;
+    s_urange[1] = ux1;
+    s_urange[2] = uy0;
+    s_urange[3] = uy1;
   }
   __syncthreads();
   const int W = a.width, H = a.height, st = a.sample_stride;
@@ -107,13 +146,17 @@ __global__ void __launch_bounds__(kMetricThreads) metric_partials_kernel(MetricA
   const int64_t total = static_cast<int64_t>(sw) * sh;
   const int64_t begin = total * blockIdx.x / a.bands, end = total * (blockIdx.x + 1) / a.bands;
   const float Wm1 = static_cast<float>(W - 1), Hm1 = static_cast<float>(H - 1);
-  constexpr int kChunk = 32 * kMetricK;
+  const bool shared = s_shared != 0;
+  const int slot = (lane >> 2) & 7;  // statistic this lane holds after the reduction
+  constexpr int kChunk = 32 * kChunkK;
+  // a chunk of 128 samples per warp: its reference samples and moving-frame
+  // taps are loaded once (registers / L1) and scored for every candidate
   for (int64_t c0 = begin + static_cast<int64_t>(warp) * kChunk; c0 < end; c0 += kMetricWarps * kChunk) {
-    float rv[kMetricK];
-    int xs[kMetricK], ys[kMetricK];
-    bool rok[kMetricK];
+    float rv[kChunkK];
+    int xs[kChunkK], ys[kChunkK];
+    bool rok[kChunkK];
 #pragma unroll
-    for (int k = 0; k < kMetricK; ++k) {
+    for (int k = 0; k < kChunkK; ++k) {
       const int64_t t = c0 + lane + 32 * k;
       rok[k] = false;
       xs[k] = ys[k] = 0;
@@ -126,14 +169,87 @@ __global__ void __launch_bounds__(kMetricThreads) metric_partials_kernel(MetricA
         rok[k] = isfinite(rv[k]);
       }
     }
-    for (int c = 0; c < nc; ++c) {
-      float s[kMetricStats] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-      int n = 0;
+    FFPre px[kChunkK], py[kChunkK];
+    bool inside = false;
+    if (shared) {
+      float lo_x = kInfF, hi_x = -kInfF, lo_y = kInfF, hi_y = -kInfF;
 #pragma unroll
-      for (int k = 0; k < kMetricK; ++k) {
+      for (int k = 0; k < kChunkK; ++k) {
+        px[k] = ff_lin_pre(sc[0].m[0][0], sc[0].m[1][0], static_cast<float>(xs[k]), static_cast<float>(ys[k]));
+        py[k] = ff_lin_pre(sc[0].m[3][0], sc[0].m[4][0], static_cast<float>(xs[k]), static_cast<float>(ys[k]));
+        if (rok[k]) {
+          lo_x = fminf(lo_x, px[k].s);
+          hi_x = fmaxf(hi_x, px[k].s);
+          lo_y = fminf(lo_y, py[k].s);
+          hi_y = fmaxf(hi_y, py[k].s);
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        lo_x = fminf(lo_x, __shfl_xor_sync(0xffffffffu, lo_x, off));
+        hi_x = fmaxf(hi_x, __shfl_xor_sync(0xffffffffu, hi_x, off));
+        lo_y = fminf(lo_y, __shfl_xor_sync(0xffffffffu, lo_y, off));
+        hi_y = fmaxf(hi_y, __shfl_xor_sync(0xffffffffu, hi_y, off));
+      }
+      // Every candidate's source coordinate of every sample of the chunk lies
+      // inside [0, W-2] x [0, H-2] with a margin above the float-float low
+      // parts (a few float32 ulps of the coordinate): skip the per-sample
+      // validity tests and the edge clamps of the bilinear taps.
+      const float margin = 0.01f + 1.0e-6f * (Wm1 + Hm1);
+      inside = lo_x + s_urange[0] >= margin && hi_x + s_urange[1] <= Wm1 - 1.0f - margin &&
+               lo_y + s_urange[2] >= margin && hi_y + s_urange[3] <= Hm1 - 1.0f - margin;
+    }
+    if (inside) {
+      for (int c = 0; c < nc; ++c) {
+        float s[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // n, 7 statistics
+        const MetricCand& cd = sc[c];
+#pragma unroll
+        for (int k = 0; k < kChunkK; ++k) {
+          if (!rok[k]) continue;
+          const float xf = static_cast<float>(xs[k]), yf = static_cast<float>(ys[k]);
+          const FFv sx = ff_lin_finish(px[k], cd.m[0][1], cd.m[1][1], xf, yf, cd.m[2][0], cd.m[2][1]);
+          const FFv sy = ff_lin_finish(py[k], cd.m[3][1], cd.m[4][1], xf, yf, cd.m[5][0], cd.m[5][1]);
+          int x0, y0;
+          float tx, ty;
+          ff_floor_frac(sx, x0, tx);
+          ff_floor_frac(sy, y0, ty);
+          const float* r0 = mov + y0 * W + x0;  // y0 * W < 2^31 (checked on the host)
+          const float v00 = __ldg(r0), v01 = __ldg(r0 + 1), v10 = __ldg(r0 + W), v11 = __ldg(r0 + W + 1);
+          const float ox = __fsub_rn(1.0f, tx), oy = __fsub_rn(1.0f, ty);
+          const float top = __fadd_rn(__fmul_rn(v00, ox), __fmul_rn(v01, tx));
+          const float bottom = __fadd_rn(__fmul_rn(v10, ox), __fmul_rn(v11, tx));
+          const float w = __fadd_rn(__fmul_rn(top, oy), __fmul_rn(bottom, ty));
+          if (!isfinite(w)) continue;
+          const float r = rv[k];
+          const float rc = __fsub_rn(r, shift), wc = __fsub_rn(w, shift), d = __fsub_rn(w, r);
+          s[0] = __fadd_rn(s[0], 1.0f);
+          s[1] = __fadd_rn(s[1], rc);
+          s[2] = __fadd_rn(s[2], wc);
+          s[3] = __fmaf_rn(d, d, s[3]);
+          s[4] = __fadd_rn(s[4], fabsf(d));
+          s[5] = __fmaf_rn(rc, rc, s[5]);
+          s[6] = __fmaf_rn(wc, wc, s[6]);
+          s[7] = __fmaf_rn(rc, wc, s[7]);
+        }
+        const float z = warp_sum8_transposed(s, lane);
+        if ((lane & 3) == 0) acc[warp][c][slot] = __fadd_rn(acc[warp][c][slot], z);
+      }
+      continue;
+    }
+    for (int c = 0; c < nc; ++c) {
+      float s[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // n, 7 statistics
+      const MetricCand& cd = sc[c];
+#pragma unroll
+      for (int k = 0; k < kChunkK; ++k) {
         if (!rok[k]) continue;
         FFv sx, sy;
-        if (!source_coord(sc[c], static_cast<float>(xs[k]), static_cast<float>(ys[k]), sx, sy)) continue;
+        const float xf = static_cast<float>(xs[k]), yf = static_cast<float>(ys[k]);
+        if (shared) {
+          sx = ff_lin_finish(px[k], cd.m[0][1], cd.m[1][1], xf, yf, cd.m[2][0], cd.m[2][1]);
+          sy = ff_lin_finish(py[k], cd.m[3][1], cd.m[4][1], xf, yf, cd.m[5][0], cd.m[5][1]);
+        } else if (!source_coord(cd, xf, yf, sx, sy)) {
+          continue;
+        }
         if (!(ff_ge(sx, 0.0f) && ff_le(sx, Wm1) && ff_ge(sy, 0.0f) && ff_le(sy, Hm1))) continue;
         int x0, y0;
         float tx, ty;
@@ -143,36 +259,24 @@ __global__ void __launch_bounds__(kMetricThreads) metric_partials_kernel(MetricA
         if (!isfinite(w)) continue;
         const float r = rv[k];
         const float rc = __fsub_rn(r, shift), wc = __fsub_rn(w, shift), d = __fsub_rn(w, r);
-        ++n;
-        s[0] = __fadd_rn(s[0], rc);
-        s[1] = __fadd_rn(s[1], wc);
-        s[2] = __fmaf_rn(d, d, s[2]);
-        s[3] = __fadd_rn(s[3], fabsf(d));
-        s[4] = __fmaf_rn(rc, rc, s[4]);
-        s[5] = __fmaf_rn(wc, wc, s[5]);
-        s[6] = __fmaf_rn(rc, wc, s[6]);
+        s[0] = __fadd_rn(s[0], 1.0f);
+        s[1] = __fadd_rn(s[1], rc);
+        s[2] = __fadd_rn(s[2], wc);
+        s[3] = __fmaf_rn(d, d, s[3]);
+        s[4] = __fadd_rn(s[4], fabsf(d));
+        s[5] = __fmaf_rn(rc, rc, s[5]);
+        s[6] = __fmaf_rn(wc, wc, s[6]);
+        s[7] = __fmaf_rn(rc, wc, s[7]);
       }
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        n += __shfl_xor_sync(0xffffffffu, n, off);
-#pragma unroll
-        for (int q = 0; q < kMetricStats; ++q) s[q] = __fadd_rn(s[q], __shfl_xor_sync(0xffffffffu, s[q], off));
-      }
-      if (lane == 0 && n) {
-        cnt[warp][c] += n;
-#pragma unroll
-        for (int q = 0; q < kMetricStats; ++q) ff_accumulate(acc[warp][c][q][0], acc[warp][c][q][1], s[q]);
-      }
+      const float z = warp_sum8_transposed(s, lane);
+      if ((lane & 3) == 0) acc[warp][c][slot] = __fadd_rn(acc[warp][c][slot], z);
     }
   }
   __syncthreads();
   for (int c = threadIdx.x; c < nc; c += blockDim.x) {
     double out[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int w = 0; w < kMetricWarps; ++w) {
-      out[0] += static_cast<double>(cnt[w][c]);
-      for (int q = 0; q < kMetricStats; ++q)
-        out[1 + q] += static_cast<double>(acc[w][c][q][0]) + static_cast<double>(acc[w][c][q][1]);
-    }
+    for (int w = 0; w < kMetricWarps; ++w)
+      for (int q = 0; q < 8; ++q) out[q] += static_cast<double>(acc[w][c][q]);
     double* dst = a.partial + (static_cast<int64_t>(job.cand_begin + c) * a.bands + blockIdx.x) * 8;
     for (int q = 0; q < 8; ++q) dst[q] = out[q];
   }
@@ -267,7 +371,7 @@ static std::vector<double> evaluate_candidates(gg_stack* s, const std::vector<Pa
   std::vector<double> sums(cands.size() * 8, 0.0);
   if (jobs.empty()) return sums;
   const int64_t sw = (s->width + stride - 1) / stride, sh = (s->height + stride - 1) / stride;
-  require(sw * sh <= (int64_t{1} << 31) - 1, "too many samples for one alignment metric");
+  require(s->pixels <= (int64_t{1} << 31) - 1, "alignment metrics support frames of fewer than 2^31 pixels");
   // bands: enough CTAs to fill the GPU, at least 2048 samples each
   const int64_t samples = sw * sh;
   const int want = std::max(1, (sm_count() * 4 + static_cast<int>(jobs.size()) - 1) / static_cast<int>(jobs.size()));

@@ -619,18 +619,40 @@ __global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
     chosen[i] = sel[i].idx;
   }
   if (threadIdx.x == 0) st.kept = nout;
-  if (a.cat_xy) {
-    // registration uses the first (brightest) points of the catalog
-    // (cpu/registration.py:37-39, max_stars = 80)
-    const int frame = a.frames[k];
-    const int np = min(nout, kCatalogPoints);
-    for (int i = threadIdx.x; i < np; i += blockDim.x) {
-      const StarRec r = recs[sel[i].idx];
-      a.cat_xy[(static_cast<int64_t>(frame) * kCatalogPoints + i) * 2] = r.x;
-      a.cat_xy[(static_cast<int64_t>(frame) * kCatalogPoints + i) * 2 + 1] = r.y;
+}
+
+// Registration catalog of each frame: the first kCatalogPoints output stars
+// (brightest first, cpu/registration.py:37-39) that pass the optional shape
+// filter.  One warp per frame, order-preserving ballot compaction.
+__global__ void star_catalog_kernel(CatalogArgs a, float min_fwhm, float max_ecc) {
+  const int k = blockIdx.x;
+  const int lane = threadIdx.x;
+  const int nout = a.state[k].kept;
+  const gg_star_t* out = a.out + static_cast<int64_t>(k) * a.max_stars;
+  const int frame = a.frames[k];
+  double* dst = a.cat_xy + static_cast<int64_t>(frame) * kCatalogPoints * 2;
+  const bool test_fwhm = min_fwhm > 0.0f, test_ecc = max_ecc < 1.0f;
+  int taken = 0;
+  for (int base = 0; base < nout && taken < kCatalogPoints; base += 32) {
+    const int i = base + lane;
+    bool pass = false;
+    double x = 0.0, y = 0.0;
+    if (i < nout) {
+      const gg_star_t s = out[i];
+      pass = (!test_fwhm || s.fwhm >= static_cast<double>(min_fwhm)) &&
+             (!test_ecc || s.eccentricity <= static_cast<double>(max_ecc));
+      x = s.x;
+      y = s.y;
     }
-    if (threadIdx.x == 0) a.cat_n[frame] = np;
+    const unsigned mask = __ballot_sync(0xffffffffu, pass);
+    const int pos = taken + __popc(mask & ((1u << lane) - 1u));
+    if (pass && pos < kCatalogPoints) {
+      dst[2 * pos] = x;
+      dst[2 * pos + 1] = y;
+    }
+    taken += __popc(mask);
   }
+  if (lane == 0) a.cat_n[frame] = min(taken, kCatalogPoints);
 }
 
 // Second moments of the selected stars (star_detect.py:83-99): intensity
@@ -1082,6 +1104,10 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
   note_launch();
   star_moments_kernel<<<dim3(mom_blocks, static_cast<unsigned>(count)), 256, 0, s->stream>>>(ca);
   check_cuda(cudaGetLastError(), "star_moments launch");
+  note_launch();
+  star_catalog_kernel<<<static_cast<unsigned>(count), 32, 0, s->stream>>>(ca, p.catalog_min_fwhm,
+                                                                           p.catalog_max_eccentricity);
+  check_cuda(cudaGetLastError(), "star_catalog launch");
 }
 
 }  // namespace gg
@@ -1100,6 +1126,8 @@ int gg_stack_detect_stars(gg_stack* s, const int64_t* indices, int64_t count, co
   require(p.window_radius >= 0 && p.window_radius <= 16, "window_radius must be in [0, 16]");
   require(std::isfinite(p.threshold_sigma), "threshold_sigma must be finite");
   require(std::isfinite(p.min_separation_px), "min_separation_px must be finite");
+  require(std::isfinite(p.catalog_min_fwhm) && std::isfinite(p.catalog_max_eccentricity),
+          "catalog filter thresholds must be finite");
   for (int64_t k = 0; k < count; ++k) stack_require_loaded(s, indices[k], "star detection");
   stack_activate(s);
   detect_stars(s, indices, static_cast<int>(count), p);

@@ -82,7 +82,11 @@ class StepConfig:
     dark_exposure_s: float | None = 300.0
     # star catalogs + triangle registration (resident_cuda.py:10790-11400)
     star_threshold_sigma: float = 5.0
-    star_max_stars: int = 80
+    star_max_stars: int = 400
+    # registration catalog = first 80 detections that look like stars: cosmic
+    # ray streaks are elongated (eccentricity near 1), stars round
+    catalog_min_fwhm: float = 0.0
+    catalog_max_eccentricity: float = 0.8
     registration_tolerance_px: float = 3.0
     registration_min_inliers: int = 6
     # sub-pixel translation refinement of the triangle matrices (a coarse
@@ -136,9 +140,11 @@ class ResidentPipeline:
 
     def detect(self) -> None:
         """Star catalogs of every frame; they stay on the device for register()."""
+        cfg = self.config
+        params = _lib.StarParams(float(cfg.star_threshold_sigma), int(cfg.star_max_stars), 4, 2.0, np.nan, np.nan,
+                                 float(cfg.catalog_min_fwhm), float(cfg.catalog_max_eccentricity))
         _lib.call("gg_stack_detect_stars", self.stack.handle, _lib.ptr(self._indices), ctypes.c_int64(self.frames),
-                  ctypes.byref(_lib.StarParams(float(self.config.star_threshold_sigma), int(self.config.star_max_stars),
-                                               4, 2.0, np.nan, np.nan)), None, None, None)
+                  ctypes.byref(params), None, None, None)
 
     def register(self, reference_index: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """Triangle registration of every frame to the reference frame from the

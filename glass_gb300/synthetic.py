@@ -190,9 +190,9 @@ def generate(config: StackConfig | str, frames: int | None = None) -> SyntheticS
             cx = rng.integers(0, w, hits)
             length = rng.integers(2, 7, hits)
             ang = rng.uniform(0, np.pi, hits)
-            # a few hundred to a few thousand ADU per hit pixel (CMOS-like
-            # deposits): fainter in total than the brightest stars
-            energy = rng.uniform(300.0, 6000.0, hits).astype(np.float32)
+            # 5k-60k ADU per hit pixel: as bright as the brightest stars, so
+            # a brightness-ranked catalog needs a shape filter
+            energy = rng.uniform(5000.0, 60000.0, hits).astype(np.float32)
             for step in range(6):
                 on = step < length
                 sy = np.clip(np.rint(cy + step * np.sin(ang)).astype(np.int64), 0, h - 1)

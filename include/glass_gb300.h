@@ -253,6 +253,14 @@ typedef struct {
   float min_separation_px; /* 2.0   */
   float background;        /* NaN   */
   float noise;             /* NaN   */
+  /* Registration catalog (the first 80 detected stars, brightest first, as
+   * cpu/registration.py:37-39 takes them) optionally skips stars whose
+   * fwhm < catalog_min_fwhm or eccentricity > catalog_max_eccentricity
+   * (undefined values fail an active test).  0 and 1 (or more) switch the
+   * tests off, which is the reference's behaviour.  No reference counterpart:
+   * a shape filter against cosmic-ray hits as bright as stars. */
+  float catalog_min_fwhm;
+  float catalog_max_eccentricity;
 } gg_star_params_t;
 
 /* One star (cpu/star_detect.py:8-18); fwhm / eccentricity NaN when undefined. */

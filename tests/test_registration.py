@@ -223,6 +223,36 @@ def test_gpu_stack_registration_from_device_catalogs(native):
 
 
 @pytest.mark.gpu
+def test_gpu_catalog_shape_filter_skips_streaks(native):
+    """Streaks brighter than every star fill an unfiltered top-80 catalog;
+    the eccentricity filter keeps the round stars and registration works."""
+    rng = np.random.default_rng(23)
+    h, w = 200, 240
+    stars = [(rng.uniform(12, w - 12), rng.uniform(12, h - 12), rng.uniform(800, 9000)) for _ in range(90)]
+    shifts = [(0.0, 0.0), (2.5, -1.75)]
+    frames = []
+    for sh in shifts:
+        img = _field(rng, h, w, stars, sh)
+        for _ in range(120):  # streaks 3-6 px long, 1 px wide
+            x0, y0 = rng.integers(5, w - 12), rng.integers(5, h - 12)
+            length = int(rng.integers(3, 7))
+            img[y0, x0:x0 + length] += np.float32(rng.uniform(40000, 60000))
+        frames.append(img)
+    s = native.ResidentCalibratedStack(2, h, w)
+    try:
+        for k in range(2):
+            s.upload_calibrated_frame(k, frames[k])
+        cats = s.detect_stars([0, 1], threshold_sigma=5.0, max_stars=400, catalog_max_eccentricity=0.8)
+        got = s.register_frames_triangle(0, [1], tolerance_px=2.0)[0]
+    finally:
+        s.close()
+    first80 = cats[0][:80]
+    assert np.count_nonzero(first80["eccentricity"] > 0.8) > 20  # the raw ranking is polluted
+    assert got["status"] == "ok" and got["inliers"] >= 40
+    np.testing.assert_allclose(got["matrix"][:2, 2], -np.asarray(shifts[1]), atol=0.1)
+
+
+@pytest.mark.gpu
 def test_gpu_registration_argument_errors(native):
     with pytest.raises(ValueError):
         native.estimate_triangle_asterism_transform(np.zeros((5, 2)), np.zeros((5, 2)), transform_model="affine")
