@@ -47,7 +47,6 @@ def parse_args():
     p.add_argument("--config", default="c2", choices=["c1", "c2"])
     p.add_argument("--frames", type=int, default=0, help="override frame count (smaller smoke runs)")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--cpu-seconds", type=float, default=12.0)
     return p.parse_args()
 
 
@@ -154,54 +153,98 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline (the oracle port of the reference algorithm, host cores)
 # ---------------------------------------------------------------------------
-def _cpu_tile_job(args):
-    raw, bias, dark, flat, scale, rejection = args
+CPU_CROP = 384  # side of the crops the warp, refinement and integration samples use
+
+
+_CPU_DATA = None  # (lights, bias, dark, flat, truth) shared with the forked sample processes
+
+
+def _cpu_step_sample(spec):
+    """One bounded sample of every stage of the step, timed with the oracle
+    port of the reference's CPU code; returns seconds per stage.  Full frames
+    for calibration, detection and registration; crops for the warp, the
+    refinement and the integration."""
+    from oracle import alignment, registration, stars, warp
     from oracle.calibration import calibrate_light
     from oracle.integration import weighted_integrate_stack
 
-    frames = np.stack([calibrate_light(raw[i], bias, dark, flat, 1.0, 1.0 / scale,
-                                       master_dark_includes_bias=False) for i in range(raw.shape[0])])
-    valid = np.isfinite(frames)
-    means = np.array([frames[i][valid[i]].astype(np.float64).mean() for i in range(frames.shape[0])])
-    stds = np.array([frames[i][valid[i]].astype(np.float64).std() for i in range(frames.shape[0])])
+    lights, bias, dark, flat, truth = _CPU_DATA
+    mov, y0, x0 = spec
+    n = lights.shape[0]
+    raw = lights[[0, mov]]
+    matrix = truth[mov]
+    c = CPU_CROP
+    times = {}
+    t = time.perf_counter()
+    cal = [calibrate_light(raw[k], bias, dark, flat, 1.0, 1.0, master_dark_includes_bias=False) for k in (0, 1)]
+    times["calibrate"] = (time.perf_counter() - t) / 2
+    t = time.perf_counter()
+    cats = []
+    for k in (0, 1):
+        found = stars.detect_stars(cal[k], threshold_sigma=5.0, max_stars=400)
+        cats.append([(s[0], s[1]) for s in found if s[5] is not None and s[5] <= 0.8][:80])
+    times["detect_stars"] = (time.perf_counter() - t) / 2
+    t = time.perf_counter()
+    registration.estimate_triangle_asterism_transform(cats[0], cats[1])
+    times["register"] = time.perf_counter() - t
+    ref_crop = np.ascontiguousarray(cal[0][y0:y0 + c, x0:x0 + c])
+    mov_crop = np.ascontiguousarray(cal[1][y0:y0 + c, x0:x0 + c])
+    t = time.perf_counter()
+    alignment.refine_translation(ref_crop, mov_crop, matrix, 1.0, 0.25, 0.25, 0.0625, 4, 8)
+    times["refine_translation"] = time.perf_counter() - t
+    t = time.perf_counter()
+    warp.warp_matrix(mov_crop, matrix, "lanczos3", np.nan)
+    times["warp_lanczos3"] = time.perf_counter() - t
+    stack = np.stack([calibrate_light(lights[k, y0:y0 + c, x0:x0 + c], bias[y0:y0 + c, x0:x0 + c],
+                                      dark[y0:y0 + c, x0:x0 + c], flat[y0:y0 + c, x0:x0 + c], 1.0, 1.0,
+                                      master_dark_includes_bias=False) for k in range(n)])
+    t = time.perf_counter()
+    finite = np.isfinite(stack)
+    means = np.array([stack[k][finite[k]].astype(np.float64).mean() for k in range(n)])
+    stds = np.array([stack[k][finite[k]].astype(np.float64).std() for k in range(n)])
     weights = np.maximum(np.abs(means) / np.maximum(stds, 1e-6), 1e-6).astype(np.float32)
-    weighted_integrate_stack(frames, weights, rejection)
-    return int(raw.size)
+    weighted_integrate_stack(stack, weights, "winsorized_sigma")
+    times["weights_integrate"] = time.perf_counter() - t
+    return times
 
 
-def cpu_baseline(data, masters, seconds: float, processes: int):
-    """Times the oracle port on crops of the workload for ~`seconds`."""
+def cpu_step_estimate(data, masters, processes: int):
+    """Seconds one full step takes on the host cores (oracle port), composed
+    from `processes` concurrent samples: per-frame stages x frames, per-pixel
+    stages scaled from their crops.  Returns (Mpix-frames/s over all the
+    processes, mean seconds per step, stage seconds per step, description)."""
     import multiprocessing as mp
 
+    global _CPU_DATA
     n, h, w = data.lights.shape
-    tile = 256
-    jobs = []
+    c = CPU_CROP
+    _CPU_DATA = (data.lights, masters.bias, masters.dark, masters.flat, data.truth_matrices)
     rng = np.random.default_rng(0)
-    for _ in range(4096):
-        y = int(rng.integers(0, h - tile + 1))
-        x = int(rng.integers(0, w - tile + 1))
-        sl = (slice(y, y + tile), slice(x, x + tile))
-        jobs.append((data.lights[:, sl[0], sl[1]].copy(),
-                     None if masters.bias is None else masters.bias[sl],
-                     None if masters.dark is None else masters.dark[sl],
-                     None if masters.flat is None else masters.flat[sl], 1.0, "winsorized_sigma"))
-    done_px = 0
-    start = time.perf_counter()
+    specs = [(1 + k % (n - 1), int(rng.integers(0, h - c + 1)), int(rng.integers(0, w - c + 1)))
+             for k in range(processes)]
     if processes <= 1:
-        for job in jobs:
-            done_px += _cpu_tile_job(job)
-            if time.perf_counter() - start >= seconds:
-                break
+        samples = [_cpu_step_sample(specs[0])]
     else:
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(processes) as pool:
-            for px in pool.imap_unordered(_cpu_tile_job, jobs, chunksize=1):
-                done_px += px
-                if time.perf_counter() - start >= seconds:
-                    pool.terminate()
-                    break
-    elapsed = time.perf_counter() - start
-    return done_px / 1e6 / elapsed, elapsed, done_px
+        # forked workers share the stack without pickling it; this process
+        # has not touched CUDA (the reference arm never does)
+        with mp.get_context("fork").Pool(processes) as pool:
+            samples = pool.map(_cpu_step_sample, specs)
+    px_scale = (h * w) / (c * c)
+    steps = []
+    for s in samples:
+        stage = {"calibrate": n * s["calibrate"], "detect_stars": n * s["detect_stars"],
+                 "register": (n - 1) * s["register"],
+                 "refine_translation": (n - 1) * s["refine_translation"] * px_scale,
+                 "warp_lanczos3": (n - 1) * s["warp_lanczos3"] * px_scale,
+                 "weights_integrate": s["weights_integrate"] * px_scale}
+        steps.append(stage)
+    mean = {k: float(np.mean([st[k] for st in steps])) for k in steps[0]}
+    step_s = sum(mean.values())
+    value = processes * n * h * w / 1e6 / step_s
+    desc = (f"{processes} process(es), each: calibrate + detect 2 full {h}x{w} frames, triangle registration of one "
+            f"pair, NCC refine + Lanczos3 warp of one {c}x{c} crop pair, weights + winsorized integration of a "
+            f"{n}x{c}x{c} crop; composed to one {n}-frame step (per-pixel stages scaled by {px_scale:.0f}x)")
+    return value, step_s, mean, desc
 
 
 # ---------------------------------------------------------------------------
@@ -234,23 +277,23 @@ def main():
         m = M()
         m.bias, m.dark, m.flat = bias, dark, flat
         procs = os.cpu_count() or 1
-        per_step = []
-        for _ in range(args.warmup):
-            cpu_baseline(data, m, 1.0, procs)
+        if args.warmup > 0:  # one untimed sample batch warms the caches and imports
+            cpu_step_estimate(data, m, procs)
+        values, step_s, desc, stages = [], [], "", {}
         for _ in range(args.steps):
-            rate, elapsed, px = cpu_baseline(data, m, max(2.0, args.cpu_seconds / max(args.steps, 1)), procs)
-            per_step.append((rate, elapsed, px))
-        total_px = sum(p for _, _, p in per_step)
-        total_t = sum(t for _, t, _ in per_step)
-        value = total_px / 1e6 / total_t
+            v, s, stages, desc = cpu_step_estimate(data, m, procs)
+            values.append(v)
+            step_s.append(s)
+        value = float(np.mean(values))
         line = {
             "metric": metric, "value": value, "unit": "Mpix-frames/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(len(per_step), 1),
+            "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(step_s)) / procs,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload, "sample": "random 256x256 crops x all frames"},
+            "config": {"workload": workload, "sample": desc},
+            "stages_s_per_step_one_process": stages,
             "cpu_baseline": {"value": value, "unit": "Mpix-frames/s", "cores": procs, "kind": "port",
-                             "sample": f"{total_px / 1e6:.1f} Mpix-frames in 256x256 crops of the workload"},
+                             "sample": desc},
             "e2e": {"value": value, "unit": "Mpix-frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line))
@@ -284,11 +327,24 @@ def main():
     def refine():
         reg["matrices"] = pipe.refine(reg["triangle"], 0)
 
+    # NCC refine: 8 B per sampled pixel per candidate (reference + moving
+    # sample), coarse and fine grids, every frame but the reference
+    rp = DEFAULT_REFINE
+    n_coarse = len(np.arange(-rp["search_radius_px"], rp["search_radius_px"] + rp["coarse_step_px"] * 0.5,
+                             rp["coarse_step_px"], dtype=np.float32)) ** 2
+    n_fine = len(np.arange(-rp["fine_radius_px"], rp["fine_radius_px"] + rp["fine_step_px"] * 0.5,
+                           rp["fine_step_px"], dtype=np.float32)) ** 2
+
+    def sampled(stride):
+        return -(-w // stride) * -(-h // stride)
+
+    refine_bytes = 8 * (n - 1) * (n_coarse * sampled(rp["coarse_sample_stride"]) +
+                                  n_fine * sampled(rp["final_sample_stride"]))
     stages = [
         ("calibrate", lambda: pipe.calibrate_device(dev_raw.data_ptr()), 6 * n * P + 12 * P),
         ("detect_stars", pipe.detect, 4 * n * P),
         ("register", register, None),
-        ("refine_translation", refine, None),
+        ("refine_translation", refine, refine_bytes),
         ("warp_lanczos3", lambda: pipe.warp(reg["matrices"]), 8 * (n - 1) * P),
         ("weights", pipe.weights, 4 * n * P),
         ("integrate_winsorized", pipe.integrate, 4 * n * P + 16 * P),
@@ -369,10 +425,11 @@ def main():
     top = max((k for k in kernels if kernels[k]["algorithmic_bytes"]), key=lambda k: kernels[k]["ms"])
     cpu = None
     if not args.no_cpu_baseline:
-        rate, elapsed, px = cpu_baseline(data, masters, args.cpu_seconds, 1)
+        t_cpu = time.perf_counter()
+        rate, step_s, cpu_stages, desc = cpu_step_estimate(data, masters, 1)
         cpu = {"value": rate, "unit": "Mpix-frames/s", "cores": 1, "kind": "port",
-               "sample": f"{px / 1e6:.1f} Mpix-frames (random 256x256 crops x {n} frames) in {elapsed:.1f} s, "
-                         "oracle calibrate + simple_snr weights + winsorized integration"}
+               "sample": f"{desc}; sample took {time.perf_counter() - t_cpu:.1f} s, one step {step_s:.1f} s",
+               "stages_s_per_step": cpu_stages}
     line = {
         "metric": metric,
         "value": value,

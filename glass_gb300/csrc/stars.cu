@@ -12,20 +12,21 @@
 //   moments of max(v - background, 0) (star_detect.py:45-100),
 //   greedy de-duplication in flux order (stable: raster order breaks ties,
 //   star_detect.py:103-118), then the brightest `max_stars`.
-// Background modes: GLOBAL reproduces detect_stars (one median/MAD per
-// frame); MESH computes median/MAD per cell of a background mesh (no
-// reference counterpart; its own float64 restatement lives in
-// oracle/stars.py) and thresholds each pixel against its cell.
 //
 // GB300 layout:
 //   - order statistics by a 3-pass radix select over the frame (11+11+10 key
-//     bits, per-CTA shared-memory histograms folded with global atomics); the
-//     MAD reuses it with key |v - median|;
+//     bits, per-CTA shared-memory histograms fed by per-thread run-length
+//     counters and folded with global atomics); the MAD reuses it with key
+//     |v - median|;
 //   - candidates are appended with one atomic per warp, then one CTA per
-//     frame sorts them into raster order in shared memory, measures them one
-//     warp per candidate, resolves the flux-ordered de-duplication with a
-//     row-range neighbour search (centroids stay within the window of their
-//     peak) and selects the brightest by a bisection on the flux bits.
+//     frame sorts them into raster order in shared memory, measures flux and
+//     centroid one warp per candidate, resolves the flux-ordered
+//     de-duplication with a row-range neighbour search (centroids stay within
+//     the window of their peak) and selects the brightest by an 8-bit radix
+//     select on the flux bits; second moments (fwhm, eccentricity) are
+//     measured only for the selected stars;
+//   - the first 80 selected stars (optionally only those passing a shape
+//     filter) stay on the device as the frame's registration catalog.
 #include <cmath>
 #include <cstring>
 #include <vector>
