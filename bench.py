@@ -47,6 +47,7 @@ def parse_args():
     p.add_argument("--config", default="c2", choices=["c1", "c2"])
     p.add_argument("--frames", type=int, default=0, help="override frame count (smaller smoke runs)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the gradient-refinement registration report")
     return p.parse_args()
 
 
@@ -247,6 +248,51 @@ def cpu_step_estimate(data, masters, processes: int):
     return value, step_s, mean, desc
 
 
+def adjoint_report(pipe, dev_raw, reg, truth, h, w, stream) -> dict:
+    """Registration accuracy against the synthetic truth, same GPU, same
+    frames: triangle asterism (plain), plus the NCC translation grid refine,
+    plus the gradient (adjoint-warp) similarity refine started from the
+    triangle matrices.  Outside the timed step."""
+    import torch
+
+    from glass_gb300.adjoint import RefineConfig, registration_rms_px
+
+    pipe.calibrate_device(dev_raw.data_ptr())  # the timed steps left warped frames behind
+    stream.synchronize()
+    ok = [k for k in range(1, pipe.frames) if reg["ok"][k]]
+
+    def rms(mats):
+        return registration_rms_px([mats[k] for k in ok], [truth[k] for k in ok], h, w)
+
+    def timed(method, reps=3):
+        pipe.config.refine_method = method
+        try:
+            out = pipe.refine(reg["triangle"], 0)
+            stream.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                out = pipe.refine(reg["triangle"], 0)
+            stream.synchronize()
+            return out, 1e3 * (time.perf_counter() - t0) / reps
+        finally:
+            pipe.config.refine_method = "ncc"
+
+    ncc, ncc_ms = timed("ncc")
+    gn, gn_ms = timed("gradient")
+    # the generic autograd path (L-BFGS over torch ops, one frame at a time)
+    t0 = time.perf_counter()
+    torch_mats, outcomes = pipe.refine_adjoint(reg["triangle"], 0, RefineConfig(model="similarity", rounds=2,
+                                                                                iterations=15))
+    torch.cuda.synchronize()
+    torch_ms = 1e3 * (time.perf_counter() - t0) / max(1, len(ok))
+    return {"rms_px_vs_truth": {"triangle": rms(reg["triangle"]), "ncc_translation": rms(ncc),
+                                "gradient_gauss_newton": rms(gn), "gradient_autograd_lbfgs": rms(torch_mats)},
+            "refine_ms_per_step": {"ncc_translation": ncc_ms, "gradient_gauss_newton": gn_ms,
+                                   "gradient_autograd_lbfgs": torch_ms * len(ok)},
+            "autograd_evaluations_mean": float(np.mean([o.evaluations for o in outcomes])) if outcomes else 0.0,
+            "frames_compared": len(ok)}
+
+
 # ---------------------------------------------------------------------------
 def main():
     args = parse_args()
@@ -391,6 +437,8 @@ def main():
     registration = {"frames_ok": int(reg["ok"].sum()), "frames": n,
                     "max_corner_error_px_vs_truth": {"triangle": corner_err(reg["triangle"]),
                                                      "refined": corner_err(reg["matrices"])}}
+    if not args.no_adjoint:
+        registration.update(adjoint_report(pipe, dev_raw, reg, truth, h, w, stream))
     pinned = torch.from_numpy(data.lights.view(np.int16)).pin_memory().numpy().view(np.uint16)
     # reused pinned destinations for the six maps (master, weight f32; coverage,
     # low, high uint16; dq int16)
@@ -410,6 +458,21 @@ def main():
     h2d = int(pinned.nbytes)
     d2h = int(sum(m.nbytes for m in maps if m is not None))
     e2e_value = replicas.replica_throughput(world, mpix_frames, e2e_steps, e2e_s)
+    if not args.no_adjoint:
+        # the same end-to-end step with the gradient refinement in place of the grid search
+        pipe.config.refine_method = "gradient"
+        for _ in range(2):
+            pipe.step_host(pinned, register=True, out=map_out)
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            pipe.step_host(pinned, register=True, out=map_out)
+        gn_s = replicas.max_over_ranks(time.perf_counter() - t0, torch.device("cuda", local))
+        pipe.config.refine_method = "ncc"
+        registration["e2e_mpix_frames_per_s"] = {
+            "ncc_translation": e2e_value,
+            "gradient_gauss_newton": replicas.replica_throughput(world, mpix_frames, e2e_steps, gn_s)}
 
     if rank != 0:
         return 0

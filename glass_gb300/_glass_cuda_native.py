@@ -87,6 +87,20 @@ class _PinnedBuffer:
         weakref.finalize(self, _lib.load().gg_host_free_pinned, ctypes.c_void_p(self.address))
 
 
+class _DeviceView:
+    """A resident frame exposed through __cuda_array_interface__ (keeps its stack alive)."""
+
+    def __init__(self, address: int, height: int, width: int, owner: Any):
+        self.owner = owner
+        self.__cuda_array_interface__ = {
+            "shape": (height, width),
+            "typestr": "<f4",
+            "data": (address, False),
+            "version": 2,
+            "strides": None,
+        }
+
+
 def host_pinned_empty_f32(height: int, width: int) -> np.ndarray:
     h, w = int(height), int(width)
     if h <= 0 or w <= 0:
@@ -529,6 +543,18 @@ class ResidentCalibratedStack:
         _lib.call("gg_stack_device_ptrs", self._handle, ctypes.byref(ptrs))
         return {name: int(getattr(ptrs, name) or 0) for name, _ in _lib.StackDevicePtrs._fields_}
 
+    def frame_tensor(self, index: int):
+        """Zero-copy torch CUDA view (H x W float32) of loaded frame `index`.
+
+        Valid until the frame is warped (warps move frames between slots);
+        synchronises the stack's stream."""
+        import torch
+
+        addr = ctypes.c_void_p()
+        _lib.call("gg_stack_frame_device_ptr", self._handle, ctypes.c_int64(int(index)), ctypes.byref(addr))
+        info = self._info()
+        return torch.as_tensor(_DeviceView(int(addr.value), int(info.height), int(info.width), self))
+
     # ---- properties (native_bindings.cpp:20624-20645) -----------------------
     @property
     def frame_count(self) -> int:
@@ -782,6 +808,61 @@ class ResidentCalibratedStack:
                 "reference_index": int(reference_index), "moving_index": int(idx[k]), "batch_index": k,
                 "batch_count": int(idx.size), "batch_model": "gb300_candidate_grid_batch_refine"})
         return results
+
+    # ---- gradient refinement (no reference counterpart) -----------------------------
+    _MODELS = {"translation": _lib.GG_TRANSFORM_TRANSLATION, "similarity": _lib.GG_TRANSFORM_SIMILARITY,
+               "affine": _lib.GG_TRANSFORM_AFFINE}
+    _INTERPS = {"bilinear": _lib.GG_INTERP_BILINEAR, "lanczos3": _lib.GG_INTERP_LANCZOS3}
+
+    def _gradient_params(self, model, interpolation, sample_stride, stats_passes, iterations, min_samples,
+                         clip_sigma, mask_shift_px, tolerance_px, max_step_px) -> _lib.GradientRefineParams:
+        if model not in self._MODELS:
+            raise ValueError("model must be translation, similarity or affine")
+        if interpolation not in self._INTERPS:
+            raise ValueError("interpolation must be bilinear or lanczos3")
+        return _lib.GradientRefineParams(self._MODELS[model], self._INTERPS[interpolation], int(sample_stride),
+                                         int(stats_passes), int(iterations), int(min_samples), float(clip_sigma),
+                                         float(mask_shift_px), float(tolerance_px), float(max_step_px))
+
+    def refine_matrix_gradient_batch_to_reference(
+            self, reference_index: int, moving_indices: Any, matrices: Any, model: str = "similarity",
+            interpolation: str = "lanczos3", sample_stride: int = 2, stats_passes: int = 3, iterations: int = 8,
+            min_samples: int = 256, clip_sigma: float = 5.0, mask_shift_px: float = 1.0,
+            tolerance_px: float = 1.0e-3, max_step_px: float = 2.0) -> list[dict[str, Any]]:
+        """Gauss-Newton refinement of each moving frame's affine matrix against
+        the reference frame on the device (masked, photometrically matched
+        sum of squares; the warp adjoint's position derivatives)."""
+        idx = np.ascontiguousarray(np.asarray(moving_indices, dtype=np.int64).reshape(-1))
+        if idx.size == 0:
+            return []
+        mats = self._matrices(matrices, idx.size)
+        params = self._gradient_params(model, interpolation, sample_stride, stats_passes, iterations, min_samples,
+                                       clip_sigma, mask_shift_px, tolerance_px, max_step_px)
+        out = (_lib.GradientRefineResult * idx.size)()
+        _lib.call("gg_stack_refine_gradient", self._handle, ctypes.c_int64(int(reference_index)), _lib.ptr(idx),
+                  ctypes.c_int64(idx.size), _lib.ptr(mats), ctypes.byref(params), out)
+        status = {1: "converged", 2: "iteration_cap", -1: "too_few_samples", -2: "singular"}
+        return [{"matrix": np.asarray(r.matrix, dtype=np.float64).reshape(3, 3), "alpha": float(r.alpha),
+                 "beta": float(r.beta), "sigma": float(r.sigma), "rms": float(r.rms),
+                 "last_step_px": float(r.last_step_px), "samples": int(r.samples), "iterations": int(r.iterations),
+                 "status": status.get(int(r.status), str(int(r.status))), "ok": int(r.status) >= 1,
+                 "moving_index": int(idx[k]), "reference_index": int(reference_index)} for k, r in enumerate(out)]
+
+    def gradient_normal_equations(self, reference_index: int, moving_indices: Any, thetas: Any, photometric: Any,
+                                  model: str = "similarity", interpolation: str = "lanczos3", sample_stride: int = 2,
+                                  clip_sigma: float = 5.0, mask_shift_px: float = 1.0) -> np.ndarray:
+        """One accumulation pass of the gradient refinement -> (n, 48) sums:
+        J^T J upper triangle (36), J^T r (8), sum r^2, kept count, 0, 0."""
+        idx = np.ascontiguousarray(np.asarray(moving_indices, dtype=np.int64).reshape(-1))
+        th = np.ascontiguousarray(np.asarray(thetas, dtype=np.float64).reshape(idx.size, 6))
+        ph = np.ascontiguousarray(np.asarray(photometric, dtype=np.float64).reshape(idx.size, 3))
+        params = self._gradient_params(model, interpolation, sample_stride, 1, 1, 16, clip_sigma, mask_shift_px,
+                                       0.0, 1.0)
+        out = np.zeros((idx.size, 48), dtype=np.float64)
+        _lib.call("gg_stack_gradient_normal_equations", self._handle, ctypes.c_int64(int(reference_index)),
+                  _lib.ptr(idx), ctypes.c_int64(idx.size), _lib.ptr(th), _lib.ptr(ph), ctypes.byref(params),
+                  _lib.ptr(out))
+        return out
 
     # ---- warps (native_bindings.cpp:8900-9924) ------------------------------------
     @property

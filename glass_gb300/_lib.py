@@ -148,7 +148,9 @@ class IntegrateParams(ctypes.Structure):
     ]
 
 
+GG_TRANSFORM_TRANSLATION = 0
 GG_TRANSFORM_SIMILARITY = 1
+GG_TRANSFORM_AFFINE = 2
 
 
 class RegisterParams(ctypes.Structure):
@@ -221,6 +223,35 @@ class TranslationNcc(ctypes.Structure):
     ]
 
 
+class GradientRefineParams(ctypes.Structure):
+    _fields_ = [
+        ("transform_model", ctypes.c_int32),
+        ("interpolation", ctypes.c_int32),
+        ("sample_stride", ctypes.c_int32),
+        ("stats_passes", ctypes.c_int32),
+        ("iterations", ctypes.c_int32),
+        ("min_samples", ctypes.c_int32),
+        ("clip_sigma", ctypes.c_float),
+        ("mask_shift_px", ctypes.c_float),
+        ("tolerance_px", ctypes.c_double),
+        ("max_step_px", ctypes.c_double),
+    ]
+
+
+class GradientRefineResult(ctypes.Structure):
+    _fields_ = [
+        ("matrix", ctypes.c_double * 9),
+        ("alpha", ctypes.c_double),
+        ("beta", ctypes.c_double),
+        ("sigma", ctypes.c_double),
+        ("rms", ctypes.c_double),
+        ("last_step_px", ctypes.c_double),
+        ("samples", ctypes.c_int64),
+        ("iterations", ctypes.c_int32),
+        ("status", ctypes.c_int32),
+    ]
+
+
 class StackDevicePtrs(ctypes.Structure):
     _fields_ = [
         ("slots", ctypes.c_void_p),
@@ -270,6 +301,7 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_integrate_warped": [_P, _P, ctypes.c_int, ctypes.c_float, _P, ctypes.POINTER(IntegrateParams)],
     "gg_stack_download_fused_coverage": [_P, _P],
     "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
+    "gg_stack_frame_device_ptr": [_P, ctypes.c_int64, _P],
     "gg_dq_map_i16": [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P],
     "gg_stack_detect_stars": [_P, _P, ctypes.c_int64, ctypes.POINTER(StarParams), _P, _P, _P],
     "gg_triangle_descriptors": [_P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P,
@@ -291,6 +323,13 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_tma_enabled": [_P, ctypes.POINTER(ctypes.c_int)],
     "gg_warp_matrix_f32": [_P, ctypes.c_int64, ctypes.c_int64, _P, ctypes.c_int, ctypes.c_float, ctypes.c_float, _P,
                            _P],
+    "gg_warp_affine_f32_device": [_P, ctypes.c_int64, ctypes.c_int64, _P, ctypes.c_int, ctypes.c_float, ctypes.c_int,
+                                  _P, _P],
+    "gg_warp_affine_backward_f32_device": [_P, ctypes.c_int64, ctypes.c_int64, _P, ctypes.c_int, _P, _P, _P, _P],
+    "gg_stack_refine_gradient": [_P, ctypes.c_int64, _P, ctypes.c_int64, _P, ctypes.POINTER(GradientRefineParams),
+                                 _P],
+    "gg_stack_gradient_normal_equations": [_P, ctypes.c_int64, _P, ctypes.c_int64, _P, _P,
+                                           ctypes.POINTER(GradientRefineParams), _P],
 }
 
 _LIB: ctypes.CDLL | None = None

@@ -143,6 +143,7 @@ static void stack_free(gg_stack* s) {
   if (s->star_scratch && s->star_scratch_free) s->star_scratch_free(s->star_scratch);
   if (s->reg_scratch && s->reg_scratch_free) s->reg_scratch_free(s->reg_scratch);
   if (s->metric_scratch && s->metric_scratch_free) s->metric_scratch_free(s->metric_scratch);
+  if (s->gn_scratch && s->gn_scratch_free) s->gn_scratch_free(s->gn_scratch);
   void* dev_ptrs[] = {s->d_slots,    s->d_slot_of_frame, s->d_spare_slot, s->d_frame_nonfinite,
                       s->d_bias,     s->d_dark,          s->d_flat,       s->d_master,
                       s->d_weight,   s->d_coverage,      s->d_low,        s->d_high,
@@ -468,6 +469,17 @@ int gg_stack_device_ptrs(gg_stack* s, gg_stack_device_ptrs_t* out) {
   out->high = s->d_high;
   out->dq = s->d_dq;
   out->warp_coverage = s->d_warp_coverage;
+  GG_API_END
+}
+
+int gg_stack_frame_device_ptr(gg_stack* s, int64_t index, float** out) {
+  GG_API_BEGIN
+  require(s != nullptr && out != nullptr, "null argument");
+  stack_require_loaded(s, index, "frame_device_ptr");
+  stack_activate(s);
+  std::vector<int> slots;
+  stack_read_slots(s, slots);  // synchronises the stack's stream
+  *out = s->d_slots + static_cast<int64_t>(slots[static_cast<size_t>(index)]) * s->stride;
   GG_API_END
 }
 

@@ -100,6 +100,8 @@ struct gg_stack {
   void (*reg_scratch_free)(void*) = nullptr;
   void* metric_scratch = nullptr;
   void (*metric_scratch_free)(void*) = nullptr;
+  void* gn_scratch = nullptr;
+  void (*gn_scratch_free)(void*) = nullptr;
 
   // Fused warp-integration: per-frame inverse matrices, per-frame
   // non-finite sample counts of the virtual warped stack and the geometric

@@ -93,10 +93,21 @@ class StepConfig:
     # +-1 px grid of 0.25 px at stride 4, then +-0.25 px of 0.0625 px at
     # stride 8: the resident run's settings); None skips it
     refine: dict | None = None
+    # "ncc": the reference's translation grid search (refine above);
+    # "gradient": device Gauss-Newton on the masked sum of squares with the
+    # warp adjoint's derivatives (gradient_refine below)
+    refine_method: str = "ncc"
+    gradient_refine: dict | None = None
 
 
 DEFAULT_REFINE = {"search_radius_px": 1.0, "coarse_step_px": 0.25, "fine_radius_px": 0.25, "fine_step_px": 0.0625,
                   "coarse_sample_stride": 4, "final_sample_stride": 8}
+
+# similarity model, Lanczos3 derivatives, every 2nd row and column, three
+# noise passes, at most eight steps, stop below 1e-3 px
+DEFAULT_GRADIENT_REFINE = {"model": "similarity", "interpolation": "lanczos3", "sample_stride": 2,
+                           "stats_passes": 3, "iterations": 8, "min_samples": 256, "clip_sigma": 5.0,
+                           "mask_shift_px": 1.0, "tolerance_px": 1.0e-3, "max_step_px": 2.0}
 
 
 class ResidentPipeline:
@@ -175,6 +186,17 @@ class ResidentPipeline:
         out = np.array(matrices, dtype=np.float64, copy=True)
         good = np.array([k for k in range(self.frames) if k != reference_index and (ok is None or ok[k])],
                         dtype=np.int64)
+        if cfg.refine_method == "gradient":
+            if good.size == 0:
+                return out
+            gp = dict(DEFAULT_GRADIENT_REFINE, **(cfg.gradient_refine or {}))
+            res = self.stack.refine_matrix_gradient_batch_to_reference(reference_index, good, out[good], **gp)
+            for k, r in zip(good, res):
+                if r["ok"]:
+                    out[k] = r["matrix"]
+            return out
+        if cfg.refine_method != "ncc":
+            raise ValueError("refine_method must be ncc or gradient")
         if not cfg.refine or good.size == 0:
             return out
         r = cfg.refine
@@ -188,6 +210,25 @@ class ResidentPipeline:
         for pos, k in enumerate(good):
             out[k] = np.asarray(res[pos].matrix, dtype=np.float64).reshape(3, 3)
         return out
+
+    def refine_adjoint(self, matrices: np.ndarray, reference_index: int = 0, config=None) -> tuple[np.ndarray, list]:
+        """Gradient refinement (glass_gb300.adjoint.refine_affine) of every
+        registered frame's matrix against the reference frame, on the
+        calibrated frames in place (run it before warp()).  Returns the new
+        matrices and the per-frame outcomes."""
+        from glass_gb300.adjoint import refine_affine
+
+        ok = getattr(self, "_registered", None)
+        out = np.array(matrices, dtype=np.float64, copy=True)
+        ref = self.stack.frame_tensor(reference_index)
+        outcomes = []
+        for k in range(self.frames):
+            if k == reference_index or (ok is not None and not ok[k]):
+                continue
+            res = refine_affine(ref, self.stack.frame_tensor(k), out[k], config)
+            out[k] = res.matrix
+            outcomes.append(res)
+        return out, outcomes
 
     def warp(self, matrices: np.ndarray, reference_index: int = 0) -> None:
         """Warps every frame but the reference through its moving->reference matrix."""

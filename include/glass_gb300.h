@@ -242,6 +242,11 @@ typedef struct {
   void* warp_coverage;  /* float32 coverage accumulator                           */
 } gg_stack_device_ptrs_t;
 int gg_stack_device_ptrs(gg_stack* stack, gg_stack_device_ptrs_t* out);
+/* Device address of loaded frame `index` (H*W float32, row-major) as of the
+ * moment of the call: synchronises the stack's stream; a later warp of that
+ * frame moves it to another slot.  No reference counterpart (views of
+ * resident frames for the differentiable warp). */
+int gg_stack_frame_device_ptr(gg_stack* stack, int64_t index, float** out);
 
 /* ---- star detection ------------------------------------------------------ */
 /* Parameters of detect_stars (cpu/star_detect.py:121-132).  background /
@@ -297,7 +302,9 @@ int gg_stack_detect_stars(gg_stack* stack, const int64_t* indices, int64_t count
 /* ---- registration (triangle asterisms) ----------------------------------- */
 /* Point lists are (x, y) float64 pairs, brightest star first.  Catalogs hold
  * at most 80 stars. */
+#define GG_TRANSFORM_TRANSLATION 0
 #define GG_TRANSFORM_SIMILARITY 1
+#define GG_TRANSFORM_AFFINE 2
 
 /* Parameters of estimate_triangle_asterism_transform
  * (cpu/registration.py:361-373). */
@@ -442,6 +449,72 @@ int gg_warp_matrix_f32(const float* host_in, int64_t height, int64_t width, cons
 int gg_dq_map_i16(const float* host_master, const float* host_weight, const float* host_coverage,
                   const float* host_low, const float* host_high, const float* host_geometric,
                   int64_t n, int64_t active_frame_count, int16_t* host_dq);
+
+/* ---- differentiable affine warp (no reference counterpart: the adjoint
+ * behind gradient-based registration refinement; forward semantics of
+ * engine/warp.py:99-152 without the overshoot clamp) -------------------
+ * host_theta: 6 float64 parameters of the INVERSE map (output -> source):
+ * sx = t0 x + t1 y + t2, sy = t3 x + t4 y + t5.  Device pointers, row-major
+ * float32 H x W, enqueued on cuda_stream (NULL: legacy default stream).
+ * src_all_finite = 1 promises a source without NaN/Inf (fast Lanczos3 path). */
+int gg_warp_affine_f32_device(const float* dev_src, int64_t height, int64_t width, const double* host_theta,
+                              int interpolation, float fill, int src_all_finite, float* dev_out,
+                              void* cuda_stream);
+/* Adjoint of gg_warp_affine_f32_device for the incoming gradient dev_grad_out
+ * (H x W float32; zero or non-finite entries are ignored, as are invalid
+ * samples).  dev_grad_src (H x W float32, may be NULL) is ACCUMULATED into;
+ * dev_grad_theta (6 float64 on the device, may be NULL) is overwritten. */
+int gg_warp_affine_backward_f32_device(const float* dev_src, int64_t height, int64_t width, const double* host_theta,
+                                       int interpolation, const float* dev_grad_out, float* dev_grad_src,
+                                       double* dev_grad_theta, void* cuda_stream);
+
+/* ---- gradient (Gauss-Newton) registration refinement on resident frames
+ * (no reference counterpart: replaces the translation grid search of
+ * refine_matrix_translation_candidates_batch_to_reference with the warp
+ * adjoint's position derivatives).  Minimises
+ * sum m_p (O_p(theta) - alpha a_p - beta)^2 over a sample grid of the
+ * reference, O the moving frame sampled through the inverse affine theta,
+ * m_p dropping invalid samples, residuals above
+ * clip_sigma * sigma + mask_shift_px * min(|alpha| |grad a|, |grad O|) and
+ * samples with |grad O| > 2 |alpha| |grad a| + 3 sigma (sigma = 1.4826 *
+ * median |r| of the previous pass). */
+typedef struct {
+  int32_t transform_model; /* GG_TRANSFORM_TRANSLATION, _SIMILARITY or _AFFINE */
+  int32_t interpolation;   /* GG_INTERP_BILINEAR or GG_INTERP_LANCZOS3 */
+  int32_t sample_stride;   /* every stride-th row and column of the reference, 1..64 */
+  int32_t stats_passes;    /* photometric offset / noise passes first (stride x 2), 1..16 */
+  int32_t iterations;      /* Gauss-Newton steps, 1..100 */
+  int32_t min_samples;     /* fewer kept samples fail the frame (>= 16) */
+  float clip_sigma;
+  float mask_shift_px;
+  double tolerance_px;     /* converged when a step moves no image corner farther */
+  double max_step_px;      /* longer steps are scaled down to this */
+} gg_gradient_refine_params_t;
+
+typedef struct {
+  double matrix[9];        /* refined moving -> reference (the input matrix on failure) */
+  double alpha, beta;      /* photometric match: moving ~ alpha * reference + beta */
+  double sigma;            /* residual scale used by the mask in the last step */
+  double rms;              /* residual RMS over the kept samples, last pass */
+  double last_step_px;
+  int64_t samples;         /* kept samples, last pass */
+  int32_t iterations;
+  int32_t status;          /* 1 converged, 2 iteration cap, -1 too few samples, -2 singular system */
+} gg_gradient_refine_result_t;
+
+/* host_matrices: count x 9 affine moving -> reference starting matrices. */
+int gg_stack_refine_gradient(gg_stack* stack, int64_t reference_index, const int64_t* moving, int64_t count,
+                             const double* host_matrices, const gg_gradient_refine_params_t* params,
+                             gg_gradient_refine_result_t* host_out);
+/* One accumulation pass at given inverse parameters (count x 6) and
+ * photometric state (count x 3: alpha, beta, sigma; sigma = +inf keeps every
+ * valid sample): host_sums (count x 48) receives per job the upper triangle
+ * of J^T J (36, row-major over (t0..t5, alpha, beta) in centred units
+ * ((x - (W-1)/2) * 2 / max(W,H), likewise y)), J^T r (8), sum r^2, the kept
+ * sample count and two zeros. */
+int gg_stack_gradient_normal_equations(gg_stack* stack, int64_t reference_index, const int64_t* moving,
+                                       int64_t count, const double* host_theta, const double* host_photometric,
+                                       const gg_gradient_refine_params_t* params, double* host_sums);
 
 #ifdef __cplusplus
 }
