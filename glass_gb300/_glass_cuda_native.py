@@ -712,19 +712,21 @@ class ResidentCalibratedStack:
     def detect_stars(self, indices: Any, threshold_sigma: float = 5.0, max_stars: int = 500,
                      background: float | None = None, noise: float | None = None, window_radius: int = 4,
                      min_separation_px: float = 2.0, with_info: bool = False, catalog_min_fwhm: float = 0.0,
-                     catalog_max_eccentricity: float = 1.0):
+                     catalog_max_eccentricity: float = 1.0, mesh_cell: int = 0):
         """detect_stars semantics per resident frame -> list of structured arrays
         (x, y, flux, peak, fwhm, eccentricity, snr, sharpness, npix), brightest first.
 
         The first 80 stars passing the optional catalog shape filter stay on
-        the device as each frame's registration catalog."""
+        the device as each frame's registration catalog.  mesh_cell > 0
+        thresholds against a background mesh of that cell size instead of
+        the global median / MAD."""
         idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
         if idx.size == 0:
             raise ValueError("indices must contain at least one frame index")
         params = _lib.StarParams(float(threshold_sigma), int(max_stars), int(window_radius), float(min_separation_px),
                                  np.nan if background is None else float(background),
                                  np.nan if noise is None else float(noise), float(catalog_min_fwhm),
-                                 float(catalog_max_eccentricity))
+                                 float(catalog_max_eccentricity), int(mesh_cell))
         stars = np.zeros((idx.size, int(max_stars)), dtype=_lib.STAR_DTYPE)
         counts = np.zeros(idx.size, dtype=np.int32)
         info = (_lib.StarFrameInfo * idx.size)()
@@ -1088,6 +1090,66 @@ class ResidentCalibratedStack:
         out = np.empty((self.height, self.width), np.float32)
         _lib.call("gg_stack_download_fused_coverage", self._handle, _lib.ptr(out))
         return out
+
+    def integrate_warped_device_weights(self, matrices: Any, interpolation: str = "lanczos3",
+                                        clamping_threshold: float = -1.0,
+                                        rejection: int = _lib.GG_REJECT_WINSORIZED, low_sigma: float = 3.0,
+                                        high_sigma: float = 3.0, min_samples: int = 3,
+                                        max_reject_fraction: float = 0.5, count_map_dtype: str = "uint16") -> None:
+        """Fused warp + rejection + integration with the weights of the last
+        compute_frame_weights (device, no host round trip); asynchronous."""
+        interps = {"bilinear": _lib.GG_INTERP_BILINEAR, "lanczos3": _lib.GG_INTERP_LANCZOS3}
+        if interpolation not in interps:
+            raise ValueError("interpolation must be bilinear or lanczos3")
+        if count_map_dtype not in {"float32", "uint16"}:
+            raise ValueError("count_map_dtype must be float32 or uint16")
+        mats = self._matrices(matrices, self.frame_count)
+        params = _lib.IntegrateParams(int(rejection), float(low_sigma), float(high_sigma), int(min_samples),
+                                      float(max_reject_fraction),
+                                      _lib.GG_COUNT_U16 if count_map_dtype == "uint16" else _lib.GG_COUNT_F32, 5)
+        _lib.call("gg_stack_integrate_warped_device_weights", self._handle, _lib.ptr(mats), interps[interpolation],
+                  ctypes.c_float(clamping_threshold), ctypes.byref(params))
+        self._last_count_dtype = np.dtype(np.uint16 if count_map_dtype == "uint16" else np.float32)
+
+    # ---- CUDA graph of the resident step (no reference counterpart) ----------------
+    def capture_step_graph(self, dev_raw_ptr: int, matrices: Any, calib_params: Any,
+                           interpolation: str = "lanczos3", clamping_threshold: float = -1.0,
+                           weighting: str = "simple_snr", rejection: int = _lib.GG_REJECT_WINSORIZED,
+                           low_sigma: float = 3.0, high_sigma: float = 3.0, min_samples: int = 3,
+                           max_reject_fraction: float = 0.5, count_map_dtype: str = "uint16") -> int:
+        """Captures calibrate (uint16 frames at dev_raw_ptr) -> weights ->
+        fused warp + rejection + integration into a CUDA graph owned by the
+        stack; returns the number of kernels it replays."""
+        interps = {"bilinear": _lib.GG_INTERP_BILINEAR, "lanczos3": _lib.GG_INTERP_LANCZOS3}
+        if interpolation not in interps:
+            raise ValueError("interpolation must be bilinear or lanczos3")
+        modes = {"unit": 0, "simple_snr": 1}
+        if weighting not in modes:
+            raise ValueError("weighting must be unit or simple_snr")
+        if count_map_dtype not in {"float32", "uint16"}:
+            raise ValueError("count_map_dtype must be float32 or uint16")
+        mats = self._matrices(matrices, self.frame_count)
+        params = _lib.IntegrateParams(int(rejection), float(low_sigma), float(high_sigma), int(min_samples),
+                                      float(max_reject_fraction),
+                                      _lib.GG_COUNT_U16 if count_map_dtype == "uint16" else _lib.GG_COUNT_F32, 5)
+        _lib.call("gg_stack_graph_capture_step", self._handle, ctypes.c_void_p(int(dev_raw_ptr)), _lib.ptr(mats),
+                  interps[interpolation], ctypes.c_float(clamping_threshold), modes[weighting],
+                  ctypes.byref(calib_params), ctypes.byref(params))
+        self._last_count_dtype = np.dtype(np.uint16 if count_map_dtype == "uint16" else np.float32)
+        return self.step_graph_kernels
+
+    @property
+    def step_graph_kernels(self) -> int:
+        count = ctypes.c_int()
+        _lib.call("gg_stack_graph_kernel_count", self._handle, ctypes.byref(count))
+        return int(count.value)
+
+    def launch_step_graph(self) -> None:
+        """Replays the captured step on the stack's stream (asynchronous)."""
+        _lib.call("gg_stack_graph_launch", self._handle)
+
+    def destroy_step_graph(self) -> None:
+        _lib.call("gg_stack_graph_destroy", self._handle)
 
     def integrate_matrix_warped_mean(self, matrices: Any, weights: Any | None = None, interpolation: str = "bilinear",
                                      clamping_threshold: float = -1.0, download_mode: str = "full"):

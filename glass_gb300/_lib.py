@@ -103,6 +103,7 @@ class StarParams(ctypes.Structure):
         ("noise", ctypes.c_float),
         ("catalog_min_fwhm", ctypes.c_float),
         ("catalog_max_eccentricity", ctypes.c_float),
+        ("mesh_cell", ctypes.c_int32),
     ]
 
 
@@ -300,6 +301,13 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_download_maps": [_P, _P, _P, _P, _P, _P, _P],
     "gg_stack_integrate_warped": [_P, _P, ctypes.c_int, ctypes.c_float, _P, ctypes.POINTER(IntegrateParams)],
     "gg_stack_download_fused_coverage": [_P, _P],
+    "gg_stack_graph_capture_step": [_P, _P, _P, ctypes.c_int, ctypes.c_float, ctypes.c_int,
+                                    ctypes.POINTER(CalibParams), ctypes.POINTER(IntegrateParams)],
+    "gg_stack_integrate_warped_device_weights": [_P, _P, ctypes.c_int, ctypes.c_float,
+                                                 ctypes.POINTER(IntegrateParams)],
+    "gg_stack_graph_launch": [_P],
+    "gg_stack_graph_kernel_count": [_P, ctypes.POINTER(ctypes.c_int)],
+    "gg_stack_graph_destroy": [_P],
     "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
     "gg_stack_frame_device_ptr": [_P, ctypes.c_int64, _P],
     "gg_dq_map_i16": [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P],

@@ -11,8 +11,10 @@ sy = t3 x + t4 y + t5.
 ``refine_affine`` improves a registration matrix (moving -> reference, the
 convention of the reference's warps) by maximising the masked normalised
 cross-correlation (or minimising the masked, photometrically matched SSD)
-between the reference frame and the warped moving frame with L-BFGS over the
-similarity / affine / translation parameters.  The mask keeps pixels where
+between the reference frame and the warped moving frame over the similarity /
+affine / translation parameters by trust-region Newton steps (autograd
+gradients through the adjoint, the Hessian from forward differences of the
+gradient, Levenberg damping, capped steps).  The mask keeps pixels where
 both frames and the sample are finite and drops single-frame outliers
 (cosmic rays, hot pixels): a pixel whose residual after a linear photometric
 match exceeds ``clip_sigma`` noise sigmas plus what a ``mask_shift_px``
@@ -155,10 +157,15 @@ def _basis(model: str, height: int, width: int) -> np.ndarray:
 @dataclass
 class RefineConfig:
     model: str = "similarity"
-    loss: str = "ncc"  # "ncc" | "ssd"
+    # "ssd": photometrically matched sum of squares (default); "ncc": 1 - NCC,
+    # whose normalisation by the warped frame's variance favours positions
+    # where interpolation smooths the noise (half-pixel shifts)
+    loss: str = "ssd"
     interpolation: str = "lanczos3"
     rounds: int = 2  # mask re-estimations
-    iterations: int = 20  # L-BFGS iterations per round
+    iterations: int = 6  # trust-region Newton steps per round
+    max_step_px: float = 0.5  # trust radius (parameter units: about 1 px at the image edge)
+    tolerance_px: float = 1.0e-3
     clip_sigma: float = 5.0
     mask_shift_px: float = 1.0
     border_px: int = 4
@@ -264,23 +271,57 @@ def refine_affine(reference: torch.Tensor, moving: torch.Tensor, matrix, config:
         mf = mask.double()
         target = (alpha * ref0 + beta)
 
-        def closure():
+        def loss_at(uu, grad: bool):
             nonlocal evaluations
-            opt.zero_grad()
-            warped = AffineWarp.apply(moving, theta_of(u), interp, float("nan"), moving_finite)
+            p = uu.detach().clone().requires_grad_(grad)
+            warped = AffineWarp.apply(moving, theta_of(p), interp, float("nan"), moving_finite)
             b = torch.where(mask, warped, torch.zeros_like(warped)).double()
             if cfg.loss == "ncc":
                 loss = 1.0 - _masked_ncc(ref0, b, mf)
             else:
                 loss = (((b - target) * mf) ** 2).sum() / (mf.sum() * sigma * sigma)
-            loss.backward()
             evaluations += 1
             history.append(float(loss.detach()))
-            return loss
+            if not grad:
+                return float(loss.detach()), None
+            loss.backward()
+            return float(loss.detach()), p.grad.detach().clone()
 
-        opt = torch.optim.LBFGS([u], lr=1.0, max_iter=max(1, cfg.iterations), tolerance_grad=1e-12,
-                                tolerance_change=1e-15, history_size=10, line_search_fn="strong_wolfe")
-        opt.step(closure)
+        # trust-region Newton: autograd gradients, the Hessian from forward
+        # differences of the gradient (steps of 0.01 px), Levenberg damping,
+        # steps capped to the trust radius (parameter units ~ px at the edge)
+        radius = cfg.max_step_px
+        k = u.numel()
+        f0, g0 = loss_at(u, True)
+        for _ in range(max(1, cfg.iterations)):
+            eps = 1.0e-2
+            hess = torch.empty((k, k), dtype=torch.float64)
+            for i in range(k):
+                e = torch.zeros_like(u)
+                e[i] = eps
+                _, gi = loss_at(u.detach() + e, True)
+                hess[:, i] = (gi - g0) / eps
+            hess = 0.5 * (hess + hess.T)
+            lam = 0.0
+            evals = torch.linalg.eigvalsh(hess)
+            if float(evals.min()) <= 0.0:
+                lam = 1.0e-6 * float(evals.abs().max()) - float(evals.min())
+            step = -torch.linalg.solve(hess + lam * torch.eye(k, dtype=torch.float64), g0)
+            big = float(step.abs().max())
+            if big > radius:
+                step = step * (radius / big)
+            f1, g1 = loss_at(u.detach() + step, True)
+            if f1 < f0:
+                with torch.no_grad():
+                    u += step
+                f0, g0 = f1, g1
+                radius = min(2.0 * radius, cfg.max_step_px)
+                if float(step.abs().max()) < cfg.tolerance_px:
+                    break
+            else:
+                radius *= 0.25
+                if radius < cfg.tolerance_px:
+                    break
     theta = theta_of(u.detach()).numpy()
     with torch.no_grad():
         wf = AffineWarp.apply(moving, torch.from_numpy(theta), interp, float("nan"), moving_finite)

@@ -100,10 +100,13 @@ __device__ __forceinline__ void lanczos3_weights_grad(float t, float (&w)[6], fl
       dw[j] = 0.0f;
       continue;
     }
+    // one correctly rounded reciprocal per tap serves f, g and both
+    // derivative quotients (1 / a3 = 3 / a)
     const float a = kPiF * d, a3 = a * (1.0f / 3.0f);
-    const float f = s1 / a, g = sd3 / a3;
-    const float fp = kPiF * dsinc_arg(a, s1, c1);
-    const float gp = (kPiF / 3.0f) * dsinc_arg(a3, sd3, cd3);
+    const float ia = __frcp_rn(a), ia3 = 3.0f * ia;
+    const float f = s1 * ia, g = sd3 * ia3;
+    const float fp = kPiF * (fabsf(a) < 1.0f ? dsinc_arg(a, s1, c1) : (c1 * a - s1) * ia * ia);
+    const float gp = (kPiF / 3.0f) * (fabsf(a3) < 1.0f ? dsinc_arg(a3, sd3, cd3) : (cd3 * a3 - sd3) * ia3 * ia3);
     w[j] = f * g;
     dw[j] = fp * g + f * gp;
   }

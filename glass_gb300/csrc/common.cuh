@@ -44,6 +44,7 @@ inline void check_cuda(cudaError_t err, const char* what) {
 
 // Process-wide count of kernels this library has launched (gg_kernel_launches).
 void note_launch(int n = 1);
+long long launch_count();
 
 // Grid sizing for streaming kernels: a whole number of waves over the SMs.
 int sm_count();

@@ -1087,14 +1087,16 @@ static void launch_fused(const IntegrateArgs& a, cudaStream_t stream) {
 // integrate_matrix_warped_{mean,sigma_clip} (integration_kernels.cu:3840-4123):
 // the result of warping every frame through its matrix (NaN fill) and
 // integrating, without writing the warped frames.
-static void integrate_warped(gg_stack* s, const double* fwd, int interp, float clamp, const float* d_weights,
-                             const gg_integrate_params_t& p) {
+static void validate_fused(gg_stack* s, int interp, const gg_integrate_params_t& p) {
   require(s->frames <= 32, "fused warp-integration supports at most 32 frames");
   require(p.rejection == GG_REJECT_NONE || p.rejection == GG_REJECT_SIGMA_CLIP || p.rejection == GG_REJECT_WINSORIZED,
           "fused warp-integration supports the mean, sigma-clip and winsorized sigma-clip rejections");
   require(interp == GG_INTERP_BILINEAR || interp == GG_INTERP_LANCZOS3,
           "fused matrix-warped interpolation must be bilinear or lanczos3");
-  const int n = static_cast<int>(s->frames);
+}
+
+// Float-float inverse coefficients of every frame's forward matrix.
+static std::vector<FusedFrame> fused_frames_host(const double* fwd, int n) {
   std::vector<FusedFrame> frames(static_cast<size_t>(n));
   for (int f = 0; f < n; ++f) {
     const double* m = fwd + 9 * f;
@@ -1104,16 +1106,26 @@ static void integrate_warped(gg_stack* s, const double* fwd, int interp, float c
     std::memset(&ff, 0, sizeof(ff));
     if (!inverse_coefficients(m, ff.m, ff.affine)) fail(GG_ERR_INVALID_ARGUMENT, "warp matrix is singular");
   }
+  return frames;
+}
+
+static void ensure_fused_buffers(gg_stack* s) {
   stack_ensure_maps(s);
+  const int n = static_cast<int>(s->frames);
   if (!s->d_fused_frames) {
     check_cuda(cudaMalloc(&s->d_fused_frames, sizeof(FusedFrame) * n), "cudaMalloc(fused frames)");
     check_cuda(cudaMalloc(&s->d_fused_counts, sizeof(unsigned) * n), "cudaMalloc(fused counts)");
     check_cuda(cudaMalloc(&s->d_fused_geometric, sizeof(float) * s->pixels), "cudaMalloc(fused coverage)");
     s->bytes_allocated += static_cast<int64_t>(sizeof(FusedFrame) + sizeof(unsigned)) * n + 4 * s->pixels;
   }
-  auto* d_frames = static_cast<FusedFrame*>(s->d_fused_frames);
-  check_cuda(cudaMemcpyAsync(d_frames, frames.data(), sizeof(FusedFrame) * n, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(fused frames)");
+}
+
+// The device part of the fused warp-integration: every argument already on
+// the device, nothing but kernel launches on the stack's stream (so it can
+// be captured into a CUDA graph).
+static void launch_fused_sequence(gg_stack* s, FusedFrame* d_frames, int interp, float clamp, const float* d_weights,
+                                  const gg_integrate_params_t& p) {
+  const int n = static_cast<int>(s->frames);
   note_launch();
   fused_prepare_kernel<<<(n + 127) / 128, 128, 0, s->stream>>>(d_frames, s->d_frame_nonfinite, s->d_fused_counts, n);
   check_cuda(cudaGetLastError(), "fused_prepare launch");
@@ -1166,7 +1178,130 @@ static void integrate_warped(gg_stack* s, const double* fwd, int interp, float c
   s->has_fused_geometric = true;
 }
 
+static void integrate_warped(gg_stack* s, const double* fwd, int interp, float clamp, const float* d_weights,
+                             const gg_integrate_params_t& p) {
+  validate_fused(s, interp, p);
+  const std::vector<FusedFrame> frames = fused_frames_host(fwd, static_cast<int>(s->frames));
+  ensure_fused_buffers(s);
+  auto* d_frames = static_cast<FusedFrame*>(s->d_fused_frames);
+  check_cuda(cudaMemcpyAsync(d_frames, frames.data(), sizeof(FusedFrame) * frames.size(), cudaMemcpyHostToDevice,
+                             s->stream),
+             "cudaMemcpyAsync(fused frames)");
+  launch_fused_sequence(s, d_frames, interp, clamp, d_weights, p);
+}
+
+// ---- CUDA graph of the resident step with fixed matrices ---------------------
+// calibrate (uint16 frames already on the device) -> frame weights -> fused
+// warp + rejection + integration.  The graph owns its inverse-coefficient
+// buffer; it reads the raw frames from the device pointer given at capture
+// and writes the stack's maps at every replay.
+struct StepGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  FusedFrame* d_frames = nullptr;
+  int kernels = 0;
+};
+
+static void step_graph_release(StepGraph& g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  if (g.d_frames) cudaFree(g.d_frames);
+  g = StepGraph{};
+}
+
+static StepGraph& step_graph(gg_stack* s) {
+  if (!s->step_graph) {
+    s->step_graph = new StepGraph();
+    s->step_graph_free = [](void* q) {
+      auto* g = static_cast<StepGraph*>(q);
+      step_graph_release(*g);
+      delete g;
+    };
+  }
+  return *static_cast<StepGraph*>(s->step_graph);
+}
+
+static void run_step_sequence(gg_stack* s, const void* dev_raw, const std::vector<int64_t>& idx,
+                              const gg_calib_params_t& calib, int weighting, FusedFrame* d_frames, int interp,
+                              float clamp, const gg_integrate_params_t& p) {
+  int rc = gg_stack_calibrate_u16_device(s, idx.data(), static_cast<int64_t>(idx.size()), dev_raw, 0, &calib);
+  if (rc != GG_OK) fail(rc, "step graph: calibration failed");
+  rc = gg_stack_compute_weights(s, weighting, nullptr, 1.0e-6f, nullptr);
+  if (rc != GG_OK) fail(rc, "step graph: frame weighting failed");
+  launch_fused_sequence(s, d_frames, interp, clamp, s->d_weights, p);
+}
+
 }  // namespace gg
+
+extern "C" int gg_stack_graph_capture_step(gg_stack* s, const void* dev_raw, const double* host_matrices,
+                                           int interpolation, float clamping_threshold, int weighting,
+                                           const gg_calib_params_t* calib, const gg_integrate_params_t* params) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(s != nullptr && dev_raw != nullptr && host_matrices != nullptr && calib != nullptr && params != nullptr,
+          "null argument");
+  require(weighting == GG_WEIGHTS_PRIOR || weighting == GG_WEIGHTS_SIMPLE_SNR, "unsupported weighting mode");
+  validate_integrate(*params);
+  validate_fused(s, interpolation, *params);
+  stack_activate(s);
+  const std::vector<FusedFrame> frames = fused_frames_host(host_matrices, static_cast<int>(s->frames));
+  StepGraph& g = step_graph(s);
+  step_graph_release(g);
+  check_cuda(cudaMalloc(&g.d_frames, sizeof(FusedFrame) * frames.size()), "cudaMalloc(step graph frames)");
+  check_cuda(cudaMemcpy(g.d_frames, frames.data(), sizeof(FusedFrame) * frames.size(), cudaMemcpyHostToDevice),
+             "cudaMemcpy(step graph frames)");
+  ensure_fused_buffers(s);
+  std::vector<int64_t> idx(static_cast<size_t>(s->frames));
+  for (int64_t k = 0; k < s->frames; ++k) idx[static_cast<size_t>(k)] = k;
+  // one eager pass: validates the inputs, sizes every lazily allocated
+  // buffer, so the capture only records launches and stream-ordered copies
+  run_step_sequence(s, dev_raw, idx, *calib, weighting, g.d_frames, interpolation, clamping_threshold, *params);
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(step graph warm-up)");
+  const int64_t before = gg::launch_count();
+  check_cuda(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
+  try {
+    run_step_sequence(s, dev_raw, idx, *calib, weighting, g.d_frames, interpolation, clamping_threshold, *params);
+  } catch (...) {
+    cudaGraph_t broken = nullptr;
+    cudaStreamEndCapture(s->stream, &broken);
+    if (broken) cudaGraphDestroy(broken);
+    note_launch(static_cast<int>(before - gg::launch_count()));
+    throw;
+  }
+  check_cuda(cudaStreamEndCapture(s->stream, &g.graph), "cudaStreamEndCapture");
+  g.kernels = static_cast<int>(gg::launch_count() - before);
+  note_launch(-g.kernels);  // recorded, not executed
+  check_cuda(cudaGraphInstantiate(&g.exec, g.graph, 0), "cudaGraphInstantiate");
+  GG_API_END
+}
+
+extern "C" int gg_stack_graph_launch(gg_stack* s) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(s != nullptr, "null argument");
+  require(s->step_graph && static_cast<StepGraph*>(s->step_graph)->exec, "no step graph has been captured");
+  stack_activate(s);
+  StepGraph& g = *static_cast<StepGraph*>(s->step_graph);
+  check_cuda(cudaGraphLaunch(g.exec, s->stream), "cudaGraphLaunch");
+  note_launch(g.kernels);
+  GG_API_END
+}
+
+extern "C" int gg_stack_graph_kernel_count(gg_stack* s, int* out) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(s != nullptr && out != nullptr, "null argument");
+  *out = s->step_graph ? static_cast<StepGraph*>(s->step_graph)->kernels : 0;
+  GG_API_END
+}
+
+extern "C" int gg_stack_graph_destroy(gg_stack* s) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(s != nullptr, "null argument");
+  if (s->step_graph) step_graph_release(*static_cast<StepGraph*>(s->step_graph));
+  GG_API_END
+}
 
 using namespace gg;
 
@@ -1207,6 +1342,17 @@ int gg_stack_integrate_warped(gg_stack* s, const double* host_matrices, int inte
   check_cuda(cudaMemcpyAsync(s->d_weights, s->h_weights_pinned, sizeof(float) * s->frames, cudaMemcpyHostToDevice,
                              s->stream),
              "cudaMemcpyAsync(weights)");
+  integrate_warped(s, host_matrices, interpolation, clamping_threshold, s->d_weights, *params);
+  GG_API_END
+}
+
+int gg_stack_integrate_warped_device_weights(gg_stack* s, const double* host_matrices, int interpolation,
+                                             float clamping_threshold, const gg_integrate_params_t* params) {
+  GG_API_BEGIN
+  require(s != nullptr && host_matrices != nullptr && params != nullptr, "null argument");
+  validate_integrate(*params);
+  stack_require_all_loaded(s, "fused warp-integration");
+  stack_activate(s);
   integrate_warped(s, host_matrices, interpolation, clamping_threshold, s->d_weights, *params);
   GG_API_END
 }

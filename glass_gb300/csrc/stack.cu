@@ -26,6 +26,7 @@ void set_last_error(int code, const char* msg) {
 
 static std::atomic<long long> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 int sm_count() {
   static int cached = 0;
@@ -144,6 +145,7 @@ static void stack_free(gg_stack* s) {
   if (s->reg_scratch && s->reg_scratch_free) s->reg_scratch_free(s->reg_scratch);
   if (s->metric_scratch && s->metric_scratch_free) s->metric_scratch_free(s->metric_scratch);
   if (s->gn_scratch && s->gn_scratch_free) s->gn_scratch_free(s->gn_scratch);
+  if (s->step_graph && s->step_graph_free) s->step_graph_free(s->step_graph);
   void* dev_ptrs[] = {s->d_slots,    s->d_slot_of_frame, s->d_spare_slot, s->d_frame_nonfinite,
                       s->d_bias,     s->d_dark,          s->d_flat,       s->d_master,
                       s->d_weight,   s->d_coverage,      s->d_low,        s->d_high,

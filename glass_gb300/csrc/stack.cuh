@@ -102,6 +102,8 @@ struct gg_stack {
   void (*metric_scratch_free)(void*) = nullptr;
   void* gn_scratch = nullptr;
   void (*gn_scratch_free)(void*) = nullptr;
+  void* step_graph = nullptr;  // captured resident step (integrate.cu)
+  void (*step_graph_free)(void*) = nullptr;
 
   // Fused warp-integration: per-frame inverse matrices, per-frame
   // non-finite sample counts of the virtual warped stack and the geometric

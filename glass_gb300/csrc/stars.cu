@@ -249,6 +249,135 @@ __global__ void star_threshold_kernel(StarFrameState* state, int frames, float k
   st.background = med;
 }
 
+// ---- background mesh (no reference counterpart) ------------------------------
+// Cells of `cell` x `cell` pixels from the top-left corner (edge cells
+// smaller).  Each cell's finite pixels give the float64 median (an even count
+// takes 0.5 * (a + b) of the two middle values) and noise 1.4826 * MAD (1
+// when the MAD is 0; NaN median and noise without finite pixels).  Values at
+// a pixel interpolate bilinearly between cell centres, u = (x + 0.5) / cell -
+// 0.5, clamped at the first and last centre, in float64 without fused
+// multiply-adds (the oracle evaluates the same operations in NumPy).
+constexpr int kMeshMaxCell = 64;
+constexpr int kMeshElems = kMeshMaxCell * kMeshMaxCell;
+
+struct MeshView {
+  const double* bg;  // [count][ny * nx] or nullptr (global statistics)
+  const double* nz;
+  int cell, nx, ny;
+};
+
+__device__ __forceinline__ void mesh_axis(int coord, int cell, int n, int& i0, int& i1, double& f) {
+  const double u = __dsub_rn(__ddiv_rn(__dadd_rn(static_cast<double>(coord), 0.5), static_cast<double>(cell)), 0.5);
+  const double fl = floor(u);
+  if (fl < 0.0) {
+    i0 = 0;
+    f = 0.0;
+  } else if (fl >= static_cast<double>(n - 1)) {
+    i0 = n - 1;
+    f = 0.0;
+  } else {
+    i0 = static_cast<int>(fl);
+    f = __dsub_rn(u, fl);
+  }
+  i1 = min(i0 + 1, n - 1);
+}
+
+__device__ __forceinline__ double mesh_lerp(const double* m, int nx, int i0, int i1, int j0, int j1, double fx,
+                                            double fy) {
+  const double gx = __dsub_rn(1.0, fx), gy = __dsub_rn(1.0, fy);
+  const double top = __dadd_rn(__dmul_rn(gx, m[j0 * nx + i0]), __dmul_rn(fx, m[j0 * nx + i1]));
+  const double bot = __dadd_rn(__dmul_rn(gx, m[j1 * nx + i0]), __dmul_rn(fx, m[j1 * nx + i1]));
+  return __dadd_rn(__dmul_rn(gy, top), __dmul_rn(fy, bot));
+}
+
+// Interpolated background and noise of frame k at pixel (x, y).
+__device__ __forceinline__ void mesh_at(const MeshView& m, int k, int x, int y, double& bg, double& nz) {
+  int i0, i1, j0, j1;
+  double fx, fy;
+  mesh_axis(x, m.cell, m.nx, i0, i1, fx);
+  mesh_axis(y, m.cell, m.ny, j0, j1, fy);
+  const int64_t off = static_cast<int64_t>(k) * m.nx * m.ny;
+  bg = mesh_lerp(m.bg + off, m.nx, i0, i1, j0, j1, fx, fy);
+  nz = mesh_lerp(m.nz + off, m.nx, i0, i1, j0, j1, fx, fy);
+}
+
+__device__ void bitonic_sort_shared(double* v, int n) {
+  for (int k = 2; k <= n; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const bool up = (i & k) == 0;
+          const double a = v[i], b = v[ixj];
+          if ((a > b) == up) {
+            v[i] = b;
+            v[ixj] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+}
+
+__device__ __forceinline__ double median_sorted(const double* v, int n) {
+  const int m = n / 2;
+  return (n & 1) ? v[m] : __dmul_rn(__dadd_rn(v[m - 1], v[m]), 0.5);
+}
+
+struct MeshArgs {
+  const float* slots;
+  const int* slot_of_frame;
+  int64_t stride;
+  int width, height;
+  const int* frames;
+  double* bg;
+  double* nz;
+  int cell, nx, ny;
+};
+
+// One CTA per (cell, frame): gather the finite pixels, sort, median; sort the
+// absolute deviations, MAD.
+__global__ void __launch_bounds__(1024) mesh_stats_kernel(MeshArgs a) {
+  __shared__ double v[kMeshElems];
+  __shared__ int s_n;
+  __shared__ double s_med;
+  const int c = blockIdx.x, k = blockIdx.y;
+  const int cx = c % a.nx, cy = c / a.nx;
+  const int x0 = cx * a.cell, y0 = cy * a.cell;
+  const int w = min(a.cell, a.width - x0), h = min(a.cell, a.height - y0);
+  const float* img = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  for (int q = threadIdx.x; q < w * h; q += blockDim.x) {
+    const float val = __ldg(img + static_cast<int64_t>(y0 + q / w) * a.width + x0 + q % w);
+    if (isfinite(val)) v[atomicAdd(&s_n, 1)] = static_cast<double>(val);
+  }
+  __syncthreads();
+  const int n = s_n;
+  const int64_t out = static_cast<int64_t>(k) * a.nx * a.ny + c;
+  if (n == 0) {
+    if (threadIdx.x == 0) a.bg[out] = a.nz[out] = __longlong_as_double(0x7ff8000000000000LL);
+    return;
+  }
+  int p2 = 1;
+  while (p2 < n) p2 <<= 1;
+  const double inf = __longlong_as_double(0x7ff0000000000000LL);
+  for (int q = n + threadIdx.x; q < p2; q += blockDim.x) v[q] = inf;
+  __syncthreads();
+  bitonic_sort_shared(v, p2);
+  if (threadIdx.x == 0) s_med = median_sorted(v, n);
+  __syncthreads();
+  const double med = s_med;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) v[q] = fabs(__dsub_rn(v[q], med));
+  __syncthreads();
+  bitonic_sort_shared(v, p2);
+  if (threadIdx.x == 0) {
+    const double mad = median_sorted(v, n);
+    a.bg[out] = med;
+    a.nz[out] = mad > 0.0 ? __dmul_rn(1.4826, mad) : 1.0;
+  }
+}
+
 struct DetectArgs {
   const float* slots;
   const int* slot_of_frame;
@@ -257,6 +386,8 @@ struct DetectArgs {
   const int* frames;
   StarFrameState* state;
   unsigned* cand;  // [count][kMaxCandidates] raster indices
+  MeshView mesh;
+  double k_sigma;
 };
 
 // Local-maximum candidates (star_detect.py:142-151).
@@ -279,7 +410,16 @@ __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
     const int64_t idx = static_cast<int64_t>(y) * W + x;
     if (interior > 0 && x <= cols) {
       const float c = __ldg(img + idx);
-      if (isfinite(c) && c > thr) {
+      bool above;
+      if (a.mesh.bg) {
+        double bg, nz;
+        mesh_at(a.mesh, k, x, y, bg, nz);
+        const double nzc = (nz >= 1.0e-6 || isnan(nz)) ? nz : 1.0e-6;  // np.maximum keeps NaN
+        above = static_cast<double>(c) > __dadd_rn(bg, __dmul_rn(a.k_sigma, nzc));
+      } else {
+        above = c > thr;
+      }
+      if (isfinite(c) && above) {
         hit = true;
 #pragma unroll
         for (int dy = -1; dy <= 1; ++dy)
@@ -327,6 +467,7 @@ struct CatalogArgs {
   int* error;
   double* cat_xy;  // [frames][kCatalogPoints][2]: brightest stars, for registration
   int* cat_n;      // [frames]
+  MeshView mesh;   // local background / noise per star when mesh.bg is set
 };
 
 // Sort candidate raster indices ascending (one CTA per frame, bitonic in
@@ -373,12 +514,13 @@ __global__ void __launch_bounds__(256) star_measure_kernel(CatalogArgs a) {
   const unsigned* cand = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
   StarRec* recs = a.recs + static_cast<int64_t>(k) * kMaxCandidates;
   const int W = a.width, H = a.height, r = a.radius;
-  const float bg32 = st.background_f32;
-  const double bg = st.background;
   for (int c = warp; c < n; c += nwarps) {
     const unsigned idx = cand[c];
     const int x = static_cast<int>(idx % static_cast<unsigned>(W));
     const int y = static_cast<int>(idx / static_cast<unsigned>(W));
+    double bg = st.background, noise = st.noise;
+    if (a.mesh.bg) mesh_at(a.mesh, k, x, y, bg, noise);
+    const float bg32 = a.mesh.bg ? __double2float_rn(bg) : st.background_f32;
     const int x0 = max(0, x - r), x1 = min(W, x + r + 1);
     const int y0 = max(0, y - r), y1 = min(H, y + r + 1);
     const int ww = x1 - x0, npx = ww * (y1 - y0);
@@ -414,7 +556,7 @@ __global__ void __launch_bounds__(256) star_measure_kernel(CatalogArgs a) {
       const float center = __ldg(img + static_cast<int64_t>(y) * W + x);
       rec.peak = fmax(static_cast<double>(center) - bg, 0.0);
       rec.npix = pos;
-      rec.snr = f / fmax(st.noise * sqrt(static_cast<double>(max(pos, 1))), 1.0e-6);
+      rec.snr = f / fmax(noise * sqrt(static_cast<double>(max(pos, 1))), 1.0e-6);
       rec.sharpness = rec.peak / fmax(f, 1.0e-6);
     }
     if (lane == 0) recs[c] = rec;
@@ -672,13 +814,18 @@ __global__ void __launch_bounds__(256) star_moments_kernel(CatalogArgs a) {
   const int* chosen = a.kept + static_cast<int64_t>(k) * kMaxCandidates;
   gg_star_t* out = a.out + static_cast<int64_t>(k) * a.max_stars;
   const int W = a.width, H = a.height, r = a.radius;
-  const float bg32 = st.background_f32;
   for (int i = warp; i < nout; i += nwarps) {
     const int c = chosen[i];
     const StarRec rec = recs[c];
     const unsigned idx = cand[c];
     const int x = static_cast<int>(idx % static_cast<unsigned>(W));
     const int y = static_cast<int>(idx / static_cast<unsigned>(W));
+    float bg32 = st.background_f32;
+    if (a.mesh.bg) {
+      double bg, noise;
+      mesh_at(a.mesh, k, x, y, bg, noise);
+      bg32 = __double2float_rn(bg);
+    }
     const int x0 = max(0, x - r), x1 = min(W, x + r + 1);
     const int y0 = max(0, y - r), y1 = min(H, y + r + 1);
     const int ww = x1 - x0, npx = ww * (y1 - y0);
@@ -921,10 +1068,14 @@ struct StarScratch {
   int64_t pw_pixels = 0;
   int capacity_frames = 0;
   int max_stars = 0;
+  double* mesh_bg = nullptr;  // [frames][cells]
+  double* mesh_nz = nullptr;
+  int64_t mesh_cap = 0;       // doubles per array
 };
 
 static void free_star_scratch(StarScratch& s) {
-  void* ps[] = {s.state, s.hist, s.cand, s.recs, s.kept, s.out, s.frames, s.rms, s.pw_prefix, s.pw_leaves, s.pw_sums};
+  void* ps[] = {s.state,  s.hist,      s.cand,      s.recs,    s.kept,    s.out,    s.frames,
+                s.rms,    s.pw_prefix, s.pw_leaves, s.pw_sums, s.mesh_bg, s.mesh_nz};
   for (void* p : ps)
     if (p) cudaFree(p);
   s = StarScratch{};
@@ -1062,6 +1213,36 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
   da.frames = sc.frames;
   da.state = sc.state;
   da.cand = sc.cand;
+  da.k_sigma = static_cast<double>(p.threshold_sigma);
+  if (p.mesh_cell > 0) {
+    MeshArgs ma{};
+    ma.cell = p.mesh_cell;
+    ma.nx = static_cast<int>((s->width + p.mesh_cell - 1) / p.mesh_cell);
+    ma.ny = static_cast<int>((s->height + p.mesh_cell - 1) / p.mesh_cell);
+    const int64_t need = static_cast<int64_t>(ma.nx) * ma.ny * count;
+    if (sc.mesh_cap < need) {
+      if (sc.mesh_bg) cudaFree(sc.mesh_bg);
+      if (sc.mesh_nz) cudaFree(sc.mesh_nz);
+      sc.mesh_bg = sc.mesh_nz = nullptr;
+      sc.mesh_cap = 0;
+      check_cuda(cudaMalloc(&sc.mesh_bg, sizeof(double) * need), "cudaMalloc(background mesh)");
+      check_cuda(cudaMalloc(&sc.mesh_nz, sizeof(double) * need), "cudaMalloc(noise mesh)");
+      sc.mesh_cap = need;
+    }
+    ma.slots = s->d_slots;
+    ma.slot_of_frame = s->d_slot_of_frame;
+    ma.stride = s->stride;
+    ma.width = static_cast<int>(s->width);
+    ma.height = static_cast<int>(s->height);
+    ma.frames = sc.frames;
+    ma.bg = sc.mesh_bg;
+    ma.nz = sc.mesh_nz;
+    note_launch();
+    mesh_stats_kernel<<<dim3(static_cast<unsigned>(ma.nx * ma.ny), static_cast<unsigned>(count)), 1024, 0,
+                        s->stream>>>(ma);
+    check_cuda(cudaGetLastError(), "mesh_stats launch");
+    da.mesh = MeshView{sc.mesh_bg, sc.mesh_nz, ma.cell, ma.nx, ma.ny};
+  }
   note_launch();
   star_detect_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), 256, 0, s->stream>>>(da);
   check_cuda(cudaGetLastError(), "star_detect launch");
@@ -1084,6 +1265,7 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
   ensure_catalog_storage(s);
   ca.cat_xy = s->d_cat_xy;
   ca.cat_n = s->d_cat_n;
+  ca.mesh = da.mesh;
   const size_t sort_smem = sizeof(unsigned) * kMaxCandidates;
   check_cuda(cudaFuncSetAttribute(star_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(sort_smem)),
@@ -1129,6 +1311,9 @@ int gg_stack_detect_stars(gg_stack* s, const int64_t* indices, int64_t count, co
   require(std::isfinite(p.min_separation_px), "min_separation_px must be finite");
   require(std::isfinite(p.catalog_min_fwhm) && std::isfinite(p.catalog_max_eccentricity),
           "catalog filter thresholds must be finite");
+  require(p.mesh_cell == 0 || (p.mesh_cell >= 8 && p.mesh_cell <= kMeshMaxCell), "mesh_cell must be 0 or in [8, 64]");
+  require(p.mesh_cell == 0 || (std::isnan(p.background) && std::isnan(p.noise)),
+          "a background mesh estimates background and noise itself (pass NaN)");
   for (int64_t k = 0; k < count; ++k) stack_require_loaded(s, indices[k], "star detection");
   stack_activate(s);
   detect_stars(s, indices, static_cast<int>(count), p);

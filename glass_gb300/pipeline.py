@@ -87,6 +87,9 @@ class StepConfig:
     # ray streaks are elongated (eccentricity near 1), stars round
     catalog_min_fwhm: float = 0.0
     catalog_max_eccentricity: float = 0.8
+    # 0: the reference's global median / MAD threshold; 8..64: background
+    # mesh of that cell size (local threshold, local background per star)
+    background_mesh_cell: int = 0
     registration_tolerance_px: float = 3.0
     registration_min_inliers: int = 6
     # sub-pixel translation refinement of the triangle matrices (a coarse
@@ -103,10 +106,10 @@ class StepConfig:
 DEFAULT_REFINE = {"search_radius_px": 1.0, "coarse_step_px": 0.25, "fine_radius_px": 0.25, "fine_step_px": 0.0625,
                   "coarse_sample_stride": 4, "final_sample_stride": 8}
 
-# similarity model, Lanczos3 derivatives, every 2nd row and column, three
-# noise passes, at most eight steps, stop below 1e-3 px
-DEFAULT_GRADIENT_REFINE = {"model": "similarity", "interpolation": "lanczos3", "sample_stride": 2,
-                           "stats_passes": 3, "iterations": 8, "min_samples": 256, "clip_sigma": 5.0,
+# similarity model, Lanczos3 derivatives, every 3rd row and column, three
+# noise passes (every 6th), at most five steps, stop below 1e-3 px
+DEFAULT_GRADIENT_REFINE = {"model": "similarity", "interpolation": "lanczos3", "sample_stride": 3,
+                           "stats_passes": 3, "iterations": 5, "min_samples": 256, "clip_sigma": 5.0,
                            "mask_shift_px": 1.0, "tolerance_px": 1.0e-3, "max_step_px": 2.0}
 
 
@@ -153,7 +156,8 @@ class ResidentPipeline:
         """Star catalogs of every frame; they stay on the device for register()."""
         cfg = self.config
         params = _lib.StarParams(float(cfg.star_threshold_sigma), int(cfg.star_max_stars), 4, 2.0, np.nan, np.nan,
-                                 float(cfg.catalog_min_fwhm), float(cfg.catalog_max_eccentricity))
+                                 float(cfg.catalog_min_fwhm), float(cfg.catalog_max_eccentricity),
+                                 int(cfg.background_mesh_cell))
         _lib.call("gg_stack_detect_stars", self.stack.handle, _lib.ptr(self._indices), ctypes.c_int64(self.frames),
                   ctypes.byref(params), None, None, None)
 
@@ -211,18 +215,20 @@ class ResidentPipeline:
             out[k] = np.asarray(res[pos].matrix, dtype=np.float64).reshape(3, 3)
         return out
 
-    def refine_adjoint(self, matrices: np.ndarray, reference_index: int = 0, config=None) -> tuple[np.ndarray, list]:
-        """Gradient refinement (glass_gb300.adjoint.refine_affine) of every
-        registered frame's matrix against the reference frame, on the
-        calibrated frames in place (run it before warp()).  Returns the new
-        matrices and the per-frame outcomes."""
+    def refine_adjoint(self, matrices: np.ndarray, reference_index: int = 0, config=None,
+                       frames: list[int] | None = None) -> tuple[np.ndarray, list]:
+        """Gradient refinement (glass_gb300.adjoint.refine_affine: torch
+        autograd through the warp adjoint) of the registered frames' matrices
+        (all, or `frames`) against the reference frame, on the calibrated
+        frames in place (run it before warp()).  Returns the new matrices and
+        the per-frame outcomes."""
         from glass_gb300.adjoint import refine_affine
 
         ok = getattr(self, "_registered", None)
         out = np.array(matrices, dtype=np.float64, copy=True)
         ref = self.stack.frame_tensor(reference_index)
         outcomes = []
-        for k in range(self.frames):
+        for k in range(self.frames) if frames is None else frames:
             if k == reference_index or (ok is not None and not ok[k]):
                 continue
             res = refine_affine(ref, self.stack.frame_tensor(k), out[k], config)
@@ -250,6 +256,28 @@ class ResidentPipeline:
         cfg = self.config
         self.stack.integrate_async("device", cfg.rejection, cfg.low_sigma, cfg.high_sigma, cfg.min_samples,
                                    cfg.max_reject_fraction, cfg.count_map_dtype)
+
+    def capture_graph(self, dev_raw_ptr: int, matrices: np.ndarray) -> int:
+        """Captures calibrate -> weights -> fused warp + rejection + integration
+        with fixed matrices into a CUDA graph (at most 32 frames); returns the
+        number of kernels one replay launches."""
+        cfg = self.config
+        return self.stack.capture_step_graph(dev_raw_ptr, matrices, self._calib_params(), cfg.interpolation,
+                                             cfg.clamping_threshold, cfg.weighting, cfg.rejection, cfg.low_sigma,
+                                             cfg.high_sigma, cfg.min_samples, cfg.max_reject_fraction,
+                                             cfg.count_map_dtype)
+
+    def launch_graph(self) -> None:
+        self.stack.launch_step_graph()
+
+    def step_device_fused(self, dev_raw_ptr: int, matrices: np.ndarray) -> None:
+        """The eager launch sequence that capture_graph records."""
+        cfg = self.config
+        self.calibrate_device(dev_raw_ptr)
+        self.weights()
+        self.stack.integrate_warped_device_weights(matrices, cfg.interpolation, cfg.clamping_threshold, cfg.rejection,
+                                                   cfg.low_sigma, cfg.high_sigma, cfg.min_samples,
+                                                   cfg.max_reject_fraction, cfg.count_map_dtype)
 
     def step_device(self, dev_raw_ptr: int, matrices: np.ndarray | None = None) -> None:
         self.calibrate_device(dev_raw_ptr)

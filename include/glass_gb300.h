@@ -224,6 +224,26 @@ int gg_stack_integrate_warped(gg_stack* stack, const double* host_matrices, int 
                               const gg_integrate_params_t* params);
 /* Geometric coverage (float32 H*W) of the last fused warp-integration. */
 int gg_stack_download_fused_coverage(gg_stack* stack, float* host_out);
+/* gg_stack_integrate_warped with the weights of the last
+ * gg_stack_compute_weights (left on the device; no host round trip). */
+int gg_stack_integrate_warped_device_weights(gg_stack* stack, const double* host_matrices, int interpolation,
+                                             float clamping_threshold, const gg_integrate_params_t* params);
+
+/* CUDA graph of the resident step with fixed matrices (no reference
+ * counterpart; the reference launches every kernel from the host):
+ * calibrate all frames from uint16 frames already on the device (dev_raw,
+ * frame-major, H*W each, read at every replay) -> frame weights (weighting =
+ * GG_WEIGHTS_PRIOR (unit) or GG_WEIGHTS_SIMPLE_SNR, on the device) -> fused
+ * warp + rejection + integration through host_matrices (as
+ * gg_stack_integrate_warped; at most 32 frames).  Capture runs the sequence
+ * once eagerly first.  gg_stack_graph_launch replays it on the stack's
+ * stream (asynchronous; maps as after gg_stack_integrate_warped). */
+int gg_stack_graph_capture_step(gg_stack* stack, const void* dev_raw, const double* host_matrices, int interpolation,
+                                float clamping_threshold, int weighting, const gg_calib_params_t* calib,
+                                const gg_integrate_params_t* params);
+int gg_stack_graph_launch(gg_stack* stack);
+int gg_stack_graph_kernel_count(gg_stack* stack, int* out);
+int gg_stack_graph_destroy(gg_stack* stack);
 /* Downloads the maps of the last integration; any pointer may be NULL.  Count
  * maps are float32 or uint16 per the count_dtype used. */
 int gg_stack_download_maps(gg_stack* stack, float* host_master, float* host_weight, void* host_coverage,
@@ -266,6 +286,17 @@ typedef struct {
    * a shape filter against cosmic-ray hits as bright as stars. */
   float catalog_min_fwhm;
   float catalog_max_eccentricity;
+  /* Background mesh (no reference counterpart; 0 = the reference's global
+   * median / MAD).  mesh_cell in [8, 64]: the frame is cut into cells of
+   * mesh_cell x mesh_cell pixels from the top-left corner (edge cells
+   * smaller); each cell's finite pixels give a float64 median and noise
+   * 1.4826 * MAD (1 when the MAD is 0; NaN for a cell without finite
+   * pixels); background and noise at a pixel are the bilinear interpolation
+   * between cell centres (clamped at the border), the threshold there is
+   * background + k * max(noise, 1e-6) compared in float64, and each star is
+   * measured against the interpolated background and noise at its peak.
+   * background / noise must then be NaN. */
+  int32_t mesh_cell;
 } gg_star_params_t;
 
 /* One star (cpu/star_detect.py:8-18); fwhm / eccentricity NaN when undefined. */

@@ -81,3 +81,94 @@ def test_gpu_detect_stars_batch_and_info(native):
         np.testing.assert_allclose(cats[pos]["x"], [e[0] for e in exp], rtol=1e-9)
         np.testing.assert_allclose(cats[pos]["flux"], [e[2] for e in exp], rtol=1e-9)
     s.close()
+
+
+# ---- background mesh (this project's extension; the oracle is the spec) ----------
+
+def _gradient_field(seed, h=192, w=256, n=40):
+    """Stars on a sky with a steep gradient (300 -> 2300 ADU across the frame)."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    img = 300.0 + 2000.0 * xx / (w - 1) + 150.0 * np.sin(yy / 40.0)
+    pos = []
+    for _ in range(n):
+        x0, y0 = rng.uniform(6, w - 7), rng.uniform(6, h - 7)
+        img += rng.uniform(150, 4000) * np.exp(-((xx - x0) ** 2 + (yy - y0) ** 2) / (2 * 1.3 ** 2))
+        pos.append((x0, y0))
+    img += 8.0 * rng.standard_normal((h, w))
+    return img.astype(np.float32), np.asarray(pos)
+
+
+def test_oracle_mesh_background_tracks_gradient():
+    img, pos = _gradient_field(1)
+    bg, nz = ostars.background_mesh(img, 32)
+    assert bg.shape == (6, 8)
+    # cell medians follow the sky (the gradient inside a 32-px cell, 250 ADU,
+    # sets its MAD: the noise estimate is local but not gradient-free)
+    assert np.all(np.diff(bg, axis=1) > 100.0)
+    assert np.all(nz < 130.0)
+    glob = ostars.detect_stars(img, threshold_sigma=5.0, max_stars=500)
+    mesh = ostars.detect_stars(img, threshold_sigma=5.0, max_stars=500, mesh_cell=32)
+
+    def matched(cat):
+        got = np.asarray([(s[0], s[1]) for s in cat]).reshape(-1, 2)
+        if got.size == 0:
+            return 0
+        d = np.sqrt(((pos[:, None, :] - got[None]) ** 2).sum(-1)).min(axis=1)
+        return int(np.count_nonzero(d < 1.0))
+
+    # the global threshold (median + 5 MAD-sigma of the whole gradient) sits
+    # above most stars; the mesh finds every one of them
+    assert matched(mesh) == len(pos) and matched(glob) < len(pos) // 2
+    # every mesh detection is a real star (no sky-gradient peaks)
+    got = np.asarray([(s[0], s[1]) for s in mesh])
+    d = np.sqrt(((got[:, None, :] - pos[None]) ** 2).sum(-1)).min(axis=1)
+    assert np.all(d < 2.0)
+
+
+def test_oracle_mesh_value_interpolates_between_centres():
+    mesh = np.array([[0.0, 10.0], [20.0, 30.0]])
+    # centres at (cell - 1) / 2 = 7.5 and 23.5 for cell 16; clamped outside
+    assert ostars.mesh_value(mesh, 16, 0, 0) == 0.0
+    assert ostars.mesh_value(mesh, 16, 31, 31) == 30.0
+    assert abs(ostars.mesh_value(mesh, 16, 15.5, 7.5) - 5.0) < 1e-12
+    assert abs(ostars.mesh_value(mesh, 16, 15.5, 15.5) - 15.0) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cell", [16, 32, 64])
+def test_gpu_mesh_detection_matches_oracle(native, cell):
+    frames = [_gradient_field(s)[0] for s in (2, 3)]
+    frames[1][10:40, 200:230] = np.nan  # a masked patch: one cell partly, others fully
+    h, w = frames[0].shape
+    s = native.ResidentCalibratedStack(2, h, w)
+    try:
+        for k in range(2):
+            s.upload_calibrated_frame(k, frames[k])
+        cats = s.detect_stars([0, 1], threshold_sigma=5.0, max_stars=300, mesh_cell=cell)
+    finally:
+        s.close()
+    gpu_fields = ("x", "y", "flux", "peak", "fwhm", "eccentricity", "snr", "sharpness", "npix")
+    for k in range(2):
+        exp = ostars.detect_stars(frames[k], threshold_sigma=5.0, max_stars=300, mesh_cell=cell)
+        assert cats[k].size == len(exp), (k, cats[k].size, len(exp))
+        for j, gf in enumerate(gpu_fields):
+            e = np.asarray([np.nan if s_[j] is None else s_[j] for s_ in exp], dtype=np.float64)
+            np.testing.assert_allclose(cats[k][gf].astype(np.float64), e, rtol=1e-9, atol=1e-12,
+                                       err_msg=f"frame {k} {gf}")
+
+
+@pytest.mark.gpu
+def test_gpu_mesh_detection_arguments(native):
+    img = _gradient_field(4)[0]
+    s = native.ResidentCalibratedStack(1, *img.shape)
+    try:
+        s.upload_calibrated_frame(0, img)
+        with pytest.raises(ValueError):
+            s.detect_stars([0], mesh_cell=4)
+        with pytest.raises(ValueError):
+            s.detect_stars([0], mesh_cell=128)
+        with pytest.raises(ValueError):
+            s.detect_stars([0], mesh_cell=32, background=300.0)
+    finally:
+        s.close()
