@@ -558,6 +558,7 @@ def main():
         "stages": kernels,
         "registration": registration,
         "graph_step": graph,
+        "autotune": _lib.autotune_entries(),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mpix-frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * e2e_s / e2e_steps},

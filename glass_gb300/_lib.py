@@ -306,6 +306,12 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_integrate_warped_device_weights": [_P, _P, ctypes.c_int, ctypes.c_float,
                                                  ctypes.POINTER(IntegrateParams)],
     "gg_stack_graph_launch": [_P],
+    "gg_autotune_set_enabled": [ctypes.c_int],
+    "gg_autotune_clear": [],
+    "gg_autotune_count": [ctypes.POINTER(ctypes.c_int32)],
+    "gg_autotune_entry": [ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t,
+                          ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_float),
+                          ctypes.POINTER(ctypes.c_int32)],
     "gg_stack_graph_kernel_count": [_P, ctypes.POINTER(ctypes.c_int)],
     "gg_stack_graph_destroy": [_P],
     "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
@@ -409,6 +415,28 @@ def kernel_launches() -> int:
     count = ctypes.c_int64()
     call("gg_kernel_launches", ctypes.byref(count))
     return int(count.value)
+
+
+def autotune_set_enabled(enabled: bool) -> None:
+    call("gg_autotune_set_enabled", int(bool(enabled)))
+
+
+def autotune_clear() -> None:
+    call("gg_autotune_clear")
+
+
+def autotune_entries() -> list[dict]:
+    """The launch shapes the autotuner has chosen in this process."""
+    count = ctypes.c_int32()
+    call("gg_autotune_count", ctypes.byref(count))
+    out = []
+    for i in range(count.value):
+        kernel, shape, choice = (ctypes.create_string_buffer(256) for _ in range(3))
+        ms, cands = ctypes.c_float(), ctypes.c_int32()
+        call("gg_autotune_entry", i, kernel, 256, shape, 256, choice, 256, ctypes.byref(ms), ctypes.byref(cands))
+        out.append({"kernel": kernel.value.decode(), "shape": shape.value.decode(), "choice": choice.value.decode(),
+                    "ms": float(ms.value), "candidates": int(cands.value)})
+    return out
 
 
 def ptr(array: np.ndarray | None) -> int | None:

@@ -218,6 +218,19 @@ def _outlier_mask(ref: torch.Tensor, warped: torch.Tensor, valid: torch.Tensor, 
     return mask, float(alpha), float(beta), float(sigma)
 
 
+def _matched_ssd(a: torch.Tensor, b: torch.Tensor, m: torch.Tensor) -> torch.Tensor:
+    """Mean of (b - alpha a - beta)^2 over the mask with (alpha, beta) the
+    least-squares photometric match, computed in the graph (the gradient of
+    the minimum is the partial gradient at the minimiser)."""
+    n = m.sum()
+    am = (a * m).sum() / n
+    bm = (b * m).sum() / n
+    da, db = (a - am) * m, (b - bm) * m
+    alpha = (da * db).sum() / (da * da).sum()
+    r = db - alpha * da
+    return (r * r).sum() / n
+
+
 def _masked_ncc(a: torch.Tensor, b: torch.Tensor, m: torch.Tensor) -> torch.Tensor:
     n = m.sum()
     am = (a * m).sum() / n
@@ -269,7 +282,6 @@ def refine_affine(reference: torch.Tensor, moving: torch.Tensor, matrix, config:
         with torch.no_grad():
             valid, mask, alpha, beta, sigma = current_mask(theta_of(u.detach()))
         mf = mask.double()
-        target = (alpha * ref0 + beta)
 
         def loss_at(uu, grad: bool):
             nonlocal evaluations
@@ -279,7 +291,7 @@ def refine_affine(reference: torch.Tensor, moving: torch.Tensor, matrix, config:
             if cfg.loss == "ncc":
                 loss = 1.0 - _masked_ncc(ref0, b, mf)
             else:
-                loss = (((b - target) * mf) ** 2).sum() / (mf.sum() * sigma * sigma)
+                loss = _matched_ssd(ref0, b, mf) / (sigma * sigma)
             evaluations += 1
             history.append(float(loss.detach()))
             if not grad:

@@ -28,6 +28,7 @@
 #include <cstring>
 #include <vector>
 
+#include "autotune.cuh"
 #include "sampling.cuh"
 #include "stack.cuh"
 
@@ -69,6 +70,9 @@ struct IntegrateArgs {
   int width, height;
   float clamp;
   float* geometric_out;  // frames with a geometrically valid sample, per pixel
+  int tile_w, tile_h;    // fused path: 2-D pixel tiles (tile_w * tile_h == threads), 0 = rows
+  int64_t tiles_x;       // tiles per image row
+  int64_t tile_slots;    // tiles * threads
 };
 
 // One fused sample of frame f at output pixel (x, y): the value the warp
@@ -654,7 +658,20 @@ __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
   const int64_t P = a.pixels;
   const float ls = a.low_sigma, hs = a.high_sigma;
   float* St = S + tid;
-  for (int64_t p = static_cast<int64_t>(blockIdx.x) * T + tid; p < P; p += static_cast<int64_t>(gridDim.x) * T) {
+  // The fused path may walk the image in tiles of tile_w x tile_h pixels
+  // (one tile per CTA iteration; neighbouring rows share Lanczos taps in L1);
+  // otherwise a CTA covers T consecutive pixels.
+  const bool tiled = WARP != 0 && a.tile_w > 0;
+  const int64_t Q = tiled ? a.tile_slots : P;
+  for (int64_t q = static_cast<int64_t>(blockIdx.x) * T + tid; q < Q; q += static_cast<int64_t>(gridDim.x) * T) {
+    int64_t p = q;
+    if (tiled) {
+      const int64_t t = q / T;
+      const int px0 = static_cast<int>(t % a.tiles_x) * a.tile_w + tid % a.tile_w;
+      const int py0 = static_cast<int>(t / a.tiles_x) * a.tile_h + tid / a.tile_w;
+      if (px0 >= a.width || py0 >= a.height) continue;
+      p = static_cast<int64_t>(py0) * a.width + px0;
+    }
     float x[NB];
     if constexpr (WARP == 0) {
 #pragma unroll
@@ -1078,10 +1095,24 @@ static void launch_fused(const IntegrateArgs& a, cudaStream_t stream) {
              "cudaFuncSetAttribute(fused integrate)");
   int per_sm = 0;
   check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem), "occupancy");
-  const unsigned grid = grid_for(static_cast<size_t>(a.pixels), T, std::max(per_sm, 1));
-  note_launch();
-  kern<<<grid, T, smem, stream>>>(a);
-  check_cuda(cudaGetLastError(), "fused integrate launch");
+  // pixel tile shape (tile_w x tile_h = T): wider tiles coalesce the map
+  // writes, taller ones share the Lanczos / bilinear source rows in L1
+  static const int kTiles[3][2] = {{128, 1}, {64, 2}, {32, 4}};
+  auto run = [&](int c) {
+    IntegrateArgs b = a;
+    b.tile_w = kTiles[c][0];
+    b.tile_h = kTiles[c][1];
+    b.tiles_x = (a.width + b.tile_w - 1) / b.tile_w;
+    b.tile_slots = b.tiles_x * ((a.height + b.tile_h - 1) / b.tile_h) * T;
+    const unsigned grid = grid_for(static_cast<size_t>(b.tile_slots), T, std::max(per_sm, 1));
+    note_launch();
+    kern<<<grid, T, smem, stream>>>(b);
+    check_cuda(cudaGetLastError(), "fused integrate launch");
+  };
+  const std::string shape = std::to_string(a.frames) + "x" + std::to_string(a.height) + "x" +
+                            std::to_string(a.width) + (INTERP == GG_INTERP_LANCZOS3 ? " lanczos3" : " bilinear") +
+                            " mode" + std::to_string(MODE);
+  run(autotune_choose("fused_warp_integrate tile", shape, {"128x1", "64x2", "32x4"}, 0, stream, run));
 }
 
 // integrate_matrix_warped_{mean,sigma_clip} (integration_kernels.cu:3840-4123):

@@ -32,6 +32,7 @@
 #include <cstring>
 #include <vector>
 
+#include "autotune.cuh"
 #include "sampling.cuh"
 #include "stack.cuh"
 
@@ -372,10 +373,16 @@ static std::vector<double> evaluate_candidates(gg_stack* s, const std::vector<Pa
   if (jobs.empty()) return sums;
   const int64_t sw = (s->width + stride - 1) / stride, sh = (s->height + stride - 1) / stride;
   require(s->pixels <= (int64_t{1} << 31) - 1, "alignment metrics support frames of fewer than 2^31 pixels");
-  // bands: enough CTAs to fill the GPU, at least 2048 samples each
+  // bands: enough CTAs to fill the GPU (2, 4 or 8 per SM over all jobs,
+  // picked by the autotuner), at least 2048 samples each
   const int64_t samples = sw * sh;
-  const int want = std::max(1, (sm_count() * 4 + static_cast<int>(jobs.size()) - 1) / static_cast<int>(jobs.size()));
-  const int bands = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(want, (samples + 2047) / 2048)));
+  int band_options[3];
+  for (int i = 0; i < 3; ++i) {
+    const int want = std::max(1, (sm_count() * (2 << i) + static_cast<int>(jobs.size()) - 1) /
+                                     static_cast<int>(jobs.size()));
+    band_options[i] = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(want, (samples + 2047) / 2048)));
+  }
+  const int bands = std::max(band_options[0], std::max(band_options[1], band_options[2]));  // capacity
   MetricScratch& m = metric_scratch(s);
   const int nj = static_cast<int>(jobs.size()), ncand = static_cast<int>(cands.size());
   if (m.job_cap < nj || m.cand_cap < ncand || m.bands_cap < bands) {
@@ -407,19 +414,25 @@ static std::vector<double> evaluate_candidates(gg_stack* s, const std::vector<Pa
   a.width = static_cast<int>(s->width);
   a.height = static_cast<int>(s->height);
   a.sample_stride = stride;
-  a.bands = bands;
   a.jobs = m.jobs;
   a.cands = m.cands;
   a.partial = m.partial;
   check_cuda(cudaFuncSetAttribute(metric_partials_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(sizeof(MetricShared))),
              "cudaFuncSetAttribute(metric_partials)");
-  note_launch();
-  metric_partials_kernel<<<dim3(bands, nj), kMetricThreads, sizeof(MetricShared), s->stream>>>(a);
-  check_cuda(cudaGetLastError(), "metric_partials launch");
-  note_launch();
-  metric_reduce_kernel<<<(ncand + 127) / 128, 128, 0, s->stream>>>(m.partial, ncand, bands, m.sums);
-  check_cuda(cudaGetLastError(), "metric_reduce launch");
+  auto run = [&](int c) {
+    MetricArgs b = a;
+    b.bands = band_options[c];
+    note_launch();
+    metric_partials_kernel<<<dim3(b.bands, nj), kMetricThreads, sizeof(MetricShared), s->stream>>>(b);
+    check_cuda(cudaGetLastError(), "metric_partials launch");
+    note_launch();
+    metric_reduce_kernel<<<(ncand + 127) / 128, 128, 0, s->stream>>>(m.partial, ncand, b.bands, m.sums);
+    check_cuda(cudaGetLastError(), "metric_reduce launch");
+  };
+  const std::string shape = std::to_string(nj) + " jobs x " + std::to_string(ncand / std::max(nj, 1)) +
+                            " candidates x " + std::to_string(samples) + " samples";
+  run(autotune_choose("metric_partials bands", shape, {"2/SM", "4/SM", "8/SM"}, 1, s->stream, run));
   check_cuda(cudaMemcpyAsync(sums.data(), m.sums, sizeof(double) * 8 * ncand, cudaMemcpyDeviceToHost, s->stream),
              "cudaMemcpyAsync(metric sums)");
   check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(metrics)");

@@ -242,6 +242,21 @@ int gg_stack_graph_capture_step(gg_stack* stack, const void* dev_raw, const doub
                                 float clamping_threshold, int weighting, const gg_calib_params_t* calib,
                                 const gg_integrate_params_t* params);
 int gg_stack_graph_launch(gg_stack* stack);
+
+/* Launch-shape autotuner (no reference counterpart).  Kernels with
+ * equivalent launch shapes (the fused warp-integration's pixel tile, the
+ * alignment-metric kernel's CTA bands) time their candidates with CUDA
+ * events on the first eager call for a problem shape and keep the fastest;
+ * calls during stream capture use the kept or default choice.  On by
+ * default (GG_AUTOTUNE=0 in the environment starts it off). */
+int gg_autotune_set_enabled(int enabled);
+int gg_autotune_clear(void);
+int gg_autotune_count(int32_t* out);
+/* Entry `index`: kernel family, shape key and chosen candidate (NUL-
+ * terminated, truncated to the buffer lengths), its time per launch in ms
+ * and the number of candidates. */
+int gg_autotune_entry(int32_t index, char* kernel, size_t kernel_len, char* shape, size_t shape_len, char* choice,
+                      size_t choice_len, float* best_ms, int32_t* candidates);
 int gg_stack_graph_kernel_count(gg_stack* stack, int* out);
 int gg_stack_graph_destroy(gg_stack* stack);
 /* Downloads the maps of the last integration; any pointer may be NULL.  Count
