@@ -959,6 +959,114 @@ class ResidentCalibratedStack:
             for s in out
         ]
 
+    # ---- local normalisation (native_bindings.cpp:10645-11200) ---------------------
+    def _grid_dims(self, tile_height: int, tile_width: int) -> tuple[int, int]:
+        if int(tile_height) <= 0 or int(tile_width) <= 0:
+            raise ValueError("tile dimensions must be positive")
+        info = self._info()
+        return (-(-int(info.height) // int(tile_height)), -(-int(info.width) // int(tile_width)))
+
+    def frame_pair_grid_stats_batch(self, reference_index: int, source_indices: Any, tile_height: int,
+                                    tile_width: int) -> dict[str, Any]:
+        """Per-tile float32 mean / std of each source frame and of the
+        reference over the pixels finite in both, and the pixel counts."""
+        idx = np.ascontiguousarray(np.asarray(source_indices, dtype=np.int64).reshape(-1))
+        rows, cols = self._grid_dims(tile_height, tile_width)
+        start = perf_counter()
+        shape = (idx.size, rows, cols)
+        sm, ss, rm, rs = (np.zeros(shape, np.float32) for _ in range(4))
+        valid = np.zeros(shape, np.uint64)
+        if idx.size:
+            _lib.call("gg_stack_pair_grid_stats", self._handle, ctypes.c_int64(int(reference_index)), _lib.ptr(idx),
+                      ctypes.c_int64(idx.size), int(tile_height), int(tile_width), _lib.ptr(sm), _lib.ptr(ss),
+                      _lib.ptr(rm), _lib.ptr(rs), _lib.ptr(valid))
+        frames = []
+        for k in range(idx.size):
+            frames.append({"source_mean": sm[k], "source_std": ss[k], "reference_mean": rm[k], "reference_std": rs[k],
+                           "valid_pixels": valid[k], "grid_rows": rows, "grid_cols": cols,
+                           "tile_height": int(tile_height), "tile_width": int(tile_width),
+                           "valid_pixel_total": int(valid[k].sum(dtype=np.uint64)),
+                           "model": "resident_grid_pair_mean_std", "source_index": int(idx[k]),
+                           "reference_index": int(reference_index), "batch_position": k})
+        return {"schema_version": 1, "model": "resident_grid_pair_mean_std_batch",
+                "batch_model": "gb300_tile_pair_float_float_sums", "reference_index": int(reference_index),
+                "source_count": int(idx.size), "grid_rows": rows, "grid_cols": cols, "grid_count": rows * cols,
+                "tile_height": int(tile_height), "tile_width": int(tile_width),
+                "source_indices": idx.astype(np.int32), "total_s": perf_counter() - start, "frames": frames}
+
+    def frame_pair_grid_stats(self, reference_index: int, source_index: int, tile_height: int,
+                              tile_width: int) -> dict[str, Any]:
+        frame = self.frame_pair_grid_stats_batch(reference_index, [source_index], tile_height, tile_width)["frames"][0]
+        for key in ("source_index", "reference_index", "batch_position"):
+            frame.pop(key)
+        return frame
+
+    def apply_grid_normalization_frames(self, frame_indices: Any, scales: Any, offsets: Any, tile_height: int,
+                                        tile_width: int) -> dict[str, Any]:
+        """In place v * scale + offset per tile for each frame (coefficients
+        of shape (frame_count, grid_rows, grid_cols))."""
+        idx = np.ascontiguousarray(np.asarray(frame_indices, dtype=np.int64).reshape(-1))
+        sc = np.ascontiguousarray(np.asarray(scales, dtype=np.float32))
+        of = np.ascontiguousarray(np.asarray(offsets, dtype=np.float32))
+        if sc.ndim != 3 or of.ndim != 3:
+            raise ValueError("scales and offsets must have shape (frame_count, grid_rows, grid_cols)")
+        if sc.shape[0] != idx.size or of.shape[0] != idx.size:
+            raise ValueError("coefficient frame count must match frame_indices length")
+        if sc.shape != of.shape:
+            raise ValueError("scales and offsets grid shapes must match")
+        if int(tile_height) <= 0 or int(tile_width) <= 0:
+            raise ValueError("tile dimensions must be positive")
+        start = perf_counter()
+        if idx.size:
+            _lib.call("gg_stack_apply_grid_normalization", self._handle, _lib.ptr(idx), ctypes.c_int64(idx.size),
+                      _lib.ptr(sc), _lib.ptr(of), int(sc.shape[1]), int(sc.shape[2]), int(tile_height),
+                      int(tile_width))
+        return {"schema_version": 1, "mode": "in_place_device_update_batch",
+                "model": "resident_grid_mean_std_batch_apply", "frame_count": int(idx.size),
+                "grid_rows": int(sc.shape[1]), "grid_cols": int(sc.shape[2]),
+                "grid_count": int(sc.shape[1] * sc.shape[2]), "coefficient_count": int(sc.size),
+                "coefficient_bytes": int(sc.nbytes + of.nbytes), "total_s": perf_counter() - start}
+
+    def apply_grid_normalization_frame(self, index: int, scales: Any, offsets: Any, tile_height: int,
+                                       tile_width: int) -> dict[str, Any]:
+        sc = np.asarray(scales, dtype=np.float32)
+        of = np.asarray(offsets, dtype=np.float32)
+        if sc.ndim != 2 or of.ndim != 2:
+            raise ValueError("scales and offsets must have shape (grid_rows, grid_cols)")
+        if sc.shape != of.shape:
+            raise ValueError("scales and offsets shapes must match")
+        out = self.apply_grid_normalization_frames([index], sc[None], of[None], tile_height, tile_width)
+        out.update(mode="in_place_device_update", model="resident_grid_mean_std", frame_index=int(index))
+        return out
+
+    def apply_global_normalization_frame(self, index: int, scale: float, offset: float) -> dict[str, Any]:
+        start = perf_counter()
+        _lib.call("gg_stack_apply_global_normalization", self._handle, ctypes.c_int64(int(index)),
+                  ctypes.c_float(scale), ctypes.c_float(offset))
+        return {"schema_version": 1, "mode": "in_place_device_update", "model": "resident_global_mean_std",
+                "frame_index": int(index), "total_s": perf_counter() - start}
+
+    def device_frame_weights(self) -> np.ndarray:
+        """The frame weights currently on the device (synchronises)."""
+        out = np.empty(self.frame_count, np.float32)
+        _lib.call("gg_stack_download_weights", self._handle, _lib.ptr(out))
+        return out
+
+    def local_normalize_grid(self, reference_index: int, source_indices: Any, tile: int = 256, eps: float = 1.0e-6,
+                             update_weights: bool = True, download: bool = False):
+        """Statistics, coefficients and the in-place apply on the device (no
+        host round trip unless download=True, which returns (scales, offsets))."""
+        idx = np.ascontiguousarray(np.asarray(source_indices, dtype=np.int64).reshape(-1))
+        if idx.size == 0:
+            return None
+        rows, cols = self._grid_dims(tile, tile)
+        sc = np.empty((idx.size, rows, cols), np.float32) if download else None
+        of = np.empty((idx.size, rows, cols), np.float32) if download else None
+        _lib.call("gg_stack_local_normalize_grid", self._handle, ctypes.c_int64(int(reference_index)), _lib.ptr(idx),
+                  ctypes.c_int64(idx.size), int(tile), int(tile), ctypes.c_double(eps), int(bool(update_weights)),
+                  _lib.ptr(sc), _lib.ptr(of))
+        return (sc, of) if download else None
+
     # ---- integration -------------------------------------------------------------
     def _weights(self, weights: Any | None) -> np.ndarray | None:
         if weights is None:

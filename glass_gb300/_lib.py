@@ -306,6 +306,13 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_integrate_warped_device_weights": [_P, _P, ctypes.c_int, ctypes.c_float,
                                                  ctypes.POINTER(IntegrateParams)],
     "gg_stack_graph_launch": [_P],
+    "gg_stack_pair_grid_stats": [_P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _P, _P, _P,
+                                 _P, _P],
+    "gg_stack_apply_grid_normalization": [_P, _P, ctypes.c_int64, _P, _P, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.c_int32, ctypes.c_int32],
+    "gg_stack_local_normalize_grid": [_P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_double, ctypes.c_int, _P, _P],
+    "gg_stack_apply_global_normalization": [_P, ctypes.c_int64, ctypes.c_float, ctypes.c_float],
     "gg_autotune_set_enabled": [ctypes.c_int],
     "gg_autotune_clear": [],
     "gg_autotune_count": [ctypes.POINTER(ctypes.c_int32)],
@@ -316,6 +323,7 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_graph_destroy": [_P],
     "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
     "gg_stack_frame_device_ptr": [_P, ctypes.c_int64, _P],
+    "gg_stack_download_weights": [_P, _P],
     "gg_dq_map_i16": [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P],
     "gg_stack_detect_stars": [_P, _P, ctypes.c_int64, ctypes.POINTER(StarParams), _P, _P, _P],
     "gg_triangle_descriptors": [_P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P,

@@ -146,6 +146,7 @@ static void stack_free(gg_stack* s) {
   if (s->metric_scratch && s->metric_scratch_free) s->metric_scratch_free(s->metric_scratch);
   if (s->gn_scratch && s->gn_scratch_free) s->gn_scratch_free(s->gn_scratch);
   if (s->step_graph && s->step_graph_free) s->step_graph_free(s->step_graph);
+  if (s->ln_scratch && s->ln_scratch_free) s->ln_scratch_free(s->ln_scratch);
   void* dev_ptrs[] = {s->d_slots,    s->d_slot_of_frame, s->d_spare_slot, s->d_frame_nonfinite,
                       s->d_bias,     s->d_dark,          s->d_flat,       s->d_master,
                       s->d_weight,   s->d_coverage,      s->d_low,        s->d_high,
@@ -471,6 +472,18 @@ int gg_stack_device_ptrs(gg_stack* s, gg_stack_device_ptrs_t* out) {
   out->high = s->d_high;
   out->dq = s->d_dq;
   out->warp_coverage = s->d_warp_coverage;
+  GG_API_END
+}
+
+int gg_stack_download_weights(gg_stack* s, float* host_out) {
+  GG_API_BEGIN
+  require(s != nullptr && host_out != nullptr, "null argument");
+  stack_activate(s);
+  check_cuda(cudaMemcpyAsync(s->h_weights_pinned, s->d_weights, sizeof(float) * s->frames, cudaMemcpyDeviceToHost,
+                             s->stream),
+             "cudaMemcpyAsync(weights)");
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(weights)");
+  std::copy(s->h_weights_pinned, s->h_weights_pinned + s->frames, host_out);
   GG_API_END
 }
 

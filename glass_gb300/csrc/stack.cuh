@@ -104,6 +104,8 @@ struct gg_stack {
   void (*gn_scratch_free)(void*) = nullptr;
   void* step_graph = nullptr;  // captured resident step (integrate.cu)
   void (*step_graph_free)(void*) = nullptr;
+  void* ln_scratch = nullptr;  // local normalisation (localnorm.cu)
+  void (*ln_scratch_free)(void*) = nullptr;
 
   // Fused warp-integration: per-frame inverse matrices, per-frame
   // non-finite sample counts of the virtual warped stack and the geometric

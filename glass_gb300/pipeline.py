@@ -90,6 +90,9 @@ class StepConfig:
     # 0: the reference's global median / MAD threshold; 8..64: background
     # mesh of that cell size (local threshold, local background per star)
     background_mesh_cell: int = 0
+    # grid local normalisation between warp and integration (the resident
+    # grid_mean_std mode; 256 is the reference CLI's tile), 0 = off
+    local_normalization_tile: int = 0
     registration_tolerance_px: float = 3.0
     registration_min_inliers: int = 6
     # sub-pixel translation refinement of the triangle matrices (a coarse
@@ -252,6 +255,17 @@ class ResidentPipeline:
         prior = None if ok is None else ok.astype(np.float32)
         self.stack.compute_frame_weights(self.config.weighting, prior, 1.0e-6, download=False)
 
+    def local_normalize(self, reference_index: int = 0) -> None:
+        """Grid local normalisation (config.local_normalization_tile) of every
+        registered frame to the reference frame, after the warp and the
+        weights (a frame without paired finite pixels gets weight 0)."""
+        tile = int(self.config.local_normalization_tile)
+        if tile <= 0:
+            return
+        ok = getattr(self, "_registered", None)
+        idx = [k for k in range(self.frames) if k != reference_index and (ok is None or ok[k])]
+        self.stack.local_normalize_grid(reference_index, idx, tile, 1.0e-6, update_weights=True)
+
     def integrate(self) -> None:
         cfg = self.config
         self.stack.integrate_async("device", cfg.rejection, cfg.low_sigma, cfg.high_sigma, cfg.min_samples,
@@ -284,6 +298,7 @@ class ResidentPipeline:
         if matrices is not None:
             self.warp(matrices)
         self.weights()
+        self.local_normalize()
         self.integrate()
 
     def step_host(self, host_raw: np.ndarray, matrices: np.ndarray | None = None, register: bool = False,
@@ -299,6 +314,7 @@ class ResidentPipeline:
         if matrices is not None:
             self.warp(matrices)
         self.weights()
+        self.local_normalize()
         self.integrate()
         return self.stack.download_maps("full", include_dq=True, out=out)
 

@@ -243,6 +243,35 @@ int gg_stack_graph_capture_step(gg_stack* stack, const void* dev_raw, const doub
                                 const gg_integrate_params_t* params);
 int gg_stack_graph_launch(gg_stack* stack);
 
+/* ---- local normalisation (resident grid_mean_std / global_mean_std) -------
+ * Replaces frame_pair_grid_stats[_batch], apply_grid_normalization_frame[s]
+ * and apply_global_normalization_frame (native_bindings.cpp:10645-11200;
+ * resident_cuda.py:12902-13060).  Tiles of tile_h x tile_w pixels from the
+ * top-left corner, rows = ceil(H / tile_h), cols = ceil(W / tile_w).
+ * gg_stack_pair_grid_stats: per source frame and tile, over the pixels finite
+ * in both frames, float32 mean / std of source and reference (float64 sums,
+ * std = sqrt(max(sum2/n - mean^2, 0))) and the pixel count; outputs are
+ * count x rows x cols (any may be NULL). */
+int gg_stack_pair_grid_stats(gg_stack* stack, int64_t reference_index, const int64_t* sources, int64_t count,
+                             int32_t tile_h, int32_t tile_w, float* host_source_mean, float* host_source_std,
+                             float* host_reference_mean, float* host_reference_std, uint64_t* host_valid);
+/* In place v * scale + offset (float32 multiply then add) with the tile's
+ * coefficients, count x grid_rows x grid_cols; pixels past the grid use its
+ * last row / column. */
+int gg_stack_apply_grid_normalization(gg_stack* stack, const int64_t* indices, int64_t count,
+                                      const float* host_scales, const float* host_offsets, int32_t grid_rows,
+                                      int32_t grid_cols, int32_t tile_h, int32_t tile_w);
+/* The resident sequence on the device: statistics, coefficients (empty tile
+ * 1 / 0; std <= eps: 1 / ref_mean - src_mean; else ref_std / src_std,
+ * ref_mean - src_mean * scale in float32) and the in-place apply for every
+ * source frame (not the reference); update_weights = 1 zeroes the device
+ * frame weight of a source without any paired finite pixel.  Asynchronous
+ * unless host_scales / host_offsets (count x rows x cols) are requested. */
+int gg_stack_local_normalize_grid(gg_stack* stack, int64_t reference_index, const int64_t* sources, int64_t count,
+                                  int32_t tile_h, int32_t tile_w, double eps, int update_weights, float* host_scales,
+                                  float* host_offsets);
+int gg_stack_apply_global_normalization(gg_stack* stack, int64_t index, float scale, float offset);
+
 /* Launch-shape autotuner (no reference counterpart).  Kernels with
  * equivalent launch shapes (the fused warp-integration's pixel tile, the
  * alignment-metric kernel's CTA bands) time their candidates with CUDA
@@ -282,6 +311,9 @@ int gg_stack_device_ptrs(gg_stack* stack, gg_stack_device_ptrs_t* out);
  * frame moves it to another slot.  No reference counterpart (views of
  * resident frames for the differentiable warp). */
 int gg_stack_frame_device_ptr(gg_stack* stack, int64_t index, float** out);
+/* The device frame weights (last gg_stack_compute_weights, as updated by
+ * gg_stack_local_normalize_grid), frame_count float32; synchronises. */
+int gg_stack_download_weights(gg_stack* stack, float* host_out);
 
 /* ---- star detection ------------------------------------------------------ */
 /* Parameters of detect_stars (cpu/star_detect.py:121-132).  background /

@@ -600,6 +600,52 @@ def make_alignment(ref_src: Path) -> None:
     np.savez_compressed(HERE / "alignment.npz", **arrays)
 
 
+# ---------------------------------------------------------------------------
+# local normalisation
+# ---------------------------------------------------------------------------
+def make_local_norm(ref_src: Path) -> None:
+    """_grid_local_norm_coefficients (src/glass/engine/resident_cuda.py:1897)
+    on seeded tile statistics with empty and offset-only tiles, and
+    apply_grid_normalization (src/glass/cpu/local_norm.py:197) on seeded
+    frames whose size is not a multiple of the tile."""
+    ns: dict = {"np": np, "Any": object}
+    _load_functions(ref_src / "glass" / "engine" / "resident_cuda.py", ["_grid_local_norm_coefficients"], ns)
+    _load_functions(ref_src / "glass" / "cpu" / "local_norm.py", ["apply_grid_normalization"], ns)
+    rng = np.random.default_rng(31)
+    arrays: dict = {}
+    rows, cols = 5, 7
+    stats = {
+        "source_mean": rng.uniform(500, 1500, (rows, cols)).astype(np.float32),
+        "source_std": rng.uniform(5, 60, (rows, cols)).astype(np.float32),
+        "reference_mean": rng.uniform(500, 1500, (rows, cols)).astype(np.float32),
+        "reference_std": rng.uniform(5, 60, (rows, cols)).astype(np.float32),
+        "valid_pixels": rng.integers(1, 65536, (rows, cols)).astype(np.uint64),
+    }
+    stats["valid_pixels"][0, 0] = 0
+    stats["valid_pixels"][3, 6] = 0
+    stats["source_std"][1, 2] = np.float32(5e-7)
+    stats["reference_std"][2, 4] = np.float32(1e-6)
+    stats["source_std"][4, 1] = np.float32(0.0)
+    coeffs = ns["_grid_local_norm_coefficients"](stats, eps=1.0e-6)
+    for k, v in stats.items():
+        arrays[f"coeff/{k}"] = v
+    arrays["coeff/scales"] = coeffs["scales"]
+    arrays["coeff/offsets"] = coeffs["offsets"]
+    for name, (h, w, th, tw) in {"odd": (150, 210, 64, 96), "exact": (128, 192, 64, 64)}.items():
+        data = rng.normal(1000.0, 40.0, (h, w)).astype(np.float32)
+        data[rng.integers(0, h, 20), rng.integers(0, w, 20)] = np.nan
+        gr, gc = -(-h // th), -(-w // tw)
+        scales = rng.uniform(0.8, 1.25, (gr, gc)).astype(np.float32)
+        offsets = rng.uniform(-200, 200, (gr, gc)).astype(np.float32)
+        arrays[f"apply/{name}/data"] = data
+        arrays[f"apply/{name}/scales"] = scales
+        arrays[f"apply/{name}/offsets"] = offsets
+        arrays[f"apply/{name}/tile"] = np.array([th, tw], dtype=np.int64)
+        arrays[f"apply/{name}/out"] = ns["apply_grid_normalization"](data, scales, offsets, th, tw)
+    arrays["_apply_names"] = np.array(["odd", "exact"])
+    np.savez_compressed(HERE / "local_norm.npz", **arrays)
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__)
     parser.add_argument("--reference", default="/root/reference", help="GLASS reference checkout")
@@ -608,7 +654,8 @@ def main() -> int:
     ref = Path(args.reference)
     src = ref / "src"
     jobs = {"integration": make_integration, "calibration": make_calibration, "warp": make_warp,
-            "stars": make_stars, "registration": make_registration, "alignment": make_alignment}
+            "stars": make_stars, "registration": make_registration, "alignment": make_alignment,
+            "local_norm": make_local_norm}
     only = [j for j in args.only.split(",") if j] or list(jobs)
     for job in only:
         jobs[job](src)
