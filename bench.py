@@ -325,6 +325,57 @@ def local_norm_report(pipe, stream, reps: int, peak: float) -> dict:
             "achieved_gbs": achieved, "frac_of_measured_hbm": achieved / peak}
 
 
+def batch_report(reps: int) -> dict:
+    """Four uneven stacks (25/20/16/12 frames at 1024x1024, 1536x1024,
+    1024x768, 2048x512; the 25 x 1024^2 one is the c4 C shape) winsorized-
+    integrated one after another vs in one batched launch, CUDA events on one
+    stream, seeded noise frames resident on the device."""
+    import torch
+
+    from glass_gb300 import _glass_cuda_native as native
+    from glass_gb300 import _lib
+
+    shapes = [(25, 1024, 1024), (20, 1536, 1024), (16, 1024, 768), (12, 2048, 512)]
+    stream = torch.cuda.Stream()
+    stacks = []
+    try:
+        rng = np.random.default_rng(3)
+        for n, h, w in shapes:
+            s = native.ResidentCalibratedStack(n, h, w)
+            s.set_stream(stream.cuda_stream)
+            frames = rng.normal(1000.0, 20.0, (n, h, w)).astype(np.float32)
+            for k in range(n):
+                s.upload_calibrated_frame(k, frames[k])
+            s.compute_frame_weights("simple_snr", None, 1.0e-6, download=False)
+            stacks.append(s)
+
+        def sequential():
+            for s in stacks:
+                s.integrate_async("device", _lib.GG_REJECT_WINSORIZED, 3.0, 3.0, 3, 0.5, "uint16")
+
+        def batched():
+            native.integrate_stacks_batch(stacks, _lib.GG_REJECT_WINSORIZED, 3.0, 3.0, 3, 0.5, "uint16")
+
+        def timed(fn):
+            for _ in range(2):
+                fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            stream.synchronize()
+            return e0.elapsed_time(e1) / reps
+
+        seq_ms, batch_ms = timed(sequential), timed(batched)
+        mpix = sum(n * h * w for n, h, w in shapes) / 1e6
+        return {"stacks": [list(s) for s in shapes], "sequential_ms": seq_ms, "batched_ms": batch_ms,
+                "mpix_frames_per_s_batched": mpix / (batch_ms / 1e3)}
+    finally:
+        for s in stacks:
+            s.close()
+
+
 def graph_report(pipe, dev_raw, matrices, stream, reps: int) -> dict:
     """calibrate -> weights -> fused warp + winsorized integration with fixed
     matrices: the eager launch sequence against its CUDA-graph replay, same
@@ -503,6 +554,7 @@ def main():
         registration.update(adjoint_report(pipe, dev_raw, reg, truth, h, w, stream))
     graph = graph_report(pipe, dev_raw, reg["matrices"], stream, max(3, args.steps))
     local_norm = local_norm_report(pipe, stream, max(3, args.steps), measured_peak()[0])
+    batch = batch_report(max(3, args.steps))
     pinned =torch.from_numpy(data.lights.view(np.int16)).pin_memory().numpy().view(np.uint16)
     # reused pinned destinations for the six maps (master, weight f32; coverage,
     # low, high uint16; dq int16)
@@ -582,6 +634,7 @@ def main():
         "registration": registration,
         "graph_step": graph,
         "local_normalization": local_norm,
+        "batched_stacks": batch,
         "autotune": _lib.autotune_entries(),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mpix-frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -87,6 +87,25 @@ class _PinnedBuffer:
         weakref.finalize(self, _lib.load().gg_host_free_pinned, ctypes.c_void_p(self.address))
 
 
+def integrate_stacks_batch(stacks: list, rejection: int = _lib.GG_REJECT_WINSORIZED, low_sigma: float = 3.0,
+                           high_sigma: float = 3.0, min_samples: int = 3, max_reject_fraction: float = 0.5,
+                           count_map_dtype: str = "uint16") -> None:
+    """Integrates several resident stacks (each at most 32 frames, uneven
+    frame counts and shapes allowed) in one kernel launch, each with its own
+    device weights; read each stack's maps with its download_maps()."""
+    if count_map_dtype not in {"float32", "uint16"}:
+        raise ValueError("count_map_dtype must be float32 or uint16")
+    if not stacks:
+        return
+    params = _lib.IntegrateParams(int(rejection), float(low_sigma), float(high_sigma), int(min_samples),
+                                  float(max_reject_fraction),
+                                  _lib.GG_COUNT_U16 if count_map_dtype == "uint16" else _lib.GG_COUNT_F32, 5)
+    handles = (ctypes.c_void_p * len(stacks))(*[s.handle.value for s in stacks])
+    _lib.call("gg_stacks_integrate_batch", handles, len(stacks), ctypes.byref(params))
+    for s in stacks:
+        s._last_count_dtype = np.dtype(np.uint16 if count_map_dtype == "uint16" else np.float32)
+
+
 class _DeviceView:
     """A resident frame exposed through __cuda_array_interface__ (keeps its stack alive)."""
 
@@ -1198,6 +1217,44 @@ class ResidentCalibratedStack:
         out = np.empty((self.height, self.width), np.float32)
         _lib.call("gg_stack_download_fused_coverage", self._handle, _lib.ptr(out))
         return out
+
+    def _tile_local(self, mode: int, target_mask, tile_extents, tile_multipliers, weights, low_sigma, high_sigma):
+        tm = np.ascontiguousarray(np.asarray(target_mask).astype(np.uint8).reshape(-1))
+        if tm.shape != (self.frame_count,):
+            raise ValueError("target_mask must have shape (frame_count,)")
+        ext = np.ascontiguousarray(np.asarray(tile_extents, dtype=np.int32))
+        if ext.ndim != 2 or ext.shape[1] != 4:
+            raise ValueError("tile_extents must have shape (tile_count, 4)")
+        mult = np.ascontiguousarray(np.asarray(tile_multipliers, dtype=np.float32).reshape(-1))
+        if mult.shape != (ext.shape[0],):
+            raise ValueError("tile_multipliers must have shape (tile_count,)")
+        w = self._weights(weights)
+        start = perf_counter()
+        _lib.call("gg_stack_integrate_tile_local", self._handle, int(mode), _lib.ptr(w), _lib.ptr(tm), _lib.ptr(ext),
+                  _lib.ptr(mult), int(ext.shape[0]), ctypes.c_float(low_sigma), ctypes.c_float(high_sigma))
+        self._last_count_dtype = np.dtype(np.float32)
+        maps = self.download_maps("full" if mode else "master_weight", include_dq=False)
+        timing = {"schema_version": 1, "tile_count": int(ext.shape[0]), "target_frame_count": int(tm.sum()),
+                  "total_s": perf_counter() - start, "timing_model": "gb300_tile_local_column_in_shared_memory"}
+        return maps, timing
+
+    def integrate_tile_local_mean(self, target_mask: Any, tile_extents: Any, tile_multipliers: Any,
+                                  weights: Any | None = None):
+        """Weighted mean with per-tile multipliers on the target frames'
+        weights -> (master, weight_map, timing)."""
+        maps, timing = self._tile_local(0, target_mask, tile_extents, tile_multipliers, weights, 3.0, 3.0)
+        return maps[0], maps[1], timing
+
+    def integrate_tile_local_sigma_clip(self, target_mask: Any, tile_extents: Any, tile_multipliers: Any,
+                                        weights: Any | None = None, low_sigma: float = 3.0, high_sigma: float = 3.0,
+                                        winsorize: bool = True):
+        """Sigma clip (winsorized when winsorize) with per-tile multipliers ->
+        (master, weight, coverage, low, high, timing), float32 maps."""
+        if low_sigma <= 0.0 or high_sigma <= 0.0:
+            raise ValueError("sigma thresholds must be positive")
+        maps, timing = self._tile_local(2 if winsorize else 1, target_mask, tile_extents, tile_multipliers, weights,
+                                        low_sigma, high_sigma)
+        return maps[0], maps[1], maps[2], maps[3], maps[4], timing
 
     def integrate_warped_device_weights(self, matrices: Any, interpolation: str = "lanczos3",
                                         clamping_threshold: float = -1.0,

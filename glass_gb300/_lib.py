@@ -303,6 +303,9 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_download_fused_coverage": [_P, _P],
     "gg_stack_graph_capture_step": [_P, _P, _P, ctypes.c_int, ctypes.c_float, ctypes.c_int,
                                     ctypes.POINTER(CalibParams), ctypes.POINTER(IntegrateParams)],
+    "gg_stacks_integrate_batch": [_P, ctypes.c_int32, ctypes.POINTER(IntegrateParams)],
+    "gg_stack_integrate_tile_local": [_P, ctypes.c_int, _P, _P, _P, _P, ctypes.c_int32, ctypes.c_float,
+                                      ctypes.c_float],
     "gg_stack_integrate_warped_device_weights": [_P, _P, ctypes.c_int, ctypes.c_float,
                                                  ctypes.POINTER(IntegrateParams)],
     "gg_stack_graph_launch": [_P],

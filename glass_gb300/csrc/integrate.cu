@@ -633,8 +633,9 @@ __device__ __forceinline__ CenterScale winsorized_sorted(const float* S, int T, 
 
 // WARP = 0 reads the stack; GG_INTERP_BILINEAR / GG_INTERP_LANCZOS3 sample
 // every frame through its inverse matrix (fused warp + integration).
-template <int NB, int T, int MODE, int WARP = 0>
-__global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
+// One CTA's share (block `bid` of `nblocks`) of one stack's pixels.
+template <int NB, int T, int MODE, int WARP>
+__device__ __forceinline__ void integrate_col_run(const IntegrateArgs& a, int bid, int nblocks) {
   extern __shared__ float smem[];
   float* S = smem;  // [NB][T] ascending valid samples
   __shared__ FrameTable<NB> tab;
@@ -663,7 +664,7 @@ __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
   // otherwise a CTA covers T consecutive pixels.
   const bool tiled = WARP != 0 && a.tile_w > 0;
   const int64_t Q = tiled ? a.tile_slots : P;
-  for (int64_t q = static_cast<int64_t>(blockIdx.x) * T + tid; q < Q; q += static_cast<int64_t>(gridDim.x) * T) {
+  for (int64_t q = static_cast<int64_t>(bid) * T + tid; q < Q; q += static_cast<int64_t>(nblocks) * T) {
     int64_t p = q;
     if (tiled) {
       const int64_t t = q / T;
@@ -794,6 +795,31 @@ __global__ void __launch_bounds__(T) integrate_col_kernel(IntegrateArgs a) {
     }
     write_outputs(a, p, master, weight, kept, nl, nh, tab.active);
   }
+}
+
+// MINB > 1 asks the compiler for MINB resident CTAs per SM (a register cap:
+// more warps to hide the sort network's dependent latencies, against a few
+// spilled registers); the autotuner picks per problem shape.
+template <int NB, int T, int MODE, int WARP = 0, int MINB = 1>
+__global__ void __launch_bounds__(T, MINB) integrate_col_kernel(IntegrateArgs a) {
+  integrate_col_run<NB, T, MODE, WARP>(a, blockIdx.x, gridDim.x);
+}
+
+// Several stacks (of different frame counts and shapes, each with its own
+// maps and weights) in one launch: CTAs [start[k], start[k+1]) work on stack
+// k, so a CTA loads one frame table and never mixes stacks.
+constexpr int kMaxBatchStacks = 64;
+struct BatchTable {
+  int start[kMaxBatchStacks + 1];
+  int stacks;
+};
+
+template <int NB, int T, int MODE, int MINB = 1>
+__global__ void __launch_bounds__(T, MINB) integrate_batch_kernel(const IntegrateArgs* args, BatchTable bt) {
+  int k = 0;
+  while (k + 1 < bt.stacks && static_cast<int>(blockIdx.x) >= bt.start[k + 1]) ++k;
+  const IntegrateArgs a = args[k];
+  integrate_col_run<NB, T, MODE, 0>(a, static_cast<int>(blockIdx.x) - bt.start[k], bt.start[k + 1] - bt.start[k]);
 }
 
 // ---- kernel A: N <= NB <= 64, column in registers ----------------------------
@@ -931,15 +957,27 @@ template <int NB, int MODE>
 static void launch_col(const IntegrateArgs& args, cudaStream_t stream) {
   constexpr int T = 128;
   const size_t smem = size_t(NB) * T * sizeof(float);
-  auto kern = integrate_col_kernel<NB, T, MODE>;
-  check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
-             "cudaFuncSetAttribute(integrate)");
-  int per_sm = 0;
-  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem), "occupancy");
-  const unsigned grid = grid_for(static_cast<size_t>(args.pixels), T, std::max(per_sm, 1));
-  note_launch();
-  kern<<<grid, T, smem, stream>>>(args);
-  check_cuda(cudaGetLastError(), "integrate kernel launch");
+  auto run_kernel = [&](auto kern) {
+    check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+               "cudaFuncSetAttribute(integrate)");
+    int per_sm = 0;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem), "occupancy");
+    const unsigned grid = grid_for(static_cast<size_t>(args.pixels), T, std::max(per_sm, 1));
+    note_launch();
+    kern<<<grid, T, smem, stream>>>(args);
+    check_cuda(cudaGetLastError(), "integrate kernel launch");
+  };
+  if constexpr (NB == 32 && MODE != GG_REJECT_NONE) {
+    auto run = [&](int c) {
+      if (c == 0) run_kernel(integrate_col_kernel<NB, T, MODE, 0, 1>);
+      else run_kernel(integrate_col_kernel<NB, T, MODE, 0, 4>);
+    };
+    const std::string shape = std::to_string(args.frames) + " frames x " + std::to_string(args.pixels) +
+                              " px mode" + std::to_string(MODE);
+    run(autotune_choose("integrate_col registers", shape, {"unbounded", "4 CTAs/SM"}, 0, stream, run));
+  } else {
+    run_kernel(integrate_col_kernel<NB, T, MODE>);
+  }
 }
 
 // Non-finite warped samples per frame for the fused path: the count the warp
@@ -1023,30 +1061,10 @@ static void validate_integrate(const gg_integrate_params_t& p) {
   }
 }
 
+static IntegrateArgs integrate_args(gg_stack* s, const float* d_weights, const gg_integrate_params_t& p);
+
 void launch_integrate(gg_stack* s, const float* d_weights, const gg_integrate_params_t& p) {
-  stack_ensure_maps(s);
-  IntegrateArgs a{};
-  a.slots = s->d_slots;
-  a.slot_of_frame = s->d_slot_of_frame;
-  a.stride = s->stride;
-  a.pixels = s->pixels;
-  a.frames = static_cast<int>(s->frames);
-  a.weights = d_weights;
-  a.nonfinite = s->d_frame_nonfinite;
-  a.rejection = p.rejection;
-  a.low_sigma = p.low_sigma;
-  a.high_sigma = p.high_sigma;
-  a.min_samples = p.min_samples;
-  a.max_frac = p.max_reject_fraction;
-  a.lfc_iterations = p.linear_fit_iterations > 0 ? p.linear_fit_iterations : 5;
-  a.master = s->d_master;
-  a.weight = s->d_weight;
-  a.coverage = s->d_coverage;
-  a.low = s->d_low;
-  a.high = s->d_high;
-  a.dq = s->d_dq;
-  a.count_u16 = p.count_dtype == GG_COUNT_U16;
-  a.geometric = (s->d_warp_coverage && s->warp_coverage_frames > 0) ? s->d_warp_coverage : nullptr;
+  const IntegrateArgs a = integrate_args(s, d_weights, p);
   const int n = a.frames;
   if (n <= 32) {
     switch (p.rejection) {
@@ -1077,6 +1095,131 @@ void launch_integrate(gg_stack* s, const float* d_weights, const gg_integrate_pa
   else if (n <= 512) launch_smem<16>(a, s->stream);
   else fail(GG_ERR_INVALID_ARGUMENT, "frame_count above 512 is not supported by the resident integrator");
   s->last_count_dtype = p.count_dtype;
+}
+
+// Several stacks of at most 32 frames in one launch of the column kernel
+// (NB = the largest frame count's bucket); CTAs are shared out in proportion
+// to each stack's samples (pixels x frames), at least one per stack.
+template <int MODE>
+static void launch_batch(std::vector<gg_stack*>& stacks, const std::vector<IntegrateArgs>& args, int nb,
+                         IntegrateArgs* d_args) {
+  constexpr int T = 128;
+  cudaStream_t stream = stacks[0]->stream;
+  BatchTable bt{};
+  bt.stacks = static_cast<int>(stacks.size());
+  auto launch = [&](auto kern, int NBv) {
+    const size_t smem = size_t(NBv) * T * sizeof(float);
+    check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+               "cudaFuncSetAttribute(integrate batch)");
+    int per_sm = 0;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem), "occupancy");
+    const double budget = static_cast<double>(sm_count()) * std::max(per_sm, 1);
+    double work = 0.0;
+    for (const IntegrateArgs& a : args) work += static_cast<double>(a.pixels) * a.frames;
+    bt.start[0] = 0;
+    for (size_t k = 0; k < args.size(); ++k) {
+      const int64_t most = (args[k].pixels + T - 1) / T;
+      const int64_t share = static_cast<int64_t>(budget * static_cast<double>(args[k].pixels) * args[k].frames / work);
+      bt.start[k + 1] = bt.start[k] + static_cast<int>(std::max<int64_t>(1, std::min(most, share)));
+    }
+    note_launch();
+    kern<<<static_cast<unsigned>(bt.start[args.size()]), T, smem, stream>>>(d_args, bt);
+    check_cuda(cudaGetLastError(), "integrate batch launch");
+  };
+  if (nb <= 8) launch(integrate_batch_kernel<8, T, MODE>, 8);
+  else if (nb <= 16) launch(integrate_batch_kernel<16, T, MODE>, 16);
+  else launch(integrate_batch_kernel<32, T, MODE, MODE == GG_REJECT_NONE ? 1 : 4>, 32);
+}
+
+static IntegrateArgs integrate_args(gg_stack* s, const float* d_weights, const gg_integrate_params_t& p) {
+  stack_ensure_maps(s);
+  IntegrateArgs a{};
+  a.slots = s->d_slots;
+  a.slot_of_frame = s->d_slot_of_frame;
+  a.stride = s->stride;
+  a.pixels = s->pixels;
+  a.frames = static_cast<int>(s->frames);
+  a.weights = d_weights;
+  a.nonfinite = s->d_frame_nonfinite;
+  a.rejection = p.rejection;
+  a.low_sigma = p.low_sigma;
+  a.high_sigma = p.high_sigma;
+  a.min_samples = p.min_samples;
+  a.max_frac = p.max_reject_fraction;
+  a.lfc_iterations = p.linear_fit_iterations > 0 ? p.linear_fit_iterations : 5;
+  a.master = s->d_master;
+  a.weight = s->d_weight;
+  a.coverage = s->d_coverage;
+  a.low = s->d_low;
+  a.high = s->d_high;
+  a.dq = s->d_dq;
+  a.count_u16 = p.count_dtype == GG_COUNT_U16;
+  a.geometric = (s->d_warp_coverage && s->warp_coverage_frames > 0) ? s->d_warp_coverage : nullptr;
+  return a;
+}
+
+// Integrates `count` stacks (same device, each at most 32 frames, each with
+// its own device weights) in one launch on the first stack's stream; the
+// other stacks' streams are joined before and after it.
+static void integrate_batch(std::vector<gg_stack*>& stacks, const gg_integrate_params_t& p) {
+  const int count = static_cast<int>(stacks.size());
+  // one launch per frame-count bucket (8 / 16 / 32): a stack never pays for
+  // a larger sorting network than its own
+  auto bucket = [](int n) { return n <= 8 ? 0 : (n <= 16 ? 1 : 2); };
+  std::vector<IntegrateArgs> args;
+  int bucket_start[4] = {0, 0, 0, 0};
+  for (int b = 0; b < 3; ++b) {
+    bucket_start[b] = static_cast<int>(args.size());
+    for (gg_stack* s : stacks)
+      if (bucket(static_cast<int>(s->frames)) == b) args.push_back(integrate_args(s, s->d_weights, p));
+  }
+  bucket_start[3] = static_cast<int>(args.size());
+  gg_stack* lead = stacks[0];
+  // join: the lead stream waits for every stack's queued work
+  std::vector<cudaEvent_t> events;
+  auto cleanup = [&]() {
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+  };
+  try {
+    for (int k = 1; k < count; ++k) {
+      cudaEvent_t e = nullptr;
+      check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate(batch)");
+      events.push_back(e);
+      check_cuda(cudaEventRecord(e, stacks[static_cast<size_t>(k)]->stream), "cudaEventRecord(batch)");
+      check_cuda(cudaStreamWaitEvent(lead->stream, e, 0), "cudaStreamWaitEvent(batch)");
+    }
+    IntegrateArgs* d_args = nullptr;
+    check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&d_args), sizeof(IntegrateArgs) * count, lead->stream),
+               "cudaMallocAsync(batch args)");
+    check_cuda(cudaMemcpyAsync(d_args, args.data(), sizeof(IntegrateArgs) * count, cudaMemcpyHostToDevice,
+                               lead->stream),
+               "cudaMemcpyAsync(batch args)");
+    for (int b = 0; b < 3; ++b) {
+      if (bucket_start[b + 1] == bucket_start[b]) continue;
+      const std::vector<IntegrateArgs> sub(args.begin() + bucket_start[b], args.begin() + bucket_start[b + 1]);
+      const int nb = b == 0 ? 8 : (b == 1 ? 16 : 32);
+      IntegrateArgs* d_sub = d_args + bucket_start[b];
+      switch (p.rejection) {
+        case GG_REJECT_NONE: launch_batch<GG_REJECT_NONE>(stacks, sub, nb, d_sub); break;
+        case GG_REJECT_SIGMA_CLIP: launch_batch<GG_REJECT_SIGMA_CLIP>(stacks, sub, nb, d_sub); break;
+        case GG_REJECT_WINSORIZED: launch_batch<GG_REJECT_WINSORIZED>(stacks, sub, nb, d_sub); break;
+        default: launch_batch<GG_REJECT_LINEAR_FIT>(stacks, sub, nb, d_sub); break;
+      }
+    }
+    check_cuda(cudaFreeAsync(d_args, lead->stream), "cudaFreeAsync(batch args)");
+    // the other stacks' later work waits for the batch
+    cudaEvent_t done = nullptr;
+    check_cuda(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "cudaEventCreate(batch)");
+    events.push_back(done);
+    check_cuda(cudaEventRecord(done, lead->stream), "cudaEventRecord(batch)");
+    for (int k = 1; k < count; ++k)
+      check_cuda(cudaStreamWaitEvent(stacks[static_cast<size_t>(k)]->stream, done, 0), "cudaStreamWaitEvent(batch)");
+  } catch (...) {
+    cleanup();
+    throw;
+  }
+  cleanup();
+  for (gg_stack* s : stacks) s->last_count_dtype = p.count_dtype;
 }
 
 __global__ void fused_prepare_kernel(FusedFrame* fused, const unsigned* src_nonfinite, unsigned* counts, int frames) {
@@ -1359,6 +1502,26 @@ int gg_stack_integrate_device_weights(gg_stack* s, const void* dev_weights, cons
   stack_require_all_loaded(s, "integration");
   stack_activate(s);
   launch_integrate(s, dev_weights ? static_cast<const float*>(dev_weights) : s->d_weights, *params);
+  GG_API_END
+}
+
+int gg_stacks_integrate_batch(gg_stack* const* stacks, int32_t count, const gg_integrate_params_t* params) {
+  GG_API_BEGIN
+  require(stacks != nullptr && params != nullptr, "null argument");
+  require(count >= 1 && count <= kMaxBatchStacks, "stack count must be in [1, 64]");
+  validate_integrate(*params);
+  std::vector<gg_stack*> v(static_cast<size_t>(count));
+  for (int k = 0; k < count; ++k) {
+    gg_stack* s = stacks[k];
+    require(s != nullptr, "null stack");
+    require(s->device == stacks[0]->device, "batched stacks must live on one device");
+    require(s->frames <= 32, "batched integration takes stacks of at most 32 frames");
+    for (int j = 0; j < k; ++j) require(stacks[j] != s, "a stack appears twice in the batch");
+    stack_require_all_loaded(s, "batched integration");
+    v[static_cast<size_t>(k)] = s;
+  }
+  stack_activate(stacks[0]);
+  integrate_batch(v, *params);
   GG_API_END
 }
 

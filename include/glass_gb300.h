@@ -224,6 +224,26 @@ int gg_stack_integrate_warped(gg_stack* stack, const double* host_matrices, int 
                               const gg_integrate_params_t* params);
 /* Geometric coverage (float32 H*W) of the last fused warp-integration. */
 int gg_stack_download_fused_coverage(gg_stack* stack, float* host_out);
+/* Tile-local weighted integration (integrate_tile_local_mean / _sigma_clip,
+ * native_bindings.cpp:12998-13210, 14337-14630; integration_kernels.cu:
+ * 1658-1711, 3622-3796).  mode 0 mean, 1 sigma clip, 2 winsorized sigma
+ * clip; host_weights may be NULL (1); host_target_mask: frame_count bytes
+ * (at least one set); host_tile_extents: tile_count x (x0, y0, x1, y1)
+ * half-open, inside the image, not overlapping; multipliers finite >= 0.
+ * At most 128 frames and 2048 tiles.  Maps as float32 counts
+ * (gg_stack_download_maps with GG_COUNT_F32). */
+int gg_stack_integrate_tile_local(gg_stack* stack, int mode, const float* host_weights,
+                                  const uint8_t* host_target_mask, const int32_t* host_tile_extents,
+                                  const float* host_multipliers, int32_t tile_count, float low_sigma,
+                                  float high_sigma);
+/* Several resident stacks (same device, each at most 32 frames; frame
+ * counts and shapes may differ) integrated in one launch of the column
+ * kernel, each with the device weights of its last gg_stack_compute_weights
+ * and the same rejection parameters; the maps land in each stack as after
+ * gg_stack_integrate_device_weights.  Enqueued on the first stack's stream,
+ * ordered after and before the other stacks' streams.  No reference
+ * counterpart (the reference integrates one group at a time). */
+int gg_stacks_integrate_batch(gg_stack* const* stacks, int32_t count, const gg_integrate_params_t* params);
 /* gg_stack_integrate_warped with the weights of the last
  * gg_stack_compute_weights (left on the device; no host round trip). */
 int gg_stack_integrate_warped_device_weights(gg_stack* stack, const double* host_matrices, int interpolation,
