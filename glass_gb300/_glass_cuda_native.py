@@ -759,6 +759,43 @@ class ResidentCalibratedStack:
             return catalogs, meta
         return catalogs
 
+    def cosmetic_mask_frames(self, indices: Any, hot_sigma: float = 8.0, cold_sigma: float = 8.0,
+                             structure_sigma: float = 1.5, min_neighbor_support: int = 2,
+                             star_protection: bool = False, star_threshold_sigma: float = 5.0,
+                             star_protection_radius_px: float = 3.0, star_min_pixels: int = 3,
+                             star_max_sharpness: float = 0.95, apply: bool = True) -> list[dict[str, Any]]:
+        """Isolated hot / cold pixels of each frame (cpu/cosmetic.py rules)
+        set to NaN on the device (apply=False only counts); returns the
+        per-frame counts and statistics."""
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+        if idx.size == 0:
+            return []
+        params = _lib.CosmeticParams(float(hot_sigma), float(cold_sigma), float(structure_sigma),
+                                     int(min_neighbor_support), int(bool(star_protection)),
+                                     float(star_threshold_sigma), float(star_protection_radius_px),
+                                     int(star_min_pixels), float(star_max_sharpness), int(bool(apply)))
+        out = (_lib.CosmeticResult * idx.size)()
+        _lib.call("gg_stack_cosmetic_mask", self._handle, _lib.ptr(idx), ctypes.c_int64(idx.size),
+                  ctypes.byref(params), out)
+        model = "star_protected_isolated_cosmetic" if star_protection else "isolated_cosmetic"
+        return [{"frame_index": int(idx[k]), "hot_pixels": int(r.hot_pixels), "cold_pixels": int(r.cold_pixels),
+                 "candidate_hot_pixels": int(r.candidate_hot_pixels),
+                 "candidate_cold_pixels": int(r.candidate_cold_pixels),
+                 "star_protected_hot_pixels": int(r.star_protected_hot_pixels),
+                 "star_protected_cold_pixels": int(r.star_protected_cold_pixels), "median": float(r.median),
+                 "sigma": float(r.sigma), "star_count": int(r.star_count), "applied": bool(apply),
+                 "model": model} for k, r in enumerate(out)]
+
+    def apply_invalid_mask_frame(self, index: int, invalid_mask: Any) -> dict[str, Any]:
+        """Source-DQ invalid samples (non-zero mask entries) become NaN."""
+        mask = np.ascontiguousarray(np.asarray(invalid_mask).astype(np.uint8))
+        if mask.shape != (self.height, self.width):
+            raise ValueError("invalid_mask must have the frame's shape")
+        n = ctypes.c_int64()
+        _lib.call("gg_stack_apply_invalid_mask", self._handle, ctypes.c_int64(int(index)), _lib.ptr(mask),
+                  ctypes.byref(n))
+        return {"frame_index": int(index), "invalid_samples": int(n.value)}
+
     def register_frames_triangle(self, reference_index: int, indices: Any, transform_model: str = "similarity",
                                  min_inliers: int = 6, tolerance_px: float = 3.0, max_stars: int = 80,
                                  neighbors: int = 5, descriptor_radius: float = 0.1, max_descriptors: int = 1200,

@@ -224,6 +224,36 @@ class TranslationNcc(ctypes.Structure):
     ]
 
 
+class CosmeticParams(ctypes.Structure):
+    _fields_ = [
+        ("hot_sigma", ctypes.c_float),
+        ("cold_sigma", ctypes.c_float),
+        ("structure_sigma", ctypes.c_float),
+        ("min_neighbor_support", ctypes.c_int32),
+        ("star_protection", ctypes.c_int32),
+        ("star_threshold_sigma", ctypes.c_float),
+        ("star_protection_radius_px", ctypes.c_float),
+        ("star_min_pixels", ctypes.c_int32),
+        ("star_max_sharpness", ctypes.c_float),
+        ("apply", ctypes.c_int32),
+    ]
+
+
+class CosmeticResult(ctypes.Structure):
+    _fields_ = [
+        ("hot_pixels", ctypes.c_int64),
+        ("cold_pixels", ctypes.c_int64),
+        ("candidate_hot_pixels", ctypes.c_int64),
+        ("candidate_cold_pixels", ctypes.c_int64),
+        ("star_protected_hot_pixels", ctypes.c_int64),
+        ("star_protected_cold_pixels", ctypes.c_int64),
+        ("median", ctypes.c_double),
+        ("sigma", ctypes.c_double),
+        ("star_count", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
 class GradientRefineParams(ctypes.Structure):
     _fields_ = [
         ("transform_model", ctypes.c_int32),
@@ -304,6 +334,8 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_graph_capture_step": [_P, _P, _P, ctypes.c_int, ctypes.c_float, ctypes.c_int,
                                     ctypes.POINTER(CalibParams), ctypes.POINTER(IntegrateParams)],
     "gg_stacks_integrate_batch": [_P, ctypes.c_int32, ctypes.POINTER(IntegrateParams)],
+    "gg_stack_cosmetic_mask": [_P, _P, ctypes.c_int64, ctypes.POINTER(CosmeticParams), _P],
+    "gg_stack_apply_invalid_mask": [_P, ctypes.c_int64, _P, _P],
     "gg_stack_integrate_tile_local": [_P, ctypes.c_int, _P, _P, _P, _P, ctypes.c_int32, ctypes.c_float,
                                       ctypes.c_float],
     "gg_stack_integrate_warped_device_weights": [_P, _P, ctypes.c_int, ctypes.c_float,

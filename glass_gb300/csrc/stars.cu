@@ -1345,3 +1345,305 @@ int gg_stack_detect_stars(gg_stack* s, const int64_t* indices, int64_t count, co
 }
 
 }  // extern "C"
+
+// ---- isolated cosmetic defects (source DQ) ------------------------------------
+// cpu/cosmetic.py:97-307 on resident frames: a finite pixel is a hot (cold)
+// candidate when it exceeds float32(median + k_hot sigma) (is below
+// float32(median - k_cold sigma)) and its distance to the float32 median of
+// its finite 8-neighbours (edge-clamped; float32 (a + b) / 2 for an even
+// count; the global median without any) exceeds float32(k sigma); it is a
+// defect when fewer than min_support neighbours pass float32(median -/+
+// max(0, structure_sigma) sigma) on the same side; the protected variant
+// keeps defects inside the radius of catalog stars with npix >= min_pixels
+// and sharpness <= max_sharpness.  median and sigma are the frame's star-
+// detection statistics (the same robust_background).  Defects become NaN
+// (resident_source_dq.py:825-925: no replacement).
+namespace gg {
+
+struct CosmeticArgs {
+  const float* slots;
+  const int* slot_of_frame;
+  int64_t stride;
+  int width, height;
+  const int* frames;
+  const StarFrameState* state;
+  const gg_star_t* stars;  // [count][max_stars] (protected variant)
+  int max_stars;
+  unsigned* hot_bits;      // [count][words]
+  unsigned* cold_bits;
+  int64_t words;
+  unsigned long long* counts;  // [count][8]
+  double hot_sigma, cold_sigma, support_sigma;
+  int min_support;
+  int protect;
+  int min_pixels;
+  double max_sharpness, radius_sq;
+};
+
+__device__ __forceinline__ bool star_protected(const CosmeticArgs& a, int k, int x, int y) {
+  const int n = a.state[k].kept;
+  const gg_star_t* st = a.stars + static_cast<int64_t>(k) * a.max_stars;
+  for (int i = 0; i < n; ++i) {
+    const gg_star_t s = st[i];
+    if (s.npix < a.min_pixels || s.sharpness > a.max_sharpness) continue;
+    if (!isfinite(s.x) || !isfinite(s.y)) continue;
+    const double dx = static_cast<double>(x) - s.x, dy = static_cast<double>(y) - s.y;
+    if (__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)) <= a.radius_sq) return true;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(256) cosmetic_classify_kernel(CosmeticArgs a) {
+  __shared__ unsigned long long s_counts[8];
+  if (threadIdx.x < 8) s_counts[threadIdx.x] = 0;
+  __syncthreads();
+  const int k = blockIdx.y;
+  const float* img = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+  const StarFrameState& st = a.state[k];
+  const double med = static_cast<double>(st.median), sigma = st.noise;
+  const float medf = st.median;
+  const float hot_limit = __double2float_rn(__dadd_rn(med, __dmul_rn(a.hot_sigma, sigma)));
+  const float cold_limit = __double2float_rn(__dsub_rn(med, __dmul_rn(a.cold_sigma, sigma)));
+  const float hot_delta = __double2float_rn(__dmul_rn(a.hot_sigma, sigma));
+  const float cold_delta = __double2float_rn(__dmul_rn(a.cold_sigma, sigma));
+  const float sup_hi = __double2float_rn(__dadd_rn(med, __dmul_rn(a.support_sigma, sigma)));
+  const float sup_lo = __double2float_rn(__dsub_rn(med, __dmul_rn(a.support_sigma, sigma)));
+  const int W = a.width, H = a.height;
+  const int64_t P = static_cast<int64_t>(W) * H;
+  unsigned c_hot = 0, c_cold = 0, c_cand_hot = 0, c_cand_cold = 0, c_prot_hot = 0, c_prot_cold = 0;
+  for (int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; p < P;
+       p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const float v = __ldg(img + p);
+    if (!isfinite(v) || !(v > hot_limit || v < cold_limit)) continue;  // only global outliers go on
+    const int y = static_cast<int>(p / W), x = static_cast<int>(p - static_cast<int64_t>(y) * W);
+    float nb[8];
+    int n = 0, hs = 0, cs = 0;
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (!dx && !dy) continue;
+        const int yy = min(max(y + dy, 0), H - 1), xx = min(max(x + dx, 0), W - 1);
+        const float u = __ldg(img + static_cast<int64_t>(yy) * W + xx);
+        if (isfinite(u)) {
+          nb[n++] = u;
+          hs += u > sup_hi;
+          cs += u < sup_lo;
+        }
+      }
+    for (int i = 1; i < n; ++i) {  // insertion sort of <= 8 values
+      const float t = nb[i];
+      int j = i - 1;
+      while (j >= 0 && nb[j] > t) {
+        nb[j + 1] = nb[j];
+        --j;
+      }
+      nb[j + 1] = t;
+    }
+    const float lmed = n == 0 ? medf : ((n & 1) ? nb[n / 2] : __fmul_rn(__fadd_rn(nb[n / 2 - 1], nb[n / 2]), 0.5f));
+    const bool cand_hot = v > hot_limit && __fsub_rn(v, lmed) > hot_delta;
+    const bool cand_cold = v < cold_limit && __fsub_rn(lmed, v) > cold_delta;
+    c_cand_hot += cand_hot;
+    c_cand_cold += cand_cold;
+    bool hot = cand_hot && hs < a.min_support;
+    bool cold = cand_cold && cs < a.min_support;
+    if ((hot || cold) && a.protect && star_protected(a, k, x, y)) {
+      c_prot_hot += hot;
+      c_prot_cold += cold;
+      hot = cold = false;
+    }
+    const int64_t word = static_cast<int64_t>(k) * a.words + (p >> 5);
+    const unsigned bit = 1u << (p & 31);
+    if (hot) {
+      ++c_hot;
+      atomicOr(a.hot_bits + word, bit);
+    }
+    if (cold) {
+      ++c_cold;
+      atomicOr(a.cold_bits + word, bit);
+    }
+  }
+  const unsigned vals[6] = {c_hot, c_cold, c_cand_hot, c_cand_cold, c_prot_hot, c_prot_cold};
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    unsigned v = vals[i];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&s_counts[i], static_cast<unsigned long long>(v));
+  }
+  __syncthreads();
+  if (threadIdx.x < 6 && s_counts[threadIdx.x])
+    atomicAdd(a.counts + static_cast<int64_t>(k) * 8 + threadIdx.x, s_counts[threadIdx.x]);
+}
+
+// Defects -> NaN; the frame's non-finite counter grows by the pixels set.
+__global__ void __launch_bounds__(256) cosmetic_apply_kernel(CosmeticArgs a, unsigned* frame_nonfinite) {
+  const int k = blockIdx.y;
+  float* img = const_cast<float*>(a.slots) + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+  const int64_t P = static_cast<int64_t>(a.width) * a.height;
+  unsigned added = 0;
+  for (int64_t w = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; w < a.words;
+       w += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    unsigned bits = a.hot_bits[static_cast<int64_t>(k) * a.words + w] | a.cold_bits[static_cast<int64_t>(k) * a.words + w];
+    while (bits) {
+      const int b = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const int64_t p = w * 32 + b;
+      if (p < P) {
+        img[p] = __int_as_float(0x7fc00000);
+        ++added;
+      }
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) added += __shfl_xor_sync(0xffffffffu, added, off);
+  if ((threadIdx.x & 31) == 0 && added) atomicAdd(frame_nonfinite + a.frames[k], added);
+}
+
+}  // namespace gg
+
+extern "C" int gg_stack_cosmetic_mask(gg_stack* s, const int64_t* indices, int64_t count,
+                                      const gg_cosmetic_params_t* params, gg_cosmetic_result_t* host_out) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(s != nullptr && indices != nullptr && params != nullptr, "null argument");
+  require(count > 0 && count <= 65535, "frame count must be in [1, 65535]");
+  const gg_cosmetic_params_t& p = *params;
+  require(std::isfinite(p.hot_sigma) && std::isfinite(p.cold_sigma) && std::isfinite(p.structure_sigma),
+          "cosmetic sigmas must be finite");
+  require(!p.star_protection || (std::isfinite(p.star_protection_radius_px) && std::isfinite(p.star_threshold_sigma) &&
+                                 std::isfinite(p.star_max_sharpness)),
+          "star protection parameters must be finite");
+  for (int64_t k = 0; k < count; ++k) stack_require_loaded(s, indices[k], "cosmetic defect detection");
+  stack_activate(s);
+  gg_star_params_t sp{};
+  sp.threshold_sigma = p.star_threshold_sigma;
+  sp.max_stars = 500;
+  sp.window_radius = 4;
+  sp.min_separation_px = std::max(2.0f, p.star_protection_radius_px * 0.5f);
+  sp.background = std::nanf("");
+  sp.noise = std::nanf("");
+  sp.catalog_min_fwhm = 0.0f;
+  sp.catalog_max_eccentricity = 1.0f;
+  sp.mesh_cell = 0;
+  detect_stars(s, indices, static_cast<int>(count), sp);
+  StarScratch& sc = star_scratch(s);
+  const int64_t words = (s->pixels + 31) / 32;
+  unsigned* bits = nullptr;
+  unsigned long long* counts = nullptr;
+  check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&bits), sizeof(unsigned) * words * count * 2, s->stream),
+             "cudaMallocAsync(cosmetic bits)");
+  check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&counts), sizeof(unsigned long long) * 8 * count, s->stream),
+             "cudaMallocAsync(cosmetic counts)");
+  check_cuda(cudaMemsetAsync(bits, 0, sizeof(unsigned) * words * count * 2, s->stream), "cudaMemsetAsync(bits)");
+  check_cuda(cudaMemsetAsync(counts, 0, sizeof(unsigned long long) * 8 * count, s->stream), "cudaMemsetAsync(counts)");
+  CosmeticArgs a{};
+  a.slots = s->d_slots;
+  a.slot_of_frame = s->d_slot_of_frame;
+  a.stride = s->stride;
+  a.width = static_cast<int>(s->width);
+  a.height = static_cast<int>(s->height);
+  a.frames = sc.frames;
+  a.state = sc.state;
+  a.stars = sc.out;
+  a.max_stars = sp.max_stars;
+  a.hot_bits = bits;
+  a.cold_bits = bits + words * count;
+  a.words = words;
+  a.counts = counts;
+  a.hot_sigma = p.hot_sigma;
+  a.cold_sigma = p.cold_sigma;
+  a.support_sigma = std::max(0.0, static_cast<double>(p.structure_sigma));
+  a.min_support = std::max(0, p.min_neighbor_support);
+  a.protect = p.star_protection ? 1 : 0;
+  a.min_pixels = p.star_min_pixels;
+  a.max_sharpness = p.star_max_sharpness;
+  const double r = std::max(0.0, static_cast<double>(p.star_protection_radius_px));
+  a.radius_sq = r * r;
+  if (!(r > 0.0)) a.protect = 0;
+  const unsigned per_frame = grid_for(static_cast<size_t>(s->pixels), 256, std::max(1, 8 / static_cast<int>(std::min<int64_t>(count, 8))));
+  note_launch();
+  cosmetic_classify_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), 256, 0, s->stream>>>(a);
+  check_cuda(cudaGetLastError(), "cosmetic_classify launch");
+  if (p.apply) {
+    note_launch();
+    cosmetic_apply_kernel<<<dim3(std::max(1u, static_cast<unsigned>(std::min<int64_t>((words + 255) / 256, 1024))),
+                                 static_cast<unsigned>(count)), 256, 0, s->stream>>>(a, s->d_frame_nonfinite);
+    check_cuda(cudaGetLastError(), "cosmetic_apply launch");
+  }
+  std::vector<unsigned long long> host(static_cast<size_t>(8 * count));
+  std::vector<StarFrameState> states(static_cast<size_t>(count));
+  check_cuda(cudaMemcpyAsync(host.data(), counts, sizeof(unsigned long long) * 8 * count, cudaMemcpyDeviceToHost,
+                             s->stream),
+             "cudaMemcpyAsync(cosmetic counts)");
+  check_cuda(cudaMemcpyAsync(states.data(), sc.state, sizeof(StarFrameState) * count, cudaMemcpyDeviceToHost, s->stream),
+             "cudaMemcpyAsync(cosmetic state)");
+  check_cuda(cudaFreeAsync(bits, s->stream), "cudaFreeAsync(cosmetic bits)");
+  check_cuda(cudaFreeAsync(counts, s->stream), "cudaFreeAsync(cosmetic counts)");
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(cosmetic)");
+  if (host_out) {
+    for (int64_t k = 0; k < count; ++k) {
+      gg_cosmetic_result_t& r = host_out[k];
+      const unsigned long long* c = host.data() + 8 * k;
+      r.hot_pixels = static_cast<int64_t>(c[0]);
+      r.cold_pixels = static_cast<int64_t>(c[1]);
+      r.candidate_hot_pixels = static_cast<int64_t>(c[2]);
+      r.candidate_cold_pixels = static_cast<int64_t>(c[3]);
+      r.star_protected_hot_pixels = static_cast<int64_t>(c[4]);
+      r.star_protected_cold_pixels = static_cast<int64_t>(c[5]);
+      r.median = static_cast<double>(states[static_cast<size_t>(k)].median);
+      r.sigma = states[static_cast<size_t>(k)].noise;
+      r.star_count = states[static_cast<size_t>(k)].kept;
+      r.pad = 0;
+    }
+  }
+  GG_API_END
+}
+
+namespace gg {
+
+// Source-DQ invalid mask (glass_apply_invalid_mask_f32_kernel semantics):
+// non-zero mask bytes make the sample NaN; the frame's non-finite counter
+// counts the samples that were finite before.
+__global__ void __launch_bounds__(256) invalid_mask_kernel(float* img, const unsigned char* mask, int64_t n,
+                                                           unsigned* nonfinite) {
+  unsigned added = 0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (mask[i] && isfinite(img[i])) {
+      img[i] = __int_as_float(0x7fc00000);
+      ++added;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) added += __shfl_xor_sync(0xffffffffu, added, off);
+  if ((threadIdx.x & 31) == 0 && added) atomicAdd(nonfinite, added);
+}
+
+}  // namespace gg
+
+extern "C" int gg_stack_apply_invalid_mask(gg_stack* s, int64_t index, const uint8_t* host_mask,
+                                           int64_t* host_invalid_samples) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(s != nullptr && host_mask != nullptr, "null argument");
+  stack_require_loaded(s, index, "source-DQ invalid mask");
+  stack_activate(s);
+  std::vector<int> slots;
+  stack_read_slots(s, slots);
+  unsigned char* d_mask = nullptr;
+  check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&d_mask), static_cast<size_t>(s->pixels), s->stream),
+             "cudaMallocAsync(invalid mask)");
+  check_cuda(cudaMemcpyAsync(d_mask, host_mask, static_cast<size_t>(s->pixels), cudaMemcpyHostToDevice, s->stream),
+             "cudaMemcpyAsync(invalid mask)");
+  float* img = s->d_slots + static_cast<int64_t>(slots[static_cast<size_t>(index)]) * s->stride;
+  note_launch();
+  invalid_mask_kernel<<<grid_for(static_cast<size_t>(s->pixels), 256), 256, 0, s->stream>>>(
+      img, d_mask, s->pixels, s->d_frame_nonfinite + index);
+  check_cuda(cudaGetLastError(), "invalid_mask launch");
+  check_cuda(cudaFreeAsync(d_mask, s->stream), "cudaFreeAsync(invalid mask)");
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(invalid mask)");
+  if (host_invalid_samples) {
+    int64_t n = 0;
+    for (int64_t i = 0; i < s->pixels; ++i) n += host_mask[i] != 0;
+    *host_invalid_samples = n;
+  }
+  GG_API_END
+}

@@ -397,6 +397,49 @@ typedef struct {
 int gg_stack_detect_stars(gg_stack* stack, const int64_t* indices, int64_t count, const gg_star_params_t* params,
                           gg_star_t* host_stars, int32_t* host_counts, gg_star_frame_info_t* host_info);
 
+/* ---- source DQ: isolated cosmetic defects ----------------------------------
+ * Replaces apply_isolated_cosmetic_threshold_mask_frame(s) and the
+ * star-protected variant (resident_source_dq.py:825-1740; detection rules of
+ * cpu/cosmetic.py:97-307): per frame, with the frame's robust median / sigma
+ * (as detect_stars), isolated hot / cold pixels without enough same-side
+ * neighbour support; star_protection = 1 keeps those within
+ * star_protection_radius_px of catalog stars (threshold star_threshold_sigma,
+ * 500 stars, npix >= star_min_pixels, sharpness <= star_max_sharpness).
+ * apply = 1 sets the defects to NaN (no replacement); 0 only counts. */
+typedef struct {
+  float hot_sigma;                 /* 8    */
+  float cold_sigma;                /* 8    */
+  float structure_sigma;           /* 1.5  */
+  int32_t min_neighbor_support;    /* 2    */
+  int32_t star_protection;         /* 0/1  */
+  float star_threshold_sigma;      /* 5    */
+  float star_protection_radius_px; /* 3    */
+  int32_t star_min_pixels;         /* 3    */
+  float star_max_sharpness;        /* 0.95 */
+  int32_t apply;                   /* 1    */
+} gg_cosmetic_params_t;
+
+typedef struct {
+  int64_t hot_pixels;
+  int64_t cold_pixels;
+  int64_t candidate_hot_pixels;
+  int64_t candidate_cold_pixels;
+  int64_t star_protected_hot_pixels;
+  int64_t star_protected_cold_pixels;
+  double median;
+  double sigma;
+  int32_t star_count;
+  int32_t pad;
+} gg_cosmetic_result_t;
+
+int gg_stack_cosmetic_mask(gg_stack* stack, const int64_t* indices, int64_t count,
+                           const gg_cosmetic_params_t* params, gg_cosmetic_result_t* host_out);
+/* apply_invalid_mask (integration_kernels.cu:159-179): frame `index` samples
+ * whose host_mask byte (H*W) is non-zero become NaN; host_invalid_samples
+ * (may be NULL) receives the number of flagged samples.  Synchronises. */
+int gg_stack_apply_invalid_mask(gg_stack* stack, int64_t index, const uint8_t* host_mask,
+                                int64_t* host_invalid_samples);
+
 /* ---- registration (triangle asterisms) ----------------------------------- */
 /* Point lists are (x, y) float64 pairs, brightest star first.  Catalogs hold
  * at most 80 stars. */

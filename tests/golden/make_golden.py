@@ -646,6 +646,41 @@ def make_local_norm(ref_src: Path) -> None:
     np.savez_compressed(HERE / "local_norm.npz", **arrays)
 
 
+# ---------------------------------------------------------------------------
+# cosmetic (source DQ)
+# ---------------------------------------------------------------------------
+def make_cosmetic(ref_src: Path) -> None:
+    """detect_isolated_cosmetic_defects and detect_star_protected_cosmetic_defects
+    (src/glass/cpu/cosmetic.py:97-307) on seeded star fields with hot, cold
+    and clustered defects and a NaN patch; stores the HOT / COLD bits."""
+    sys.path.insert(0, str(ref_src))
+    from glass.cpu import cosmetic
+    from glass.engine.contracts import DQFlag
+
+    rng = np.random.default_rng(41)
+    arrays: dict = {}
+    names = []
+    for name, (h, w, nstars) in {"small": (96, 128, 25), "wide": (120, 200, 60)}.items():
+        img = _star_field(rng, h, w, nstars, 800.0, 10.0)
+        ys, xs = rng.integers(2, h - 2, 30), rng.integers(2, w - 2, 30)
+        img[ys[:15], xs[:15]] += np.float32(3000.0)  # isolated hot
+        img[ys[15:25], xs[15:25]] -= np.float32(700.0)  # isolated cold
+        y, x = int(ys[25]), int(xs[25])
+        img[y:y + 2, x:x + 2] += np.float32(4000.0)  # supported cluster (kept)
+        img[int(ys[26]), :4] = np.nan
+        img[0, 0] += np.float32(5000.0)  # corner: edge-padded neighbours
+        for kind, fn in (("isolated", cosmetic.detect_isolated_cosmetic_defects),
+                         ("protected", cosmetic.detect_star_protected_cosmetic_defects)):
+            res = fn(img)
+            bits = res.dq_mask.data
+            arrays[f"{name}/{kind}/hot"] = (bits & int(DQFlag.HOT_PIXEL)) != 0
+            arrays[f"{name}/{kind}/cold"] = (bits & int(DQFlag.COLD_PIXEL)) != 0
+        arrays[f"{name}/image"] = img
+        names.append(name)
+    arrays["_names"] = np.array(names)
+    np.savez_compressed(HERE / "cosmetic.npz", **arrays)
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__)
     parser.add_argument("--reference", default="/root/reference", help="GLASS reference checkout")
@@ -655,7 +690,7 @@ def main() -> int:
     src = ref / "src"
     jobs = {"integration": make_integration, "calibration": make_calibration, "warp": make_warp,
             "stars": make_stars, "registration": make_registration, "alignment": make_alignment,
-            "local_norm": make_local_norm}
+            "local_norm": make_local_norm, "cosmetic": make_cosmetic}
     only = [j for j in args.only.split(",") if j] or list(jobs)
     for job in only:
         jobs[job](src)

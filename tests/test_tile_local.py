@@ -74,13 +74,13 @@ def test_gpu_tile_local_matches_oracle(native, mode):
 
 @pytest.mark.gpu
 def test_gpu_tile_local_arguments(native):
-    data, weights, target = _stack(4, n=4)
+    data, weights, target = _stack(4)
     s = native.ResidentCalibratedStack(*data.shape)
     try:
         for k in range(data.shape[0]):
             s.upload_calibrated_frame(k, data[k])
         with pytest.raises(ValueError):  # no target frame
-            s.integrate_tile_local_mean(np.zeros(4, bool), EXTENTS, MULTS)
+            s.integrate_tile_local_mean(np.zeros(data.shape[0], bool), EXTENTS, MULTS)
         with pytest.raises(ValueError):  # overlapping tiles
             s.integrate_tile_local_mean(target, np.array([[0, 0, 10, 10], [5, 5, 20, 20]]), [1.0, 1.0])
         with pytest.raises(ValueError):  # outside the image
