@@ -29,8 +29,10 @@ from glass_gb300 import _lib
 _lib.load()
 
 __all__ = [
+    "RawFitsReadQueue",
     "ResidentCalibratedStack",
     "calibrate_tile_f32",
+    "integrate_stacks_batch",
     "cuda_available",
     "get_device_info",
     "host_pinned_empty_f32",
@@ -85,6 +87,61 @@ class _PinnedBuffer:
             "version": 3,
         }
         weakref.finalize(self, _lib.load().gg_host_free_pinned, ctypes.c_void_p(self.address))
+
+
+class RawFitsReadQueue:
+    """Host threads reading FITS data units into caller buffers
+    (native_bindings.cpp:2605-2915, 20417-20429): submit(frame_index, path,
+    data_offset, byte_count, output uint8[byte_count]) -> dict;
+    wait_completed(timeout_s=-1) -> dict or None; stats(); close()."""
+
+    def __init__(self, worker_count: int = 1):
+        handle = ctypes.c_void_p()
+        _lib.call("gg_read_queue_create", int(worker_count), ctypes.byref(handle))
+        self._handle = handle
+        self._buffers: dict[int, np.ndarray] = {}  # keep outputs alive until their completion
+        weakref.finalize(self, _lib.load().gg_read_queue_destroy, handle)
+
+    def submit(self, frame_index: int, path: str, data_offset: int, byte_count: int, output: np.ndarray) -> dict:
+        if int(byte_count) <= 0:
+            raise ValueError("native raw FITS queue byte count must be non-empty")
+        if (not isinstance(output, np.ndarray) or output.dtype != np.uint8 or output.ndim != 1
+                or output.shape[0] != int(byte_count) or not output.flags.c_contiguous):
+            raise ValueError("native raw FITS queue output shape does not match byte count")
+        pending = ctypes.c_uint64()
+        _lib.call("gg_read_queue_submit", self._handle, int(frame_index), str(path).encode(), int(data_offset),
+                  int(byte_count), _lib.ptr(output), ctypes.byref(pending))
+        self._buffers[int(frame_index)] = output
+        st = self.stats()
+        return {"schema_version": 1, "backend": "native_u16be_raw_queue", "frame_index": int(frame_index),
+                "pending_count": int(pending.value), "submitted_count": st["submitted_count"],
+                "worker_count": st["worker_count"]}
+
+    def wait_completed(self, timeout_s: float = -1.0):
+        done = _lib.ReadCompletion()
+        has = ctypes.c_int32()
+        status = _lib.load().gg_read_queue_wait(self._handle, float(timeout_s), ctypes.byref(done), ctypes.byref(has))
+        if has.value:
+            self._buffers.pop(int(done.frame_index), None)
+        _lib.check(status, "wait_completed")
+        if not has.value:
+            return None
+        st = self.stats()
+        return {"schema_version": 1, "backend": "native_u16be_raw_queue", "frame_index": int(done.frame_index),
+                "bytes_read": int(done.bytes_read), "file_open_s": float(done.file_open_s),
+                "file_read_s": float(done.file_read_s), "decode_s": 0.0, "total_s": float(done.total_s),
+                "completed_count": st["completed_count"], "worker_count": st["worker_count"]}
+
+    def stats(self) -> dict:
+        s = _lib.ReadQueueStats()
+        _lib.call("gg_read_queue_stats", self._handle, ctypes.byref(s))
+        out = {name: int(getattr(s, name)) for name, _ in _lib.ReadQueueStats._fields_ if name != "pad"}
+        out["closed"] = bool(out["closed"])
+        out.update(schema_version=1, backend="native_u16be_raw_queue")
+        return out
+
+    def close(self) -> None:
+        _lib.call("gg_read_queue_close", self._handle)
 
 
 def integrate_stacks_batch(stacks: list, rejection: int = _lib.GG_REJECT_WINSORIZED, low_sigma: float = 3.0,

@@ -224,6 +224,30 @@ class TranslationNcc(ctypes.Structure):
     ]
 
 
+class ReadCompletion(ctypes.Structure):
+    _fields_ = [
+        ("frame_index", ctypes.c_uint64),
+        ("bytes_read", ctypes.c_uint64),
+        ("file_open_s", ctypes.c_double),
+        ("file_read_s", ctypes.c_double),
+        ("total_s", ctypes.c_double),
+    ]
+
+
+class ReadQueueStats(ctypes.Structure):
+    _fields_ = [
+        ("worker_count", ctypes.c_uint64),
+        ("submitted_count", ctypes.c_uint64),
+        ("completed_count", ctypes.c_uint64),
+        ("queued_count", ctypes.c_uint64),
+        ("active_count", ctypes.c_uint64),
+        ("ready_count", ctypes.c_uint64),
+        ("requested_bytes", ctypes.c_uint64),
+        ("closed", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
 class CosmeticParams(ctypes.Structure):
     _fields_ = [
         ("hot_sigma", ctypes.c_float),
@@ -334,6 +358,12 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_graph_capture_step": [_P, _P, _P, ctypes.c_int, ctypes.c_float, ctypes.c_int,
                                     ctypes.POINTER(CalibParams), ctypes.POINTER(IntegrateParams)],
     "gg_stacks_integrate_batch": [_P, ctypes.c_int32, ctypes.POINTER(IntegrateParams)],
+    "gg_read_queue_create": [ctypes.c_int32, _P],
+    "gg_read_queue_submit": [_P, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_uint64, _P, _P],
+    "gg_read_queue_wait": [_P, ctypes.c_double, ctypes.POINTER(ReadCompletion), ctypes.POINTER(ctypes.c_int32)],
+    "gg_read_queue_stats": [_P, ctypes.POINTER(ReadQueueStats)],
+    "gg_read_queue_close": [_P],
+    "gg_read_queue_destroy": [_P],
     "gg_stack_cosmetic_mask": [_P, _P, ctypes.c_int64, ctypes.POINTER(CosmeticParams), _P],
     "gg_stack_apply_invalid_mask": [_P, ctypes.c_int64, _P, _P],
     "gg_stack_integrate_tile_local": [_P, ctypes.c_int, _P, _P, _P, _P, ctypes.c_int32, ctypes.c_float,

@@ -397,6 +397,42 @@ typedef struct {
 int gg_stack_detect_stars(gg_stack* stack, const int64_t* indices, int64_t count, const gg_star_params_t* params,
                           gg_star_t* host_stars, int32_t* host_counts, gg_star_frame_info_t* host_info);
 
+/* ---- raw FITS read queue (RawFitsReadQueue, native_bindings.cpp:2605-2915,
+ * 20417-20429) ---------------------------------------------------------------
+ * Host worker threads read [data_offset, data_offset + byte_count) of a file
+ * into host_out (normally pinned memory for the u16 decode + calibration
+ * entry points); completions come back in finishing order.  A failed read
+ * is reported by gg_read_queue_wait as GG_ERR_RUNTIME (the completion is
+ * still filled and consumed). */
+typedef struct gg_read_queue gg_read_queue;
+typedef struct {
+  uint64_t frame_index;
+  uint64_t bytes_read;
+  double file_open_s;
+  double file_read_s;
+  double total_s;
+} gg_read_completion_t;
+typedef struct {
+  uint64_t worker_count;
+  uint64_t submitted_count;
+  uint64_t completed_count;
+  uint64_t queued_count;
+  uint64_t active_count;
+  uint64_t ready_count;
+  uint64_t requested_bytes;
+  int32_t closed;
+  int32_t pad;
+} gg_read_queue_stats_t;
+int gg_read_queue_create(int32_t workers, gg_read_queue** out);
+int gg_read_queue_submit(gg_read_queue* queue, uint64_t frame_index, const char* path, uint64_t data_offset,
+                         uint64_t byte_count, void* host_out, uint64_t* pending_after);
+/* timeout_s < 0 waits without limit; *has_completion = 0 on time-out or
+ * when the queue is closed and drained. */
+int gg_read_queue_wait(gg_read_queue* queue, double timeout_s, gg_read_completion_t* out, int32_t* has_completion);
+int gg_read_queue_stats(gg_read_queue* queue, gg_read_queue_stats_t* out);
+int gg_read_queue_close(gg_read_queue* queue);
+int gg_read_queue_destroy(gg_read_queue* queue);
+
 /* ---- source DQ: isolated cosmetic defects ----------------------------------
  * Replaces apply_isolated_cosmetic_threshold_mask_frame(s) and the
  * star-protected variant (resident_source_dq.py:825-1740; detection rules of
