@@ -17,6 +17,7 @@ host cores instead (rank 0 only).
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -44,7 +45,8 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--config", default="c2", choices=["c1", "c2"])
+    p.add_argument("--config", default="c2", choices=["c1", "c2", "c5"],
+                   help="c5: the full 200 x 9600 x 6422 stack resident (device step only, one GPU)")
     p.add_argument("--frames", type=int, default=0, help="override frame count (smaller smoke runs)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-adjoint", action="store_true", help="skip the gradient-refinement registration report")
@@ -326,16 +328,22 @@ def local_norm_report(pipe, stream, reps: int, peak: float) -> dict:
 
 
 def batch_report(reps: int) -> dict:
-    """Four uneven stacks (25/20/16/12 frames at 1024x1024, 1536x1024,
-    1024x768, 2048x512; the 25 x 1024^2 one is the c4 C shape) winsorized-
-    integrated one after another vs in one batched launch, CUDA events on one
-    stream, seeded noise frames resident on the device."""
+    """Uneven stacks winsorized-integrated one after another vs batched (one
+    launch per frame-count bucket), CUDA events on one stream, seeded noise
+    frames resident on the device: four large stacks (25/20/16/12 frames at
+    1024x1024, 1536x1024, 1024x768, 2048x512; 25 x 1024^2 is the c4 C shape)
+    and sixteen small ones (8-16 frames at 256x256 / 256x320)."""
+    large = [(25, 1024, 1024), (20, 1536, 1024), (16, 1024, 768), (12, 2048, 512)]
+    small = [(8 + (k % 3) * 4, 256, 256 + 64 * (k % 2)) for k in range(16)]
+    return {"large_uneven": _batch_case(large, reps), "many_small": _batch_case(small, reps)}
+
+
+def _batch_case(shapes, reps: int) -> dict:
     import torch
 
     from glass_gb300 import _glass_cuda_native as native
     from glass_gb300 import _lib
 
-    shapes = [(25, 1024, 1024), (20, 1536, 1024), (16, 1024, 768), (12, 2048, 512)]
     stream = torch.cuda.Stream()
     stacks = []
     try:
@@ -406,9 +414,100 @@ def graph_report(pipe, dev_raw, matrices, stream, reps: int) -> dict:
             "mpix_frames_per_s_graph": pipe.frames * pipe.height * pipe.width / 1e6 / (graph_ms / 1e3)}
 
 
+def run_c5(args) -> int:
+    """The full c5 stack resident on one GPU: 200 frames of 9600 x 6422
+    (49.3 GB of float32 frames).  Eight distinct seeded raw frames are
+    rendered at full size (c5's star, sky and defect model; 2 calibration
+    frames of each kind) and cycled over the 200 frame slots on the device, so
+    no 24.7 GB host array is needed.  Step: calibrate -> star catalogs ->
+    triangle registration -> Lanczos3 warp -> simple-SNR weights -> winsorized
+    3/3 integration; CUDA events per stage over K steps."""
+    import dataclasses
+
+    import torch
+
+    from glass_gb300 import _lib
+    from glass_gb300.pipeline import ResidentPipeline, StepConfig, build_masters
+    from glass_gb300.synthetic import CONFIGS, generate
+
+    torch.cuda.set_device(0)
+    n = args.frames or 200
+    unique = 8
+    cfg = dataclasses.replace(CONFIGS["c5"], calibration_frames=2)
+    data = generate(cfg, unique)
+    _, h, w = data.lights.shape
+    masters = build_masters(data.bias_frames, data.dark_frames, data.flat_frames)
+    pipe = ResidentPipeline(n, h, w, masters, StepConfig())
+    stream = torch.cuda.Stream()
+    pipe.set_stream(stream.cuda_stream)
+    dev_raw = torch.from_numpy(data.lights.view(np.int16)).cuda()
+    truth = np.asarray([data.truth_matrices[k % unique] for k in range(n)])
+    idx_groups = [np.arange(k, min(k + unique, n), dtype=np.int64) for k in range(0, n, unique)]
+    reg = {}
+
+    def calibrate():
+        for g in idx_groups:
+            _lib.call("gg_stack_calibrate_u16_device", pipe.stack.handle, _lib.ptr(g), ctypes.c_int64(g.size),
+                      ctypes.c_void_p(dev_raw.data_ptr()), 0, ctypes.byref(pipe._calib_params()))
+
+    def register():
+        reg["m"], reg["ok"] = pipe.register(0)
+
+    P = h * w
+    stages = [("calibrate", calibrate, 6 * n * P + 12 * P), ("detect_stars", pipe.detect, 4 * n * P),
+              ("register", register, None), ("warp_lanczos3", lambda: pipe.warp(reg["m"]), 8 * (n - 1) * P),
+              ("weights", pipe.weights, 4 * n * P), ("integrate_winsorized", pipe.integrate, 4 * n * P + 16 * P)]
+    for _ in range(max(1, args.warmup)):
+        for _, fn, _ in stages:
+            fn()
+    stream.synchronize()
+    events = {name: [] for name, _, _ in stages}
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        for name, fn, _ in stages:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            events[name].append((e0, e1))
+    stop.record(stream)
+    stream.synchronize()
+    ms = start.elapsed_time(stop) / args.steps
+    peak, kind = measured_peak()
+    out_stages = {}
+    for name, _, nbytes in stages:
+        t = statistics.mean(a.elapsed_time(b) for a, b in events[name])
+        gbs = None if nbytes is None else nbytes / (t / 1e3) / 1e9
+        out_stages[name] = {"ms": t, "algorithmic_bytes": nbytes, "achieved_gbs": gbs,
+                            "frac": None if gbs is None else gbs / peak}
+    ok = [k for k in range(1, n) if reg["ok"][k]]
+    from glass_gb300.adjoint import registration_rms_px
+
+    line = {"metric": "stacked Mpix-frames/s", "value": n * P / 1e6 / (ms / 1e3), "unit": "Mpix-frames/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (8 distinct seeded raw frames cycled over the frame slots)",
+            "config": {"workload": f"c5:{n}x{h}x{w} uint16 -> calibrate -> star catalogs -> triangle registration "
+                                   "-> Lanczos3 warp -> simple_snr weights -> winsorized 3/3 integration",
+                       "frames": n, "height": h, "width": w, "unique_raw_frames": unique,
+                       "l2": "inputs larger than L2", "peak_source": kind},
+            "resident": {"stack_bytes_allocated": pipe.stack.bytes_allocated,
+                         "device_bytes_in_use": int(torch.cuda.mem_get_info()[1] - torch.cuda.mem_get_info()[0])},
+            "stages": out_stages,
+            "registration": {"frames_ok": len(ok) + 1, "frames": n,
+                             "rms_px_vs_truth_triangle": registration_rms_px([reg["m"][k] for k in ok],
+                                                                             [truth[k] for k in ok], h, w)}}
+    print(json.dumps(line))
+    pipe.close()
+    return 0
+
+
 # ---------------------------------------------------------------------------
 def main():
     args = parse_args()
+    if args.config == "c5" and args.impl == "gb300":
+        return run_c5(args)
     rank, world, local = dist_env()
     from glass_gb300.synthetic import CONFIGS, generate
 
