@@ -343,9 +343,12 @@ def refine_affine(reference: torch.Tensor, moving: torch.Tensor, matrix, config:
                          history)
 
 
-def registration_rms_px(estimated, truth, height: int, width: int, grid: int = 16) -> float:
+def registration_rms_px(estimated, truth, height: int, width: int, grid: int = 16) -> float | None:
     """RMS over a grid of reference pixels of the distance between the source
-    positions that two moving -> reference matrices sample."""
+    positions that two moving -> reference matrices sample (None for no
+    matrices)."""
+    if len(estimated) == 0:
+        return None
     ys, xs = np.meshgrid(np.linspace(0, height - 1, grid), np.linspace(0, width - 1, grid), indexing="ij")
     pts = np.stack([xs.ravel(), ys.ravel(), np.ones(xs.size)])
     sq = []

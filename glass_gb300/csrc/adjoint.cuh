@@ -115,6 +115,9 @@ __device__ __forceinline__ void lanczos3_weights_grad(float t, float (&w)[6], fl
 // Lanczos3 value and its derivatives with respect to the sample position
 // over a window whose 36 taps are all finite; false when a tap is not finite
 // or the weights cancel (|D| <= 1e-12).
+// UNROLL = true issues all 36 tap loads of the window at once (more loads in
+// flight, more registers); false walks it row by row.
+template <bool UNROLL = false>
 __device__ __forceinline__ bool lanczos3_value_grad(const float* src, int W, int x0, int y0, float tx, float ty,
                                                     float& O, float& Ox, float& Oy) {
   float wx[6], wy[6], dwx[6], dwy[6];
@@ -130,7 +133,7 @@ __device__ __forceinline__ bool lanczos3_value_grad(const float* src, int W, int
   }
   float N = 0.0f, Nx = 0.0f, Ny = 0.0f;
   bool finite = true;
-#pragma unroll 1
+#pragma unroll(UNROLL ? 6 : 1)
   for (int j = 0; j < 6; ++j) {
     const float* row = src + static_cast<int64_t>(y0 - 2 + j) * W + (x0 - 2);
     float r = 0.0f, rx = 0.0f;

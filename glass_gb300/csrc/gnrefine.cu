@@ -23,9 +23,12 @@
 // sampler's position derivative (adjoint.cuh, the same derivative the warp
 // adjoint uses) times (x, y, 1).  Everything stays on the device:
 //   gn_accumulate_kernel  one pass over the samples of every job: J^T J
-//                         (8 x 8, upper triangle), J^T r, r^2 and the count
-//                         of kept samples, float32 per thread, float64
-//                         across threads and blocks (fixed order);
+//                         (upper triangle of the model's columns, projected
+//                         in the kernel, or all 8 for the affine model),
+//                         J^T r, r^2 and the count of kept samples, float32
+//                         per thread, float64 across threads and blocks
+//                         (fixed order); statistics passes keep only sum r,
+//                         sum r^2 and the count;
 //   gn_solve_kernel       one warp per job in float64: reduce the block
 //                         partials, then either update (beta, sigma) from the
 //                         kept residuals (statistics passes) or solve the
@@ -42,6 +45,7 @@
 #include <vector>
 
 #include "adjoint.cuh"
+#include "autotune.cuh"
 #include "stack.cuh"
 
 namespace gg {
@@ -92,12 +96,106 @@ struct GnArgs {
   float cx, cy, inv_r;
 };
 
-template <int INTERP>
-__global__ void __launch_bounds__(kGnThreads) gn_accumulate_kernel(GnArgs a) {
+// Accumulators of one pass.  K = 0: statistics pass (sum r, sum r^2, count);
+// K = 4 / 6: the translation / similarity Jacobian columns, projected in the
+// kernel (x shift, y shift[, scale, rotation], alpha, beta); K = 8: all eight
+// columns (affine model, normal-equation export).  Slots of the 48 sums: the
+// packed upper triangle of J^T J at [0, K(K+1)/2), J^T r at [36, 36 + K),
+// sum r^2 at 44, the count at 45; the statistics pass keeps J_beta^T r =
+// -sum r at 43.
+template <int K>
+struct GnLayout {
+  static constexpr int kTri = K * (K + 1) / 2;
+  static constexpr int kAcc = K == 0 ? 3 : kTri + K + 2;
+  __host__ __device__ static constexpr int slot(int q) {
+    return K == 0 ? 43 + q : (q < kTri ? q : (q < kTri + K ? 36 + (q - kTri) : 44 + (q - kTri - K)));
+  }
+};
+
+// One reference-frame sample of a pass: its residual goes into the
+// histogram, and unless the mask drops it, into the pass's accumulators.
+template <int INTERP, int K, bool UNROLL>
+__device__ __forceinline__ void gn_sample(const GnArgs& a, const AffineCoef& coef, const float* ref, const float* mov,
+                                          int x, int y, float alpha, float beta, float clip, float sigma,
+                                          unsigned* s_hist, float (&acc)[GnLayout<K>::kAcc]) {
+  const int W = a.width, H = a.height;
+  const float fW = static_cast<float>(W), fH = static_cast<float>(H);
+  const float* rp = ref + static_cast<int64_t>(y) * W + x;
+  const float av = __ldg(rp);
+  if (!isfinite(av)) return;
+  FFv sx, sy;
+  source_coord(coef, static_cast<float>(x), static_cast<float>(y), sx, sy);
+  const bool inside = INTERP == GG_INTERP_BILINEAR
+                          ? (ff_ge(sx, 0.0f) && ff_le(sx, fW - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, fH - 1.0f))
+                          : (ff_ge(sx, 2.0f) && ff_lt(sx, fW - 3.0f) && ff_ge(sy, 2.0f) && ff_lt(sy, fH - 3.0f));
+  if (!inside) return;
+  int x0, y0;
+  float tx, ty;
+  ff_floor_frac(sx, x0, tx);
+  ff_floor_frac(sy, y0, ty);
+  float O, Ox, Oy;
+  bool ok;
+  if constexpr (INTERP == GG_INTERP_BILINEAR)
+    ok = bilinear_value_grad(mov, W, H, x0, y0, tx, ty, O, Ox, Oy);
+  else
+    ok = lanczos3_value_grad<UNROLL>(mov, W, x0, y0, tx, ty, O, Ox, Oy);
+  if (!ok) return;
+  const float r = O - alpha * av - beta;
+  atomicAdd(&s_hist[residual_bin(r)], 1u);
+  float ga = 0.0f;
+  if (x > 0 && x < W - 1 && y > 0 && y < H - 1) {
+    ga = 0.5f * fmaxf(fabsf(__ldg(rp + 1) - __ldg(rp - 1)), fabsf(__ldg(rp + W) - __ldg(rp - W)));
+    if (!isfinite(ga)) ga = 0.0f;
+  }
+  const float gb = fmaxf(fabsf(Ox), fabsf(Oy));
+  const float allow = clip + a.shift_px * fminf(fabsf(alpha) * ga, gb);
+  if (!(fabsf(r) <= allow)) return;
+  // structure the reference lacks (a cosmic ray's interpolation ringing:
+  // small residual, large Jacobian) fails the gradient-consistency test
+  if (!(gb <= kGnGradFactor * fabsf(alpha) * ga + kGnGradSigmas * sigma)) return;
+  if constexpr (K == 0) {
+    acc[0] = __fmaf_rn(-1.0f, r, acc[0]);
+    acc[1] = __fmaf_rn(r, r, acc[1]);
+    acc[2] += 1.0f;
+  } else {
+    const float xt = (static_cast<float>(x) - a.cx) * a.inv_r, yt = (static_cast<float>(y) - a.cy) * a.inv_r;
+    float J[K];
+    if constexpr (K == 8) {
+      J[0] = Ox * xt, J[1] = Ox * yt, J[2] = Ox, J[3] = Oy * xt, J[4] = Oy * yt, J[5] = Oy;
+    } else if constexpr (K == 6) {
+      J[0] = Ox, J[1] = Oy;
+      J[2] = __fmaf_rn(Oy, yt, Ox * xt);   // scale: columns 0 + 4
+      J[3] = __fmaf_rn(Oy, xt, -Ox * yt);  // rotation: columns 3 - 1
+    } else {
+      J[0] = Ox, J[1] = Oy;
+    }
+    J[K - 2] = -av;
+    J[K - 1] = -1.0f;
+    int q = 0;
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+      for (int j = i; j < K; ++j) {
+        acc[q] = __fmaf_rn(J[i], J[j], acc[q]);
+        ++q;
+      }
+#pragma unroll
+    for (int i = 0; i < K; ++i) acc[GnLayout<K>::kTri + i] = __fmaf_rn(J[i], r, acc[GnLayout<K>::kTri + i]);
+    acc[GnLayout<K>::kTri + K] = __fmaf_rn(r, r, acc[GnLayout<K>::kTri + K]);
+    acc[GnLayout<K>::kTri + K + 1] += 1.0f;
+  }
+}
+
+// Three CTAs per SM for the statistics and projected passes (at most a few
+// bytes of spills); the 46 accumulators of the full pass keep the compiler's
+// register count.
+template <int INTERP, int K, bool UNROLL>
+__global__ void __launch_bounds__(kGnThreads, K == 8 ? 1 : 3) gn_accumulate_kernel(GnArgs a) {
+  using L = GnLayout<K>;
   __shared__ AffineCoef s_coef;
   __shared__ float s_phot[3];
   __shared__ int s_run;
-  __shared__ double s_red[kGnThreads / 32][kGnSums];
+  __shared__ double s_red[kGnThreads / 32][L::kAcc];
   __shared__ unsigned s_hist[kGnBins];
   const int job = blockIdx.y;
   for (int b = threadIdx.x; b < kGnBins; b += blockDim.x) s_hist[b] = 0u;
@@ -114,77 +212,32 @@ __global__ void __launch_bounds__(kGnThreads) gn_accumulate_kernel(GnArgs a) {
   const int2 jb = a.jobs[job];
   const float* ref = a.slots + static_cast<int64_t>(a.slot_of_frame[jb.x]) * a.stride;
   const float* mov = a.slots + static_cast<int64_t>(a.slot_of_frame[jb.y]) * a.stride;
-  const int W = a.width, H = a.height;
-  const float alpha = s_phot[0], beta = s_phot[1];
-  const float clip = a.clip_sigma * s_phot[2];  // +inf in the first statistics pass
-  const float fW = static_cast<float>(W), fH = static_cast<float>(H);
-  float acc[kGnUsed];
+  const float alpha = s_phot[0], beta = s_phot[1], sigma = s_phot[2];
+  const float clip = a.clip_sigma * sigma;  // +inf in the first statistics pass
+  float acc[L::kAcc];
 #pragma unroll
-  for (int q = 0; q < kGnUsed; ++q) acc[q] = 0.0f;
+  for (int q = 0; q < L::kAcc; ++q) acc[q] = 0.0f;
   const int64_t items = static_cast<int64_t>(a.nsx) * a.nsy;
   for (int64_t it = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; it < items;
        it += static_cast<int64_t>(a.blocks_per_job) * blockDim.x) {
     const int iy = static_cast<int>(it / a.nsx), ix = static_cast<int>(it - static_cast<int64_t>(iy) * a.nsx);
-    const int x = ix * a.sample_stride, y = iy * a.sample_stride;
-    const float* rp = ref + static_cast<int64_t>(y) * W + x;
-    const float av = __ldg(rp);
-    if (!isfinite(av)) continue;
-    FFv sx, sy;
-    source_coord(s_coef, static_cast<float>(x), static_cast<float>(y), sx, sy);
-    const bool inside = INTERP == GG_INTERP_BILINEAR
-                            ? (ff_ge(sx, 0.0f) && ff_le(sx, fW - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, fH - 1.0f))
-                            : (ff_ge(sx, 2.0f) && ff_lt(sx, fW - 3.0f) && ff_ge(sy, 2.0f) && ff_lt(sy, fH - 3.0f));
-    if (!inside) continue;
-    int x0, y0;
-    float tx, ty;
-    ff_floor_frac(sx, x0, tx);
-    ff_floor_frac(sy, y0, ty);
-    float O, Ox, Oy;
-    const bool ok = INTERP == GG_INTERP_BILINEAR ? bilinear_value_grad(mov, W, H, x0, y0, tx, ty, O, Ox, Oy)
-                                                 : lanczos3_value_grad(mov, W, x0, y0, tx, ty, O, Ox, Oy);
-    if (!ok) continue;
-    const float r = O - alpha * av - beta;
-    atomicAdd(&s_hist[residual_bin(r)], 1u);
-    float ga = 0.0f;
-    if (x > 0 && x < W - 1 && y > 0 && y < H - 1) {
-      ga = 0.5f * fmaxf(fabsf(__ldg(rp + 1) - __ldg(rp - 1)), fabsf(__ldg(rp + W) - __ldg(rp - W)));
-      if (!isfinite(ga)) ga = 0.0f;
-    }
-    const float gb = fmaxf(fabsf(Ox), fabsf(Oy));
-    const float allow = clip + a.shift_px * fminf(fabsf(alpha) * ga, gb);
-    if (!(fabsf(r) <= allow)) continue;
-    // structure the reference lacks (a cosmic ray's interpolation ringing:
-    // small residual, large Jacobian) fails the gradient-consistency test
-    if (!(gb <= kGnGradFactor * fabsf(alpha) * ga + kGnGradSigmas * s_phot[2])) continue;
-    const float xt = (static_cast<float>(x) - a.cx) * a.inv_r, yt = (static_cast<float>(y) - a.cy) * a.inv_r;
-    const float J[8] = {Ox * xt, Ox * yt, Ox, Oy * xt, Oy * yt, Oy, -av, -1.0f};
-    int q = 0;
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = i; j < 8; ++j) {
-        acc[q] = __fmaf_rn(J[i], J[j], acc[q]);
-        ++q;
-      }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) acc[36 + i] = __fmaf_rn(J[i], r, acc[36 + i]);
-    acc[44] = __fmaf_rn(r, r, acc[44]);
-    acc[45] += 1.0f;
+    gn_sample<INTERP, K, UNROLL>(a, s_coef, ref, mov, ix * a.sample_stride, iy * a.sample_stride, alpha, beta,
+                                 clip, sigma, s_hist, acc);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int q = 0; q < kGnUsed; ++q) {
+  for (int q = 0; q < L::kAcc; ++q) {
     double d = static_cast<double>(acc[q]);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
     if (lane == 0) s_red[warp][q] = d;
   }
   __syncthreads();
-  if (threadIdx.x < kGnUsed) {
+  if (threadIdx.x < L::kAcc) {
     double t = 0.0;
 #pragma unroll
     for (int w = 0; w < kGnThreads / 32; ++w) t += s_red[w][threadIdx.x];
-    a.partials[(static_cast<int64_t>(job) * a.blocks_per_job + blockIdx.x) * kGnSums + threadIdx.x] = t;
+    a.partials[(static_cast<int64_t>(job) * a.blocks_per_job + blockIdx.x) * kGnSums + L::slot(threadIdx.x)] = t;
   }
   for (int b = threadIdx.x; b < kGnBins; b += blockDim.x)
     if (s_hist[b]) atomicAdd(&a.hist[static_cast<int64_t>(job) * kGnBins + b], s_hist[b]);
@@ -273,31 +326,24 @@ __global__ void gn_solve_kernel(GnArgs a, int mode, int model, double min_sample
     st.sigma = robust_sigma + 1.0e-12;
     return;
   }
-  // unpack J^T J and J^T r
+  // unpack J^T J and J^T r: already projected on the model's k columns by
+  // the pass (translation, similarity), or all 8 columns (affine: P = I)
+  float P[8][8];
+  const int k = model_columns(model, P);
+  const int kc = model == GG_TRANSFORM_AFFINE ? 8 : k;
   double H[8][8], g[8];
   int q = 0;
-  for (int i = 0; i < 8; ++i)
-    for (int j = i; j < 8; ++j) {
+  for (int i = 0; i < kc; ++i)
+    for (int j = i; j < kc; ++j) {
       H[i][j] = s[q];
       H[j][i] = s[q];
       ++q;
     }
-  for (int i = 0; i < 8; ++i) g[i] = s[36 + i];
-  float P[8][8];
-  const int k = model_columns(model, P);
+  for (int i = 0; i < kc; ++i) g[i] = s[36 + i];
   double A[8][8], b[8];
   for (int i = 0; i < k; ++i) {
-    double bi = 0.0;
-    for (int u = 0; u < 8; ++u) bi -= P[u][i] * g[u];
-    b[i] = bi;
-    for (int j = 0; j < k; ++j) {
-      double t = 0.0;
-      for (int u = 0; u < 8; ++u) {
-        if (P[u][i] == 0.0f) continue;
-        for (int v = 0; v < 8; ++v) t += P[u][i] * H[u][v] * P[v][j];
-      }
-      A[i][j] = t;
-    }
+    b[i] = -g[i];
+    for (int j = 0; j < k; ++j) A[i][j] = H[i][j];
   }
   // damped Cholesky solve (A + 1e-10 diag(A)) d = b
   for (int i = 0; i < k; ++i) A[i][i] *= 1.0 + 1.0e-10;
@@ -458,9 +504,8 @@ static GnPlan gn_prepare(gg_stack* s, int64_t reference_index, const int64_t* mo
   plan.interp = interp;
   const int64_t nsx = (s->width + sample_stride - 1) / sample_stride;
   const int64_t nsy = (s->height + sample_stride - 1) / sample_stride;
-  const int64_t samples = nsx * nsy;
-  const int want = std::max(1, (sm_count() * 4 + plan.jobs - 1) / plan.jobs);
-  const int bpj = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(want, (samples + 1023) / 1024)));
+  // partial sums for up to two waves of 8 resident CTAs per SM
+  const int bpj = std::max(1, (2 * 8 * sm_count() + plan.jobs - 1) / plan.jobs);
   GnScratch& g = gn_scratch(s, plan.jobs, bpj);
   std::vector<int2> jobs(static_cast<size_t>(count));
   for (int64_t k = 0; k < count; ++k) jobs[k] = make_int2(static_cast<int>(reference_index), static_cast<int>(moving[k]));
@@ -494,18 +539,74 @@ static GnPlan gn_prepare(gg_stack* s, int64_t reference_index, const int64_t* mo
   return plan;
 }
 
-static void gn_accumulate(gg_stack* s, const GnPlan& plan, int sample_stride) {
+using GnKernelFn = void (*)(GnArgs);
+
+template <int K>
+static GnKernelFn gn_kernel_k(int interp, bool unroll) {
+  if (interp == GG_INTERP_BILINEAR) return gn_accumulate_kernel<GG_INTERP_BILINEAR, K, false>;
+  return unroll ? gn_accumulate_kernel<GG_INTERP_LANCZOS3, K, true> : gn_accumulate_kernel<GG_INTERP_LANCZOS3, K, false>;
+}
+
+static GnKernelFn gn_kernel(int interp, int K, bool unroll) {
+  switch (K) {
+    case 0: return gn_kernel_k<0>(interp, unroll);
+    case 4: return gn_kernel_k<4>(interp, unroll);
+    case 6: return gn_kernel_k<6>(interp, unroll);
+    default: return gn_kernel_k<8>(interp, unroll);
+  }
+}
+
+// Blocks per job: whole waves of the kernel's resident CTAs (the first count
+// that fills at least 98 % of its last wave, unless a later wave count fills
+// noticeably more), at most `cap` and at least two samples per thread.
+static int gn_blocks_per_job(GnKernelFn fn, int jobs, int64_t samples, int cap) {
+  int occ = 0;
+  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kGnThreads, 0), "cudaOccupancy(gn_accumulate)");
+  const int64_t resident = static_cast<int64_t>(std::max(occ, 1)) * sm_count();
+  const int64_t limit = std::max<int64_t>(1, std::min<int64_t>(cap, (samples + 2 * kGnThreads - 1) / (2 * kGnThreads)));
+  const int64_t bmax = std::min<int64_t>(limit, std::max<int64_t>(1, (2 * resident + jobs - 1) / jobs));
+  int64_t best = 1;
+  double best_eff = -1.0;
+  for (int64_t b = 1; b <= bmax; ++b) {
+    const int64_t total = b * jobs;
+    const int64_t waves = (total + resident - 1) / resident;
+    const double eff = static_cast<double>(total) / static_cast<double>(waves * resident);
+    if (eff > best_eff + 0.02) {
+      best_eff = eff;
+      best = b;
+    }
+  }
+  return static_cast<int>(best);
+}
+
+// One pass over the samples: K = 0 statistics, else the model's projected
+// columns (see GnLayout).  Lanczos3 passes tune row-by-row against
+// whole-window tap loads per shape.
+static void gn_accumulate(gg_stack* s, GnPlan& plan, int sample_stride, int K) {
   GnArgs a = plan.args;
   a.sample_stride = sample_stride;
   a.nsx = static_cast<int>((s->width + sample_stride - 1) / sample_stride);
   a.nsy = static_cast<int>((s->height + sample_stride - 1) / sample_stride);
-  const dim3 grid(static_cast<unsigned>(a.blocks_per_job), static_cast<unsigned>(plan.jobs));
-  note_launch();
-  if (plan.interp == GG_INTERP_BILINEAR)
-    gn_accumulate_kernel<GG_INTERP_BILINEAR><<<grid, kGnThreads, 0, s->stream>>>(a);
-  else
-    gn_accumulate_kernel<GG_INTERP_LANCZOS3><<<grid, kGnThreads, 0, s->stream>>>(a);
-  check_cuda(cudaGetLastError(), "gn_accumulate launch");
+  const int64_t samples = static_cast<int64_t>(a.nsx) * a.nsy;
+  GnScratch& g = *static_cast<GnScratch*>(s->gn_scratch);
+  auto run = [&](int variant) {
+    GnKernelFn fn = gn_kernel(plan.interp, K, variant == 1);
+    a.blocks_per_job = gn_blocks_per_job(fn, plan.jobs, samples, g.block_cap);
+    check_cuda(cudaMemsetAsync(g.hist, 0, sizeof(unsigned) * kGnBins * plan.jobs, s->stream),
+               "cudaMemsetAsync(gradient refine histogram)");
+    const dim3 grid(static_cast<unsigned>(a.blocks_per_job), static_cast<unsigned>(plan.jobs));
+    note_launch();
+    fn<<<grid, kGnThreads, 0, s->stream>>>(a);
+    check_cuda(cudaGetLastError(), "gn_accumulate launch");
+  };
+  int variant = 0;
+  if (plan.interp == GG_INTERP_LANCZOS3) {
+    const std::string shape = std::to_string(plan.jobs) + " jobs x " + std::to_string(samples) + " samples, " +
+                              std::to_string(K) + " columns";
+    variant = autotune_choose("gn_accumulate taps", shape, {"rows", "window"}, 0, s->stream, run);
+  }
+  run(variant);
+  plan.args.blocks_per_job = a.blocks_per_job;
 }
 
 static void gn_solve(gg_stack* s, const GnPlan& plan, int mode, int model, int min_samples, double tol,
@@ -547,13 +648,16 @@ int gg_stack_refine_gradient(gg_stack* s, int64_t reference_index, const int64_t
   }
   GnPlan plan = gn_prepare(s, reference_index, moving, count, states, p.interpolation, p.sample_stride,
                            p.clip_sigma, p.mask_shift_px);
+  const int model_k = p.transform_model == GG_TRANSFORM_TRANSLATION ? 4
+                      : p.transform_model == GG_TRANSFORM_SIMILARITY ? 6
+                                                                      : 8;
   // statistics passes on a grid twice as coarse (photometric offset and noise)
   for (int k = 0; k < p.stats_passes; ++k) {
-    gn_accumulate(s, plan, std::min(2 * p.sample_stride, 64));
+    gn_accumulate(s, plan, std::min(2 * p.sample_stride, 64), 0);
     gn_solve(s, plan, 0, p.transform_model, p.min_samples, p.tolerance_px, p.max_step_px, 0);
   }
   for (int k = 0; k < p.iterations; ++k) {
-    gn_accumulate(s, plan, p.sample_stride);
+    gn_accumulate(s, plan, p.sample_stride, model_k);
     gn_solve(s, plan, 1, p.transform_model, p.min_samples, p.tolerance_px, p.max_step_px,
              k == p.iterations - 1 ? 1 : 0);
   }
@@ -614,7 +718,7 @@ int gg_stack_gradient_normal_equations(gg_stack* s, int64_t reference_index, con
   }
   GnPlan plan = gn_prepare(s, reference_index, moving, count, states, params->interpolation,
                            params->sample_stride, params->clip_sigma, params->mask_shift_px);
-  gn_accumulate(s, plan, params->sample_stride);
+  gn_accumulate(s, plan, params->sample_stride, 8);
   gn_solve(s, plan, 2, params->transform_model, params->min_samples, 0.0, 1.0, 0);
   GnScratch& g = *static_cast<GnScratch*>(s->gn_scratch);
   check_cuda(cudaMemcpyAsync(host_sums, g.sums, sizeof(double) * kGnSums * count, cudaMemcpyDeviceToHost, s->stream),

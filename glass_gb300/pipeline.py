@@ -155,14 +155,22 @@ class ResidentPipeline:
         _lib.call("gg_stack_calibrate_u16", self.stack.handle, _lib.ptr(self._indices),
                   ctypes.c_int64(self.frames), _lib.ptr(host_raw), 0, ctypes.byref(self._calib_params()))
 
-    def detect(self) -> None:
-        """Star catalogs of every frame; they stay on the device for register()."""
+    def detect(self, info: bool = False) -> list[dict] | None:
+        """Star catalogs of every frame; they stay on the device for register().
+        info=True also returns each frame's background statistics and
+        candidate count (and raises when a frame's candidates overflow)."""
         cfg = self.config
         params = _lib.StarParams(float(cfg.star_threshold_sigma), int(cfg.star_max_stars), 4, 2.0, np.nan, np.nan,
                                  float(cfg.catalog_min_fwhm), float(cfg.catalog_max_eccentricity),
                                  int(cfg.background_mesh_cell))
+        host_info = (_lib.StarFrameInfo * self.frames)() if info else None
+        counts = np.zeros(self.frames, dtype=np.int32) if info else None
         _lib.call("gg_stack_detect_stars", self.stack.handle, _lib.ptr(self._indices), ctypes.c_int64(self.frames),
-                  ctypes.byref(params), None, None, None)
+                  ctypes.byref(params), None, None if counts is None else _lib.ptr(counts), host_info)
+        if not info:
+            return None
+        return [{"frame": k, "median": float(r.median), "noise": float(r.noise), "threshold": float(r.threshold),
+                 "candidates": int(r.candidates), "stars": int(counts[k])} for k, r in enumerate(host_info)]
 
     def register(self, reference_index: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """Triangle registration of every frame to the reference frame from the
@@ -182,6 +190,11 @@ class ResidentPipeline:
                 ok[k] = out[pos].status == 1
                 if ok[k]:
                     matrices[k] = np.asarray(out[pos].matrix, dtype=np.float64).reshape(3, 3)
+            self.last_registration = [
+                {"frame": int(k), "status": int(r.status), "inliers": int(r.inliers), "matches": int(r.matches),
+                 "descriptors_reference": int(r.descriptors_reference),
+                 "descriptors_moving": int(r.descriptors_moving), "rms_px": float(r.rms_px)}
+                for k, r in zip(idx, out)]
         self._registered = ok
         return matrices, ok
 
