@@ -421,6 +421,13 @@ def graph_report(pipe, dev_raw, matrices, stream, reps: int) -> dict:
             "mpix_frames_per_s_graph": pipe.frames * pipe.height * pipe.width / 1e6 / (graph_ms / 1e3)}
 
 
+def refinement_by(results: list, frame: int) -> dict:
+    for r in results:
+        if r.get("frame") == frame:
+            return r
+    return {}
+
+
 def run_c5(args) -> int:
     """The full c5 stack resident on one GPU: 200 frames of 9600 x 6422
     (49.3 GB of float32 frames).  Eight distinct seeded raw frames are
@@ -499,10 +506,14 @@ def run_c5(args) -> int:
     ok = [k for k in range(1, n) if reg["ok"][k]]
     from glass_gb300.adjoint import registration_rms_px
 
+    calibrate()  # detection statistics of the calibrated (not the warped) frames
     info = pipe.detect(info=True)
     inliers = [r["inliers"] for r in pipe.last_registration]
     rms_tri = registration_rms_px([reg["triangle"][k] for k in ok], [truth[k] for k in ok], h, w)
     rms_gn = registration_rms_px([reg["m"][k] for k in ok], [truth[k] for k in ok], h, w)
+    refinement = getattr(pipe, "last_refinement", [])
+    per_frame = sorted(((registration_rms_px([reg["m"][k]], [truth[k]], h, w),
+                         registration_rms_px([reg["triangle"][k]], [truth[k]], h, w), k) for k in ok), reverse=True)
 
     line = {"metric": "stacked Mpix-frames/s", "value": n * P / 1e6 / (ms / 1e3), "unit": "Mpix-frames/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -522,7 +533,15 @@ def run_c5(args) -> int:
                           "catalog_stars_min": min(r["stars"] for r in info)},
             "registration": {"frames_ok": len(ok) + 1, "frames": n,
                              "inliers_median": float(np.median(inliers)) if inliers else None,
-                             "rms_px_vs_truth": {"triangle": rms_tri, "gradient_gauss_newton": rms_gn}}}
+                             "rms_px_vs_truth": {"triangle": rms_tri, "gradient_gauss_newton": rms_gn},
+                             "refine_status": {str(v): sum(1 for r in refinement if r.get("status") == v)
+                                               for v in sorted({r.get("status") for r in refinement})},
+                             "refine_iterations_mean": (float(np.mean([r["iterations"] for r in refinement]))
+                                                        if refinement else None),
+                             "worst_frames": [{"frame": k, "gradient_px": g, "triangle_px": t,
+                                               **{q: refinement_by(refinement, k).get(q)
+                                                  for q in ("status", "iterations", "alpha", "sigma", "samples")}}
+                                              for g, t, k in per_frame[:6]]}}
     print(json.dumps(line))
     pipe.close()
     return 0

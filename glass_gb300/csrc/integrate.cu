@@ -938,6 +938,312 @@ __global__ void __launch_bounds__(T) integrate_smem_kernel(IntegrateArgs a) {
   }
 }
 
+// ---- kernel W: 32 < N <= 32 * NPL, one warp per pixel ------------------------
+// A CTA stages a tile of kWarpTilePx consecutive pixels of every frame in
+// shared memory ([frame][pixel], rows padded to kWarpTilePx + 1 floats so a
+// warp reading one pixel's column is bank-conflict free; every frame row is
+// one coalesced 128 B load), then each warp takes one pixel at a time.  The
+// column is spread over the lanes (NPL values per lane), sorted by a
+// warp-wide bitonic network (in-register steps within a lane, shuffles
+// across lanes), and every sum of the statistics and of the integration is a
+// per-lane float-float sum combined across the warp.  The shared-memory cost
+// is 4 * 33 B per frame instead of a sorted column per thread, so an SM keeps
+// tens of warps in flight at N = 200.
+constexpr int kWarpTilePx = 32;
+constexpr int kWarpTileRow = kWarpTilePx + 1;
+constexpr int kWarpThreads = 256;
+
+// (hi, lo) float-float sum of the whole warp, in every lane.  TwoSum is exact
+// and symmetric, so both partners of each butterfly step hold the same pair.
+__device__ __forceinline__ void ff_warp_reduce(FF& s) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, s.hi, off);
+    const float ol = __shfl_xor_sync(0xffffffffu, s.lo, off);
+    float h, e;
+    two_sum(s.hi, oh, h, e);
+    s.hi = h;
+    s.lo = __fadd_rn(__fadd_rn(s.lo, ol), e);
+  }
+}
+
+// Ascending bitonic sort of the warp's 32 * NPL values; rank e lives in lane
+// e / NPL, register e % NPL.
+template <int NPL>
+__device__ __forceinline__ void warp_bitonic_sort(float (&v)[NPL], int lane) {
+  constexpr int LOGM = (NPL == 2) ? 6 : (NPL == 4) ? 7 : (NPL == 8) ? 8 : 9;
+  static_assert((32 * NPL) == (1 << LOGM), "NPL must be 2, 4, 8 or 16");
+#pragma unroll
+  for (int ls = 1; ls <= LOGM; ++ls) {
+#pragma unroll
+    for (int lj = ls - 1; lj >= 0; --lj) {
+      const int size = 1 << ls, j = 1 << lj;
+      if (j >= NPL) {
+        const int lm = j / NPL;
+        const bool up = ((lane * NPL) & size) == 0;  // always true in the last merge
+        const bool keep_min = ((lane & lm) == 0) == up;
+#pragma unroll
+        for (int k = 0; k < NPL; ++k) {
+          const float o = __shfl_xor_sync(0xffffffffu, v[k], lm);
+          v[k] = keep_min ? fminf(v[k], o) : fmaxf(v[k], o);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < NPL; ++k) {
+          if ((k ^ j) > k) {
+            const int q = k ^ j;
+            const bool up = ((lane * NPL + k) & size) == 0;
+            const float lo = fminf(v[k], v[q]), hi = fmaxf(v[k], v[q]);
+            v[k] = up ? lo : hi;
+            v[q] = up ? hi : lo;
+          }
+        }
+      }
+    }
+  }
+}
+
+// Value of warp-uniform rank i.
+template <int NPL>
+__device__ __forceinline__ float warp_rank(const float (&v)[NPL], int i) {
+  const int k = i % NPL;
+  float t = v[0];
+#pragma unroll
+  for (int q = 1; q < NPL; ++q)
+    if (q == k) t = v[q];
+  return __shfl_sync(0xffffffffu, t, i / NPL);
+}
+
+// percentile_valid / percentile_all on the warp's sorted column.
+template <int NPL>
+__device__ __forceinline__ float warp_percentile_valid(const float (&v)[NPL], int cnt, float fraction) {
+  if (cnt <= 0) return 0.0f;
+  const float pos = __fmul_rn(static_cast<float>(cnt - 1), fraction);
+  const int lower = static_cast<int>(floorf(pos));
+  const int upper = min(lower + 1, cnt - 1);
+  const float t = __fsub_rn(pos, static_cast<float>(lower));
+  const float lv = warp_rank(v, lower);
+  const float uv = warp_rank(v, upper);
+  return __fadd_rn(__fmul_rn(lv, __fsub_rn(1.0f, t)), __fmul_rn(uv, t));
+}
+
+template <int NPL>
+__device__ __forceinline__ float warp_percentile_all(const float (&v)[NPL], int n, float percent) {
+  if (n == 1) return warp_rank(v, 0);
+  const float pos = __fmul_rn(__fdiv_rn(percent, 100.0f), static_cast<float>(n - 1));
+  const int lower = static_cast<int>(floorf(pos));
+  const int upper = static_cast<int>(ceilf(pos));
+  const float f = __fsub_rn(pos, static_cast<float>(lower));
+  const float lv = warp_rank(v, lower);
+  if (upper == lower) return lv;
+  const float uv = warp_rank(v, upper);
+  return __fadd_rn(lv, __fmul_rn(__fsub_rn(uv, lv), f));
+}
+
+// Mean (hi, lo) and float-float squared deviations of the valid ranks after
+// clipping to [lo, hi] (+-inf: no clipping); the two passes of std_of_valid
+// and winsorized_stats.
+template <int NPL>
+__device__ __forceinline__ float warp_clipped_std(const float (&v)[NPL], int lane, int cnt, bool allvalid, float lo,
+                                                  float hi, float& mean_out) {
+  FF s1;
+#pragma unroll
+  for (int k = 0; k < NPL; ++k)
+    if (lane * NPL + k < cnt) s1.add(clipf(v[k], lo, hi));
+  ff_warp_reduce(s1);
+  float mh, ml;
+  if (allvalid) {
+    ff_div_pair(s1.hi, s1.lo, static_cast<float>(cnt), mh, ml);
+    mean_out = __fadd_rn(mh, ml);
+  } else {
+    mh = ff_div_f32(s1.hi, s1.lo, static_cast<float>(cnt));
+    ml = 0.0f;
+    mean_out = mh;
+  }
+  FF sv;
+#pragma unroll
+  for (int k = 0; k < NPL; ++k)
+    if (lane * NPL + k < cnt) ff_add_sqdev(sv, clipf(v[k], lo, hi), mh, ml);
+  ff_warp_reduce(sv);
+  float q, ql;
+  ff_div_pair(sv.hi, sv.lo, static_cast<float>(cnt), q, ql);
+  return ff_sqrt_f32(q, ql);
+}
+
+template <int NPL>
+__global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateArgs a) {
+  extern __shared__ float tile[];  // [frames][kWarpTileRow]
+  __shared__ FrameTable<32 * NPL> tab;
+  load_frame_table<32 * NPL>(a, tab);
+  const bool allvalid = tab.allvalid != 0;
+  const bool unit = tab.unit != 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int N = a.frames;
+  const int64_t P = a.pixels;
+  const int64_t tiles = (P + kWarpTilePx - 1) / kWarpTilePx;
+  const float ls = a.low_sigma, hs = a.high_sigma;
+  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int64_t p0 = t * kWarpTilePx;
+    __syncthreads();  // the previous tile's columns are consumed
+    for (int i = threadIdx.x; i < N * kWarpTilePx; i += kWarpThreads) {
+      const int f = i / kWarpTilePx, px = i - f * kWarpTilePx;
+      const int64_t p = p0 + px;
+      tile[f * kWarpTileRow + px] = p < P ? __ldcs(tab.base[f] + p) : 0.0f;
+    }
+    __syncthreads();
+    for (int px = warp; px < kWarpTilePx; px += kWarpThreads / 32) {
+      const int64_t p = p0 + px;
+      if (p >= P) break;
+      const float* col = tile + px;
+      // column: lane l holds frames l, l + 32, ... (+inf when invalid)
+      float v[NPL];
+      int c = 0;
+#pragma unroll
+      for (int k = 0; k < NPL; ++k) {
+        const int f = k * 32 + lane;
+        const float x = f < N ? col[f * kWarpTileRow] : kInf;
+        const bool ok = f < N && tab.w[f] > 0.0f && isfinite(x);
+        v[k] = ok ? x : kInf;
+        c += ok ? 1 : 0;
+      }
+      const int cnt = __reduce_add_sync(0xffffffffu, c);
+      int nl = 0, nh = 0;
+      float lt = -kInf, ht = kInf;
+      bool use_thresholds = false;
+      if (a.rejection != GG_REJECT_NONE) {
+        warp_bitonic_sort<NPL>(v, lane);
+        CenterScale cs{0.0f, 0.0f};
+        if (cnt > 0 && a.rejection == GG_REJECT_WINSORIZED) {
+          float med, q25, q75;
+          if (allvalid) {
+            med = warp_percentile_all(v, N, 50.0f);
+            q25 = warp_percentile_all(v, N, 25.0f);
+            q75 = warp_percentile_all(v, N, 75.0f);
+          } else {
+            med = warp_percentile_valid(v, cnt, 0.5f);
+            q25 = warp_percentile_valid(v, cnt, 0.25f);
+            q75 = warp_percentile_valid(v, cnt, 0.75f);
+          }
+          float scale1 = __fdiv_rn(__fsub_rn(q75, q25), 1.349f);
+          const bool ok1 = allvalid ? (scale1 > 0.0f) : (scale1 > 0.0f && isfinite(scale1));
+          float unused;
+          if (!ok1) scale1 = warp_clipped_std(v, lane, cnt, allvalid, -kInf, kInf, unused);
+          const float lo1 = __fsub_rn(med, __fmul_rn(ls, scale1));
+          const float hi1 = __fadd_rn(med, __fmul_rn(hs, scale1));
+          const float scale = warp_clipped_std(v, lane, cnt, allvalid, lo1, hi1, cs.center);
+          const bool ok2 = allvalid ? (scale > 0.0f) : (scale > 0.0f && isfinite(scale));
+          cs.scale = ok2 ? scale : scale1;
+        } else if (cnt > 0) {
+          // sigma clip: median, then float32 frame-order sums (sequential, as
+          // NumPy reduces over the frame axis)
+          const int h = cnt / 2;
+          const int l = (cnt & 1) ? h : h - 1;
+          cs.center = __fmul_rn(__fadd_rn(warp_rank(v, l), warp_rank(v, h)), 0.5f);
+          float scale = 0.0f;
+          if (lane == 0) {
+            float sum = 0.0f;
+            for (int f = 0; f < N; ++f) {
+              const float x = col[f * kWarpTileRow];
+              if (tab.w[f] > 0.0f && isfinite(x)) sum = __fadd_rn(sum, x);
+            }
+            const float mean = __fdiv_rn(sum, static_cast<float>(cnt));
+            float var = 0.0f;
+            for (int f = 0; f < N; ++f) {
+              const float x = col[f * kWarpTileRow];
+              if (tab.w[f] > 0.0f && isfinite(x)) {
+                const float d = __fsub_rn(x, mean);
+                var = __fadd_rn(var, __fmul_rn(d, d));
+              }
+            }
+            scale = __fsqrt_rn(__fdiv_rn(var, static_cast<float>(cnt)));
+          }
+          cs.scale = __shfl_sync(0xffffffffu, scale, 0);
+        }
+        lt = __fsub_rn(cs.center, __fmul_rn(ls, cs.scale));
+        ht = __fadd_rn(cs.center, __fmul_rn(hs, cs.scale));
+        int cl = 0, ch = 0;
+#pragma unroll
+        for (int k = 0; k < NPL; ++k) {
+          if (lane * NPL + k < cnt) {
+            cl += v[k] < lt;
+            ch += v[k] > ht;
+          }
+        }
+        nl = __reduce_add_sync(0xffffffffu, cl);
+        nh = __reduce_add_sync(0xffffffffu, ch);
+        use_thresholds = true;
+        if (nl + nh > 0) {
+          // cpu/integration.py:85-99
+          const int rej = nl + nh;
+          const float frac = __fdiv_rn(static_cast<float>(rej), static_cast<float>(cnt));
+          if (!((cnt - rej >= a.min_samples) && (frac <= a.max_frac))) {
+            nl = nh = 0;
+            use_thresholds = false;
+          }
+        }
+      }
+      float master = 0.0f, weight = 0.0f;
+      int kept = 0;
+      if (unit && a.rejection != GG_REJECT_NONE) {
+        FF ws;
+#pragma unroll
+        for (int k = 0; k < NPL; ++k) {
+          const float x = v[k];
+          if (lane * NPL + k < cnt && !(use_thresholds && (x < lt || x > ht))) {
+            ws.add(x);
+            ++kept;
+          }
+        }
+        ff_warp_reduce(ws);
+        kept = __reduce_add_sync(0xffffffffu, kept);
+        if (kept > 0) {
+          master = ff_div_f32(ws.hi, ws.lo, static_cast<float>(kept));
+          weight = static_cast<float>(kept);
+        }
+      } else {
+        FF ws, wsum;
+#pragma unroll
+        for (int k = 0; k < NPL; ++k) {
+          const int f = k * 32 + lane;
+          if (f < N) {
+            const float x = col[f * kWarpTileRow];
+            const float w = tab.w[f];
+            if (w > 0.0f && isfinite(x) && !(use_thresholds && (x < lt || x > ht))) {
+              ws.add_prod(x, w);
+              wsum.add(w);
+              ++kept;
+            }
+          }
+        }
+        ff_warp_reduce(ws);
+        ff_warp_reduce(wsum);
+        kept = __reduce_add_sync(0xffffffffu, kept);
+        if (kept > 0 && wsum.hi > 0.0f) {
+          master = ff_div_ff(ws.hi, ws.lo, wsum.hi, wsum.lo);
+          weight = wsum.value_f32();
+        }
+      }
+      if (lane == 0) write_outputs(a, p, master, weight, kept, nl, nh, tab.active);
+    }
+  }
+}
+
+template <int NPL>
+static void launch_warp(const IntegrateArgs& args, cudaStream_t stream) {
+  const size_t smem = static_cast<size_t>(args.frames) * kWarpTileRow * sizeof(float);
+  auto kern = integrate_warp_kernel<NPL>;
+  check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+             "cudaFuncSetAttribute(integrate_warp)");
+  int per_sm = 0;
+  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpThreads, smem), "occupancy");
+  const int64_t tiles = (args.pixels + kWarpTilePx - 1) / kWarpTilePx;
+  const int64_t resident = static_cast<int64_t>(std::max(per_sm, 1)) * sm_count();
+  const unsigned grid = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(tiles, resident)));
+  note_launch();
+  kern<<<grid, kWarpThreads, smem, stream>>>(args);
+  check_cuda(cudaGetLastError(), "integrate_warp launch");
+}
+
 template <int NB>
 static void launch_reg(const IntegrateArgs& args, cudaStream_t stream) {
   constexpr int T = 128;
@@ -1088,6 +1394,13 @@ void launch_integrate(gg_stack* s, const float* d_weights, const gg_integrate_pa
                          : launch_col<32, GG_REJECT_LINEAR_FIT>(a, s->stream);
         break;
     }
+  }
+  else if (p.rejection != GG_REJECT_LINEAR_FIT && n <= 512) {
+    // one warp per pixel (the linear fit's serial rank walks stay below)
+    if (n <= 64) launch_warp<2>(a, s->stream);
+    else if (n <= 128) launch_warp<4>(a, s->stream);
+    else if (n <= 256) launch_warp<8>(a, s->stream);
+    else launch_warp<16>(a, s->stream);
   }
   else if (n <= 64) launch_reg<64>(a, s->stream);
   else if (n <= 128) launch_smem<4>(a, s->stream);

@@ -157,8 +157,8 @@ class ResidentPipeline:
 
     def detect(self, info: bool = False) -> list[dict] | None:
         """Star catalogs of every frame; they stay on the device for register().
-        info=True also returns each frame's background statistics and
-        candidate count (and raises when a frame's candidates overflow)."""
+        info=True also returns each frame's background statistics, candidate
+        count and catalog size."""
         cfg = self.config
         params = _lib.StarParams(float(cfg.star_threshold_sigma), int(cfg.star_max_stars), 4, 2.0, np.nan, np.nan,
                                  float(cfg.catalog_min_fwhm), float(cfg.catalog_max_eccentricity),
@@ -211,6 +211,7 @@ class ResidentPipeline:
                 return out
             gp = dict(DEFAULT_GRADIENT_REFINE, **(cfg.gradient_refine or {}))
             res = self.stack.refine_matrix_gradient_batch_to_reference(reference_index, good, out[good], **gp)
+            self.last_refinement = [dict(r, frame=int(k)) for k, r in zip(good, res)]
             for k, r in zip(good, res):
                 if r["ok"]:
                     out[k] = r["matrix"]

@@ -107,6 +107,36 @@ def test_integration_odd_shapes_and_single_frame(native):
         s.close()
 
 
+@pytest.mark.parametrize("n", [33, 64, 100, 200, 257, 512])
+def test_integration_large_stacks_warp_per_pixel(native, n):
+    """32 < N <= 512 runs one warp per pixel (warp-wide sort, float-float sums
+    combined across lanes): same bar as the column kernels, for the all-valid
+    and the partly-valid formula families, unit and non-unit weights."""
+    rng = np.random.default_rng(100 + n)
+    h, w = 7, 37  # 259 pixels: a partial last tile of 32
+    base = (800 + 12 * rng.standard_normal((n, h, w))).astype(np.float32)
+    base[rng.random(base.shape) < 0.03] += 5000.0  # outliers to reject
+    holes = base.copy()
+    holes[rng.random(base.shape) < 0.05] = np.nan
+    holes[:, 0, 0] = np.nan  # a pixel without samples
+    weights = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    weights[3] = 0.0  # an excluded frame
+    for tag, stack in (("all-valid", base), ("holes", holes)):
+        s = _stack_from(native, stack)
+        for wv in (None, weights):
+            for rej in ("winsorized_sigma", "sigma_clip", "none"):
+                s.integrate_async(wv, MODES[rej], 3.0, 3.0, 3, 0.5, count_map_dtype="float32")
+                master, weight, cov, low, high, _ = s.download_maps("full")
+                em, ew, ec, el, eh = oint.weighted_integrate_stack(stack, wv, rej, 3.0, 3.0, 3, 0.5)
+                what = f"n={n} {tag} {'weights' if wv is not None else 'unit'} {rej}"
+                np.testing.assert_array_equal(cov, ec, err_msg=what)
+                np.testing.assert_array_equal(low, el, err_msg=what)
+                np.testing.assert_array_equal(high, eh, err_msg=what)
+                assert_within_ulp(weight, ew, 1, what + " weight")
+                assert_within_ulp(master, em, 1, what + " master")
+        s.close()
+
+
 def test_linear_fit_clip_against_fp64_definition(native):
     rng = np.random.default_rng(5)
     n, h, w = 25, 6, 9
