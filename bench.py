@@ -283,8 +283,8 @@ def adjoint_report(pipe, dev_raw, reg, truth, h, w, stream) -> dict:
 
     ncc, ncc_ms = timed("ncc")
     gn, gn_ms = timed("gradient")
-    gn2, gn2_ms = timed("gradient", gradient={"sample_stride": 2})
-    gn4, gn4_ms = timed("gradient", gradient={"sample_stride": 4})
+    gn2, gn2_ms = timed("gradient", gradient={"sample_stride": 2, "target_samples": None})
+    gn4, gn4_ms = timed("gradient", gradient={"sample_stride": 4, "target_samples": None})
     # the generic autograd path (torch.autograd through the warp adjoint,
     # trust-region Newton over torch ops, one frame at a time) on 4 frames
     sub = ok[:4]

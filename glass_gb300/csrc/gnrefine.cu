@@ -60,9 +60,38 @@ constexpr int kGnUsed = 46;
 constexpr int kGnBins = 256;
 constexpr float kGnBinsPerOctave = 8.0f;
 constexpr float kGnLog2Min = -10.0f;
+// Photometric start, two coarse passes before the statistics passes:
+//  1. histograms of log2 v (32 bins per octave over [2^-2, 2^22)) of the
+//     sampled reference and moving values give each frame's median m and a
+//     noise scale s = m - (15.87th percentile), which stars and cosmic rays
+//     (both on the bright side) do not move;
+//  2. alpha = median of (O - m_O) / (a - m_a) over the samples bright in both
+//     frames (more than 10 s above m): star pixels, which scale with alpha;
+//     a cosmic ray is bright in one frame only.  beta = m_O - alpha m_a.
+// The ratio histogram has 21.3 bins per octave over [2^-6, 2^6).
+constexpr int kGnVBins = 768;
+constexpr float kGnVBinsPerOctave = 32.0f;
+constexpr float kGnVLog2Min = -2.0f;
+constexpr int kGnRBins = 256;
+constexpr float kGnRBinsPerOctave = 256.0f / 12.0f;
+constexpr float kGnRLog2Min = -6.0f;
+constexpr double kGnNoiseQuantile = 0.15865525393145707;  // Phi(-1)
+constexpr float kGnBrightSigmas = 10.0f;
+constexpr int kGnHistWords = kGnBins + 2 * kGnVBins;  // per job: residual, reference, moving
 // Gradient consistency: keep a sample only while |grad O| <= 2 |alpha| |grad a| + 3 sigma.
 constexpr float kGnGradFactor = 2.0f;
 constexpr float kGnGradSigmas = 3.0f;
+
+__device__ __forceinline__ int ratio_bin(float q) {
+  const float b = (log2f(q) - kGnRLog2Min) * kGnRBinsPerOctave;
+  return b < 0.0f ? 0 : (b >= static_cast<float>(kGnRBins - 1) ? kGnRBins - 1 : static_cast<int>(b));
+}
+
+__device__ __forceinline__ int value_bin(float v) {
+  if (!(v > 0.0f)) return 0;
+  const float b = (log2f(v) - kGnVLog2Min) * kGnVBinsPerOctave;
+  return b < 0.0f ? 0 : (b >= static_cast<float>(kGnVBins - 1) ? kGnVBins - 1 : static_cast<int>(b));
+}
 
 __device__ __forceinline__ int residual_bin(float r) {
   const float l = log2f(fabsf(r));  // -inf for 0: first bin
@@ -76,6 +105,8 @@ struct GnState {
   double rms;       // residual RMS over the kept samples (last pass)
   double step_px;   // corner displacement of the last step
   double samples;   // kept samples (last pass)
+  double med_ref, med_mov;  // photometric start: medians and brightness thresholds
+  double thr_ref, thr_mov;
   int iterations;
   int status;       // 0 running, 1 converged, 2 iteration cap, -1 too few samples, -2 singular
 };
@@ -88,10 +119,11 @@ struct GnArgs {
   GnState* state;
   double* partials;  // [job][block][kGnSums]
   double* sums_out;  // [job][kGnSums] (normal-equation export) or nullptr
-  unsigned* hist;    // [job][kGnBins] residual magnitude histogram, zeroed by the solve
+  unsigned* hist;    // [job][kGnHistWords] residual magnitude and value histograms, zeroed by the solve
   int width, height;
   int sample_stride, nsx, nsy;
   int blocks_per_job;
+  int phase;  // 1, 2: the photometric-start passes (value, ratio histograms)
   float clip_sigma, shift_px;
   float cx, cy, inv_r;
 };
@@ -117,7 +149,8 @@ struct GnLayout {
 template <int INTERP, int K, bool UNROLL>
 __device__ __forceinline__ void gn_sample(const GnArgs& a, const AffineCoef& coef, const float* ref, const float* mov,
                                           int x, int y, float alpha, float beta, float clip, float sigma,
-                                          unsigned* s_hist, float (&acc)[GnLayout<K>::kAcc]) {
+                                          unsigned* s_hist, unsigned* s_vhist, const float* s_start,
+                                          float (&acc)[GnLayout<K>::kAcc]) {
   const int W = a.width, H = a.height;
   const float fW = static_cast<float>(W), fH = static_cast<float>(H);
   const float* rp = ref + static_cast<int64_t>(y) * W + x;
@@ -140,6 +173,15 @@ __device__ __forceinline__ void gn_sample(const GnArgs& a, const AffineCoef& coe
   else
     ok = lanczos3_value_grad<UNROLL>(mov, W, x0, y0, tx, ty, O, Ox, Oy);
   if (!ok) return;
+  if constexpr (K == 0) {
+    if (a.phase == 1) {
+      atomicAdd(&s_vhist[value_bin(av)], 1u);
+      atomicAdd(&s_vhist[kGnVBins + value_bin(O)], 1u);
+    } else if (a.phase == 2) {
+      const float da = av - s_start[0], dm = O - s_start[1];
+      if (da > s_start[2] && dm > s_start[3]) atomicAdd(&s_vhist[ratio_bin(dm / da)], 1u);
+    }
+  }
   const float r = O - alpha * av - beta;
   atomicAdd(&s_hist[residual_bin(r)], 1u);
   float ga = 0.0f;
@@ -194,11 +236,15 @@ __global__ void __launch_bounds__(kGnThreads, K == 8 ? 1 : 3) gn_accumulate_kern
   using L = GnLayout<K>;
   __shared__ AffineCoef s_coef;
   __shared__ float s_phot[3];
+  __shared__ float s_start[4];
   __shared__ int s_run;
   __shared__ double s_red[kGnThreads / 32][L::kAcc];
   __shared__ unsigned s_hist[kGnBins];
+  __shared__ unsigned s_vhist[K == 0 ? 2 * kGnVBins : 1];
   const int job = blockIdx.y;
   for (int b = threadIdx.x; b < kGnBins; b += blockDim.x) s_hist[b] = 0u;
+  if constexpr (K == 0)
+    for (int b = threadIdx.x; b < 2 * kGnVBins; b += blockDim.x) s_vhist[b] = 0u;
   if (threadIdx.x == 0) {
     const GnState& st = a.state[job];
     s_run = st.status == 0;
@@ -206,6 +252,10 @@ __global__ void __launch_bounds__(kGnThreads, K == 8 ? 1 : 3) gn_accumulate_kern
     s_phot[0] = static_cast<float>(st.alpha);
     s_phot[1] = static_cast<float>(st.beta);
     s_phot[2] = static_cast<float>(st.sigma);
+    s_start[0] = static_cast<float>(st.med_ref);
+    s_start[1] = static_cast<float>(st.med_mov);
+    s_start[2] = static_cast<float>(st.thr_ref);
+    s_start[3] = static_cast<float>(st.thr_mov);
   }
   __syncthreads();
   if (!s_run) return;
@@ -222,7 +272,7 @@ __global__ void __launch_bounds__(kGnThreads, K == 8 ? 1 : 3) gn_accumulate_kern
        it += static_cast<int64_t>(a.blocks_per_job) * blockDim.x) {
     const int iy = static_cast<int>(it / a.nsx), ix = static_cast<int>(it - static_cast<int64_t>(iy) * a.nsx);
     gn_sample<INTERP, K, UNROLL>(a, s_coef, ref, mov, ix * a.sample_stride, iy * a.sample_stride, alpha, beta,
-                                 clip, sigma, s_hist, acc);
+                                 clip, sigma, s_hist, s_vhist, s_start, acc);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -240,7 +290,27 @@ __global__ void __launch_bounds__(kGnThreads, K == 8 ? 1 : 3) gn_accumulate_kern
     a.partials[(static_cast<int64_t>(job) * a.blocks_per_job + blockIdx.x) * kGnSums + L::slot(threadIdx.x)] = t;
   }
   for (int b = threadIdx.x; b < kGnBins; b += blockDim.x)
-    if (s_hist[b]) atomicAdd(&a.hist[static_cast<int64_t>(job) * kGnBins + b], s_hist[b]);
+    if (s_hist[b]) atomicAdd(&a.hist[static_cast<int64_t>(job) * kGnHistWords + b], s_hist[b]);
+  if constexpr (K == 0) {
+    if (a.phase != 0)
+      for (int b = threadIdx.x; b < 2 * kGnVBins; b += blockDim.x)
+        if (s_vhist[b]) atomicAdd(&a.hist[static_cast<int64_t>(job) * kGnHistWords + kGnBins + b], s_vhist[b]);
+  }
+}
+
+// Quantile q of a log2 value histogram (log-linear inside the bin).
+__device__ double histogram_quantile(const unsigned* h, int bins, double q, double log2min, double per_octave) {
+  unsigned long long total = 0;
+  for (int b = 0; b < bins; ++b) total += h[b];
+  if (total == 0) return 0.0;
+  const double want = q * static_cast<double>(total);
+  double cum = 0.0;
+  for (int b = 0; b < bins; ++b) {
+    const double c = static_cast<double>(h[b]);
+    if (cum + c >= want && c > 0.0) return exp2(log2min + (b + (want - cum) / c) / per_octave);
+    cum += c;
+  }
+  return exp2(log2min + bins / per_octave);
 }
 
 // 1.4826 * median |r| from the job's histogram (log-linear inside the bin).
@@ -289,7 +359,8 @@ __device__ __forceinline__ int model_columns(int model, float (&P)[8][8]) {
   return k;
 }
 
-// mode 0: statistics pass (beta, sigma); 1: Gauss-Newton step; 2: export sums.
+// mode 0: statistics pass (beta, sigma); 1: Gauss-Newton step; 2: export sums;
+// 3, 4: photometric start (medians and thresholds; alpha, beta).
 __global__ void gn_solve_kernel(GnArgs a, int mode, int model, double min_samples, double tol_px, double max_step_px,
                                 int last) {
   __shared__ double s[kGnSums];
@@ -303,11 +374,36 @@ __global__ void gn_solve_kernel(GnArgs a, int mode, int model, double min_sample
     s[q] = t;
   }
   __syncwarp();
-  unsigned* hist = a.hist + static_cast<int64_t>(job) * kGnBins;
+  unsigned* hist = a.hist + static_cast<int64_t>(job) * kGnHistWords;
   double robust_sigma = 0.0;
   if (lane == 0) robust_sigma = histogram_sigma(hist);
   __syncwarp();
   for (int b = lane; b < kGnBins; b += 32) hist[b] = 0u;  // ready for the next pass
+  if (mode == 3 || mode == 4) {  // photometric start
+    unsigned* vh = hist + kGnBins;
+    if (lane == 0 && mode == 3) {
+      const double ma = histogram_quantile(vh, kGnVBins, 0.5, kGnVLog2Min, kGnVBinsPerOctave);
+      const double la = histogram_quantile(vh, kGnVBins, kGnNoiseQuantile, kGnVLog2Min, kGnVBinsPerOctave);
+      const double mo = histogram_quantile(vh + kGnVBins, kGnVBins, 0.5, kGnVLog2Min, kGnVBinsPerOctave);
+      const double lo = histogram_quantile(vh + kGnVBins, kGnVBins, kGnNoiseQuantile, kGnVLog2Min, kGnVBinsPerOctave);
+      st.med_ref = ma;
+      st.med_mov = mo;
+      // +inf (no ratio samples, alpha stays) when a frame has no spread
+      st.thr_ref = ma > la ? kGnBrightSigmas * (ma - la) : HUGE_VAL;
+      st.thr_mov = mo > lo ? kGnBrightSigmas * (mo - lo) : HUGE_VAL;
+    } else if (lane == 0) {
+      unsigned long long n = 0;
+      for (int b = 0; b < kGnRBins; ++b) n += vh[b];
+      if (n >= 16) {
+        const double alpha = histogram_quantile(vh, kGnRBins, 0.5, kGnRLog2Min, kGnRBinsPerOctave);
+        st.alpha = alpha;
+        st.beta = st.med_mov - alpha * st.med_ref;
+      }
+    }
+    __syncwarp();
+    for (int b = lane; b < 2 * kGnVBins; b += 32) vh[b] = 0u;
+    return;
+  }
   if (lane != 0) return;
   if (mode == 2) {
     for (int q = 0; q < kGnSums; ++q) a.sums_out[static_cast<int64_t>(job) * kGnSums + q] = q < kGnUsed ? s[q] : 0.0;
@@ -445,7 +541,7 @@ static GnScratch& gn_scratch(gg_stack* s, int jobs, int blocks) {
   if (g.job_cap < jobs || g.block_cap < blocks) {
     auto bytes = [](int64_t jc, int64_t bc) {
       return jc * static_cast<int64_t>(sizeof(int2) + sizeof(GnState) + sizeof(double) * kGnSums * (bc + 1) +
-                                          sizeof(unsigned) * kGnBins);
+                                          sizeof(unsigned) * kGnHistWords);
     };
     const int64_t before = bytes(g.job_cap, g.block_cap);
     check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(gradient refine scratch)");
@@ -457,7 +553,7 @@ static GnScratch& gn_scratch(gg_stack* s, int jobs, int blocks) {
                "cudaMalloc(gradient refine partials)");
     check_cuda(cudaMalloc(&g.sums, sizeof(double) * kGnSums * static_cast<size_t>(jc)),
                "cudaMalloc(gradient refine sums)");
-    check_cuda(cudaMalloc(&g.hist, sizeof(unsigned) * kGnBins * static_cast<size_t>(jc)),
+    check_cuda(cudaMalloc(&g.hist, sizeof(unsigned) * kGnHistWords * static_cast<size_t>(jc)),
                "cudaMalloc(gradient refine histogram)");
     check_cuda(cudaHostAlloc(reinterpret_cast<void**>(&g.h_state), sizeof(GnState) * jc, cudaHostAllocDefault),
                "cudaHostAlloc(gradient refine state)");
@@ -523,7 +619,7 @@ static GnPlan gn_prepare(gg_stack* s, int64_t reference_index, const int64_t* mo
   a.partials = g.partials;
   a.sums_out = g.sums;
   a.hist = g.hist;
-  check_cuda(cudaMemsetAsync(g.hist, 0, sizeof(unsigned) * kGnBins * count, s->stream),
+  check_cuda(cudaMemsetAsync(g.hist, 0, sizeof(unsigned) * kGnHistWords * count, s->stream),
              "cudaMemsetAsync(gradient refine histogram)");
   a.width = static_cast<int>(s->width);
   a.height = static_cast<int>(s->height);
@@ -582,9 +678,10 @@ static int gn_blocks_per_job(GnKernelFn fn, int jobs, int64_t samples, int cap) 
 // One pass over the samples: K = 0 statistics, else the model's projected
 // columns (see GnLayout).  Lanczos3 passes tune row-by-row against
 // whole-window tap loads per shape.
-static void gn_accumulate(gg_stack* s, GnPlan& plan, int sample_stride, int K) {
+static void gn_accumulate(gg_stack* s, GnPlan& plan, int sample_stride, int K, int phase = 0) {
   GnArgs a = plan.args;
   a.sample_stride = sample_stride;
+  a.phase = phase;
   a.nsx = static_cast<int>((s->width + sample_stride - 1) / sample_stride);
   a.nsy = static_cast<int>((s->height + sample_stride - 1) / sample_stride);
   const int64_t samples = static_cast<int64_t>(a.nsx) * a.nsy;
@@ -592,7 +689,7 @@ static void gn_accumulate(gg_stack* s, GnPlan& plan, int sample_stride, int K) {
   auto run = [&](int variant) {
     GnKernelFn fn = gn_kernel(plan.interp, K, variant == 1);
     a.blocks_per_job = gn_blocks_per_job(fn, plan.jobs, samples, g.block_cap);
-    check_cuda(cudaMemsetAsync(g.hist, 0, sizeof(unsigned) * kGnBins * plan.jobs, s->stream),
+    check_cuda(cudaMemsetAsync(g.hist, 0, sizeof(unsigned) * kGnHistWords * plan.jobs, s->stream),
                "cudaMemsetAsync(gradient refine histogram)");
     const dim3 grid(static_cast<unsigned>(a.blocks_per_job), static_cast<unsigned>(plan.jobs));
     note_launch();
@@ -602,7 +699,7 @@ static void gn_accumulate(gg_stack* s, GnPlan& plan, int sample_stride, int K) {
   int variant = 0;
   if (plan.interp == GG_INTERP_LANCZOS3) {
     const std::string shape = std::to_string(plan.jobs) + " jobs x " + std::to_string(samples) + " samples, " +
-                              std::to_string(K) + " columns";
+                              std::to_string(K) + " columns" + (phase ? ", start pass " + std::to_string(phase) : "");
     variant = autotune_choose("gn_accumulate taps", shape, {"rows", "window"}, 0, s->stream, run);
   }
   run(variant);
@@ -651,7 +748,12 @@ int gg_stack_refine_gradient(gg_stack* s, int64_t reference_index, const int64_t
   const int model_k = p.transform_model == GG_TRANSFORM_TRANSLATION ? 4
                       : p.transform_model == GG_TRANSFORM_SIMILARITY ? 6
                                                                       : 8;
-  // statistics passes on a grid twice as coarse (photometric offset and noise)
+  // photometric start (alpha, beta), then statistics passes (offset and
+  // noise), all on a grid twice as coarse
+  gn_accumulate(s, plan, std::min(2 * p.sample_stride, 64), 0, 1);
+  gn_solve(s, plan, 3, p.transform_model, p.min_samples, p.tolerance_px, p.max_step_px, 0);
+  gn_accumulate(s, plan, std::min(2 * p.sample_stride, 64), 0, 2);
+  gn_solve(s, plan, 4, p.transform_model, p.min_samples, p.tolerance_px, p.max_step_px, 0);
   for (int k = 0; k < p.stats_passes; ++k) {
     gn_accumulate(s, plan, std::min(2 * p.sample_stride, 64), 0);
     gn_solve(s, plan, 0, p.transform_model, p.min_samples, p.tolerance_px, p.max_step_px, 0);

@@ -255,6 +255,28 @@ def test_gpu_gradient_refine_recovers_truth(native, model):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("gain,offset", [(0.5, 900.0), (2.0, -700.0)])
+def test_gpu_gradient_refine_large_photometric_ratio(native, gain, offset):
+    """A thin-cloud frame against a clear reference (and the reverse): the
+    photometric start (value-distribution quantiles) puts alpha near the
+    gain before the masked passes, so star pixels are not clipped away."""
+    h, w = 256, 288
+    truth = _similarity(0.003, 1.0, 3.2, -1.7)
+    start = _similarity(0.0038, 1.0, 3.2 + 0.4, -1.7 - 0.3)
+    ref, mov = _pair(9, h, w, truth, gain=gain, offset=offset, cosmic=40)
+    s = _stack(native, [ref, mov])
+    try:
+        res = s.refine_matrix_gradient_batch_to_reference(0, [1], start[None])
+    finally:
+        s.close()
+    assert res[0]["ok"], res[0]
+    # 0.5 px start -> under 0.01 px (unscaled cosmic rays weigh more against
+    # the scaled stars than at gain 1)
+    assert _rms(res[0]["matrix"], truth, h, w) < 0.01, res[0]
+    assert abs(res[0]["alpha"] - gain) < 0.02 * gain
+
+
+@pytest.mark.gpu
 def test_gpu_gradient_refine_arguments(native):
     h, w = 64, 64
     s = _stack(native, [np.zeros((h, w), np.float32), np.zeros((h, w), np.float32)])
