@@ -334,6 +334,49 @@ def local_norm_report(pipe, stream, reps: int, peak: float) -> dict:
             "achieved_gbs": achieved, "frac_of_measured_hbm": achieved / peak}
 
 
+def large_stack_report(reps: int, frames: int = 200, height: int = 1024, width: int = 1024) -> dict:
+    """Winsorized 3/3 weighted integration of a 200-frame stack (c5's frame
+    count at 1024 x 1024: the warp-per-pixel integrator), seeded noise frames
+    with 1 % outliers resident on the device, device simple-SNR weights, CUDA
+    events over `reps` launches on the stack's stream."""
+    import torch
+
+    from glass_gb300 import _glass_cuda_native as native
+    from glass_gb300 import _lib
+
+    stream = torch.cuda.Stream()
+    rng = np.random.default_rng(17)
+    s = native.ResidentCalibratedStack(frames, height, width)
+    try:
+        s.set_stream(stream.cuda_stream)
+        base = rng.normal(1000.0, 20.0, (8, height, width)).astype(np.float32)
+        base[rng.random(base.shape) < 0.01] += 5000.0
+        for k in range(frames):
+            s.upload_calibrated_frame(k, base[k % 8] + np.float32(k % 5))
+        s.compute_frame_weights("simple_snr", None, 1.0e-6, download=False)
+
+        def run():
+            s.integrate_async("device", _lib.GG_REJECT_WINSORIZED, 3.0, 3.0, 3, 0.5, "uint16")
+
+        for _ in range(2):
+            run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            run()
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+    finally:
+        s.close()
+    px = height * width
+    nbytes = 4 * frames * px + 16 * px
+    peak, kind = measured_peak()
+    return {"stack": [frames, height, width], "kernel": "integrate_warp_kernel<8>", "ms": ms,
+            "algorithmic_bytes": nbytes, "achieved_gbs": nbytes / (ms / 1e3) / 1e9,
+            "frac": nbytes / (ms / 1e3) / 1e9 / peak, "peak_source": kind}
+
+
 def batch_report(reps: int) -> dict:
     """Uneven stacks winsorized-integrated one after another vs batched (one
     launch per frame-count bucket), CUDA events on one stream, seeded noise
@@ -698,6 +741,7 @@ def main():
     graph = graph_report(pipe, dev_raw, reg["matrices"], stream, max(3, args.steps))
     local_norm = local_norm_report(pipe, stream, max(3, args.steps), measured_peak()[0])
     batch = batch_report(max(3, args.steps))
+    large = large_stack_report(max(3, args.steps))
     pinned =torch.from_numpy(data.lights.view(np.int16)).pin_memory().numpy().view(np.uint16)
     # reused pinned destinations for the six maps (master, weight f32; coverage,
     # low, high uint16; dq int16)
@@ -778,6 +822,7 @@ def main():
         "graph_step": graph,
         "local_normalization": local_norm,
         "batched_stacks": batch,
+        "large_stack_integration": large,
         "autotune": _lib.autotune_entries(),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mpix-frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
