@@ -80,7 +80,9 @@ struct SelectArgs {
 // Histogram pass: digit of `pass` for keys matching each rank's prefix.
 // Sky pixels share their leading digits, so each thread keeps a run-length
 // counter per histogram (last digit, count) and only touches shared memory
-// when the digit changes; four pixels per float4 load.
+// when the digit changes; four pixels per float4 load.  When both ranks
+// share their prefix (the usual case: the two middle values of an even
+// count lie in one bucket) only the first histogram is built and copied.
 template <int PASS>
 __global__ void __launch_bounds__(256) select_hist_kernel(SelectArgs a) {
   __shared__ unsigned h[2][kSelBins];
@@ -90,6 +92,7 @@ __global__ void __launch_bounds__(256) select_hist_kernel(SelectArgs a) {
   if (threadIdx.x == 0) s_valid = 0;
   __syncthreads();
   const unsigned p0 = a.state[k].prefix[0], p1 = a.state[k].prefix[1];
+  const bool shared_prefix = p0 == p1;
   const float median = a.state[k].median;
   const bool absdev = a.mode == 1;
   const float* src = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
@@ -108,7 +111,7 @@ __global__ void __launch_bounds__(256) select_hist_kernel(SelectArgs a) {
     if constexpr (PASS != 0) {
       const unsigned hp = key >> kPrefixShift;
       in0 = hp == p0;
-      in1 = hp == p1;
+      in1 = !shared_prefix && hp == p1;
     }
     if (in0) {
       if (digit == d0) {
@@ -151,7 +154,7 @@ __global__ void __launch_bounds__(256) select_hist_kernel(SelectArgs a) {
   unsigned* g = a.hist + static_cast<int64_t>(k) * 2 * kSelBins;
   const int nh = PASS == 0 ? 1 : 2;
   for (int i = threadIdx.x; i < nh * kSelBins; i += blockDim.x) {
-    const unsigned v = (&h[0][0])[i];
+    const unsigned v = (shared_prefix && i >= kSelBins) ? h[0][i - kSelBins] : (&h[0][0])[i];
     if (v) atomicAdd(g + i, v);
   }
   if (PASS == 0 && a.mode == 0 && threadIdx.x == 0 && s_valid) atomicAdd(&a.state[k].count, s_valid);
