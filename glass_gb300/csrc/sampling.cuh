@@ -112,9 +112,11 @@ static __device__ __noinline__ bool lanczos3_nonfinite(const TapSource& ts, int 
   return true;
 }
 
-// Returns false when the tap weights sum to (almost) zero.
-__device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int y0, float tx, float ty,
-                                                bool all_finite, float clamp, float& out) {
+// Returns false when the tap weights sum to (almost) zero.  CLAMP = false
+// compiles the window loops without the min/max tracking (clamp < 0).
+template <bool CLAMP>
+__device__ __forceinline__ bool sample_lanczos3_impl(const TapSource& ts, int x0, int y0, float tx, float ty,
+                                                     bool all_finite, float clamp, float& out) {
   float wx[6], wy[6];
   lanczos3_weights(tx, wx);
   lanczos3_weights(ty, wy);
@@ -137,7 +139,7 @@ __device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int
         for (int i = 0; i < 6; ++i) {
           const float v = r0[j * kBoxW + i];
           row = __fmaf_rn(wx[i], v, row);
-          if (clamp >= 0.0f) {
+          if (CLAMP) {
             vmin = fminf(vmin, v);
             vmax = fmaxf(vmax, v);
           }
@@ -152,7 +154,7 @@ __device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int
         for (int i = 0; i < 6; ++i) {
           const float v = ts.at(x0 - 2 + i, y0 - 2 + j);
           row = __fmaf_rn(wx[i], v, row);
-          if (clamp >= 0.0f) {
+          if (CLAMP) {
             vmin = fminf(vmin, v);
             vmax = fmaxf(vmax, v);
           }
@@ -167,12 +169,19 @@ __device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int
   }
   if (!(fabsf(wsum) > 1.0e-12f)) return false;
   float value = __fdiv_rn(acc, wsum);
-  if (clamp >= 0.0f && vmin <= vmax) {
+  if (CLAMP && vmin <= vmax) {
     const float range = vmax - vmin;
     value = fminf(vmax + clamp * range, fmaxf(vmin - clamp * range, value));
   }
   out = value;
   return true;
+}
+
+// clamp >= 0: clamp to [min - clamp * range, max + clamp * range] of the taps.
+__device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int y0, float tx, float ty,
+                                                bool all_finite, float clamp, float& out) {
+  return clamp >= 0.0f ? sample_lanczos3_impl<true>(ts, x0, y0, tx, ty, all_finite, clamp, out)
+                       : sample_lanczos3_impl<false>(ts, x0, y0, tx, ty, all_finite, clamp, out);
 }
 
 }  // namespace gg
