@@ -296,3 +296,15 @@ def test_gpu_gradient_refine_arguments(native):
         np.testing.assert_array_equal(res[0]["matrix"], np.eye(3))
     finally:
         s.close()
+
+
+def test_gradient_sample_stride_targets_sample_count():
+    from glass_gb300.pipeline import DEFAULT_GRADIENT_REFINE, gradient_sample_stride
+
+    p = dict(DEFAULT_GRADIENT_REFINE)
+    assert gradient_sample_stride(p, 2048, 2048) == 3  # 466k samples: the minimum stride holds
+    assert gradient_sample_stride(p, 6422, 9600) == 8  # c5 frame: about 1e6 samples
+    assert (6422 // 8) * (9600 // 8) < 1.1e6
+    assert gradient_sample_stride(dict(p, target_samples=None), 6422, 9600) == 3
+    assert gradient_sample_stride(dict(p, sample_stride=5), 512, 512) == 5
+    assert gradient_sample_stride(dict(p, target_samples=1), 6422, 9600) == 32
