@@ -29,24 +29,37 @@ class Masters:
 
 
 def build_masters(bias_frames: np.ndarray | None, dark_frames: np.ndarray | None,
-                  flat_frames: np.ndarray | None, flat_floor: float = 1.0e-6) -> Masters:
-    """Master bias / dark / flat on the GPU (cpu/master_frames.py:97-165).
+                  flat_frames: np.ndarray | None, flat_floor: float = 1.0e-6, method: str = "mean",
+                  low_sigma: float = 3.0, high_sigma: float = 3.0) -> Masters:
+    """Master bias / dark / flat on the GPU (cpu/master_frames.py:97-165;
+    resident _stack_resident_master_array_with_resident_cuda_{mean,
+    hardened_winsorized}, resident_cuda.py:6150, 6351).
 
-    Each master is the mean of its frames (the stack integrator with no
-    rejection, float64-exact sums); the dark has the master bias subtracted
-    and the flat is bias-subtracted, divided by its median and floored.
+    Each master is the mean of its frames ("mean": the stack integrator with
+    no rejection, float64-exact sums) or their winsorized sigma-clipped mean
+    ("winsorized": low_sigma / high_sigma, min 3 samples, at most half
+    rejected); the dark has the master bias subtracted and the flat is
+    bias-subtracted, divided by its median and floored.
     """
+    if method not in ("mean", "winsorized"):
+        raise ValueError("method must be mean or winsorized")
 
     def combine(frames: np.ndarray) -> np.ndarray:
         n, h, w = frames.shape
         stack = ResidentCalibratedStack(n, h, w)
-        raw = np.ascontiguousarray(frames.astype(np.uint16, copy=False))
-        params = _lib.CalibParams(1, 1.0, 1.0e-6, 0.0)
-        idx = np.arange(n, dtype=np.int64)
-        _lib.call("gg_stack_calibrate_u16", stack.handle, _lib.ptr(idx), ctypes.c_int64(n), _lib.ptr(raw), 0,
-                  ctypes.byref(params))
-        master, _ = stack.integrate_mean()
-        stack.close()
+        try:
+            raw = np.ascontiguousarray(frames.astype(np.uint16, copy=False))
+            params = _lib.CalibParams(1, 1.0, 1.0e-6, 0.0)
+            idx = np.arange(n, dtype=np.int64)
+            _lib.call("gg_stack_calibrate_u16", stack.handle, _lib.ptr(idx), ctypes.c_int64(n), _lib.ptr(raw), 0,
+                      ctypes.byref(params))
+            if method == "mean":
+                master, _ = stack.integrate_mean()
+            else:
+                master = stack.integrate_hardened_winsorized_sigma(None, low_sigma, high_sigma, 3, 0.5,
+                                                                   download_mode="master_only")[0]
+        finally:
+            stack.close()
         return master
 
     bias = combine(bias_frames) if bias_frames is not None else None

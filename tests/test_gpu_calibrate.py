@@ -87,3 +87,23 @@ def test_many_frames_through_pinned_lanes(native):
     s.calibrate_frames_u16(np.arange(n), pinned, 1.0, None)
     tiles = s.download_frames_tile(np.arange(n), 3, 5, 50, 33)
     np.testing.assert_array_equal(tiles, (raw.astype(np.float32) - bias)[:, 5:33, 3:50])
+
+
+def test_winsorized_masters_match_oracle(native):
+    """Master frames by winsorized sigma clipping (the reference's hardened
+    winsorized master path) equal the oracle's integration of the decoded
+    calibration frames; a hot streak in one frame is rejected."""
+    from glass_gb300.pipeline import build_masters
+    from oracle.integration import weighted_integrate_stack
+
+    rng = np.random.default_rng(21)
+    bias = rng.integers(480, 520, size=(7, 24, 40)).astype(np.uint16)
+    bias[2, 5, 3:9] = 9000  # a cosmic-ray streak in one bias frame
+    m = build_masters(bias, None, None, method="winsorized")
+    exp, *_ = weighted_integrate_stack(bias.astype(np.float32), None, "winsorized_sigma", 3.0, 3.0, 3, 0.5)
+    np.testing.assert_allclose(m.bias, exp, rtol=2e-7, atol=0)
+    assert float(m.bias[5, 5]) < 530.0
+    mean = build_masters(bias, None, None)
+    assert float(mean.bias[5, 5]) > 1000.0
+    with pytest.raises(ValueError):
+        build_masters(bias, None, None, method="median")
