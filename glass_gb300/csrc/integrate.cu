@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "autotune.cuh"
@@ -948,7 +949,10 @@ __global__ void __launch_bounds__(T) integrate_smem_kernel(IntegrateArgs a) {
 // across lanes), and every sum of the statistics and of the integration is a
 // per-lane float-float sum combined across the warp.  The shared-memory cost
 // is 4 * 33 B per frame instead of a sorted column per thread, so an SM keeps
-// tens of warps in flight at N = 200.
+// tens of warps in flight at N = 200.  WARP = GG_INTERP_* fills the tile by
+// sampling every frame through its inverse matrix (fused warp + integration
+// of more than 32 frames) and counts each pixel's geometrically valid
+// samples in shared memory.
 constexpr int kWarpTilePx = 32;
 constexpr int kWarpTileRow = kWarpTilePx + 1;
 constexpr int kWarpThreads = 256;
@@ -1070,10 +1074,14 @@ __device__ __forceinline__ float warp_clipped_std(const float (&v)[NPL], int lan
   return ff_sqrt_f32(q, ql);
 }
 
-template <int NPL>
+template <int NPL, int WARP>
 __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateArgs a) {
-  extern __shared__ float tile[];  // [frames][kWarpTileRow]
+  extern __shared__ float tile[];  // [frames][kWarpTileRow], then (fused) [frames] FusedFrame
   __shared__ FrameTable<32 * NPL> tab;
+  __shared__ int s_geo[kWarpTilePx];
+  FusedFrame* fz = reinterpret_cast<FusedFrame*>(tile + a.frames * kWarpTileRow);
+  if constexpr (WARP != 0)
+    for (int f = threadIdx.x; f < a.frames; f += blockDim.x) fz[f] = a.fused[f];
   load_frame_table<32 * NPL>(a, tab);
   const bool allvalid = tab.allvalid != 0;
   const bool unit = tab.unit != 0;
@@ -1085,10 +1093,23 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
   for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
     const int64_t p0 = t * kWarpTilePx;
     __syncthreads();  // the previous tile's columns are consumed
+    if constexpr (WARP != 0) {
+      if (threadIdx.x < kWarpTilePx) s_geo[threadIdx.x] = 0;
+      __syncthreads();
+    }
     for (int i = threadIdx.x; i < N * kWarpTilePx; i += kWarpThreads) {
       const int f = i / kWarpTilePx, px = i - f * kWarpTilePx;
       const int64_t p = p0 + px;
-      tile[f * kWarpTileRow + px] = p < P ? __ldcs(tab.base[f] + p) : 0.0f;
+      float v = 0.0f;
+      if constexpr (WARP == 0) {
+        if (p < P) v = __ldcs(tab.base[f] + p);
+      } else if (p < P) {
+        const int py = static_cast<int>(p / a.width), pxx = static_cast<int>(p - static_cast<int64_t>(py) * a.width);
+        int geo = 0;
+        v = fused_sample<WARP>(a, tab.base[f], fz[f], pxx, py, geo);
+        if (geo) atomicAdd(&s_geo[px], 1);
+      }
+      tile[f * kWarpTileRow + px] = v;
     }
     __syncthreads();
     for (int px = warp; px < kWarpTilePx; px += kWarpThreads / 32) {
@@ -1223,15 +1244,19 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
           weight = wsum.value_f32();
         }
       }
-      if (lane == 0) write_outputs(a, p, master, weight, kept, nl, nh, tab.active);
+      if (lane == 0) {
+        if constexpr (WARP != 0) a.geometric_out[p] = static_cast<float>(s_geo[px]);
+        write_outputs(a, p, master, weight, kept, nl, nh, tab.active);
+      }
     }
   }
 }
 
-template <int NPL>
+template <int NPL, int WARP = 0>
 static void launch_warp(const IntegrateArgs& args, cudaStream_t stream) {
-  const size_t smem = static_cast<size_t>(args.frames) * kWarpTileRow * sizeof(float);
-  auto kern = integrate_warp_kernel<NPL>;
+  const size_t smem = static_cast<size_t>(args.frames) * kWarpTileRow * sizeof(float) +
+                      (WARP != 0 ? static_cast<size_t>(args.frames) * sizeof(FusedFrame) : 0);
+  auto kern = integrate_warp_kernel<NPL, WARP>;
   check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
              "cudaFuncSetAttribute(integrate_warp)");
   int per_sm = 0;
@@ -1575,7 +1600,7 @@ static void launch_fused(const IntegrateArgs& a, cudaStream_t stream) {
 // the result of warping every frame through its matrix (NaN fill) and
 // integrating, without writing the warped frames.
 static void validate_fused(gg_stack* s, int interp, const gg_integrate_params_t& p) {
-  require(s->frames <= 32, "fused warp-integration supports at most 32 frames");
+  require(s->frames <= 512, "fused warp-integration supports at most 512 frames");
   require(p.rejection == GG_REJECT_NONE || p.rejection == GG_REJECT_SIGMA_CLIP || p.rejection == GG_REJECT_WINSORIZED,
           "fused warp-integration supports the mean, sigma-clip and winsorized sigma-clip rejections");
   require(interp == GG_INTERP_BILINEAR || interp == GG_INTERP_LANCZOS3,
@@ -1652,7 +1677,17 @@ static void launch_fused_sequence(gg_stack* s, FusedFrame* d_frames, int interp,
   else
     fused_nonfinite_kernel<GG_INTERP_LANCZOS3><<<count_grid, 256, 0, s->stream>>>(a, s->d_fused_counts);
   check_cuda(cudaGetLastError(), "fused_nonfinite launch");
-  if (interp == GG_INTERP_BILINEAR) {
+  if (n > 32) {  // one warp per pixel over a sampled [frame][32 px] tile
+    auto run = [&](auto tag) {
+      constexpr int I = decltype(tag)::value;
+      if (n <= 64) launch_warp<2, I>(a, s->stream);
+      else if (n <= 128) launch_warp<4, I>(a, s->stream);
+      else if (n <= 256) launch_warp<8, I>(a, s->stream);
+      else launch_warp<16, I>(a, s->stream);
+    };
+    if (interp == GG_INTERP_BILINEAR) run(std::integral_constant<int, GG_INTERP_BILINEAR>{});
+    else run(std::integral_constant<int, GG_INTERP_LANCZOS3>{});
+  } else if (interp == GG_INTERP_BILINEAR) {
     if (p.rejection == GG_REJECT_NONE) launch_fused<GG_REJECT_NONE, GG_INTERP_BILINEAR>(a, s->stream);
     else if (p.rejection == GG_REJECT_SIGMA_CLIP) launch_fused<GG_REJECT_SIGMA_CLIP, GG_INTERP_BILINEAR>(a, s->stream);
     else launch_fused<GG_REJECT_WINSORIZED, GG_INTERP_BILINEAR>(a, s->stream);

@@ -49,8 +49,9 @@ CASES = [("bilinear", False, -1.0), ("bilinear", True, -1.0), ("lanczos3", False
 
 
 @pytest.mark.parametrize("interp,winsorize,clamp", CASES)
-@pytest.mark.parametrize("n", [5, 13, 32])
+@pytest.mark.parametrize("n", [5, 13, 32, 40, 70])
 def test_fused_equals_two_step(native, interp, winsorize, clamp, n):
+    """n > 32 runs the warp-per-pixel integrator on a sampled tile."""
     rng = np.random.default_rng(100 + n)
     h, w = 37, 45
     frames = _stack(rng, n, h, w, nan_frac=0.01 if winsorize else 0.0)
