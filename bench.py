@@ -570,6 +570,25 @@ def run_c5(args) -> int:
     ingest_wall_ms = 1e3 * (time.perf_counter() - t0)
     ingest_ms = i0.elapsed_time(i1)
     raw_bytes = 2 * n * P
+    # fused Lanczos3 warp + winsorized integration of the 200 frames (the
+    # warp-per-pixel integrator sampling every frame; nothing written to the
+    # stack) against the warp + integrate stages above
+    calibrate()
+    pipe.weights()
+    cfg = pipe.config
+
+    def fused():
+        pipe.stack.integrate_warped_device_weights(reg["m"], cfg.interpolation, cfg.clamping_threshold, cfg.rejection,
+                                                   cfg.low_sigma, cfg.high_sigma, cfg.min_samples,
+                                                   cfg.max_reject_fraction, cfg.count_map_dtype)
+
+    fused()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    fused()
+    f1.record(stream)
+    stream.synchronize()
+    fused_ms = f0.elapsed_time(f1)
     calibrate()  # detection statistics of the calibrated (not the warped) frames
     info = pipe.detect(info=True)
     inliers = [r["inliers"] for r in pipe.last_registration]
@@ -592,6 +611,8 @@ def run_c5(args) -> int:
             "resident": {"stack_bytes_allocated": pipe.stack.bytes_allocated,
                          "device_bytes_in_use": int(torch.cuda.mem_get_info()[1] - torch.cuda.mem_get_info()[0])},
             "stages": out_stages,
+            "fused_warp_integrate": {"ms": fused_ms, "vs_warp_plus_integrate_ms":
+                                     out_stages["warp_lanczos3"]["ms"] + out_stages["integrate_winsorized"]["ms"]},
             "ingest_from_pinned_host": {"frames": n, "raw_bytes": raw_bytes, "ms_events": ingest_ms,
                                         "ms_wall": ingest_wall_ms,
                                         "raw_gb_per_s": raw_bytes / (max(ingest_ms, ingest_wall_ms) / 1e3) / 1e9},
