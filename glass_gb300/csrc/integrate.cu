@@ -80,8 +80,8 @@ struct IntegrateArgs {
 // kernel would have written (NaN fill when invalid); `geo` counts the
 // samples the warp would have marked covered.
 template <int INTERP>
-__device__ __noinline__ float fused_sample(const IntegrateArgs& a, const float* src, const FusedFrame& fz, int x,
-                                           int y, int& geo) {
+__device__ __forceinline__ float fused_sample_inline(const IntegrateArgs& a, const float* src, const FusedFrame& fz,
+                                                     int x, int y, int& geo) {
   const float nan = __int_as_float(0x7fc00000);
   FFv sx, sy;
   if (!source_coord(fz, static_cast<float>(x), static_cast<float>(y), sx, sy)) return nan;
@@ -107,6 +107,14 @@ __device__ __noinline__ float fused_sample(const IntegrateArgs& a, const float* 
   }
   ++geo;
   return v;
+}
+
+// Out-of-line copy for the column kernel, which keeps the sampler out of its
+// unrolled register code; the warp-per-pixel tile fill inlines it.
+template <int INTERP>
+__device__ __noinline__ float fused_sample(const IntegrateArgs& a, const float* src, const FusedFrame& fz, int x,
+                                           int y, int& geo) {
+  return fused_sample_inline<INTERP>(a, src, fz, x, y, geo);
 }
 
 constexpr float kInf = __builtin_huge_valf();
@@ -1106,7 +1114,7 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
       } else if (p < P) {
         const int py = static_cast<int>(p / a.width), pxx = static_cast<int>(p - static_cast<int64_t>(py) * a.width);
         int geo = 0;
-        v = fused_sample<WARP>(a, tab.base[f], fz[f], pxx, py, geo);
+        v = fused_sample_inline<WARP>(a, tab.base[f], fz[f], pxx, py, geo);
         if (geo) atomicAdd(&s_geo[px], 1);
       }
       tile[f * kWarpTileRow + px] = v;
