@@ -217,8 +217,9 @@ int gg_stack_integrate_device_weights(gg_stack* stack, const void* dev_weights,
  * the geometric coverage (frames with a valid sample per pixel).  Replaces
  * integrate_matrix_warped_{mean,sigma_clip} (glass_cuda.py:5142-5287;
  * integration_kernels.cu:3840-4123).  interpolation GG_INTERP_BILINEAR or
- * GG_INTERP_LANCZOS3; rejection NONE, SIGMA_CLIP or WINSORIZED; at most 32
- * frames.  host_weights may be NULL (unit).  Asynchronous. */
+ * GG_INTERP_LANCZOS3; rejection NONE, SIGMA_CLIP or WINSORIZED; at most 512
+ * frames (above 32 one warp per pixel over a sampled tile).  host_weights
+ * may be NULL (unit).  Asynchronous. */
 int gg_stack_integrate_warped(gg_stack* stack, const double* host_matrices, int interpolation,
                               float clamping_threshold, const float* host_weights,
                               const gg_integrate_params_t* params);
@@ -255,7 +256,7 @@ int gg_stack_integrate_warped_device_weights(gg_stack* stack, const double* host
  * frame-major, H*W each, read at every replay) -> frame weights (weighting =
  * GG_WEIGHTS_PRIOR (unit) or GG_WEIGHTS_SIMPLE_SNR, on the device) -> fused
  * warp + rejection + integration through host_matrices (as
- * gg_stack_integrate_warped; at most 32 frames).  Capture runs the sequence
+ * gg_stack_integrate_warped; at most 512 frames).  Capture runs the sequence
  * once eagerly first.  gg_stack_graph_launch replays it on the stack's
  * stream (asynchronous; maps as after gg_stack_integrate_warped). */
 int gg_stack_graph_capture_step(gg_stack* stack, const void* dev_raw, const double* host_matrices, int interpolation,
