@@ -626,9 +626,14 @@ def run_c5(args) -> int:
                                                for v in sorted({r.get("status") for r in refinement})},
                              "refine_iterations_mean": (float(np.mean([r["iterations"] for r in refinement]))
                                                         if refinement else None),
+                             "refine_last_step_px_median_at_cap": (
+                                 float(np.median([r["last_step_px"] for r in refinement
+                                                  if r.get("status") == "iteration_cap"]))
+                                 if any(r.get("status") == "iteration_cap" for r in refinement) else None),
                              "worst_frames": [{"frame": k, "gradient_px": g, "triangle_px": t,
                                                **{q: refinement_by(refinement, k).get(q)
-                                                  for q in ("status", "iterations", "alpha", "sigma", "samples")}}
+                                                  for q in ("status", "iterations", "alpha", "sigma", "samples",
+                                                            "last_step_px")}}
                                               for g, t, k in per_frame[:6]]}}
     print(json.dumps(line))
     pipe.close()
