@@ -14,21 +14,23 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _data(seed):
+def _data(seed, frames=8):
     from glass_gb300.synthetic import StackConfig, generate
 
-    cfg = StackConfig(frames=8, height=160, width=192, stars=60, hot_pixel_fraction=1e-4, cosmic_ray_density=1e-4,
-                      max_shift=5.0, max_rotation_deg=0.2, calibration_frames=3, seed=seed)
+    cfg = StackConfig(frames=frames, height=160, width=192, stars=60, hot_pixel_fraction=1e-4,
+                      cosmic_ray_density=1e-4, max_shift=5.0, max_rotation_deg=0.2, calibration_frames=3, seed=seed)
     return generate(cfg)
 
 
-def test_graph_replay_matches_eager(native):
+@pytest.mark.parametrize("frames", [8, 40])
+def test_graph_replay_matches_eager(native, frames):
+    """8 frames: the column kernel; 40: the warp-per-pixel fused kernel."""
     import torch
 
     from glass_gb300 import _lib
     from glass_gb300.pipeline import ResidentPipeline, StepConfig, build_masters
 
-    a, b = _data(11), _data(12)
+    a, b = _data(11, frames), _data(12, frames)
     n, h, w = a.lights.shape
     masters = build_masters(a.bias_frames, a.dark_frames, a.flat_frames)
     pipe = ResidentPipeline(n, h, w, masters, StepConfig())
