@@ -1,12 +1,17 @@
 """Benchmark of the resident light-stack hot path on GB300.
 
-Workload (default): the 32 x 2048 x 2048 uint16 stack (synthetic, seeded;
-~2000 stars, hot pixels, cosmic rays, satellite trails) -> fused decode +
-calibration -> simple_snr frame weights -> winsorized sigma-clip weighted
-integration into the six maps.  Metric: stacked Mpix-frames/s (N*H*W/1e6 per
-step / step time), plus the HBM roofline of the dominant kernel.
+Workload (default, c5): 200 uint16 frames of 9600 x 6422 (seeded synthetic,
+rendered on the device: ~20,000 stars, sky drift, cosmic rays, 7 thin-cloud
+frames; 20 bias / dark / flat frames) resident on one GPU -> fused decode +
+calibration -> star catalogs -> triangle registration -> Gauss-Newton
+refinement -> registration quality -> Lanczos3 warp -> simple_snr weights ->
+winsorized sigma-clip weighted integration into the six maps.  Metric:
+stacked Mpix-frames/s (N*H*W/1e6 per step / step time), plus the HBM roofline
+of the dominant kernel, the end-to-end rate from pinned host memory to host
+maps, and the CPU baseline (the oracle port of the reference's CPU path on a
+bounded sample).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c5|c2|c1]
 
 Under torchrun each rank processes its own stack (replicas: the path has no
 exchange step), value = all ranks' Mpix-frames / max-over-ranks time.
@@ -45,11 +50,13 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--config", default="c2", choices=["c1", "c2", "c5"],
-                   help="c5: the full 200 x 9600 x 6422 stack resident (device step only, one GPU)")
+    p.add_argument("--config", default="c5", choices=["c1", "c2", "c5"],
+                   help="c5 (default): the full 200 x 9600 x 6422 stack resident on one GPU; c1/c2: smaller stacks "
+                        "with the side reports")
     p.add_argument("--frames", type=int, default=0, help="override frame count (smaller smoke runs)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-adjoint", action="store_true", help="skip the gradient-refinement registration report")
+    p.add_argument("--no-side", action="store_true", help="c5: skip the c2 side report")
     return p.parse_args()
 
 
@@ -156,98 +163,138 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline (the oracle port of the reference algorithm, host cores)
 # ---------------------------------------------------------------------------
-CPU_CROP = 384  # side of the crops the warp, refinement and integration samples use
+CPU_TILE = 384  # side of the crop every frame of the CPU sample is cut to
+_SAMPLE = None  # per worker process: the tile stack, its masters and truth
 
 
-_CPU_DATA = None  # (lights, bias, dark, flat, truth) shared with the forked sample processes
+def cpu_sample_config(name: str, tile: int = CPU_TILE):
+    """`name`'s model on a tile x tile crop: the same frame count, noise,
+    defects and transforms, the star count scaled by area."""
+    import dataclasses
+
+    from glass_gb300.synthetic import CONFIGS
+
+    cfg = CONFIGS[name]
+    stars = max(8, int(round(cfg.stars * tile * tile / (cfg.height * cfg.width))))
+    return dataclasses.replace(cfg, height=tile, width=tile, stars=stars)
 
 
-def _cpu_step_sample(spec):
-    """One bounded sample of every stage of the step, timed with the oracle
-    port of the reference's CPU code; returns seconds per stage.  Full frames
-    for calibration, detection and registration; crops for the warp, the
-    refinement and the integration."""
-    from oracle import alignment, registration, stars, warp
+def _sample_load(path: str) -> None:
+    global _SAMPLE
+    with np.load(path) as z:
+        _SAMPLE = {k: z[k] for k in z.files}
+
+
+def _sample_frames(job):
+    """calibrate -> star catalog -> triangle registration to the reference
+    catalog -> Lanczos3 warp -> frame statistics, for a chunk of frames
+    (oracle port; the reference's CPU path for these stages)."""
+    from oracle import registration, stars, warp
     from oracle.calibration import calibrate_light
+
+    frames, ref_catalog = job
+    d = _SAMPLE
+    out = []
+    for k in frames:
+        cal = calibrate_light(d["lights"][k], d["bias"], d["dark"], d["flat"], 300.0, 300.0,
+                              master_dark_includes_bias=False)
+        found = stars.detect_stars(cal, threshold_sigma=5.0, max_stars=400)
+        catalog = [(s[0], s[1]) for s in found if s[5] is not None and s[5] <= 0.8][:80]
+        ok = k == 0
+        if k:
+            reg = registration.estimate_triangle_asterism_transform(ref_catalog, catalog)
+            ok = reg["status"] == "ok"
+            matrix = np.asarray(reg["matrix"], dtype=np.float64) if ok else d["truth"][k]
+            cal, _cov = warp.warp_matrix(cal, matrix.astype(np.float32), "lanczos3", np.nan)
+        finite = np.isfinite(cal)
+        vals = cal[finite].astype(np.float64)
+        mean, std = (float(vals.mean()), float(vals.std())) if vals.size else (0.0, 0.0)
+        weight = max(abs(mean) / std, 1.0e-6) if std > 1.0e-6 else (1.0e6 if vals.size else 0.0)
+        out.append((int(k), cal, float(weight) if ok else 0.0))
+    return out
+
+
+def _sample_integrate(job):
     from oracle.integration import weighted_integrate_stack
 
-    lights, bias, dark, flat, truth = _CPU_DATA
-    mov, y0, x0 = spec
-    n = lights.shape[0]
-    raw = lights[[0, mov]]
-    matrix = truth[mov]
-    c = CPU_CROP
-    times = {}
-    t = time.perf_counter()
-    cal = [calibrate_light(raw[k], bias, dark, flat, 1.0, 1.0, master_dark_includes_bias=False) for k in (0, 1)]
-    times["calibrate"] = (time.perf_counter() - t) / 2
-    t = time.perf_counter()
-    cats = []
-    for k in (0, 1):
-        found = stars.detect_stars(cal[k], threshold_sigma=5.0, max_stars=400)
-        cats.append([(s[0], s[1]) for s in found if s[5] is not None and s[5] <= 0.8][:80])
-    times["detect_stars"] = (time.perf_counter() - t) / 2
-    t = time.perf_counter()
-    registration.estimate_triangle_asterism_transform(cats[0], cats[1])
-    times["register"] = time.perf_counter() - t
-    ref_crop = np.ascontiguousarray(cal[0][y0:y0 + c, x0:x0 + c])
-    mov_crop = np.ascontiguousarray(cal[1][y0:y0 + c, x0:x0 + c])
-    t = time.perf_counter()
-    alignment.refine_translation(ref_crop, mov_crop, matrix, 1.0, 0.25, 0.25, 0.0625, 4, 8)
-    times["refine_translation"] = time.perf_counter() - t
-    t = time.perf_counter()
-    warp.warp_matrix(mov_crop, matrix, "lanczos3", np.nan)
-    times["warp_lanczos3"] = time.perf_counter() - t
-    stack = np.stack([calibrate_light(lights[k, y0:y0 + c, x0:x0 + c], bias[y0:y0 + c, x0:x0 + c],
-                                      dark[y0:y0 + c, x0:x0 + c], flat[y0:y0 + c, x0:x0 + c], 1.0, 1.0,
-                                      master_dark_includes_bias=False) for k in range(n)])
-    t = time.perf_counter()
-    finite = np.isfinite(stack)
-    means = np.array([stack[k][finite[k]].astype(np.float64).mean() for k in range(n)])
-    stds = np.array([stack[k][finite[k]].astype(np.float64).std() for k in range(n)])
-    weights = np.maximum(np.abs(means) / np.maximum(stds, 1e-6), 1e-6).astype(np.float32)
-    weighted_integrate_stack(stack, weights, "winsorized_sigma")
-    times["weights_integrate"] = time.perf_counter() - t
-    return times
+    band, weights = job
+    return weighted_integrate_stack(band, weights, "winsorized_sigma")[0]
 
 
-def cpu_step_estimate(data, masters, processes: int):
-    """Seconds one full step takes on the host cores (oracle port), composed
-    from `processes` concurrent samples: per-frame stages x frames, per-pixel
-    stages scaled from their crops.  Returns (Mpix-frames/s over all the
-    processes, mean seconds per step, stage seconds per step, description)."""
-    import multiprocessing as mp
+class CpuSample:
+    """The oracle port of the reference's CPU path run on a bounded sample of
+    the workload: every frame of `config_name` cut to a tile x tile crop of
+    the same model, through calibration, star catalogs, triangle registration,
+    Lanczos3 warp, simple_snr weights and winsorized 3/3 integration, spread
+    over `processes` host processes (frames, then row bands).  One step() is
+    one pass over the sample; its throughput is the sample's Mpix-frames over
+    the step's wall time.  `start` is "fork" only in a process that has not
+    touched CUDA; after CUDA it must be "spawn"."""
 
-    global _CPU_DATA
-    n, h, w = data.lights.shape
-    c = CPU_CROP
-    _CPU_DATA = (data.lights, masters.bias, masters.dark, masters.flat, data.truth_matrices)
-    rng = np.random.default_rng(0)
-    specs = [(1 + k % (n - 1), int(rng.integers(0, h - c + 1)), int(rng.integers(0, w - c + 1)))
-             for k in range(processes)]
-    if processes <= 1:
-        samples = [_cpu_step_sample(specs[0])]
-    else:
-        # forked workers share the stack without pickling it; this process
-        # has not touched CUDA (the reference arm never does)
-        with mp.get_context("fork").Pool(processes) as pool:
-            samples = pool.map(_cpu_step_sample, specs)
-    px_scale = (h * w) / (c * c)
-    steps = []
-    for s in samples:
-        stage = {"calibrate": n * s["calibrate"], "detect_stars": n * s["detect_stars"],
-                 "register": (n - 1) * s["register"],
-                 "refine_translation": (n - 1) * s["refine_translation"] * px_scale,
-                 "warp_lanczos3": (n - 1) * s["warp_lanczos3"] * px_scale,
-                 "weights_integrate": s["weights_integrate"] * px_scale}
-        steps.append(stage)
-    mean = {k: float(np.mean([st[k] for st in steps])) for k in steps[0]}
-    step_s = sum(mean.values())
-    value = processes * n * h * w / 1e6 / step_s
-    desc = (f"{processes} process(es), each: calibrate + detect 2 full {h}x{w} frames, triangle registration of one "
-            f"pair, NCC refine + Lanczos3 warp of one {c}x{c} crop pair, weights + winsorized integration of a "
-            f"{n}x{c}x{c} crop; composed to one {n}-frame step (per-pixel stages scaled by {px_scale:.0f}x)")
-    return value, step_s, mean, desc
+    def __init__(self, config_name: str, processes: int, start: str, tile: int = CPU_TILE):
+        import multiprocessing as mp
+
+        from glass_gb300.synthetic import generate
+        from oracle.calibration import calibrate_light
+        from oracle import stars
+
+        cfg = cpu_sample_config(config_name, tile)
+        data = generate(cfg)
+        bias = data.bias_frames.astype(np.float64).mean(0).astype(np.float32)
+        dark = (data.dark_frames.astype(np.float64).mean(0) - bias).astype(np.float32)
+        flat = data.flat_frames.astype(np.float64).mean(0) - bias
+        flat = np.maximum(flat / np.median(flat), 1.0e-6).astype(np.float32)
+        self.frames, self.tile, self.processes = cfg.frames, tile, processes
+        self.path = tempfile.NamedTemporaryFile(suffix=".npz", delete=False).name
+        np.savez(self.path, lights=data.lights, bias=bias, dark=dark, flat=flat, truth=data.truth_matrices)
+        _sample_load(self.path)
+        ref = calibrate_light(data.lights[0], bias, dark, flat, 300.0, 300.0, master_dark_includes_bias=False)
+        found = stars.detect_stars(ref, threshold_sigma=5.0, max_stars=400)
+        self.ref_catalog = [(s[0], s[1]) for s in found if s[5] is not None and s[5] <= 0.8][:80]
+        self.pool = mp.get_context(start).Pool(processes, initializer=_sample_load, initargs=(self.path,))
+        self.description = (f"{self.frames} frames x {tile}x{tile} crop of the {config_name} model (stars scaled by "
+                            f"area), oracle port of calibrate -> detect_stars -> triangle registration -> Lanczos3 "
+                            f"warp -> simple_snr weights -> winsorized 3/3 integration on {processes} host "
+                            f"process(es); no sub-pixel refinement (the reference CPU path has none)")
+
+    def step(self) -> float:
+        """One pass over the sample; returns its wall seconds."""
+        t0 = time.perf_counter()
+        chunks = [list(range(k, self.frames, self.processes)) for k in range(self.processes)]
+        results = self.pool.map(_sample_frames, [(c, self.ref_catalog) for c in chunks if c])
+        stack = np.empty((self.frames, self.tile, self.tile), np.float32)
+        weights = np.zeros(self.frames, np.float32)
+        for part in results:
+            for k, frame, w in part:
+                stack[k] = frame
+                weights[k] = w
+        bands = np.array_split(np.arange(self.tile), self.processes)
+        self.pool.map(_sample_integrate, [(np.ascontiguousarray(stack[:, b]), weights) for b in bands if b.size])
+        return time.perf_counter() - t0
+
+    def mpix_frames(self) -> float:
+        return self.frames * self.tile * self.tile / 1e6
+
+    def close(self) -> None:
+        self.pool.close()
+        self.pool.join()
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
+
+
+def cpu_baseline_line(config_name: str, processes: int, start: str, steps: int = 1) -> dict:
+    """cpu_baseline of the bench line: `steps` sample passes after one warm-up pass."""
+    sample = CpuSample(config_name, processes, start)
+    try:
+        sample.step()
+        secs = [sample.step() for _ in range(steps)]
+    finally:
+        sample.close()
+    mean = float(np.mean(secs))
+    return {"value": sample.mpix_frames() / mean, "unit": "Mpix-frames/s", "cores": processes, "kind": "port",
+            "sample": f"{sample.description}; {mean:.2f} s per pass"}
 
 
 def adjoint_report(pipe, dev_raw, reg, truth, h, w, stream) -> dict:
@@ -455,7 +502,7 @@ def graph_report(pipe, dev_raw, matrices, stream, reps: int) -> dict:
     import torch
 
     if pipe.frames > 32:
-        return {"skipped": "the fused warp-integration takes at most 32 frames"}
+        return {"skipped": "the captured step graph takes at most 32 frames"}
     ptr = dev_raw.data_ptr()
 
     def timed(fn):
@@ -485,45 +532,58 @@ def refinement_by(results: list, frame: int) -> dict:
     return {}
 
 
-def run_c5(args) -> int:
-    """The full c5 stack resident on one GPU: 200 frames of 9600 x 6422
-    (49.3 GB of float32 frames).  Eight distinct seeded raw frames are
-    rendered at full size (c5's star, sky and defect model; 2 calibration
-    frames of each kind) and cycled over the 200 frame slots on the device, so
-    no 24.7 GB host array is needed.  Step: calibrate -> star catalogs ->
-    triangle registration -> Gauss-Newton refinement -> Lanczos3 warp ->
-    simple-SNR weights -> winsorized 3/3 integration; CUDA events per stage
-    over K steps.  About 6000 cosmic-ray hits per frame are as bright as the
-    brightest stars, so the catalog keeps the 4096 brightest detections for
-    the shape filter to find 80 round stars among them (with 400, fewer than
-    ten survive and no frame registers)."""
-    import dataclasses
+C5_CLOUD_SLOTS = (23, 57, 88, 104, 131, 162, 190)  # the 7 thin-cloud frames (frame 0 is the reference)
+C5_AGREEMENT = {"min_score": 0.3, "rms_scale_adu": 200.0, "action": "fail", "min_weight": 0.0, "sample_stride": 8}
+C5_WORKLOAD = ("uint16 -> calibrate (20 bias/dark/flat) -> star catalogs -> triangle registration -> Gauss-Newton "
+               "refinement -> registration quality (agreement score) -> Lanczos3 warp -> simple_snr weights -> "
+               "winsorized 3/3 weighted integration (6 maps)")
 
+
+def c5_config(n: int, h: int, w: int) -> dict:
+    return {"workload": f"c5:{n}x{h}x{w} {C5_WORKLOAD}", "frames": n, "height": h, "width": w,
+            "thin_cloud_frames": list(C5_CLOUD_SLOTS), "calibration_frames_per_kind": 20,
+            "agreement_min_score": C5_AGREEMENT["min_score"],
+            "l2": "inputs larger than L2 (raw stack %.1f GB, frames %.1f GB > 129 MB)" % (2 * n * h * w / 1e9,
+                                                                                         4 * n * h * w / 1e9),
+            "parallelism": "single GPU"}
+
+
+def run_c5(args) -> int:
+    """The headline: the full c5 stack resident on one GPU - 200 uint16
+    frames of 9600 x 6422 (49.3 GB as float32 frames), 20 bias / dark / flat
+    frames, ~20,000 stars per frame, sky drift +/-15 %, cosmic rays 1e-4,
+    +/-40 px and +/-0.3 deg, and exactly 7 thin-cloud frames (50 % flux,
+    2x sky) that the registration-quality policy must weight 0.  Every frame
+    is rendered on the device (seeded).  `value`: CUDA events around K device
+    steps on the raw stack already in HBM; `e2e`: the same step through the
+    public API from pinned host uint16 to host maps."""
     import torch
 
     from glass_gb300 import _lib
+    from glass_gb300.adjoint import registration_rms_px
     from glass_gb300.pipeline import ResidentPipeline, StepConfig, build_masters
-    from glass_gb300.synthetic import CONFIGS, generate
+    from glass_gb300.synthetic import CONFIGS, generate_device
 
-    torch.cuda.set_device(0)
-    n = args.frames or 200
-    unique = 8
-    cfg = dataclasses.replace(CONFIGS["c5"], calibration_frames=2)
-    data = generate(cfg, unique)
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    replicas.init("nccl", torch.device("cuda", local))
+    cfg = CONFIGS["c5"]
+    n = args.frames or cfg.frames
+    slots = [k for k in C5_CLOUD_SLOTS if k < n]
+    t_gen = time.perf_counter()
+    data = generate_device(cfg, n, cloud_slots=slots, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t_gen
     _, h, w = data.lights.shape
+    P = h * w
     masters = build_masters(data.bias_frames, data.dark_frames, data.flat_frames)
-    pipe = ResidentPipeline(n, h, w, masters, StepConfig(star_max_stars=4096, refine_method="gradient"))
+    pipe = ResidentPipeline(n, h, w, masters, StepConfig(star_max_stars=4096, refine_method="gradient",
+                                                         agreement=dict(C5_AGREEMENT)))
     stream = torch.cuda.Stream()
     pipe.set_stream(stream.cuda_stream)
-    dev_raw = torch.from_numpy(data.lights.view(np.int16)).cuda()
-    truth = np.asarray([data.truth_matrices[k % unique] for k in range(n)])
-    idx_groups = [np.arange(k, min(k + unique, n), dtype=np.int64) for k in range(0, n, unique)]
+    dev_raw = data.lights
+    truth = data.truth_matrices
     reg = {}
-
-    def calibrate():
-        for g in idx_groups:
-            _lib.call("gg_stack_calibrate_u16_device", pipe.stack.handle, _lib.ptr(g), ctypes.c_int64(g.size),
-                      ctypes.c_void_p(dev_raw.data_ptr()), 0, ctypes.byref(pipe._calib_params()))
 
     def register():
         reg["triangle"], reg["ok"] = pipe.register(0)
@@ -531,183 +591,244 @@ def run_c5(args) -> int:
     def refine():
         reg["m"] = pipe.refine(reg["triangle"], 0)
 
-    P = h * w
-    stages = [("calibrate", calibrate, 6 * n * P + 12 * P), ("detect_stars", pipe.detect, 4 * n * P),
-              ("register", register, None), ("refine_gradient", refine, None),
+    def assess():
+        reg["quality"] = pipe.assess(reg["m"], 0)
+
+    sampled = -(-h // C5_AGREEMENT["sample_stride"]) * -(-w // C5_AGREEMENT["sample_stride"])
+    stages = [("calibrate", lambda: pipe.calibrate_device(dev_raw.data_ptr()), 6 * n * P + 12 * P),
+              ("detect_stars", pipe.detect, 4 * n * P),
+              ("register", register, None),
+              ("refine_gradient", refine, None),
+              ("registration_quality", assess, 8 * (n - 1) * sampled),
               ("warp_lanczos3", lambda: pipe.warp(reg["m"]), 8 * (n - 1) * P),
-              ("weights", pipe.weights, 4 * n * P), ("integrate_winsorized", pipe.integrate, 4 * n * P + 16 * P)]
+              ("weights", pipe.weights, 4 * n * P),
+              ("integrate_winsorized", pipe.integrate, 4 * n * P + 16 * P)]
     for _ in range(max(1, args.warmup)):
         for _, fn, _ in stages:
             fn()
     stream.synchronize()
+    replicas.barrier()
+    torch.cuda.synchronize()
+    launches0 = _lib.kernel_launches()
     events = {name: [] for name, _, _ in stages}
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    start.record(stream)
-    for _ in range(args.steps):
-        for name, fn, _ in stages:
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            events[name].append((e0, e1))
-    stop.record(stream)
-    stream.synchronize()
-    ms = start.elapsed_time(stop) / args.steps
-    peak, kind = measured_peak()
+    with ClockSampler(local) as clocks:
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clocks.mark_start()
+        start.record(stream)
+        for _ in range(args.steps):
+            for name, fn, _ in stages:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                events[name].append((e0, e1))
+        stop.record(stream)
+        stream.synchronize()
+        clocks.mark_stop()
+    torch.cuda.synchronize()
+    replicas.barrier()
+    launches = _lib.kernel_launches() - launches0
+    elapsed_ms = replicas.max_over_ranks(start.elapsed_time(stop), torch.device("cuda", local))
+    mpix = n * P / 1e6
+    value = replicas.replica_throughput(world, mpix, args.steps, elapsed_ms / 1e3)
+    peak, peak_kind = measured_peak()
     out_stages = {}
     for name, _, nbytes in stages:
         t = statistics.mean(a.elapsed_time(b) for a, b in events[name])
         gbs = None if nbytes is None else nbytes / (t / 1e3) / 1e9
         out_stages[name] = {"ms": t, "algorithmic_bytes": nbytes, "achieved_gbs": gbs,
                             "frac": None if gbs is None else gbs / peak}
+    weights = pipe.stack.device_frame_weights()
     ok = [k for k in range(1, n) if reg["ok"][k]]
-    from glass_gb300.adjoint import registration_rms_px
 
-    # ingest: the 200 raw frames from pinned host memory (the 8 distinct
-    # frames cycled) -> H2D -> decode + calibration, the reference's
-    # host-read/H2D-bound stage
-    host_raw = torch.from_numpy(data.lights.view(np.int16)).pin_memory()
-
-    def ingest():
-        for g in idx_groups:
-            _lib.call("gg_stack_calibrate_u16", pipe.stack.handle, _lib.ptr(g), ctypes.c_int64(g.size),
-                      ctypes.c_void_p(host_raw.data_ptr()), 0, ctypes.byref(pipe._calib_params()))
-
-    ingest()
-    stream.synchronize()
-    i0, i1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # ---- end to end through the public API: pinned host uint16 in, host maps out ----
+    pinned = torch.empty((n, h, w), dtype=torch.int16, pin_memory=True)
+    for k in range(n):
+        pinned[k].copy_(dev_raw[k])
+    host_raw = pinned.numpy().view(np.uint16)
+    map_out = tuple(torch.empty((h, w), dtype=torch.float32).pin_memory().numpy() for _ in range(2))
+    map_out += tuple(torch.empty((h, w), dtype=torch.int16).pin_memory().numpy().view(np.uint16) for _ in range(3))
+    map_out += (torch.empty((h, w), dtype=torch.int16).pin_memory().numpy(),)
+    e2e_steps = max(3, min(args.steps, 10))
+    pipe.step_host(host_raw, register=True, out=map_out)
+    replicas.barrier()
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    i0.record(stream)
-    ingest()
-    i1.record(stream)
-    stream.synchronize()
-    ingest_wall_ms = 1e3 * (time.perf_counter() - t0)
-    ingest_ms = i0.elapsed_time(i1)
-    raw_bytes = 2 * n * P
-    # fused Lanczos3 warp + winsorized integration of the 200 frames (the
-    # warp-per-pixel integrator sampling every frame; nothing written to the
-    # stack) against the warp + integrate stages above
-    calibrate()
-    pipe.weights()
-    cfg = pipe.config
+    for _ in range(e2e_steps):
+        maps = pipe.step_host(host_raw, register=True, out=map_out)
+    e2e_s = replicas.max_over_ranks(time.perf_counter() - t0, torch.device("cuda", local))
+    e2e_value = replicas.replica_throughput(world, mpix, e2e_steps, e2e_s)
+    h2d = int(host_raw.nbytes)
+    d2h = int(sum(m.nbytes for m in maps if m is not None))
+    e2e_weights = pipe.stack.device_frame_weights()
+    del pinned, host_raw
 
-    def fused():
-        pipe.stack.integrate_warped_device_weights(reg["m"], cfg.interpolation, cfg.clamping_threshold, cfg.rejection,
-                                                   cfg.low_sigma, cfg.high_sigma, cfg.min_samples,
-                                                   cfg.max_reject_fraction, cfg.count_map_dtype)
-
-    fused()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    fused()
-    f1.record(stream)
-    stream.synchronize()
-    fused_ms = f0.elapsed_time(f1)
-    calibrate()  # detection statistics of the calibrated (not the warped) frames
-    info = pipe.detect(info=True)
-    inliers = [r["inliers"] for r in pipe.last_registration]
     rms_tri = registration_rms_px([reg["triangle"][k] for k in ok], [truth[k] for k in ok], h, w)
     rms_gn = registration_rms_px([reg["m"][k] for k in ok], [truth[k] for k in ok], h, w)
     refinement = getattr(pipe, "last_refinement", [])
-    per_frame = sorted(((registration_rms_px([reg["m"][k]], [truth[k]], h, w),
-                         registration_rms_px([reg["triangle"][k]], [truth[k]], h, w), k) for k in ok), reverse=True)
-
-    line = {"metric": "stacked Mpix-frames/s", "value": n * P / 1e6 / (ms / 1e3), "unit": "Mpix-frames/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (8 distinct seeded raw frames cycled over the frame slots)",
-            "config": {"workload": f"c5:{n}x{h}x{w} uint16 -> calibrate -> star catalogs -> triangle registration "
-                                   "-> Gauss-Newton refinement -> Lanczos3 warp -> simple_snr weights -> "
-                                   "winsorized 3/3 integration",
-                       "star_max_stars": 4096,
-                       "frames": n, "height": h, "width": w, "unique_raw_frames": unique,
-                       "l2": "inputs larger than L2", "peak_source": kind},
-            "resident": {"stack_bytes_allocated": pipe.stack.bytes_allocated,
-                         "device_bytes_in_use": int(torch.cuda.mem_get_info()[1] - torch.cuda.mem_get_info()[0])},
-            "stages": out_stages,
-            "fused_warp_integrate": {"ms": fused_ms, "vs_warp_plus_integrate_ms":
-                                     out_stages["warp_lanczos3"]["ms"] + out_stages["integrate_winsorized"]["ms"]},
-            "ingest_from_pinned_host": {"frames": n, "raw_bytes": raw_bytes, "ms_events": ingest_ms,
-                                        "ms_wall": ingest_wall_ms,
-                                        "raw_gb_per_s": raw_bytes / (max(ingest_ms, ingest_wall_ms) / 1e3) / 1e9},
-            "detection": {"candidates_max": max(r["candidates"] for r in info),
-                          "candidates_min": min(r["candidates"] for r in info), "candidate_capacity": 32768,
-                          "catalog_stars_min": min(r["stars"] for r in info)},
-            "registration": {"frames_ok": len(ok) + 1, "frames": n,
-                             "inliers_median": float(np.median(inliers)) if inliers else None,
-                             "rms_px_vs_truth": {"triangle": rms_tri, "gradient_gauss_newton": rms_gn},
-                             "refine_status": {str(v): sum(1 for r in refinement if r.get("status") == v)
-                                               for v in sorted({r.get("status") for r in refinement})},
-                             "refine_iterations_mean": (float(np.mean([r["iterations"] for r in refinement]))
-                                                        if refinement else None),
-                             "refine_last_step_px_median_at_cap": (
-                                 float(np.median([r["last_step_px"] for r in refinement
-                                                  if r.get("status") == "iteration_cap"]))
-                                 if any(r.get("status") == "iteration_cap" for r in refinement) else None),
-                             "worst_frames": [{"frame": k, "gradient_px": g, "triangle_px": t,
-                                               **{q: refinement_by(refinement, k).get(q)
-                                                  for q in ("status", "iterations", "alpha", "sigma", "samples",
-                                                            "last_step_px")}}
-                                              for g, t, k in per_frame[:6]]}}
-    print(json.dumps(line))
+    qual = reg.get("quality", [])
+    cloud = [int(k) for k in slots]
+    registration = {
+        "frames_ok": len(ok) + 1, "frames": n,
+        "inliers_median": float(np.median([r["inliers"] for r in pipe.last_registration])),
+        "rms_px_vs_truth": {"triangle": rms_tri, "gradient_gauss_newton": rms_gn},
+        "refine_status": {str(v): sum(1 for r in refinement if r.get("status") == v)
+                          for v in sorted({r.get("status") for r in refinement})},
+        "quality": {"thin_cloud_frames": cloud,
+                    "thin_cloud_weights": [float(weights[k]) for k in cloud],
+                    "zero_weight_frames": [int(k) for k in range(n) if weights[k] <= 0.0],
+                    "e2e_zero_weight_frames": [int(k) for k in range(n) if e2e_weights[k] <= 0.0],
+                    "score_clear_min": float(min((q["score"] for q in qual if q.get("score") is not None
+                                                  and q["frame"] not in cloud), default=float("nan"))),
+                    "score_cloud_max": float(max((q["score"] for q in qual if q.get("score") is not None
+                                                  and q["frame"] in cloud), default=float("nan")))}}
+    stack_bytes = pipe.stack.bytes_allocated
     pipe.close()
+    del dev_raw, data
+    torch.cuda.empty_cache()
+    side = {}
+    if not args.no_side:
+        side["c2"] = c2_side_report(local, max(3, min(args.steps, 10)))
+    if rank != 0:
+        replicas.shutdown()
+        return 0
+    top = max((k for k in out_stages if out_stages[k]["algorithmic_bytes"]), key=lambda k: out_stages[k]["ms"])
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline_line("c5", os.cpu_count() or 1, "spawn")
+    line = {
+        "metric": "stacked Mpix-frames/s", "value": value, "unit": "Mpix-frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (every frame rendered on the device from the seeded c5 model)",
+        "config": c5_config(n, h, w),
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": out_stages[top]["achieved_gbs"], "peak": peak,
+                     "unit": "GB/s", "frac": out_stages[top]["frac"], "peak_source": peak_kind,
+                     "traffic": profile_traffic(f"{top}_c5.md"),
+                     "algorithmic_bytes_per_launch": out_stages[top]["algorithmic_bytes"],
+                     "launch_ms": out_stages[top]["ms"]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "Mpix-frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": 1e3 * e2e_s / e2e_steps},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "stages": out_stages,
+        "registration": registration,
+        "resident": {"stack_bytes_allocated": stack_bytes, "generate_s": gen_s},
+        "side_reports": side,
+    }
+    print(json.dumps(line))
+    replicas.shutdown()
     return 0
+
+
+def c2_side_report(local: int, steps: int) -> dict:
+    """The 32 x 2048 x 2048 stack (c2 model, rendered on the device): the same
+    device step as the headline (Gauss-Newton refinement, quality policy in
+    audit mode), CUDA events over `steps` steps."""
+    import torch
+
+    from glass_gb300.pipeline import ResidentPipeline, StepConfig, build_masters
+    from glass_gb300.synthetic import generate_device
+
+    data = generate_device("c2", device=f"cuda:{local}")
+    n, h, w = data.lights.shape
+    masters = build_masters(data.bias_frames, data.dark_frames, data.flat_frames)
+    pipe = ResidentPipeline(n, h, w, masters, StepConfig(refine_method="gradient"))
+    stream = torch.cuda.Stream()
+    pipe.set_stream(stream.cuda_stream)
+    try:
+        def step():
+            pipe.calibrate_device(data.lights.data_ptr())
+            pipe.detect()
+            m, _ = pipe.register(0)
+            m = pipe.refine(m, 0)
+            pipe.assess(m, 0)
+            pipe.warp(m)
+            pipe.weights()
+            pipe.integrate()
+
+        for _ in range(2):
+            step()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+    finally:
+        pipe.close()
+    return {"workload": f"c2:{n}x{h}x{w} (same step as the headline)", "ms_per_step": ms,
+            "mpix_frames_per_s": n * h * w / 1e6 / (ms / 1e3), "steps": steps}
+
+
+def run_reference(args) -> int:
+    """--impl reference: the oracle port of the reference's CPU path (the
+    reference itself is not on the GPU host) on all host cores, rank 0 only,
+    no CUDA.  Each step is one pass over the bounded sample of the workload
+    (every frame cut to a 384 x 384 crop of the same model); `value` is the
+    sample's Mpix-frames over the mean step time."""
+    rank, _world, _local = dist_env()
+    if rank != 0:
+        return 0
+    from glass_gb300.synthetic import CONFIGS
+
+    cfg = CONFIGS[args.config]
+    n = args.frames or cfg.frames
+    procs = os.cpu_count() or 1
+    sample = CpuSample(args.config, procs, "fork")
+    try:
+        for _ in range(args.warmup):
+            sample.step()
+        secs = [sample.step() for _ in range(args.steps)]
+    finally:
+        sample.close()
+    step_s = float(np.mean(secs))
+    value = sample.mpix_frames() / step_s
+    config = c5_config(n, cfg.height, cfg.width) if args.config == "c5" else c2_config(args.config, n, cfg)
+    line = {"metric": "stacked Mpix-frames/s", "value": value, "unit": "Mpix-frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": config,
+            "cpu_baseline": {"value": value, "unit": "Mpix-frames/s", "cores": procs, "kind": "port",
+                             "sample": sample.description},
+            "e2e": {"value": value, "unit": "Mpix-frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def c2_config(name: str, n: int, cfg) -> dict:
+    return {"workload": f"{name}:{n}x{cfg.height}x{cfg.width} uint16 -> calibrate -> star catalogs -> triangle "
+                        f"registration -> sub-pixel translation refinement -> Lanczos3 warp -> simple_snr weights -> "
+                        f"winsorized 3/3 weighted integration (6 maps)",
+            "frames": n, "height": cfg.height, "width": cfg.width,
+            "l2": "inputs larger than L2 (stack %.0f MB > 129 MB)" % (4 * n * cfg.height * cfg.width / 1e6),
+            "parallelism": "single GPU"}
 
 
 # ---------------------------------------------------------------------------
 def main():
     args = parse_args()
-    if args.config == "c5" and args.impl == "gb300":
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.config == "c5":
         return run_c5(args)
+    return run_c2(args)
+
+
+def run_c2(args) -> int:
+    """--config c1 / c2: the smaller stack with the NCC candidate-grid
+    refinement (the reference's resident default) and the side reports
+    (registration accuracy, CUDA graph, local normalisation, batched stacks,
+    200-frame integration, autotune)."""
     rank, world, local = dist_env()
     from glass_gb300.synthetic import CONFIGS, generate
 
     cfg = CONFIGS[args.config]
     frames = args.frames or cfg.frames
-    workload = f"{args.config}:{frames}x{cfg.height}x{cfg.width} uint16 -> calibrate -> star catalogs -> " \
-               f"triangle registration -> sub-pixel translation refinement -> Lanczos3 warp -> simple_snr " \
-               f"weights -> winsorized 3/3 weighted " \
-               f"integration (6 maps)"
     metric = "stacked Mpix-frames/s"
-
-    if args.impl == "reference":
-        if rank != 0:
-            return 0
-        data = generate(cfg, frames)
-        from oracle.integration import weighted_integrate_stack  # noqa: F401  (the oracle port)
-        bias = data.bias_frames.astype(np.float64).mean(0).astype(np.float32)
-        dark = (data.dark_frames.astype(np.float64).mean(0) - bias).astype(np.float32)
-        flat = (data.flat_frames.astype(np.float64).mean(0) - bias)
-        flat = np.maximum(flat / np.median(flat), 1e-6).astype(np.float32)
-
-        class M:  # noqa: D401
-            pass
-
-        m = M()
-        m.bias, m.dark, m.flat = bias, dark, flat
-        procs = os.cpu_count() or 1
-        if args.warmup > 0:  # one untimed sample batch warms the caches and imports
-            cpu_step_estimate(data, m, procs)
-        values, step_s, desc, stages = [], [], "", {}
-        for _ in range(args.steps):
-            v, s, stages, desc = cpu_step_estimate(data, m, procs)
-            values.append(v)
-            step_s.append(s)
-        value = float(np.mean(values))
-        line = {
-            "metric": metric, "value": value, "unit": "Mpix-frames/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(step_s)) / procs,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload, "sample": desc},
-            "stages_s_per_step_one_process": stages,
-            "cpu_baseline": {"value": value, "unit": "Mpix-frames/s", "cores": procs, "kind": "port",
-                             "sample": desc},
-            "e2e": {"value": value, "unit": "Mpix-frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        }
-        print(json.dumps(line))
-        return 0
-
     import torch
 
     torch.cuda.set_device(local)
@@ -855,11 +976,7 @@ def main():
     top = max((k for k in kernels if kernels[k]["algorithmic_bytes"]), key=lambda k: kernels[k]["ms"])
     cpu = None
     if not args.no_cpu_baseline:
-        t_cpu = time.perf_counter()
-        rate, step_s, cpu_stages, desc = cpu_step_estimate(data, masters, 1)
-        cpu = {"value": rate, "unit": "Mpix-frames/s", "cores": 1, "kind": "port",
-               "sample": f"{desc}; sample took {time.perf_counter() - t_cpu:.1f} s, one step {step_s:.1f} s",
-               "stages_s_per_step": cpu_stages}
+        cpu = cpu_baseline_line(args.config, os.cpu_count() or 1, "spawn")
     line = {
         "metric": metric,
         "value": value,
@@ -873,9 +990,7 @@ def main():
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded generator, benchmark-config shapes and noise model)",
-        "config": {"workload": workload, "frames": n, "height": h, "width": w,
-                   "l2": "inputs larger than L2 (stack %.0f MB > 129 MB)" % (4 * n * h * w / 1e6),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": dict(c2_config(args.config, n, cfg), parallelism="replicas" if world > 1 else "single GPU"),
         "roofline": {"bound": "hbm", "kernel": top, "achieved": kernels[top]["achieved_gbs"], "peak": peak,
                      "unit": "GB/s", "frac": kernels[top]["frac"], "peak_source": peak_kind,
                      "traffic": profile_traffic(f"{top}_c2.md"),

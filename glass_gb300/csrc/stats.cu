@@ -74,7 +74,9 @@ __global__ void __launch_bounds__(256) frame_stats_kernel(const float* slots, co
 // simple_snr weights from the per-CTA partials (resident_cuda.py:1948-1956):
 //   valid == 0 -> 0;  std <= eps -> 1/eps;  else max(|mean|/std, eps)
 // A frame whose prior weight is not finite and positive keeps weight 0
-// (zero-weight frames are skipped, resident_cuda.py:12766-12770).
+// (zero-weight frames are skipped, resident_cuda.py:12766-12770); otherwise
+// the prior multiplies the SNR weight in float64 (the registration-agreement
+// multiplier, resident_cuda.py:12800-12804).
 // One warp per frame: lanes fold the CTA partials, then a shuffle reduction.
 __global__ void snr_weights_kernel(const double* partials, int blocks, const int* frames, int count,
                                    const float* prior, float eps, int mode, float* weights) {
@@ -110,7 +112,7 @@ __global__ void snr_weights_kernel(const double* partials, int blocks, const int
   const double sd = sqrt(var);
   const double e = static_cast<double>(eps);
   const double w = sd <= e ? 1.0 / e : fmax(fabs(mean) / sd, e);
-  weights[f] = static_cast<float>(w);
+  weights[f] = static_cast<float>(w * static_cast<double>(pw));
 }
 
 // Per-CTA (sum, sum2, count) partials of the given frames (device frame list).

@@ -117,7 +117,19 @@ class StepConfig:
     # warp adjoint's derivatives (gradient_refine below)
     refine_method: str = "ncc"
     gradient_refine: dict | None = None
+    # registration-quality weighting (glass_gb300.quality): pixel-agreement
+    # score of each frame's final matrix against the reference (NCC and RMS
+    # of the alignment metrics at `sample_stride`), its minimum (None: audit
+    # only), the action on a miss and the downweight floor; then the
+    # inlier / fit-RMS gate ("auto": exclude for this triangle mode)
+    agreement: dict | None = None
+    quality_action: str = "auto"
+    quality_min_inliers: int = 4
+    quality_max_rms_px: float | None = None
 
+
+DEFAULT_AGREEMENT = {"min_score": None, "rms_scale_adu": 200.0, "action": "fail", "min_weight": 0.0,
+                     "sample_stride": 8}
 
 DEFAULT_REFINE = {"search_radius_px": 1.0, "coarse_step_px": 0.25, "fine_radius_px": 0.25, "fine_step_px": 0.0625,
                   "coarse_sample_stride": 4, "final_sample_stride": 8}
@@ -221,6 +233,8 @@ class ResidentPipeline:
                  "descriptors_moving": int(r.descriptors_moving), "rms_px": float(r.rms_px)}
                 for k, r in zip(idx, out)]
         self._registered = ok
+        self._accepted = ok.copy()
+        self._multipliers = np.ones(self.frames, dtype=np.float64)
         return matrices, ok
 
     def refine(self, matrices: np.ndarray, reference_index: int = 0) -> np.ndarray:
@@ -280,6 +294,51 @@ class ResidentPipeline:
             outcomes.append(res)
         return out, outcomes
 
+    def assess(self, matrices: np.ndarray, reference_index: int = 0) -> list[dict]:
+        """Registration quality of every registered frame under its final
+        matrix (run before warp()): the inlier / fit-RMS gate, then the
+        pixel-agreement score and policy.  Frames that fail get weight 0 in
+        weights(); downweighted frames get the policy's multiplier.  Returns
+        one record per moving frame (one host synchronisation)."""
+        from glass_gb300 import quality
+
+        cfg = self.config
+        ag = dict(DEFAULT_AGREEMENT, **(cfg.agreement or {}))
+        ok = getattr(self, "_registered", np.ones(self.frames, dtype=bool)).copy()
+        regs = {r["frame"]: r for r in getattr(self, "last_registration", [])}
+        mult = np.ones(self.frames, dtype=np.float64)
+        records = []
+        for k in range(self.frames):
+            if k == reference_index or not ok[k] or k not in regs:
+                continue
+            r = regs[k]
+            gate = quality.registration_quality("ok", r["inliers"], r["rms_px"], "similarity_cuda_triangle",
+                                                cfg.quality_action, cfg.quality_min_inliers, cfg.quality_max_rms_px)
+            if not gate["accepted"]:
+                ok[k] = False
+            records.append({"frame": k, "gate": gate})
+        idx = np.array([rec["frame"] for rec in records if ok[rec["frame"]]], dtype=np.int64)
+        metrics = self.stack.matrix_alignment_metrics(reference_index, idx, np.asarray(matrices)[idx],
+                                                      int(ag["sample_stride"])) if idx.size else []
+        by_frame = dict(zip(idx.tolist(), metrics))
+        for rec in records:
+            k = rec["frame"]
+            if k not in by_frame:
+                continue
+            m = by_frame[k]
+            q = quality.agreement_quality(m["ncc"], m["rms"], regs[k]["rms_px"], ag["rms_scale_adu"], ag["min_score"])
+            pol = quality.agreement_policy(q, ag["action"], ag["min_weight"])
+            rec.update(score=q["score"], pixel_ncc=q["pixel_ncc"], pixel_rms_adu=q["pixel_rms_adu"],
+                       status=pol["status"], multiplier=pol["weight_multiplier"])
+            if pol["hard_failure"]:
+                ok[k] = False
+            elif pol["weight_multiplier"] < 1.0:
+                mult[k] = pol["weight_multiplier"]
+        self._accepted = ok
+        self._multipliers = mult
+        self.last_quality = records
+        return records
+
     def warp(self, matrices: np.ndarray, reference_index: int = 0) -> None:
         """Warps every frame but the reference through its moving->reference matrix."""
         ok = getattr(self, "_registered", None)
@@ -292,8 +351,14 @@ class ResidentPipeline:
         self.stack.warp_frames_async(idx, mats, interp, np.nan, self.config.clamping_threshold, False)
 
     def weights(self) -> None:
-        ok = getattr(self, "_registered", None)
-        prior = None if ok is None else ok.astype(np.float32)
+        """Frame weights on the device: simple_snr (or unit) times the
+        registration-quality multiplier; 0 for frames that failed
+        registration or its quality checks (assess())."""
+        ok = getattr(self, "_accepted", getattr(self, "_registered", None))
+        prior = None
+        if ok is not None:
+            mult = getattr(self, "_multipliers", np.ones(self.frames))
+            prior = np.where(ok, mult, 0.0).astype(np.float32)
         self.stack.compute_frame_weights(self.config.weighting, prior, 1.0e-6, download=False)
 
     def local_normalize(self, reference_index: int = 0) -> None:
@@ -352,6 +417,7 @@ class ResidentPipeline:
             self.detect()
             matrices, _ok = self.register()
             matrices = self.refine(matrices)
+            self.assess(matrices)
         if matrices is not None:
             self.warp(matrices)
         self.weights()

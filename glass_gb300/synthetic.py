@@ -155,8 +155,9 @@ def generate(config: StackConfig | str, frames: int | None = None) -> SyntheticS
     flat_frames = np.stack([noisy(vignette * cfg.flat_level) for _ in range(cal)])
 
     cloud = np.zeros(n, dtype=bool)
-    if cfg.cloud_frames:
-        cloud[rng.choice(n, size=min(cfg.cloud_frames, n), replace=False)] = True
+    if cfg.cloud_frames and n > 1:
+        # frame 0 is the registration reference: never a thin-cloud frame
+        cloud[1 + rng.choice(n - 1, size=min(cfg.cloud_frames, n - 1), replace=False)] = True
     lights = np.empty((n, h, w), dtype=np.uint16)
     truth = np.empty((n, 3, 3), dtype=np.float64)
     for i in range(n):
@@ -208,3 +209,162 @@ def generate(config: StackConfig | str, frames: int | None = None) -> SyntheticS
         lights[i] = np.clip(np.rint(frame), 0, 65535).astype(np.uint16)
     return SyntheticStack(cfg, lights, bias_frames, dark_frames, flat_frames, truth, star_xy, star_peak, cloud,
                           {"vignette_min": vmin, "vignette_max": vmax})
+
+
+@dataclass
+class DeviceStack:
+    """A synthetic stack rendered on the GPU (the same model as generate()):
+    `lights` is a (N, H, W) int16 CUDA tensor holding the uint16 raw frames
+    bit for bit; the calibration frames are host uint16 arrays."""
+
+    config: StackConfig
+    lights: "object"  # torch.Tensor (N, H, W) int16 on the device
+    bias_frames: np.ndarray
+    dark_frames: np.ndarray
+    flat_frames: np.ndarray
+    truth_matrices: np.ndarray
+    cloud: np.ndarray
+
+
+def _u16_as_i16(torch, values):
+    """Rounded float32 ADU -> int16 tensor with the uint16 bit pattern."""
+    v = torch.clamp(torch.round(values), 0.0, 65535.0).to(torch.int32)
+    return torch.where(v > 32767, v - 65536, v).to(torch.int16)
+
+
+def generate_device(config: StackConfig | str, frames: int | None = None, cloud_slots: list[int] | None = None,
+                    device: str = "cuda") -> DeviceStack:
+    """Renders a stack of `config`'s model directly in device memory, one
+    frame at a time (a 200 x 9600 x 6422 stack in seconds; the NumPy
+    generator would take most of an hour).  Star positions, fluxes, PSFs,
+    transforms and sky levels come from NumPy's seeded generator; the shot,
+    read and cosmic-ray noise from a seeded torch CUDA generator.  Thin-cloud
+    frames (50 % star flux, 2x sky) are exactly `cloud_slots` when given
+    (frame 0, the registration reference, is never one), else
+    `config.cloud_frames` frames drawn from 1..N-1."""
+    import torch
+
+    cfg = CONFIGS[config] if isinstance(config, str) else config
+    n = int(frames or cfg.frames)
+    rng = np.random.default_rng(cfg.seed)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(cfg.seed)
+    h, w = cfg.height, cfg.width
+    margin = cfg.max_shift + np.deg2rad(cfg.max_rotation_deg) * max(h, w) + 8
+    star_xy = np.column_stack([rng.uniform(-margin, w + margin, cfg.stars), rng.uniform(-margin, h + margin, cfg.stars)])
+    lo, hi = cfg.peak_flux
+    star_peak = np.exp(rng.uniform(np.log(lo), np.log(hi), cfg.stars))
+    sigma = rng.uniform(cfg.fwhm[0], cfg.fwhm[1], cfg.stars) / 2.3548200450309493
+    moffat = rng.random(cfg.stars) < cfg.moffat_fraction
+    radius = int(np.ceil(4.0 * sigma.max())) + 1
+    offs = torch.arange(-radius, radius + 1, device=device, dtype=torch.float32)
+    t_sigma = torch.as_tensor(sigma, device=device, dtype=torch.float32)
+    t_moffat = torch.as_tensor(moffat, device=device)
+
+    yy = torch.arange(h, device=device, dtype=torch.float32)[:, None]
+    xx = torch.arange(w, device=device, dtype=torch.float32)[None, :]
+    rr = ((xx - w / 2) / (w / 2)) ** 2 + ((yy - h / 2) / (h / 2)) ** 2
+    vmin, vmax = cfg.vignetting
+    vignette = vmax - (vmax - vmin) * torch.clamp(rr / 2.0, 0.0, 1.0)
+    del rr
+    dark_rate = torch.full((h, w), cfg.dark_current, device=device, dtype=torch.float32)
+    n_hot = int(round(cfg.hot_pixel_fraction * h * w))
+    if n_hot:
+        hot = rng.choice(h * w, size=n_hot, replace=False)
+        dark_rate.view(-1)[torch.as_tensor(hot, device=device)] = torch.as_tensor(
+            rng.uniform(5.0, 50.0, n_hot), device=device, dtype=torch.float32)
+
+    def noisy(signal):
+        out = torch.poisson(torch.clamp(signal, min=0.0), generator=gen)
+        out += cfg.pedestal + cfg.read_noise * torch.randn((h, w), device=device, generator=gen)
+        return _u16_as_i16(torch, out)
+
+    def host_u16(t):
+        return t.cpu().numpy().view(np.uint16)
+
+    cal = cfg.calibration_frames
+    zeros = torch.zeros((h, w), device=device)
+    bias_frames = np.stack([host_u16(noisy(zeros)) for _ in range(cal)])
+    dark_frames = np.stack([host_u16(noisy(dark_rate * cfg.exposure_s)) for _ in range(cal)])
+    flat_frames = np.stack([host_u16(noisy(vignette * cfg.flat_level)) for _ in range(cal)])
+    del zeros
+
+    cloud = np.zeros(n, dtype=bool)
+    if cloud_slots is not None:
+        cloud[np.asarray(cloud_slots, dtype=np.int64)] = True
+    elif cfg.cloud_frames and n > 1:
+        cloud[1 + rng.choice(n - 1, size=min(cfg.cloud_frames, n - 1), replace=False)] = True
+    if cloud[0]:
+        raise ValueError("frame 0 is the registration reference and cannot be a thin-cloud frame")
+    lights = torch.empty((n, h, w), device=device, dtype=torch.int16)
+    truth = np.empty((n, 3, 3), dtype=np.float64)
+    beta = 3.0
+    for i in range(n):
+        if i == 0:
+            theta, dx, dy = 0.0, 0.0, 0.0
+        elif cfg.integer_shifts:
+            theta = 0.0
+            dx, dy = (float(v) for v in rng.integers(-int(cfg.max_shift), int(cfg.max_shift) + 1, 2))
+        else:
+            theta = np.deg2rad(rng.uniform(-cfg.max_rotation_deg, cfg.max_rotation_deg))
+            dx, dy = (float(v) for v in rng.uniform(-cfg.max_shift, cfg.max_shift, 2))
+        forward = _similarity(theta, dx, dy)
+        truth[i] = np.linalg.inv(forward)
+        pos = star_xy @ forward[:2, :2].T + forward[:2, 2]
+        sky = rng.uniform(*cfg.sky) * (2.0 if cloud[i] else 1.0)
+        flux = star_peak * (0.5 if cloud[i] else 1.0)
+        gx, gy = rng.uniform(-1, 1, 2) * cfg.sky_gradient * sky
+        signal = sky + gx * (xx / w - 0.5) + gy * (yy / h - 0.5)
+        # stars: one (2r+1)^2 stamp per star, accumulated into the frame
+        px_c = torch.as_tensor(pos[:, 0], device=device)
+        py_c = torch.as_tensor(pos[:, 1], device=device)
+        inside = (px_c > -radius) & (px_c < w + radius) & (py_c > -radius) & (py_c < h + radius)
+        cx = torch.floor(px_c).to(torch.int64)
+        cy = torch.floor(py_c).to(torch.int64)
+        gxs = cx[:, None] + offs.to(torch.int64)[None, :]
+        gys = cy[:, None] + offs.to(torch.int64)[None, :]
+        ddx = (gxs.to(torch.float64) - px_c[:, None]).to(torch.float32)
+        ddy = (gys.to(torch.float64) - py_c[:, None]).to(torch.float32)
+        r2 = ddx[:, None, :] ** 2 + ddy[:, :, None] ** 2
+        s2 = (t_sigma**2)[:, None, None]
+        prof = torch.where(t_moffat[:, None, None], (1.0 + r2 / (s2 * 2.0 * np.sqrt(2.0))) ** (-beta),
+                           torch.exp(-0.5 * r2 / s2))
+        prof = prof * torch.as_tensor(flux, device=device, dtype=torch.float32)[:, None, None]
+        ys_b = gys[:, :, None].expand_as(prof)
+        xs_b = gxs[:, None, :].expand_as(prof)
+        ok = inside[:, None, None] & (ys_b >= 0) & (ys_b < h) & (xs_b >= 0) & (xs_b < w)
+        signal.view(-1).index_put_((ys_b[ok] * w + xs_b[ok],), prof[ok], accumulate=True)
+        del prof, ys_b, xs_b, ok, r2, ddx, ddy
+        signal = signal * vignette + dark_rate * cfg.exposure_s
+        frame = torch.poisson(torch.clamp(signal, min=0.0), generator=gen)
+        frame += cfg.pedestal + cfg.read_noise * torch.randn((h, w), device=device, generator=gen)
+        del signal
+        if cfg.cosmic_ray_density:
+            hits = int(rng.poisson(cfg.cosmic_ray_density * h * w))
+            crx = rng.integers(0, w, hits)
+            cry = rng.integers(0, h, hits)
+            length = rng.integers(2, 7, hits)
+            ang = rng.uniform(0, np.pi, hits)
+            energy = rng.uniform(5000.0, 60000.0, hits)
+            flat_idx, vals = [], []
+            for step in range(6):
+                on = step < length
+                sy = np.clip(np.rint(cry + step * np.sin(ang)).astype(np.int64), 0, h - 1)
+                sx = np.clip(np.rint(crx + step * np.cos(ang)).astype(np.int64), 0, w - 1)
+                flat_idx.append(sy[on] * w + sx[on])
+                vals.append(energy[on])
+            frame.view(-1).index_put_((torch.as_tensor(np.concatenate(flat_idx), device=device),),
+                                      torch.as_tensor(np.concatenate(vals), device=device, dtype=torch.float32),
+                                      accumulate=True)
+        if cfg.satellite_fraction and rng.random() < cfg.satellite_fraction:
+            y0, y1 = rng.uniform(0, h, 2)
+            xs = np.arange(w)
+            ys = np.rint(y0 + (y1 - y0) * xs / max(w - 1, 1)).astype(np.int64)
+            for t in (-1, 0, 1):
+                yt = np.clip(ys + t, 0, h - 1)
+                frame.view(-1).index_put_((torch.as_tensor(yt * w + xs, device=device),),
+                                          torch.full((w,), 3000.0 if t == 0 else 1200.0, device=device),
+                                          accumulate=True)
+        lights[i] = _u16_as_i16(torch, frame)
+        del frame
+    return DeviceStack(cfg, lights, bias_frames, dark_frames, flat_frames, truth, cloud)

@@ -166,8 +166,10 @@ int gg_stack_frame_stats(gg_stack* stack, const int64_t* indices, int64_t count,
  * (used by gg_stack_integrate_device_weights with dev_weights = NULL).
  * GG_WEIGHTS_SIMPLE_SNR: w = max(|mean|/std, eps) (1/eps when std <= eps, 0
  * without valid pixels) - resident_cuda.py:1948-1956 with the statistics of
- * frame_global_stats; GG_WEIGHTS_PRIOR: w = prior.  A frame whose prior is not
- * finite and positive gets weight 0.  host_prior (frame_count) may be NULL;
+ * frame_global_stats, times the prior (a per-frame multiplier such as the
+ * registration-agreement weight multiplier, resident_cuda.py:12800-12804);
+ * GG_WEIGHTS_PRIOR: w = prior.  A frame whose prior is not finite and
+ * positive gets weight 0.  host_prior (frame_count) may be NULL;
  * host_weights_out (frame_count) may be NULL to stay asynchronous. */
 #define GG_WEIGHTS_PRIOR 0
 #define GG_WEIGHTS_SIMPLE_SNR 1
@@ -175,16 +177,21 @@ int gg_stack_compute_weights(gg_stack* stack, int mode, const float* host_prior,
                              float* host_weights_out);
 
 /* Frame statistics (same results as gg_stack_frame_stats) for callers that
- * cannot allocate device memory: graph-capturing code, plugins whose host owns
- * every allocation, real-time loops.  No counterpart in the reference.  It
- * allocates nothing: the reduction scratch is a fixed 192 KiB __device__ array
- * that every GPU loading this library reserves until exit.  `frame_count`
- * frames of `pixels` float32 samples start `frame_stride` elements apart at
- * dev_frames (device memory).  At most 64 frames per call (larger counts are
- * rejected with GG_ERR_INVALID_ARGUMENT).  The first call on a device resolves
- * the scratch address and must come before any stream capture.  Calls share
- * the scratch, so calls that overlap on the GPU race.  Synchronises
- * cuda_stream (NULL: legacy default stream) before returning. */
+ * cannot allocate device memory: plugins whose host application owns every
+ * device allocation, real-time loops that forbid allocation after start-up.
+ * No counterpart in the reference.  It allocates nothing: the reduction
+ * scratch is a fixed 193.5 KiB __device__ array that every GPU loading this
+ * library reserves until exit.  `frame_count` frames of `pixels` float32
+ * samples start `frame_stride` elements apart at dev_frames (device memory of
+ * the stream's device).  At most 64 frames per call (larger counts are
+ * rejected with GG_ERR_INVALID_ARGUMENT).  The first call on a device
+ * resolves and caches the scratch address; after a device / primary-context
+ * reset that address is stale and the entry point must not be called again.
+ * Calls share the scratch, so calls that overlap on the GPU race.  Copies the
+ * results back and synchronises cuda_stream (NULL: legacy default stream of
+ * the current device) before returning, so it cannot run while cuda_stream is
+ * being captured: such a call returns GG_ERR_INVALID_ARGUMENT before
+ * enqueuing anything and the capture stays valid. */
 int gg_frames_stats_f32_noalloc(const float* dev_frames, int64_t frame_count, int64_t pixels,
                                 int64_t frame_stride, void* cuda_stream, gg_frame_stats_t* out);
 
