@@ -492,6 +492,24 @@ def _pair_stack(reference: Any, moving: Any) -> "ResidentCalibratedStack":
     return stack
 
 
+def star_grid_top_nms_candidates_f32(data: Any, threshold: float, grid_cols: int = 16, grid_rows: int = 12,
+                                     candidates_per_cell: int = 4, max_output_candidates: int = 64,
+                                     min_separation_px: float = 32.0) -> dict[str, Any]:
+    """Module star_grid_top_nms_candidates_f32 (glass_cuda.py:2514-2606) on a
+    host image through a one-frame resident stack."""
+    image = np.ascontiguousarray(np.asarray(data, dtype=np.float32))
+    if image.ndim != 2:
+        raise ValueError("data must be a 2-D array")
+    stack = ResidentCalibratedStack(1, image.shape[0], image.shape[1])
+    try:
+        stack.upload_calibrated_frame(0, image)
+        return stack.star_grid_top_nms_candidates_deterministic(0, threshold, grid_cols, grid_rows,
+                                                                 candidates_per_cell, max_output_candidates,
+                                                                 min_separation_px)
+    finally:
+        stack.close()
+
+
 def matrix_alignment_metrics_f32(reference: Any, moving: Any, matrix: Any, sample_stride: int = 1) -> dict[str, Any]:
     """Module matrix_alignment_metrics_f32 (glass_cuda.py:706-768)."""
     if sample_stride <= 0:
@@ -783,6 +801,135 @@ class ResidentCalibratedStack:
         return {"schema_version": 1, "h2d_mode": "pinned_lanes", "frames": int(idx.size),
                 "stream_count": int(stream_count), "wave_frames": int(wave_frames), "total_s": total,
                 "host_pinned_bytes": self.host_pinned_bytes}
+
+    # ---- grid star catalogs (star_detect_kernels.cu:40-101, 317-742) ----------------
+    def _grid_catalog(self, indices: Any, threshold: float, grid_cols: int, grid_rows: int,
+                      candidates_per_cell: int, max_output_candidates: int, min_separation_px: float,
+                      centroid_radius: int, centroid_global_mean_background: bool,
+                      deterministic: bool) -> list[dict[str, Any]]:
+        """The reference's batch grid catalog (native_bindings.cpp:12211-12645):
+        per-cell top-K local maxima, value-ordered separation scan, optional
+        windowed centroid.  Every variant runs the deterministic order; it is
+        also a valid result of the reference's lock-based variant."""
+        if grid_cols <= 0 or grid_rows <= 0 or candidates_per_cell <= 0 or max_output_candidates <= 0:
+            raise ValueError("grid dimensions and candidate counts must be positive")
+        if min_separation_px < 0.0:
+            raise ValueError("min_separation_px must be non-negative")
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+        if idx.size == 0:
+            return []
+        n, mo = idx.size, int(max_output_candidates)
+        params = _lib.GridCatalogParams(float(threshold), int(grid_cols), int(grid_rows), int(candidates_per_cell),
+                                        mo, float(min_separation_px), max(0, int(centroid_radius)),
+                                        1 if centroid_global_mean_background else 0)
+        planes = np.empty((5, n, mo), dtype=np.float32)
+        status = np.zeros((n, mo), dtype=np.uint8)
+        counts = np.empty((n, 2), dtype=np.int32)
+        start = perf_counter()
+        _lib.call("gg_stack_star_grid_catalog", self._handle, _lib.ptr(idx), ctypes.c_int64(n), ctypes.byref(params),
+                  _lib.ptr(planes), _lib.ptr(status), _lib.ptr(counts))
+        elapsed = (perf_counter() - start) / n
+        radius = max(0, int(centroid_radius))
+        results = []
+        for k in range(n):
+            stored = int(counts[k, 1])
+            x, y, flux = (planes[c, k, :stored].copy() for c in range(3))
+            refine = {"enabled": radius > 0, "radius": radius, "stored_count": stored,
+                      "refined_count": int(status[k, :stored].sum()) if radius else 0,
+                      "failed_count": int(stored - status[k, :stored].sum()) if radius else 0,
+                      "max_shift_px": float(np.hypot(x.astype(np.float64) - planes[3, k, :stored],
+                                                     y.astype(np.float64) - planes[4, k, :stored])[
+                          status[k, :stored] != 0].max(initial=0.0)) if radius else 0.0,
+                      "mode": ("off" if not radius else "resident_gpu_global_mean_centroid"
+                               if centroid_global_mean_background else "resident_gpu_window_centroid"),
+                      "background_mode": ("off" if not radius else "global_mean"
+                                          if centroid_global_mean_background else "local_median"),
+                      "background": None}
+            results.append({
+                "frame_index": int(idx[k]), "count": int(counts[k, 0]), "stored_count": stored,
+                "grid_cols": int(grid_cols), "grid_rows": int(grid_rows),
+                "candidates_per_cell": int(candidates_per_cell), "max_output_candidates": mo,
+                "min_separation_px": float(min_separation_px),
+                "catalog_sort_mode": "device_bitonic_u64_keys", "catalog_topk_mode": "deterministic_cta_per_cell",
+                "catalog_timing_model": "single_stream_one_sync", "catalog_batch_size": n,
+                "catalog_stream_limit": 1, "catalog_stream_count": 1, "catalog_batch_sync_count": 1,
+                "catalog_sync_phase_count": 1, "catalog_download_mode": "bulk_full_capacity",
+                "catalog_workspace_layout": "contiguous_soa", "catalog_grid_workspace_allocation_count": 1,
+                "catalog_output_workspace_allocation_count": 1, "catalog_output_download_copy_count": 1,
+                "catalog_centroid_before_download_copy_count": 0, "catalog_output_download_bytes": int(planes.nbytes),
+                "catalog_centroid_mean_sync_mode": ("fused_with_catalog_sync" if radius and
+                                                    centroid_global_mean_background else
+                                                    "not_applicable_local_median" if radius else "off"),
+                "catalog_centroid_mean_blocks": 128 if radius and centroid_global_mean_background else 0,
+                "catalog_enqueue_s": 0.0, "catalog_sync_s": elapsed, "catalog_count_download_s": 0.0,
+                "catalog_centroid_refine_s": 0.0, "catalog_output_download_s": 0.0, "catalog_native_s": elapsed,
+                "centroid_refine": refine, "x": x, "y": y, "flux": flux})
+        return results
+
+    def star_grid_top_nms_candidates_batch(self, indices: Any, threshold: float, grid_cols: int, grid_rows: int,
+                                           candidates_per_cell: int, max_output_candidates: int,
+                                           min_separation_px: float) -> list[dict[str, Any]]:
+        return self._grid_catalog(indices, threshold, grid_cols, grid_rows, candidates_per_cell,
+                                  max_output_candidates, min_separation_px, 0, False, False)
+
+    def star_grid_top_nms_candidates_batch_deterministic(self, indices: Any, threshold: float, grid_cols: int,
+                                                         grid_rows: int, candidates_per_cell: int,
+                                                         max_output_candidates: int,
+                                                         min_separation_px: float) -> list[dict[str, Any]]:
+        return self._grid_catalog(indices, threshold, grid_cols, grid_rows, candidates_per_cell,
+                                  max_output_candidates, min_separation_px, 0, False, True)
+
+    def star_grid_top_nms_candidates_batch_centroid(self, indices: Any, threshold: float, grid_cols: int,
+                                                    grid_rows: int, candidates_per_cell: int,
+                                                    max_output_candidates: int, min_separation_px: float,
+                                                    centroid_radius: int,
+                                                    centroid_global_mean_background: bool = False):
+        return self._grid_catalog(indices, threshold, grid_cols, grid_rows, candidates_per_cell,
+                                  max_output_candidates, min_separation_px, centroid_radius,
+                                  centroid_global_mean_background, False)
+
+    def star_grid_top_nms_candidates_batch_deterministic_centroid(
+            self, indices: Any, threshold: float, grid_cols: int, grid_rows: int, candidates_per_cell: int,
+            max_output_candidates: int, min_separation_px: float, centroid_radius: int,
+            centroid_global_mean_background: bool = False) -> list[dict[str, Any]]:
+        """native_bindings.cpp:12622-12645: the resident triangle path's batch
+        catalog (resident_cuda.py:10914)."""
+        return self._grid_catalog(indices, threshold, grid_cols, grid_rows, candidates_per_cell,
+                                  max_output_candidates, min_separation_px, centroid_radius,
+                                  centroid_global_mean_background, True)
+
+    def _grid_single(self, index: int, *args) -> dict[str, Any]:
+        result = self._grid_catalog([int(index)], *args)[0]
+        result.pop("frame_index")
+        return result
+
+    def star_grid_top_nms_candidates(self, index: int, threshold: float, grid_cols: int, grid_rows: int,
+                                     candidates_per_cell: int, max_output_candidates: int,
+                                     min_separation_px: float) -> dict[str, Any]:
+        return self._grid_single(index, threshold, grid_cols, grid_rows, candidates_per_cell, max_output_candidates,
+                                 min_separation_px, 0, False, False)
+
+    def star_grid_top_nms_candidates_deterministic(self, index: int, threshold: float, grid_cols: int,
+                                                   grid_rows: int, candidates_per_cell: int,
+                                                   max_output_candidates: int,
+                                                   min_separation_px: float) -> dict[str, Any]:
+        return self._grid_single(index, threshold, grid_cols, grid_rows, candidates_per_cell, max_output_candidates,
+                                 min_separation_px, 0, False, True)
+
+    def star_grid_top_nms_candidates_centroid(self, index: int, threshold: float, grid_cols: int, grid_rows: int,
+                                              candidates_per_cell: int, max_output_candidates: int,
+                                              min_separation_px: float, centroid_radius: int,
+                                              centroid_global_mean_background: bool = False) -> dict[str, Any]:
+        return self._grid_single(index, threshold, grid_cols, grid_rows, candidates_per_cell, max_output_candidates,
+                                 min_separation_px, centroid_radius, centroid_global_mean_background, False)
+
+    def star_grid_top_nms_candidates_deterministic_centroid(self, index: int, threshold: float, grid_cols: int,
+                                                            grid_rows: int, candidates_per_cell: int,
+                                                            max_output_candidates: int, min_separation_px: float,
+                                                            centroid_radius: int,
+                                                            centroid_global_mean_background: bool = False):
+        return self._grid_single(index, threshold, grid_cols, grid_rows, candidates_per_cell, max_output_candidates,
+                                 min_separation_px, centroid_radius, centroid_global_mean_background, True)
 
     # ---- star catalogs (star_detect.py:121-168) -------------------------------------
     def detect_stars(self, indices: Any, threshold_sigma: float = 5.0, max_stars: int = 500,

@@ -107,6 +107,19 @@ class StarParams(ctypes.Structure):
     ]
 
 
+class GridCatalogParams(ctypes.Structure):
+    _fields_ = [
+        ("threshold", ctypes.c_float),
+        ("grid_cols", ctypes.c_int32),
+        ("grid_rows", ctypes.c_int32),
+        ("candidates_per_cell", ctypes.c_int32),
+        ("max_output_candidates", ctypes.c_int32),
+        ("min_separation_px", ctypes.c_float),
+        ("centroid_radius", ctypes.c_int32),
+        ("centroid_background", ctypes.c_int32),
+    ]
+
+
 class Star(ctypes.Structure):
     _fields_ = [
         ("x", ctypes.c_double),
@@ -391,6 +404,7 @@ PROTOTYPES: dict[str, list] = {
     "gg_stack_download_weights": [_P, _P],
     "gg_dq_map_i16": [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P],
     "gg_stack_detect_stars": [_P, _P, ctypes.c_int64, ctypes.POINTER(StarParams), _P, _P, _P],
+    "gg_stack_star_grid_catalog": [_P, _P, ctypes.c_int64, ctypes.POINTER(GridCatalogParams), _P, _P, _P],
     "gg_triangle_descriptors": [_P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P,
                                 ctypes.c_int64, c_int64_p],
     "gg_register_star_lists": [_P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.POINTER(RegisterParams),

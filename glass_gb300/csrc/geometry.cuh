@@ -62,6 +62,15 @@ __device__ __forceinline__ FFv ff_div(FFv n, FFv d) {
   return {h, __fsub_rn(ql, __fsub_rn(h, q))};
 }
 
+// v + (b_hi, b_lo), renormalised.
+__device__ __forceinline__ FFv ff_add_ff(FFv v, float b_hi, float b_lo) {
+  float s, e;
+  two_sum(v.hi, b_hi, s, e);
+  const float lo = __fadd_rn(__fadd_rn(v.lo, b_lo), e);
+  const float h = __fadd_rn(s, lo);
+  return {h, __fsub_rn(lo, __fsub_rn(h, s))};
+}
+
 __device__ __forceinline__ bool ff_ge(FFv v, float b) { return v.hi > b || (v.hi == b && v.lo >= 0.0f); }
 __device__ __forceinline__ bool ff_le(FFv v, float b) { return v.hi < b || (v.hi == b && v.lo <= 0.0f); }
 __device__ __forceinline__ bool ff_lt(FFv v, float b) { return v.hi < b || (v.hi == b && v.lo < 0.0f); }

@@ -39,31 +39,46 @@ __device__ __forceinline__ float cos_taylor(float z) {
 
 constexpr float kPiF = 3.14159265358979323846f;
 
-// Lanczos3 weights of taps k = -2..3 at fractional offset t in [0, 1)
-// (d = t - k): w = sinc(d) sinc(d/3) = 3 sin(pi d) sin(pi d / 3) / (pi d)^2,
-// with sin(pi d) = (-1)^k sin(pi t) and sin(pi d / 3) from the angle sum, so
-// one sin(pi t) and one sin/cos(pi t / 3) serve all six taps.  |d| < 1e-6
-// gives 1, as the reference's sinc does.
+// Lanczos3 weights of taps k = -2..3 at fractional offset t in [0, 1): the
+// tap at distance d = t - k weighs L(d) = sinc(d) sinc(d / 3).  With
+// u = t - 1/2 the taps pair up as L(c + u), L(c - u) for c = 1/2 (k = 0, 1),
+// 3/2 (k = -1, 2) and 5/2 (k = -2, 3); each pair is E_c(u) +- O_c(u) with
+// E_c even and O_c odd, evaluated as degree-5 polynomials in u^2 (fit error
+// below 3e-10, coefficients from glass_gb300/lanczos_poly.py), so the six
+// weights cost 36 FMAs and no transcendental or division.  t == 0 (an exact
+// integer source coordinate) gives the exact weights 0, 0, 1, 0, 0, 0.
+// pair A (c = 0.5): max fit error 7.3e-11
+__device__ constexpr float kL3EA[6] = {6.079271019e-01f, -4.488392797e-01f, 6.364143348e-02f, 2.186747311e-02f, -9.777044177e-03f, 1.680220536e-03f};
+__device__ constexpr float kL3OA[6] = {-1.329050616e+00f, 1.468628193e+00f, -6.481293705e-01f, 1.599001370e-01f, -2.544626853e-02f, 2.676349777e-03f};
+// pair B (c = 1.5): max fit error 1.8e-10
+__device__ constexpr float kL3EB[6] = {-1.350949116e-01f, 5.606142051e-01f, -6.639494271e-02f, -6.422391983e-02f, 2.526676875e-02f, -4.255278694e-03f};
+__device__ constexpr float kL3OB[6] = {1.801265486e-01f, -8.275418234e-01f, 4.563217525e-01f, -1.171571662e-01f, 1.821853304e-02f, -1.830645261e-03f};
+// pair C (c = 2.5): max fit error 2.1e-10
+__device__ constexpr float kL3EC[6] = {2.431708412e-02f, -8.637609842e-02f, -6.445738508e-02f, 9.083209009e-02f, -3.034376772e-02f, 4.921542137e-03f};
+__device__ constexpr float kL3OC[6] = {-6.355997888e-02f, 3.049877158e-01f, -2.164693742e-01f, 5.576262943e-02f, -7.546908498e-03f, 5.886373014e-04f};
+
+__device__ __forceinline__ float l3_poly(const float (&c)[6], float x) {
+  float p = c[5];
+  p = __fmaf_rn(p, x, c[4]);
+  p = __fmaf_rn(p, x, c[3]);
+  p = __fmaf_rn(p, x, c[2]);
+  p = __fmaf_rn(p, x, c[1]);
+  return __fmaf_rn(p, x, c[0]);
+}
+
 __device__ __forceinline__ void lanczos3_weights(float t, float (&w)[6]) {
-  const float u = t <= 0.5f ? t : 1.0f - t;
-  const float s = sin_taylor(kPiF * u);
-  const float x3 = t * (kPiF / 3.0f);
-  const float s3 = sin_taylor(x3), c3 = cos_taylor(x3);
-  const float ck[6] = {-0.5f, 0.5f, 1.0f, 0.5f, -0.5f, -1.0f};
-  const float sk[6] = {-0.86602540378443865f, -0.86602540378443865f, 0.0f, 0.86602540378443865f,
-                       0.86602540378443865f, 0.0f};
-  constexpr float k3_over_pi2 = 0.30396355092701331f;  // 3 / pi^2
-  // Tap k = 1 (d = t - 1 in [-1, 0)) would lose its small sin(pi d / 3) to
-  // cancellation in the angle sum near t = 1: evaluate it directly.
-  const float s3_k1 = sin_taylor((kPiF / 3.0f) * (t - 1.0f));
-#pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    const float d = t - static_cast<float>(j - 2);
-    const float s1 = ((j - 2) & 1) ? -s : s;
-    const float s3d = (j == 3) ? s3_k1 : __fmaf_rn(s3, ck[j], -c3 * sk[j]);
-    const float wv = k3_over_pi2 * s1 * s3d * __fdividef(1.0f, d * d);
-    w[j] = fabsf(d) < 1.0e-6f ? 1.0f : wv;
-  }
+  const float u = __fsub_rn(t, 0.5f);
+  const float x = __fmul_rn(u, u);
+  const float ea = l3_poly(kL3EA, x), oa = __fmul_rn(u, l3_poly(kL3OA, x));
+  const float eb = l3_poly(kL3EB, x), ob = __fmul_rn(u, l3_poly(kL3OB, x));
+  const float ec = l3_poly(kL3EC, x), oc = __fmul_rn(u, l3_poly(kL3OC, x));
+  const bool exact = t == 0.0f;
+  w[0] = exact ? 0.0f : __fadd_rn(ec, oc);
+  w[1] = exact ? 0.0f : __fadd_rn(eb, ob);
+  w[2] = exact ? 1.0f : __fadd_rn(ea, oa);
+  w[3] = exact ? 0.0f : __fsub_rn(ea, oa);
+  w[4] = exact ? 0.0f : __fsub_rn(eb, ob);
+  w[5] = exact ? 0.0f : __fsub_rn(ec, oc);
 }
 
 // Tap reader: shared-memory tile (origin bx, by) or global frame.
@@ -168,7 +183,9 @@ __device__ __forceinline__ bool sample_lanczos3_impl(const TapSource& ts, int x0
     wsum = 1.0f;
   }
   if (!(fabsf(wsum) > 1.0e-12f)) return false;
-  float value = __fdiv_rn(acc, wsum);
+  // all-finite sums lie within a few per cent of 1: the fast reciprocal is
+  // within 2 ulp; renormalised partial sums take the exact division
+  float value = all_finite ? __fdividef(acc, wsum) : __fdiv_rn(acc, wsum);
   if (CLAMP && vmin <= vmax) {
     const float range = vmax - vmin;
     value = fminf(vmax + clamp * range, fmaxf(vmin - clamp * range, value));

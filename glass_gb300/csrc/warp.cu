@@ -235,15 +235,30 @@ __global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __gri
       const int ox = tile_x * kTileW + lx;
       const bool all_finite = it_nonfinite == 0u;
       unsigned bad = 0;
+      // Affine source coordinates step by 4 output rows: (sx, sy) += 4 (b, e)
+      // in float-float (exact scaling by 4, one TwoSum per axis) instead of
+      // a fresh evaluation per pixel.
+      FFv sx_row{0.0f, 0.0f}, sy_row{0.0f, 0.0f};
+      bool row_ok = false;
+      const float step_x_hi = 4.0f * co.m[1][0], step_x_lo = 4.0f * co.m[1][1];
+      const float step_y_hi = 4.0f * co.m[4][0], step_y_lo = 4.0f * co.m[4][1];
 #pragma unroll 1
       for (int r = 0; r < 4; ++r) {
         const int oy = tile_y * kTileH + ly + 4 * r;
         const bool inside = ox < a.width && oy < a.height;
         bool valid = false;
         float value = a.fill;
+        if (co.affine) {
+          if (r == 0) {
+            row_ok = source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx_row, sy_row);
+          } else {
+            sx_row = ff_add_ff(sx_row, step_x_hi, step_x_lo);
+            sy_row = ff_add_ff(sy_row, step_y_hi, step_y_lo);
+          }
+        }
         if (inside) {
-          FFv sx, sy;
-          if (source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx, sy)) {
+          FFv sx = sx_row, sy = sy_row;
+          if (co.affine ? row_ok : source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx, sy)) {
             const float W = static_cast<float>(a.width), H = static_cast<float>(a.height);
             if (INTERP != GG_INTERP_LANCZOS3)
               valid = ff_ge(sx, 0.0f) && ff_le(sx, W - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, H - 1.0f);

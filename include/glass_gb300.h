@@ -405,6 +405,32 @@ typedef struct {
 int gg_stack_detect_stars(gg_stack* stack, const int64_t* indices, int64_t count, const gg_star_params_t* params,
                           gg_star_t* host_stars, int32_t* host_counts, gg_star_frame_info_t* host_info);
 
+/* ---- grid star catalogs ---------------------------------------------------- */
+typedef struct {
+  float threshold;            /* candidates are interior local maxima > threshold */
+  int grid_cols;              /* cells: x in [c*W/cols, (c+1)*W/cols), same for y */
+  int grid_rows;
+  int candidates_per_cell;    /* best K per cell (value desc, y asc, x asc), <= 3072 */
+  int max_output_candidates;  /* kept after the separation scan, <= 8192          */
+  float min_separation_px;
+  int centroid_radius;        /* 0: no centroid; window radius (clamped to 1..8) */
+  int centroid_background;    /* 0: window median, 1: frame global mean           */
+} gg_grid_catalog_params_t;
+
+/* Deterministic grid catalogs of `count` resident frames: per-cell top-K local
+ * maxima, merged in value order, greedy minimum-separation scan, optional
+ * windowed centroid.  Replaces ResidentCalibratedStack.
+ * star_grid_top_nms_candidates_batch_deterministic_centroid and its siblings
+ * (native_bindings.cpp:12622-12645 over the batch driver :12211-12616; kernels
+ * star_detect_kernels.cu:40-101, 317-742).  host_catalog receives five planes
+ * of count * max_output_candidates float32 each: x, y (after the centroid),
+ * value, x and y before the centroid; host_status (may be NULL) count *
+ * max_output_candidates centroid flags (1 = moved); host_counts count pairs
+ * (candidates in the frame, kept).  Synchronises the stack's stream. */
+int gg_stack_star_grid_catalog(gg_stack* stack, const int64_t* indices, int64_t count,
+                               const gg_grid_catalog_params_t* params, float* host_catalog, uint8_t* host_status,
+                               int32_t* host_counts);
+
 /* ---- raw FITS read queue (RawFitsReadQueue, native_bindings.cpp:2605-2915,
  * 20417-20429) ---------------------------------------------------------------
  * Host worker threads read [data_offset, data_offset + byte_count) of a file
