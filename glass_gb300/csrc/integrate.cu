@@ -1082,12 +1082,27 @@ __device__ __forceinline__ float warp_clipped_std(const float (&v)[NPL], int lan
   return ff_sqrt_f32(q, ql);
 }
 
-template <int NPL, int WARP>
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
+}
+
+// PIPE (resident frames only): two tile buffers; the copies of the next tile
+// (cp.async, one 4-byte sample per thread and step) are in flight while the
+// warps integrate the current one.
+template <int NPL, int WARP, bool PIPE = false>
 __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateArgs a) {
-  extern __shared__ float tile[];  // [frames][kWarpTileRow], then (fused) [frames] FusedFrame
+  extern __shared__ float smem_tiles[];  // [frames][kWarpTileRow] (x2 with PIPE), then (fused) [frames] FusedFrame
   __shared__ FrameTable<32 * NPL> tab;
   __shared__ int s_geo[kWarpTilePx];
-  FusedFrame* fz = reinterpret_cast<FusedFrame*>(tile + a.frames * kWarpTileRow);
+  static_assert(!(PIPE && WARP != 0), "the pipelined tile copy serves resident frames only");
+  FusedFrame* fz = reinterpret_cast<FusedFrame*>(smem_tiles + a.frames * kWarpTileRow);
   if constexpr (WARP != 0)
     for (int f = threadIdx.x; f < a.frames; f += blockDim.x) fz[f] = a.fused[f];
   load_frame_table<32 * NPL>(a, tab);
@@ -1098,26 +1113,51 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
   const int64_t P = a.pixels;
   const int64_t tiles = (P + kWarpTilePx - 1) / kWarpTilePx;
   const float ls = a.low_sigma, hs = a.high_sigma;
-  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
-    const int64_t p0 = t * kWarpTilePx;
-    __syncthreads();  // the previous tile's columns are consumed
-    if constexpr (WARP != 0) {
-      if (threadIdx.x < kWarpTilePx) s_geo[threadIdx.x] = 0;
-      __syncthreads();
-    }
+  auto fill_async = [&](int64_t tt, float* dst) {
+    const int64_t q0 = tt * kWarpTilePx;
     for (int i = threadIdx.x; i < N * kWarpTilePx; i += kWarpThreads) {
       const int f = i / kWarpTilePx, px = i - f * kWarpTilePx;
-      const int64_t p = p0 + px;
-      float v = 0.0f;
-      if constexpr (WARP == 0) {
-        if (p < P) v = __ldcs(tab.base[f] + p);
-      } else if (p < P) {
-        const int py = static_cast<int>(p / a.width), pxx = static_cast<int>(p - static_cast<int64_t>(py) * a.width);
-        int geo = 0;
-        v = fused_sample_inline<WARP>(a, tab.base[f], fz[f], pxx, py, geo);
-        if (geo) atomicAdd(&s_geo[px], 1);
+      if (q0 + px < P) cp_async4(dst + f * kWarpTileRow + px, tab.base[f] + q0 + px);
+      else dst[f * kWarpTileRow + px] = 0.0f;
+    }
+    cp_async_commit();
+  };
+  if constexpr (PIPE) {
+    if (blockIdx.x < tiles) fill_async(blockIdx.x, smem_tiles);
+  }
+  int buf = 0;
+  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x, buf ^= 1) {
+    const int64_t p0 = t * kWarpTilePx;
+    float* tile = smem_tiles;
+    if constexpr (PIPE) {
+      tile = smem_tiles + buf * (N * kWarpTileRow);
+      if (t + gridDim.x < tiles) {
+        fill_async(t + gridDim.x, smem_tiles + (buf ^ 1) * (N * kWarpTileRow));
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
       }
-      tile[f * kWarpTileRow + px] = v;
+    } else {
+      __syncthreads();  // the previous tile's columns are consumed
+      if constexpr (WARP != 0) {
+        if (threadIdx.x < kWarpTilePx) s_geo[threadIdx.x] = 0;
+        __syncthreads();
+      }
+      for (int i = threadIdx.x; i < N * kWarpTilePx; i += kWarpThreads) {
+        const int f = i / kWarpTilePx, px = i - f * kWarpTilePx;
+        const int64_t p = p0 + px;
+        float v = 0.0f;
+        if constexpr (WARP == 0) {
+          if (p < P) v = __ldcs(tab.base[f] + p);
+        } else if (p < P) {
+          const int py = static_cast<int>(p / a.width),
+                    pxx = static_cast<int>(p - static_cast<int64_t>(py) * a.width);
+          int geo = 0;
+          v = fused_sample_inline<WARP>(a, tab.base[f], fz[f], pxx, py, geo);
+          if (geo) atomicAdd(&s_geo[px], 1);
+        }
+        tile[f * kWarpTileRow + px] = v;
+      }
     }
     __syncthreads();
     for (int px = warp; px < kWarpTilePx; px += kWarpThreads / 32) {
@@ -1257,14 +1297,19 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
         write_outputs(a, p, master, weight, kept, nl, nh, tab.active);
       }
     }
+    if constexpr (PIPE) __syncthreads();  // this buffer is refilled by the next iteration's prefetch
   }
 }
 
 template <int NPL, int WARP = 0>
 static void launch_warp(const IntegrateArgs& args, cudaStream_t stream) {
-  const size_t smem = static_cast<size_t>(args.frames) * kWarpTileRow * sizeof(float) +
+  const size_t tile_bytes = static_cast<size_t>(args.frames) * kWarpTileRow * sizeof(float);
+  // resident frames: double-buffered tiles while two of them stay under 100 KB
+  constexpr bool kCanPipe = WARP == 0;
+  const bool pipe = kCanPipe && 2 * tile_bytes <= 100 * 1024;
+  const size_t smem = tile_bytes * (pipe ? 2 : 1) +
                       (WARP != 0 ? static_cast<size_t>(args.frames) * sizeof(FusedFrame) : 0);
-  auto kern = integrate_warp_kernel<NPL, WARP>;
+  auto kern = pipe ? integrate_warp_kernel<NPL, WARP, kCanPipe> : integrate_warp_kernel<NPL, WARP, false>;
   check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
              "cudaFuncSetAttribute(integrate_warp)");
   int per_sm = 0;

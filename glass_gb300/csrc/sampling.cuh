@@ -81,6 +81,34 @@ __device__ __forceinline__ void lanczos3_weights(float t, float (&w)[6]) {
   w[5] = exact ? 0.0f : __fsub_rn(ec, oc);
 }
 
+// Lanczos3 weights with relative (not only absolute) accuracy, for the
+// renormalised sums over the finite taps: at fractional offset t in [0, 1)
+// (d = t - k): w = sinc(d) sinc(d/3) = 3 sin(pi d) sin(pi d / 3) / (pi d)^2,
+// with sin(pi d) = (-1)^k sin(pi t) and sin(pi d / 3) from the angle sum, so
+// one sin(pi t) and one sin/cos(pi t / 3) serve all six taps.  |d| < 1e-6
+// gives 1, as the reference's sinc does.
+__device__ __forceinline__ void lanczos3_weights_trig(float t, float (&w)[6]) {
+  const float u = t <= 0.5f ? t : 1.0f - t;
+  const float s = sin_taylor(kPiF * u);
+  const float x3 = t * (kPiF / 3.0f);
+  const float s3 = sin_taylor(x3), c3 = cos_taylor(x3);
+  const float ck[6] = {-0.5f, 0.5f, 1.0f, 0.5f, -0.5f, -1.0f};
+  const float sk[6] = {-0.86602540378443865f, -0.86602540378443865f, 0.0f, 0.86602540378443865f,
+                       0.86602540378443865f, 0.0f};
+  constexpr float k3_over_pi2 = 0.30396355092701331f;  // 3 / pi^2
+  // Tap k = 1 (d = t - 1 in [-1, 0)) would lose its small sin(pi d / 3) to
+  // cancellation in the angle sum near t = 1: evaluate it directly.
+  const float s3_k1 = sin_taylor((kPiF / 3.0f) * (t - 1.0f));
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const float d = t - static_cast<float>(j - 2);
+    const float s1 = ((j - 2) & 1) ? -s : s;
+    const float s3d = (j == 3) ? s3_k1 : __fmaf_rn(s3, ck[j], -c3 * sk[j]);
+    const float wv = k3_over_pi2 * s1 * s3d * __fdividef(1.0f, d * d);
+    w[j] = fabsf(d) < 1.0e-6f ? 1.0f : wv;
+  }
+}
+
 // Tap reader: shared-memory tile (origin bx, by) or global frame.
 struct TapSource {
   const float* tile;  // nullptr -> global
@@ -105,9 +133,13 @@ __device__ __forceinline__ float sample_bilinear(const TapSource& ts, int x0, in
 // Non-finite taps present: skip them and renormalise.  Dropping taps can
 // leave a small weight sum (lobes cancel), which amplifies rounding, so the
 // sums are float-float here.  Kept out of line: it is the rare path.
-static __device__ __noinline__ bool lanczos3_nonfinite(const TapSource& ts, int x0, int y0, const float (&wx)[6],
-                                                       const float (&wy)[6], float& value, float& vmin,
-                                                       float& vmax) {
+static __device__ __noinline__ bool lanczos3_nonfinite(const TapSource& ts, int x0, int y0, float tx, float ty,
+                                                       float& value, float& vmin, float& vmax) {
+  // Dropped taps can leave a small sum, so the weights here carry relative
+  // accuracy (the polynomial pairs are accurate to ~1e-7 absolute only).
+  float wx[6], wy[6];
+  lanczos3_weights_trig(tx, wx);
+  lanczos3_weights_trig(ty, wy);
   FF facc, fw;
   for (int j = 0; j < 6; ++j) {
 #pragma unroll
@@ -179,7 +211,7 @@ __device__ __forceinline__ bool sample_lanczos3_impl(const TapSource& ts, int x0
     }
     wsum = sx * sy;
   } else {
-    if (!lanczos3_nonfinite(ts, x0, y0, wx, wy, acc, vmin, vmax)) return false;
+    if (!lanczos3_nonfinite(ts, x0, y0, tx, ty, acc, vmin, vmax)) return false;
     wsum = 1.0f;
   }
   if (!(fabsf(wsum) > 1.0e-12f)) return false;

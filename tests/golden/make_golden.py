@@ -681,6 +681,164 @@ def make_cosmetic(ref_src: Path) -> None:
     np.savez_compressed(HERE / "cosmetic.npz", **arrays)
 
 
+# ---------------------------------------------------------------------------
+# DQ map (resident_cuda.py:3110-3297, helpers :2961-3100, flags contracts.py:77)
+# ---------------------------------------------------------------------------
+def make_dq(ref_src: Path) -> None:
+    sys.path.insert(0, str(ref_src))
+    from glass.engine.contracts import DQFlag
+
+    ns: dict = {"np": np, "Any": object, "DQFlag": DQFlag}
+    _load_functions(ref_src / "glass" / "engine" / "resident_cuda.py",
+                    ["_resident_dq_flag_dtype", "_resident_dq_map_python", "_resident_coverage_array_stats_from_values",
+                     "_resident_finite_count_coverage_stats", "_resident_count_map_array_stats_from_values",
+                     "_resident_finite_count_map_array_stats_from_values"], ns)
+    dq_fn = ns["_resident_dq_map_python"]
+    rng = np.random.default_rng(3110)
+    out = {}
+    names = []
+    h, w = 23, 31
+    for case in range(12):
+        master = rng.normal(1000.0, 30.0, (h, w)).astype(np.float32)
+        weight = rng.uniform(0.0, 9.0, (h, w)).astype(np.float32)
+        frames = int(rng.integers(3, 40))
+        coverage = rng.integers(0, frames + 1, (h, w)).astype(np.float32)
+        low = rng.integers(0, 3, (h, w)).astype(np.float32) * (rng.random((h, w)) < 0.2)
+        high = rng.integers(0, 4, (h, w)).astype(np.float32) * (rng.random((h, w)) < 0.3)
+        geometric = rng.integers(0, frames + 1, (h, w)).astype(np.float32)
+        geometric[rng.random((h, w)) < 0.4] = frames
+        if case % 3 == 1:  # non-finite maps, zero and negative weights
+            master[rng.random((h, w)) < 0.05] = np.nan
+            master[rng.random((h, w)) < 0.02] = np.inf
+            weight[rng.random((h, w)) < 0.05] = 0.0
+            weight[rng.random((h, w)) < 0.03] = -1.0
+            weight[rng.random((h, w)) < 0.02] = np.nan
+            coverage[rng.random((h, w)) < 0.03] = np.nan
+            low[rng.random((h, w)) < 0.02] = np.nan
+            high[rng.random((h, w)) < 0.02] = np.inf
+            geometric[rng.random((h, w)) < 0.03] = np.nan
+        coverage[rng.random((h, w)) < 0.05] = 0.5  # the <= 0.5 edge
+        geometric[rng.random((h, w)) < 0.05] = frames - 0.5  # the partial-coverage edge
+        use = [case % 2 == 0, case % 4 != 3, case % 4 != 3, case % 3 != 2]  # coverage, low, high, geometric
+        active = frames if case % 5 != 4 else 0
+        args = [master, weight, coverage if use[0] else None, low if use[1] else None, high if use[2] else None,
+                geometric if use[3] else None, active]
+        dq, _summary = dq_fn(*args, dq_dtype=np.int16)
+        name = f"case{case}"
+        names.append(name)
+        out[f"{name}/master"], out[f"{name}/weight"] = master, weight
+        for key, arr, flag in (("coverage", coverage, use[0]), ("low", low, use[1]), ("high", high, use[2]),
+                               ("geometric", geometric, use[3])):
+            if flag:
+                out[f"{name}/{key}"] = arr
+        out[f"{name}/active"] = np.int64(active)
+        out[f"{name}/dq"] = dq
+    out["_names"] = np.array(names)
+    np.savez_compressed(HERE / "dq.npz", **out)
+
+
+# ---------------------------------------------------------------------------
+# tile-local weighting: the reference test's own CPU expectation
+# (tests/test_cuda_resident_stack.py:523-583, `_expected_tile_local_sigma`)
+# ---------------------------------------------------------------------------
+def make_tile_local(ref_src: Path) -> None:
+    ns: dict = {"np": np}
+    _load_functions(ref_src.parent / "tests" / "test_cuda_resident_stack.py", ["_expected_tile_local_sigma"], ns)
+    expected = ns["_expected_tile_local_sigma"]
+    rng = np.random.default_rng(1658)
+    out = {}
+    names = []
+    for case in range(8):
+        n = int(rng.integers(3, 9))
+        h, w = int(rng.integers(5, 14)), int(rng.integers(6, 15))
+        frames = rng.normal(100.0, 5.0, (n, h, w)).astype(np.float32)
+        frames[rng.random(frames.shape) < 0.05] += 80.0
+        frames[rng.random(frames.shape) < 0.03] = np.nan
+        weights = rng.uniform(0.3, 2.0, n).astype(np.float32)
+        if case % 3 == 2:
+            weights[0] = 0.0
+        target = (rng.random(n) < 0.5).astype(np.uint8)
+        target[int(rng.integers(0, n))] = 1
+        # non-overlapping tiles (the resident path rejects overlaps,
+        # resident_cuda.py:5355-5357): cells of a 2 x 2 split, each shrunk
+        # at random, some of them dropped
+        xs, ys = int(rng.integers(2, w - 1)), int(rng.integers(2, h - 1))
+        tiles = []
+        for cx0, cx1 in ((0, xs), (xs, w)):
+            for cy0, cy1 in ((0, ys), (ys, h)):
+                if rng.random() < 0.3 and tiles:
+                    continue
+                x0 = int(rng.integers(cx0, cx1))
+                y0 = int(rng.integers(cy0, cy1))
+                tiles.append([x0, y0, int(rng.integers(x0 + 1, cx1 + 1)), int(rng.integers(y0 + 1, cy1 + 1))])
+        extents = np.asarray(tiles, dtype=np.int32)
+        multipliers = rng.uniform(0.0, 3.0, len(tiles)).astype(np.float32)
+        name = f"case{case}"
+        names.append(name)
+        out[f"{name}/frames"], out[f"{name}/weights"], out[f"{name}/target"] = frames, weights, target
+        out[f"{name}/extents"], out[f"{name}/multipliers"] = extents, multipliers
+        # no rejection (huge thresholds): the weighted mean
+        m = expected(list(frames), weights, target, extents, multipliers, 1e30, 1e30, False)
+        out[f"{name}/mean/master"], out[f"{name}/mean/weight"] = m[0], m[1]
+        for mode, wins in (("sigma", False), ("winsorized", True)):
+            r = expected(list(frames), weights, target, extents, multipliers, 3.0, 1.0, wins)
+            for key, arr in zip(("master", "weight", "coverage", "low", "high"), r):
+                out[f"{name}/{mode}/{key}"] = arr
+    out["_names"] = np.array(names)
+    np.savez_compressed(HERE / "tile_local.npz", **out)
+
+
+# ---------------------------------------------------------------------------
+# registration-quality policy (resident_cuda.py:4905-4998,
+# engine/resident_registration_quality.py:41-136)
+# ---------------------------------------------------------------------------
+def make_quality(ref_src: Path) -> None:
+    import json
+
+    sys.path.insert(0, str(ref_src))
+    from glass.engine.resident_registration_quality import evaluate_resident_registration_quality
+
+    ns: dict = {"np": np, "Any": object}
+    _load_functions(ref_src / "glass" / "engine" / "resident_cuda.py",
+                    ["_float_or_nan", "_resident_triangle_agreement_quality", "_resident_triangle_agreement_policy"], ns)
+    quality, policy = ns["_resident_triangle_agreement_quality"], ns["_resident_triangle_agreement_policy"]
+    records = []
+    for ncc in (0.95, 0.4, 0.02, -0.1, float("nan"), None):
+        for rms in (0.0, 35.0, 480.0, 5000.0, -3.0, float("nan")):
+            for scale in (200.0, 25.0):
+                for min_score in (None, 0.0, 0.02, 0.3, 1.0):
+                    q = quality(ncc, rms, 0.4, scale, min_score)
+                    for action in ("fail", "downweight", "flag"):
+                        for floor in (0.0, 0.25):
+                            pol = policy(q, action, floor)
+                            records.append({"args": [ncc, rms, 0.4, scale, min_score, action, floor],
+                                            "quality": {k: q[k] for k in ("score", "status", "reason")},
+                                            "policy": {k: pol[k] for k in ("status", "hard_failure",
+                                                                           "weight_multiplier")}})
+    gates = []
+    for status in ("ok", "failed", "reference", "excluded", "weird"):
+        for inliers in (0, 3, 4, 12):
+            for rms in (0.2, 2.5, float("nan")):
+                for action in ("auto", "off", "warn", "exclude"):
+                    for mode in ("similarity_cuda_triangle", "translation"):
+                        for max_rms in (None, 1.0):
+                            for stars in (None, (2, 50)):
+                                d = evaluate_resident_registration_quality(
+                                    frame_id="f", registration_mode=mode, requested_action=action, status=status,
+                                    matched_stars=inliers, inliers=inliers, rms_px=rms, min_inliers=4,
+                                    max_rms_px=max_rms,
+                                    diagnostics=None if stars is None else {"reference_stars": stars[0],
+                                                                             "moving_stars": stars[1]})
+                                gates.append({"args": [status, inliers, rms, mode, action, 4, max_rms,
+                                                       None if stars is None else stars[0],
+                                                       None if stars is None else stars[1]],
+                                              "out": {k: d[k] for k in ("effective_action", "final_status",
+                                                                        "decision_status", "action_applied",
+                                                                        "accepted", "reasons")}})
+    text = json.dumps({"agreement": records, "gate": gates}, allow_nan=True)
+    np.savez_compressed(HERE / "quality.npz", json=np.frombuffer(text.encode(), dtype=np.uint8))
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__)
     parser.add_argument("--reference", default="/root/reference", help="GLASS reference checkout")
@@ -690,7 +848,8 @@ def main() -> int:
     src = ref / "src"
     jobs = {"integration": make_integration, "calibration": make_calibration, "warp": make_warp,
             "stars": make_stars, "registration": make_registration, "alignment": make_alignment,
-            "local_norm": make_local_norm, "cosmetic": make_cosmetic}
+            "local_norm": make_local_norm, "cosmetic": make_cosmetic, "dq": make_dq,
+            "tile_local": make_tile_local, "quality": make_quality}
     only = [j for j in args.only.split(",") if j] or list(jobs)
     for job in only:
         jobs[job](src)

@@ -91,3 +91,58 @@ def test_gpu_tile_local_arguments(native):
             s.integrate_tile_local_sigma_clip(target, EXTENTS, MULTS, low_sigma=0.0)
     finally:
         s.close()
+
+
+# ---- pinned to the reference: tests/golden/tile_local.npz holds the
+# reference test's own CPU expectation (`_expected_tile_local_sigma`,
+# tests/test_cuda_resident_stack.py:523-583 of the reference) on seeded stacks
+# with NaNs, a zero weight and non-overlapping tiles; "mean" is that
+# expectation with no rejection.  Tolerances are the reference test's:
+# 1e-6 for the mean (:518-519), 2e-5 for the clipped maps (:634-639).
+def _golden_cases():
+    from .conftest import GOLDEN
+
+    g = np.load(GOLDEN / "tile_local.npz", allow_pickle=False)
+    for name in (str(n) for n in g["_names"]):
+        yield name, g
+
+
+def _close(got, exp, tol, tag):
+    np.testing.assert_allclose(np.asarray(got, np.float64), np.asarray(exp, np.float64), rtol=tol, atol=tol,
+                               err_msg=tag)
+
+
+def test_oracle_tile_local_matches_reference_expectation():
+    n = 0
+    for name, g in _golden_cases():
+        args = (g[f"{name}/frames"], g[f"{name}/weights"], g[f"{name}/target"], g[f"{name}/extents"],
+                g[f"{name}/multipliers"])
+        m, w = otl.integrate_tile_local(*args, "mean")
+        _close(m, g[f"{name}/mean/master"], 1e-6, name + " mean master")
+        _close(w, g[f"{name}/mean/weight"], 1e-6, name + " mean weight")
+        for mode in ("sigma", "winsorized"):
+            got = otl.integrate_tile_local(*args, mode, 3.0, 1.0)
+            for key, arr in zip(("master", "weight", "coverage", "low", "high"), got):
+                _close(arr, g[f"{name}/{mode}/{key}"], 2e-5, f"{name} {mode} {key}")
+        n += 1
+    assert n == 8
+
+
+@pytest.mark.gpu
+def test_gpu_tile_local_matches_reference_expectation(native):
+    for name, g in _golden_cases():
+        frames = g[f"{name}/frames"]
+        s = native.ResidentCalibratedStack(*frames.shape)
+        try:
+            for k in range(frames.shape[0]):
+                s.upload_calibrated_frame(k, frames[k])
+            args = (g[f"{name}/target"], g[f"{name}/extents"], g[f"{name}/multipliers"], g[f"{name}/weights"])
+            m, w = s.integrate_tile_local_mean(*args)[:2]
+            _close(m, g[f"{name}/mean/master"], 1e-6, name + " mean master")
+            _close(w, g[f"{name}/mean/weight"], 1e-6, name + " mean weight")
+            for mode in ("sigma", "winsorized"):
+                got = s.integrate_tile_local_sigma_clip(*args, 3.0, 1.0, winsorize=mode == "winsorized")[:5]
+                for key, arr in zip(("master", "weight", "coverage", "low", "high"), got):
+                    _close(arr, g[f"{name}/{mode}/{key}"], 2e-5, f"{name} {mode} {key}")
+        finally:
+            s.close()
