@@ -48,30 +48,63 @@ constexpr float kPiF = 3.14159265358979323846f;
 // weights cost 36 FMAs and no transcendental or division.  t == 0 (an exact
 // integer source coordinate) gives the exact weights 0, 0, 1, 0, 0, 0.
 // pair A (c = 0.5): max fit error 7.3e-11
-__device__ constexpr float kL3EA[6] = {6.079271019e-01f, -4.488392797e-01f, 6.364143348e-02f, 2.186747311e-02f, -9.777044177e-03f, 1.680220536e-03f};
-__device__ constexpr float kL3OA[6] = {-1.329050616e+00f, 1.468628193e+00f, -6.481293705e-01f, 1.599001370e-01f, -2.544626853e-02f, 2.676349777e-03f};
+__device__ __forceinline__ float l3_even_a(float x) {
+  float p = 1.680220594e-03f;
+  p = __fmaf_rn(p, x, -9.777043946e-03f);
+  p = __fmaf_rn(p, x, 2.186747268e-02f);
+  p = __fmaf_rn(p, x, 6.364143640e-02f);
+  p = __fmaf_rn(p, x, -4.488392770e-01f);
+  return __fmaf_rn(p, x, 6.079270840e-01f);
+}
+__device__ __forceinline__ float l3_odd_a(float x) {
+  float p = 2.676349832e-03f;
+  p = __fmaf_rn(p, x, -2.544626780e-02f);
+  p = __fmaf_rn(p, x, 1.599001437e-01f);
+  p = __fmaf_rn(p, x, -6.481293440e-01f);
+  p = __fmaf_rn(p, x, 1.468628168e+00f);
+  return __fmaf_rn(p, x, -1.329050660e+00f);
+}
 // pair B (c = 1.5): max fit error 1.8e-10
-__device__ constexpr float kL3EB[6] = {-1.350949116e-01f, 5.606142051e-01f, -6.639494271e-02f, -6.422391983e-02f, 2.526676875e-02f, -4.255278694e-03f};
-__device__ constexpr float kL3OB[6] = {1.801265486e-01f, -8.275418234e-01f, 4.563217525e-01f, -1.171571662e-01f, 1.821853304e-02f, -1.830645261e-03f};
+__device__ __forceinline__ float l3_even_b(float x) {
+  float p = -4.255278502e-03f;
+  p = __fmaf_rn(p, x, 2.526676841e-02f);
+  p = __fmaf_rn(p, x, -6.422392279e-02f);
+  p = __fmaf_rn(p, x, -6.639494002e-02f);
+  p = __fmaf_rn(p, x, 5.606142282e-01f);
+  return __fmaf_rn(p, x, -1.350949109e-01f);
+}
+__device__ __forceinline__ float l3_odd_b(float x) {
+  float p = -1.830645255e-03f;
+  p = __fmaf_rn(p, x, 1.821853220e-02f);
+  p = __fmaf_rn(p, x, -1.171571687e-01f);
+  p = __fmaf_rn(p, x, 4.563217461e-01f);
+  p = __fmaf_rn(p, x, -8.275418282e-01f);
+  return __fmaf_rn(p, x, 1.801265478e-01f);
+}
 // pair C (c = 2.5): max fit error 2.1e-10
-__device__ constexpr float kL3EC[6] = {2.431708412e-02f, -8.637609842e-02f, -6.445738508e-02f, 9.083209009e-02f, -3.034376772e-02f, 4.921542137e-03f};
-__device__ constexpr float kL3OC[6] = {-6.355997888e-02f, 3.049877158e-01f, -2.164693742e-01f, 5.576262943e-02f, -7.546908498e-03f, 5.886373014e-04f};
-
-__device__ __forceinline__ float l3_poly(const float (&c)[6], float x) {
-  float p = c[5];
-  p = __fmaf_rn(p, x, c[4]);
-  p = __fmaf_rn(p, x, c[3]);
-  p = __fmaf_rn(p, x, c[2]);
-  p = __fmaf_rn(p, x, c[1]);
-  return __fmaf_rn(p, x, c[0]);
+__device__ __forceinline__ float l3_even_c(float x) {
+  float p = 4.921542015e-03f;
+  p = __fmaf_rn(p, x, -3.034376726e-02f);
+  p = __fmaf_rn(p, x, 9.083209187e-02f);
+  p = __fmaf_rn(p, x, -6.445738673e-02f);
+  p = __fmaf_rn(p, x, -8.637610078e-02f);
+  return __fmaf_rn(p, x, 2.431708388e-02f);
+}
+__device__ __forceinline__ float l3_odd_c(float x) {
+  float p = 5.886373110e-04f;
+  p = __fmaf_rn(p, x, -7.546908688e-03f);
+  p = __fmaf_rn(p, x, 5.576262996e-02f);
+  p = __fmaf_rn(p, x, -2.164693773e-01f);
+  p = __fmaf_rn(p, x, 3.049877286e-01f);
+  return __fmaf_rn(p, x, -6.355997920e-02f);
 }
 
 __device__ __forceinline__ void lanczos3_weights(float t, float (&w)[6]) {
   const float u = __fsub_rn(t, 0.5f);
   const float x = __fmul_rn(u, u);
-  const float ea = l3_poly(kL3EA, x), oa = __fmul_rn(u, l3_poly(kL3OA, x));
-  const float eb = l3_poly(kL3EB, x), ob = __fmul_rn(u, l3_poly(kL3OB, x));
-  const float ec = l3_poly(kL3EC, x), oc = __fmul_rn(u, l3_poly(kL3OC, x));
+  const float ea = l3_even_a(x), oa = __fmul_rn(u, l3_odd_a(x));
+  const float eb = l3_even_b(x), ob = __fmul_rn(u, l3_odd_b(x));
+  const float ec = l3_even_c(x), oc = __fmul_rn(u, l3_odd_c(x));
   const bool exact = t == 0.0f;
   w[0] = exact ? 0.0f : __fadd_rn(ec, oc);
   w[1] = exact ? 0.0f : __fadd_rn(eb, ob);

@@ -55,6 +55,11 @@ struct StarFrameState {
   double background;
   int kept;
   int pad2;
+  // sample-bracket selection (per mode: 0 median, 1 MAD)
+  unsigned band_lo, band_hi;  // inclusive key band from the sample
+  unsigned below;             // finite keys under band_lo
+  unsigned inside;            // keys in the band (appended, may exceed capacity)
+  int resolved[2];            // 1: the order statistic came from the band
 };
 
 __device__ __forceinline__ unsigned float_key(float v) {
@@ -88,6 +93,7 @@ __global__ void __launch_bounds__(256) select_hist_kernel(SelectArgs a) {
   __shared__ unsigned h[2][kSelBins];
   __shared__ unsigned s_valid;
   const int k = blockIdx.y;
+  if (a.state[k].resolved[a.mode]) return;  // the sample bracket found it
   for (int i = threadIdx.x; i < 2 * kSelBins; i += blockDim.x) (&h[0][0])[i] = 0u;
   if (threadIdx.x == 0) s_valid = 0;
   __syncthreads();
@@ -170,6 +176,7 @@ __global__ void __launch_bounds__(256) select_scan_kernel(SelectArgs a, int fram
   const int k = blockIdx.x;
   if (k >= frames) return;
   StarFrameState& st = a.state[k];
+  if (st.resolved[a.mode]) return;  // the sample bracket found it
   const unsigned* g = a.hist + static_cast<int64_t>(k) * 2 * kSelBins;
   const int nbins = a.pass == 2 ? 1024 : kSelBins;
   const int nh = a.pass == 0 ? 1 : 2;
@@ -230,6 +237,208 @@ __global__ void __launch_bounds__(256) select_scan_kernel(SelectArgs a, int fram
       const float med = st.count ? __fmul_rn(__fadd_rn(lo, hi), 0.5f) : 0.0f;
       if (a.mode == 0) st.median = med; else st.mad = med;
     }
+  }
+}
+
+// ---- order statistics by a sample bracket ------------------------------------
+// One pass over the frame instead of three: a sample of kBracketSamples
+// evenly spaced pixels is sorted in shared memory and gives a key band that
+// holds the wanted ranks (the middle ranks of the finite pixels) with a
+// seven-sigma margin; the pass counts the finite keys below the band and
+// copies the keys inside it to a per-frame buffer, where a radix select over
+// the band's key range finds the exact order statistics.  A frame whose band
+// misses the ranks or overflows the buffer (heavily tied data) keeps
+// resolved = 0 and goes through the three-pass radix select above.
+constexpr int kBracketSamples = 32768;
+
+struct BracketArgs {
+  const float* slots;
+  const int* slot_of_frame;
+  int64_t stride;
+  int64_t pixels;
+  const int* frames;
+  StarFrameState* state;
+  unsigned* band;      // [count][band_cap]
+  int64_t band_cap;
+  int mode;            // 0: v, 1: |v - median|
+};
+
+__device__ __forceinline__ bool bracket_key(float v, int mode, float median, unsigned& key) {
+  if (!isfinite(v)) return false;
+  key = float_key(mode == 1 ? fabsf(__fsub_rn(v, median)) : v);
+  return true;
+}
+
+__global__ void __launch_bounds__(1024) bracket_sample_kernel(BracketArgs a) {
+  extern __shared__ unsigned keys[];  // kBracketSamples (or pixels, if fewer)
+  __shared__ unsigned s_valid;
+  const int k = blockIdx.x;
+  StarFrameState& st = a.state[k];
+  const float* src = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+  const int n = static_cast<int>(a.pixels < kBracketSamples ? a.pixels : static_cast<int64_t>(kBracketSamples));
+  int m = 1;
+  while (m < n) m <<= 1;
+  if (threadIdx.x == 0) s_valid = 0u;
+  __syncthreads();
+  unsigned valid = 0;
+  const float median = st.median;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    unsigned key = 0xffffffffu;
+    if (i < n) {
+      const int64_t pos = ((2 * static_cast<int64_t>(i) + 1) * a.pixels) / (2 * static_cast<int64_t>(n));
+      if (bracket_key(__ldg(src + pos), a.mode, median, key)) ++valid;
+      else key = 0xffffffffu;
+    }
+    keys[i] = key;
+  }
+  valid = __reduce_add_sync(0xffffffffu, valid);
+  if ((threadIdx.x & 31) == 0 && valid) atomicAdd(&s_valid, valid);
+  __syncthreads();
+  for (int size = 2; size <= m; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const unsigned x = keys[i], y = keys[j];
+          if (((i & size) == 0) == (x > y)) {
+            keys[i] = y;
+            keys[j] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0) {
+    const int sv = static_cast<int>(s_valid);
+    // middle of the finite samples +- 7 binomial sigma (+8 for small samples)
+    const int margin = static_cast<int>(ceilf(3.5f * sqrtf(static_cast<float>(sv)))) + 8;
+    const int c = sv / 2;
+    st.band_lo = sv > 0 ? keys[max(0, c - margin)] : 0u;
+    st.band_hi = sv > 0 ? keys[min(sv - 1, c + margin)] : 0u;
+    st.below = 0u;
+    st.inside = 0u;
+    if (a.mode == 0) st.count = 0u;
+  }
+}
+
+__global__ void __launch_bounds__(256) bracket_pass_kernel(BracketArgs a) {
+  const int k = blockIdx.y;
+  StarFrameState& st = a.state[k];
+  const unsigned lo = st.band_lo, hi = st.band_hi;
+  const float median = st.median;
+  const float* src = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
+  unsigned* band = a.band + static_cast<int64_t>(k) * a.band_cap;
+  const int lane = threadIdx.x & 31;
+  unsigned below = 0, valid = 0;
+  auto visit = [&](float v, bool present) {
+    unsigned key = 0;
+    const bool fin = present && bracket_key(v, a.mode, median, key);
+    valid += fin ? 1u : 0u;
+    below += (fin && key < lo) ? 1u : 0u;
+    const bool in = fin && key >= lo && key <= hi;
+    const unsigned mask = __ballot_sync(0xffffffffu, in);
+    if (mask) {
+      const int leader = __ffs(mask) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(&st.inside, static_cast<unsigned>(__popc(mask)));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (in) {
+        const int64_t pos = static_cast<int64_t>(base) + __popc(mask & ((1u << lane) - 1u));
+        if (pos < a.band_cap) band[pos] = key;
+      }
+    }
+  };
+  // every lane of a warp runs the same trip count (the ballot needs them all)
+  const int64_t n4 = a.pixels / 4;
+  const float4* src4 = reinterpret_cast<const float4*>(src);
+  const int64_t gstride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t base = blockIdx.x * int64_t(blockDim.x); base < n4; base += gstride) {
+    const int64_t i = base + threadIdx.x;
+    const bool present = i < n4;
+    const float4 q = present ? __ldg(src4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    visit(q.x, present);
+    visit(q.y, present);
+    visit(q.z, present);
+    visit(q.w, present);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    for (int64_t p = n4 * 4 + threadIdx.x; p - threadIdx.x < a.pixels; p += 32) {
+      const bool present = p < a.pixels;
+      visit(present ? __ldg(src + p) : 0.0f, present);
+    }
+  }
+  below = __reduce_add_sync(0xffffffffu, below);
+  valid = __reduce_add_sync(0xffffffffu, valid);
+  if (lane == 0) {
+    if (below) atomicAdd(&st.below, below);
+    if (a.mode == 0 && valid) atomicAdd(&st.count, valid);
+  }
+}
+
+// One CTA per frame: the two middle ranks' keys inside the band by an MSB-
+// first radix select over key - band_lo (8 bits per pass, shared
+// histograms), then the median / MAD as the float32 mean of the two middle
+// values (np.median).
+__global__ void __launch_bounds__(1024) bracket_resolve_kernel(BracketArgs a) {
+  __shared__ unsigned hist[2][256];
+  __shared__ unsigned s_prefix[2], s_rank[2];
+  __shared__ int s_ok;
+  const int k = blockIdx.x;
+  StarFrameState& st = a.state[k];
+  const unsigned* band = a.band + static_cast<int64_t>(k) * a.band_cap;
+  if (threadIdx.x == 0) {
+    const unsigned n = st.count;
+    const unsigned rhi = n / 2, rlo = (n & 1u) ? rhi : (rhi > 0 ? rhi - 1 : 0);
+    const bool ok = n > 0 && static_cast<int64_t>(st.inside) <= a.band_cap && st.below <= rlo &&
+                    rhi < st.below + st.inside;
+    s_ok = ok ? 1 : 0;
+    s_rank[0] = ok ? rlo - st.below : 0u;
+    s_rank[1] = ok ? rhi - st.below : 0u;
+    s_prefix[0] = s_prefix[1] = 0u;
+    st.resolved[a.mode] = 0;
+    if (!ok && a.mode == 0) st.count = 0u;  // the radix passes count the finite pixels again
+  }
+  __syncthreads();
+  if (!s_ok) return;
+  const unsigned lo = st.band_lo;
+  const unsigned range = st.band_hi - lo;
+  int top = 0;  // bits of the key range
+  while (top < 32 && (range >> top) != 0u) ++top;
+  const int m = static_cast<int>(st.inside);
+  for (int shift = ((top + 7) / 8) * 8 - 8; shift >= 0; shift -= 8) {
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) (&hist[0][0])[i] = 0u;
+    __syncthreads();
+    const unsigned pre0 = s_prefix[0], pre1 = s_prefix[1];
+    const int hi_shift = shift + 8;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      const unsigned d = band[i] - lo;
+      const unsigned hp = hi_shift >= 32 ? 0u : (d >> hi_shift);
+      const unsigned digit = (d >> shift) & 255u;
+      if (hp == pre0) atomicAdd(&hist[0][digit], 1u);
+      if (hp == pre1 && pre1 != pre0) atomicAdd(&hist[1][digit], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      const int r = threadIdx.x;
+      const unsigned* h = (r == 1 && s_prefix[1] == s_prefix[0]) ? hist[0] : hist[r];
+      unsigned rank = s_rank[r];
+      int b = 0;
+      while (b < 255 && rank >= h[b]) {
+        rank -= h[b];
+        ++b;
+      }
+      s_rank[r] = rank;
+      s_prefix[r] = (s_prefix[r] << 8) | static_cast<unsigned>(b);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const float vlo = key_float(lo + s_prefix[0]);
+    const float vhi = key_float(lo + s_prefix[1]);
+    const float med = __fmul_rn(__fadd_rn(vlo, vhi), 0.5f);
+    if (a.mode == 0) st.median = med; else st.mad = med;
+    st.resolved[a.mode] = 1;
   }
 }
 
@@ -399,19 +608,18 @@ __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
   const float* img = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
   const float thr = a.state[k].threshold_f32;
   const int W = a.width, H = a.height;
-  const int64_t interior = static_cast<int64_t>(W - 2) * (H - 2);
   unsigned* out = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
-  // rows are dealt to blocks, columns to threads (coalesced, no division)
+  // rows are dealt to blocks, columns to the block's threads (coalesced, no
+  // division); every thread of a row pass runs the same trip count, so the
+  // warp ballot below always sees the full warp
   const int cols = W - 2;
-  const int64_t per_row = (cols + blockDim.x - 1) / blockDim.x;  // thread slots per row
-  const int64_t slots = per_row * (H - 2);
-  for (int64_t s = blockIdx.x; s < slots; s += gridDim.x) {
-    const int y = 1 + static_cast<int>(s / per_row);
-    const int x = 1 + static_cast<int>(s - (s / per_row) * per_row) * static_cast<int>(blockDim.x) +
-                  static_cast<int>(threadIdx.x);
+  const int passes = (cols + static_cast<int>(blockDim.x) - 1) / static_cast<int>(blockDim.x);
+  for (int y = 1 + static_cast<int>(blockIdx.x); y < H - 1; y += static_cast<int>(gridDim.x)) {
+   for (int pass = 0; pass < passes; ++pass) {
+    const int x = 1 + pass * static_cast<int>(blockDim.x) + static_cast<int>(threadIdx.x);
     bool hit = false;
     const int64_t idx = static_cast<int64_t>(y) * W + x;
-    if (interior > 0 && x <= cols) {
+    if (x <= cols) {
       const float c = __ldg(img + idx);
       bool above;
       if (a.mesh.bg) {
@@ -443,10 +651,33 @@ __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
         if (pos < static_cast<unsigned>(kMaxCandidates)) out[pos] = static_cast<unsigned>(idx);
       }
     }
+   }
   }
 }
 
 // Measured star (float64 fields as the CPU's Python floats).
+// Float-float sum of the whole warp (TwoSum butterfly), in every lane.
+__device__ __forceinline__ void ff_warp_sum(FF& s) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, s.hi, off);
+    const float ol = __shfl_xor_sync(0xffffffffu, s.lo, off);
+    float h, e;
+    two_sum(s.hi, oh, h, e);
+    s.hi = h;
+    s.lo = __fadd_rn(__fadd_rn(s.lo, ol), e);
+  }
+}
+
+// (n.hi + n.lo) / (d.hi + d.lo) to about 46 bits, returned as a double.
+__device__ __forceinline__ double ff_quotient_f64(const FF& n, const FF& d) {
+  const float q = __fdiv_rn(n.hi, d.hi);
+  float r = __fmaf_rn(-q, d.hi, n.hi);
+  r = __fadd_rn(r, n.lo);
+  r = __fmaf_rn(-q, d.lo, r);
+  return static_cast<double>(q) + static_cast<double>(__fdiv_rn(r, d.hi));
+}
+
 struct StarRec {
   double x, y, flux, peak, fwhm, ecc, snr, sharpness;
   int npix;
@@ -524,43 +755,42 @@ __global__ void __launch_bounds__(256) star_measure_kernel(CatalogArgs a) {
     double bg = st.background, noise = st.noise;
     if (a.mesh.bg) mesh_at(a.mesh, k, x, y, bg, noise);
     const float bg32 = a.mesh.bg ? __double2float_rn(bg) : st.background_f32;
+    (void)noise;
     const int x0 = max(0, x - r), x1 = min(W, x + r + 1);
     const int y0 = max(0, y - r), y1 = min(H, y + r + 1);
     const int ww = x1 - x0, npx = ww * (y1 - y0);
-    double f = 0.0, sx = 0.0, sy = 0.0;
+    // float-float sums (about 48 bits; the weights are float32 and the
+    // coordinate products exact): float64 is scarce on this part
+    FF f, sx, sy;
     int fin = 0, pos = 0;
     for (int q = lane; q < npx; q += 32) {
-      const int xx = x0 + q % ww, yy = y0 + q / ww;
+      const int row = q / ww;
+      const int xx = x0 + (q - row * ww), yy = y0 + row;
       const float v = __ldg(img + static_cast<int64_t>(yy) * W + xx);
       if (!isfinite(v)) continue;
       ++fin;
       const float wv = fmaxf(__fsub_rn(v, bg32), 0.0f);
       pos += wv > 0.0f;
-      const double wd = static_cast<double>(wv);
-      f += wd;
-      sx += static_cast<double>(xx) * wd;
-      sy += static_cast<double>(yy) * wd;
+      f.add(wv);
+      sx.add_prod(static_cast<float>(xx), wv);
+      sy.add_prod(static_cast<float>(yy), wv);
     }
-    for (int off = 16; off > 0; off >>= 1) {
-      f += __shfl_xor_sync(0xffffffffu, f, off);
-      sx += __shfl_xor_sync(0xffffffffu, sx, off);
-      sy += __shfl_xor_sync(0xffffffffu, sy, off);
-      fin += __shfl_xor_sync(0xffffffffu, fin, off);
-      pos += __shfl_xor_sync(0xffffffffu, pos, off);
-    }
+    ff_warp_sum(f);
+    ff_warp_sum(sx);
+    ff_warp_sum(sy);
+    fin = __reduce_add_sync(0xffffffffu, fin);
+    pos = __reduce_add_sync(0xffffffffu, pos);
     StarRec rec{};
-    rec.valid = (fin > 0 && f > 0.0) ? 1 : 0;
-    if (rec.valid) {
-      // second moments (fwhm, eccentricity) are measured later, only for the
-      // stars that survive selection (star_moments_kernel)
-      rec.x = sx / f;
-      rec.y = sy / f;
-      rec.flux = f;
+    rec.valid = (fin > 0 && f.hi > 0.0f) ? 1 : 0;
+    if (rec.valid && lane == 0) {
+      // second moments, snr and sharpness are filled in for the selected
+      // stars only (star_select_kernel, star_moments_kernel)
+      rec.x = ff_quotient_f64(sx, f);
+      rec.y = ff_quotient_f64(sy, f);
+      rec.flux = static_cast<double>(f.hi) + static_cast<double>(f.lo);
       const float center = __ldg(img + static_cast<int64_t>(y) * W + x);
       rec.peak = fmax(static_cast<double>(center) - bg, 0.0);
       rec.npix = pos;
-      rec.snr = f / fmax(noise * sqrt(static_cast<double>(max(pos, 1))), 1.0e-6);
-      rec.sharpness = rec.peak / fmax(f, 1.0e-6);
     }
     if (lane == 0) recs[c] = rec;
   }
@@ -757,8 +987,15 @@ __global__ void __launch_bounds__(1024) star_select_kernel(CatalogArgs a) {
     s.peak = r.peak;
     s.fwhm = nan("");  // star_moments_kernel
     s.eccentricity = nan("");
-    s.snr = r.snr;
-    s.sharpness = r.sharpness;
+    double noise = st.noise;
+    if (a.mesh.bg) {
+      const unsigned idx = a.cand[static_cast<int64_t>(k) * kMaxCandidates + sel[i].idx];
+      double bg_unused;
+      mesh_at(a.mesh, k, static_cast<int>(idx % static_cast<unsigned>(a.width)),
+              static_cast<int>(idx / static_cast<unsigned>(a.width)), bg_unused, noise);
+    }
+    s.snr = r.flux / fmax(noise * sqrt(static_cast<double>(max(r.npix, 1))), 1.0e-6);
+    s.sharpness = r.peak / fmax(r.flux, 1.0e-6);
     s.npix = r.npix;
     s.pad = 0;
     out[i] = s;
@@ -1074,11 +1311,13 @@ struct StarScratch {
   double* mesh_bg = nullptr;  // [frames][cells]
   double* mesh_nz = nullptr;
   int64_t mesh_cap = 0;       // doubles per array
+  unsigned* band = nullptr;   // sample-bracket key buffers
+  int64_t band_elems = 0;
 };
 
 static void free_star_scratch(StarScratch& s) {
   void* ps[] = {s.state,  s.hist,      s.cand,      s.recs,    s.kept,    s.out,    s.frames,
-                s.rms,    s.pw_prefix, s.pw_leaves, s.pw_sums, s.mesh_bg, s.mesh_nz};
+                s.rms,    s.pw_prefix, s.pw_leaves, s.pw_sums, s.mesh_bg, s.mesh_nz, s.band};
   for (void* p : ps)
     if (p) cudaFree(p);
   s = StarScratch{};
@@ -1153,8 +1392,33 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
                                       std::max(1u, static_cast<unsigned>(sm_count() * 8 / std::max(count, 1)))));
   double* rms = nullptr;
   if (need_stats) {
+    // band buffers of the sample-bracket selection: a sixteenth of the frame
+    // (the band holds ~2.5 % of a 9600 x 6422 frame's pixels)
+    const int64_t band_cap = std::min<int64_t>(s->pixels, std::max<int64_t>(65536, s->pixels / 16));
+    if (sc.band_elems < band_cap * count) {
+      if (sc.band) cudaFree(sc.band);
+      sc.band = nullptr;
+      sc.band_elems = 0;
+      check_cuda(cudaMalloc(&sc.band, sizeof(unsigned) * band_cap * count), "cudaMalloc(bracket band)");
+      sc.band_elems = band_cap * count;
+    }
+    BracketArgs ba{s->d_slots, s->d_slot_of_frame, s->stride, s->pixels, sc.frames, sc.state, sc.band, band_cap, 0};
+    const int samples = static_cast<int>(std::min<int64_t>(kBracketSamples, s->pixels));
+    int sample_pow2 = 1;
+    while (sample_pow2 < samples) sample_pow2 <<= 1;
+    const size_t sample_smem = sizeof(unsigned) * static_cast<size_t>(sample_pow2);
+    check_cuda(cudaFuncSetAttribute(bracket_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(sample_smem)),
+               "cudaFuncSetAttribute(bracket sample)");
     for (int mode = 0; mode < 2; ++mode) {
       sa.mode = mode;
+      ba.mode = mode;
+      note_launch(3);
+      bracket_sample_kernel<<<static_cast<unsigned>(count), 1024, sample_smem, s->stream>>>(ba);
+      bracket_pass_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), 256, 0, s->stream>>>(ba);
+      bracket_resolve_kernel<<<static_cast<unsigned>(count), 1024, 0, s->stream>>>(ba);
+      check_cuda(cudaGetLastError(), "bracket select launch");
+      // frames the bracket could not settle: three-pass radix select
       for (int pass = 0; pass < 3; ++pass) {
         sa.pass = pass;
         check_cuda(cudaMemsetAsync(sc.hist, 0, sizeof(unsigned) * count * 2 * kSelBins, s->stream),
@@ -1247,7 +1511,9 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
     da.mesh = MeshView{sc.mesh_bg, sc.mesh_nz, ma.cell, ma.nx, ma.ny};
   }
   note_launch();
-  star_detect_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), 256, 0, s->stream>>>(da);
+  const unsigned detect_rows = static_cast<unsigned>(std::max<int64_t>(
+      1, std::min<int64_t>(s->height - 2, std::max<int64_t>(1, sm_count() * 8 / std::max(count, 1)))));
+  star_detect_kernel<<<dim3(detect_rows, static_cast<unsigned>(count)), 256, 0, s->stream>>>(da);
   check_cuda(cudaGetLastError(), "star_detect launch");
   CatalogArgs ca{};
   ca.slots = s->d_slots;

@@ -5,9 +5,11 @@ L(t - k) with L(d) = sinc(d) sinc(d / 3) (zero for |d| >= 3).  With
 u = t - 1/2 the taps pair up as L(c + u) and L(c - u) for c = 1/2, 3/2, 5/2
 (L is even), so each pair is E_c(u) +- O_c(u) with E_c even and O_c odd in
 u.  This script fits E_c(u) = sum_j e_j u^(2j) and O_c(u) = u sum_j o_j u^(2j)
-(j = 0..5) by float64 least squares on u in [0, 1/2] and prints the C table
-pasted into csrc/sampling.cuh; the fit error is below 3e-10, far under
-float32 rounding.  Run: python -m glass_gb300.lanczos_poly
+(j = 0..5) by float64 least squares on u in [0, 1/2] and prints the six
+Horner evaluations, with the coefficients as float literals (immediate
+operands of the fused multiply-adds), pasted into csrc/sampling.cuh; the fit
+error is below 3e-10, far under float32 rounding.
+Run: python -m glass_gb300.lanczos_poly
 """
 
 from __future__ import annotations
@@ -35,12 +37,21 @@ def fit(center: float, samples: int = 20001):
     return e, o, err
 
 
+def horner_source(name: str, coefs) -> str:
+    c = [f"{float(v):.9e}f" for v in coefs]
+    body = f"  float p = {c[5]};\n"
+    for j in (4, 3, 2, 1):
+        body += f"  p = __fmaf_rn(p, x, {c[j]});\n"
+    body += f"  return __fmaf_rn(p, x, {c[0]});\n"
+    return f"__device__ __forceinline__ float l3_{name}(float x) {{\n{body}}}"
+
+
 def main() -> None:
-    for name, center in (("A", 0.5), ("B", 1.5), ("C", 2.5)):
+    for name, center in (("a", 0.5), ("b", 1.5), ("c", 2.5)):
         e, o, err = fit(center)
-        print(f"// pair {name} (c = {center}): max fit error {err:.1e}")
-        print(f"__device__ constexpr float kL3E{name}[6] = {{" + ", ".join(f"{v:.9e}f" for v in e) + "};")
-        print(f"__device__ constexpr float kL3O{name}[6] = {{" + ", ".join(f"{v:.9e}f" for v in o) + "};")
+        print(f"// pair {name.upper()} (c = {center}): max fit error {err:.1e}")
+        print(horner_source("even_" + name, e.astype(np.float32)))
+        print(horner_source("odd_" + name, o.astype(np.float32)))
 
 
 if __name__ == "__main__":

@@ -368,3 +368,54 @@ def generate_device(config: StackConfig | str, frames: int | None = None, cloud_
         lights[i] = _u16_as_i16(torch, frame)
         del frame
     return DeviceStack(cfg, lights, bias_frames, dark_frames, flat_frames, truth, cloud)
+
+
+def render_affine_device(frames: int, height: int, width: int, stars_per_128: float = 30.0, linear_sigma: float = 1e-3,
+                         max_shift: float = 0.5, fwhm: float = 2.5, sky: float = 1000.0, read_noise: float = 5.0,
+                         seed: int = 3, device: str = "cuda"):
+    """Calibrated float32 frames of one star field under random affine maps
+    (the differentiable-registration workload): ~`stars_per_128` Gaussian
+    stars per 128 x 128 pixels (FWHM `fwhm`, peak log-uniform 500-20000 ADU),
+    sky `sky`, Poisson shot noise plus Gaussian read noise; frame i shows the
+    field under forward = I + N(0, linear_sigma) on the linear terms and a
+    uniform +-max_shift translation (frame 0: identity).  Returns a (N, H, W)
+    float32 CUDA tensor and the (N, 3, 3) moving -> reference truth
+    matrices."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    n_stars = int(round(stars_per_128 * height * width / 128.0 ** 2))
+    margin = max_shift + 4.0 * linear_sigma * max(height, width) + 8
+    xy = np.column_stack([rng.uniform(-margin, width + margin, n_stars), rng.uniform(-margin, height + margin, n_stars)])
+    peak = torch.as_tensor(np.exp(rng.uniform(np.log(500.0), np.log(20000.0), n_stars)), device=device,
+                           dtype=torch.float32)
+    sigma = fwhm / 2.3548200450309493
+    radius = int(np.ceil(4.0 * sigma)) + 1
+    offs = torch.arange(-radius, radius + 1, device=device, dtype=torch.int64)
+    out = torch.empty((frames, height, width), device=device, dtype=torch.float32)
+    truth = np.empty((frames, 3, 3))
+    for i in range(frames):
+        fwd = np.eye(3)
+        if i:
+            fwd[:2, :2] += rng.normal(0.0, linear_sigma, (2, 2))
+            fwd[:2, 2] = rng.uniform(-max_shift, max_shift, 2)
+        truth[i] = np.linalg.inv(fwd)
+        pos = torch.as_tensor(xy @ fwd[:2, :2].T + fwd[:2, 2], device=device)
+        cx = torch.floor(pos[:, 0]).to(torch.int64)
+        cy = torch.floor(pos[:, 1]).to(torch.int64)
+        gx = cx[:, None] + offs[None, :]
+        gy = cy[:, None] + offs[None, :]
+        dx = (gx.to(torch.float64) - pos[:, 0:1]).to(torch.float32)
+        dy = (gy.to(torch.float64) - pos[:, 1:2]).to(torch.float32)
+        prof = torch.exp(-0.5 * (dx[:, None, :] ** 2 + dy[:, :, None] ** 2) / (sigma * sigma)) * peak[:, None, None]
+        ys = gy[:, :, None].expand_as(prof)
+        xs = gx[:, None, :].expand_as(prof)
+        ok = (ys >= 0) & (ys < height) & (xs >= 0) & (xs < width)
+        signal = torch.full((height * width,), sky, device=device, dtype=torch.float32)
+        signal.index_put_((ys[ok] * width + xs[ok],), prof[ok], accumulate=True)
+        frame = torch.poisson(signal, generator=gen)
+        frame += read_noise * torch.randn(frame.shape, device=device, generator=gen)
+        out[i] = frame.view(height, width)
+    return out, truth

@@ -17,10 +17,13 @@ HEADER = Path(__file__).resolve().parent.parent / "glass_gb300" / "csrc" / "samp
 
 
 def _header_table() -> dict:
+    """{"EA": c0..c5, "OA": ...} from the l3_even_* / l3_odd_* Horner functions."""
     text = HEADER.read_text()
     table = {}
-    for name, body in re.findall(r"kL3([EO][ABC])\[6\] = \{([^}]*)\}", text):
-        table[name] = np.array([float(v.rstrip("f")) for v in body.split(",")], dtype=np.float32)
+    for parity, pair, body in re.findall(r"float l3_(even|odd)_([abc])\(float x\) \{(.*?)\n\}", text, re.S):
+        lits = [float(v) for v in re.findall(r"(-?\d\.\d+e[+-]\d+)f", body)]
+        table[("E" if parity == "even" else "O") + pair.upper()] = np.array(lits[::-1], dtype=np.float32)
+    assert len(table) == 6
     return table
 
 

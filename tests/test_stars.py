@@ -83,6 +83,41 @@ def test_gpu_detect_stars_batch_and_info(native):
     s.close()
 
 
+@pytest.mark.gpu
+def test_gpu_median_mad_exact_on_large_and_adversarial_frames(native):
+    """Frames larger than the sample the order statistics start from: a sky
+    frame (the sample's band settles both statistics in one pass), a frame
+    whose sampled pixels differ from all the others, and
+    a frame of heavy ties with NaNs (both fall back to the three-pass radix
+    select).  Median and MAD must equal the oracle's exactly."""
+    rng = np.random.default_rng(31)
+    h, w = 256, 384
+    sky = (1000.0 + 31.0 * rng.standard_normal((h, w))).astype(np.float32)
+    sky[rng.random((h, w)) < 1e-3] = 40000.0
+    # the sampled pixels (32768 evenly spaced positions) hold small values,
+    # every other pixel 1000: the sample's band misses the true middle ranks
+    n_pix, n_sample = h * w, 32768
+    sampled = ((2 * np.arange(n_sample, dtype=np.int64) + 1) * n_pix) // (2 * n_sample)
+    alternating = np.full(n_pix, 1000.0, dtype=np.float32)
+    alternating[sampled] = rng.normal(0.0, 1.0, n_sample).astype(np.float32)
+    alternating = alternating.reshape(h, w)
+    ties = rng.integers(0, 4, (h, w)).astype(np.float32) * 10.0
+    ties[rng.random((h, w)) < 0.1] = np.nan
+    frames = [sky, alternating, ties]
+    s = native.ResidentCalibratedStack(len(frames), h, w)
+    try:
+        for k, f in enumerate(frames):
+            s.upload_calibrated_frame(k, f)
+        _cats, info = s.detect_stars([0, 1, 2], threshold_sigma=5.0, max_stars=20, with_info=True)
+        for k, f in enumerate(frames):
+            med, _rms, mad, _noise = ostars.robust_background(f)
+            assert info[k]["median"] == np.float32(med), k
+            assert info[k]["mad"] == np.float32(mad), k
+            assert info[k]["valid_pixels"] == int(np.isfinite(f).sum())
+    finally:
+        s.close()
+
+
 # ---- background mesh (this project's extension; the oracle is the spec) ----------
 
 def _gradient_field(seed, h=192, w=256, n=40):
