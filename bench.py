@@ -501,8 +501,8 @@ def graph_report(pipe, dev_raw, matrices, stream, reps: int) -> dict:
     stream, CUDA events, inputs larger than L2 (the raw stack and the frames)."""
     import torch
 
-    if pipe.frames > 32:
-        return {"skipped": "the captured step graph takes at most 32 frames"}
+    if pipe.frames > 512:
+        return {"skipped": "the captured step graph takes at most 512 frames"}
     ptr = dev_raw.data_ptr()
 
     def timed(fn):
@@ -693,7 +693,7 @@ def run_c5(args) -> int:
     side = {}
     if not args.no_side:
         for name, fn in (("c2", lambda: c2_side_report(local, max(3, min(args.steps, 10)))),
-                         ("c3", lambda: c3_side_report(local))):
+                         ("c3", lambda: c3_side_report(local)), ("c4", lambda: c4_side_report(local))):
             try:
                 side[name] = fn()
             except Exception as exc:  # a side report must not lose the headline line
@@ -856,6 +856,114 @@ def c3_side_report(local: int, frames: int = 64, size: int = 4096) -> dict:
         return out
     finally:
         pipe.close()
+
+
+C4_STACKS = (  # name, frames, height, width, interpolation, rejection
+    ("A", 40, 2000, 3000, "bilinear", "winsorized"),
+    ("B", 120, 4000, 6000, "lanczos3", "winsorized"),
+    ("C", 25, 1024, 1024, "lanczos3", "linear_fit"),
+)
+
+
+def c4_side_report(local: int, reps: int = 3) -> dict:
+    """Batched uneven stacks: A 40 x 3000 x 2000 (bilinear, winsorized 3/3),
+    B 120 x 6000 x 4000 (Lanczos3, winsorized 3/3) and C 25 x 1024 x 1024
+    (Lanczos3, linear-fit clipping), raw uint16 rendered with the 8-frame
+    config's noise model (30 stars per 128 x 128, sky 1000, pedestal 500,
+    integer shifts +-5 px, 4 calibration frames of each kind).  Each stack's
+    calibrate -> simple_snr weights -> warp -> rejection + integration runs
+    eagerly stack after stack (CUDA events per stack) and as one CUDA graph
+    of all three (gg_stacks_graph_capture); the replayed maps are compared
+    with the eager ones bit for bit."""
+    import dataclasses
+
+    import torch
+
+    from glass_gb300 import _glass_cuda_native as native
+    from glass_gb300 import _lib
+    from glass_gb300.pipeline import build_masters
+    from glass_gb300.synthetic import CONFIGS, generate_device
+
+    rejections = {"winsorized": _lib.GG_REJECT_WINSORIZED, "linear_fit": _lib.GG_REJECT_LINEAR_FIT}
+    interps = {"bilinear": _lib.GG_INTERP_BILINEAR, "lanczos3": _lib.GG_INTERP_LANCZOS3}
+    stream = torch.cuda.Stream()
+    peak, _ = measured_peak()
+    stacks, raws, mats, steps = [], [], [], []
+    try:
+        for k, (name, n, h, w, interp, rej) in enumerate(C4_STACKS):
+            cfg = dataclasses.replace(CONFIGS["c1"], frames=n, height=h, width=w,
+                                      stars=int(round(30 * h * w / 128.0 ** 2)), seed=40 + k)
+            data = generate_device(cfg, n, device=f"cuda:{local}")
+            masters = build_masters(data.bias_frames, data.dark_frames, data.flat_frames)
+            s = native.ResidentCalibratedStack(n, h, w)
+            s.set_stream(stream.cuda_stream)
+            s.set_calibration_masters(masters.bias, masters.dark, masters.flat)
+            stacks.append(s)
+            raws.append(data.lights)
+            mats.append(np.asarray(data.truth_matrices))
+            steps.append({"stack": s, "dev_raw": data.lights.data_ptr(), "matrices": mats[-1],
+                          "interpolation": interp, "rejection": rejections[rej],
+                          "calib": _lib.CalibParams(0, 1.0, 1.0e-6, 0.0)})
+        torch.cuda.synchronize()
+
+        def eager(k):
+            st, s = steps[k], stacks[k]
+            n = s.frame_count
+            idx = np.arange(n, dtype=np.int64)
+            _lib.call("gg_stack_calibrate_u16_device", s.handle, _lib.ptr(idx), ctypes.c_int64(n),
+                      ctypes.c_void_p(st["dev_raw"]), 0, ctypes.byref(st["calib"]))
+            s.compute_frame_weights("simple_snr", None, 1.0e-6, download=False)
+            moving = np.array([f for f in range(n) if not np.array_equal(mats[k][f], np.eye(3))], dtype=np.int64)
+            s.warp_frames_async(moving, mats[k][moving], interps[st["interpolation"]], np.nan, -1.0, False)
+            s.integrate_async("device", st["rejection"], 3.0, 3.0, 3, 0.5, "uint16")
+
+        for k in range(len(stacks)):  # warm-up (autotuner, buffers)
+            eager(k)
+        stream.synchronize()
+        per_stack = {}
+        eager_maps = []
+        t_seq = 0.0
+        for k, (name, n, h, w, interp, rej) in enumerate(C4_STACKS):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                eager(k)
+            e1.record(stream)
+            stream.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            t_seq += ms
+            eager_maps.append(stacks[k].download_maps("full", include_dq=True))
+            P = h * w
+            warped = sum(1 for f in range(n) if not np.array_equal(mats[k][f], np.eye(3)))
+            nbytes = (6 * n * P + 12 * P) + 4 * n * P + 8 * warped * P + (4 * n * P + 16 * P)
+            per_stack[name] = {"frames": n, "height": h, "width": w, "interpolation": interp, "rejection": rej,
+                               "ms": ms, "mpix_frames_per_s": n * P / 1e6 / (ms / 1e3),
+                               "algorithmic_bytes": nbytes, "achieved_gbs": nbytes / (ms / 1e3) / 1e9,
+                               "frac_of_measured_hbm": nbytes / (ms / 1e3) / 1e9 / peak}
+        graph = native.StacksGraph(steps, stream.cuda_stream)
+        try:
+            graph.launch()
+            stream.synchronize()
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            for _ in range(reps):
+                graph.launch()
+            g1.record(stream)
+            stream.synchronize()
+            t_graph = g0.elapsed_time(g1) / reps
+            identical = all(all(np.array_equal(a, b) for a, b in zip(stacks[k].download_maps("full", include_dq=True),
+                                                                  eager_maps[k]))
+                            for k in range(len(stacks)))
+            kernels = graph.kernel_count
+        finally:
+            graph.close()
+        total = sum(v["frames"] * v["height"] * v["width"] for v in per_stack.values())
+        return {"stacks": per_stack, "sequential_eager_ms": t_seq, "graph_ms": t_graph,
+                "graph_kernels": kernels, "graph_maps_identical_to_eager": identical,
+                "mpix_frames_per_s_graph": total / 1e6 / (t_graph / 1e3)}
+    finally:
+        for s in stacks:
+            s.close()
 
 
 def run_reference(args) -> int:

@@ -163,6 +163,69 @@ def integrate_stacks_batch(stacks: list, rejection: int = _lib.GG_REJECT_WINSORI
         s._last_count_dtype = np.dtype(np.uint16 if count_map_dtype == "uint16" else np.float32)
 
 
+class StacksGraph:
+    """Several resident stacks' calibrate -> weights -> warp -> rejection +
+    integration captured in one CUDA graph (gg_stacks_graph_capture; no
+    counterpart in the reference).  `steps` is a list of dicts with keys
+    stack, dev_raw (device pointer of the stack's uint16 frames), matrices
+    (frame_count x 3 x 3 forward matrices; identities are not warped),
+    interpolation ("bilinear" / "lanczos3"), rejection (GG_REJECT_*), and
+    optionally weighting ("simple_snr" / "unit"), low_sigma, high_sigma,
+    min_samples, max_reject_fraction, count_map_dtype, linear_fit_iterations,
+    calib (a _lib.CalibParams).  Read each stack's maps with download_maps()
+    after launch() and a synchronisation of `stream`."""
+
+    def __init__(self, steps: list[dict], cuda_stream: int | None = None):
+        if not steps:
+            raise ValueError("at least one stack is required")
+        interps = {"bilinear": _lib.GG_INTERP_BILINEAR, "lanczos3": _lib.GG_INTERP_LANCZOS3}
+        self._keep = []
+        arr = (_lib.StackStep * len(steps))()
+        for k, st in enumerate(steps):
+            stack = st["stack"]
+            mats = np.ascontiguousarray(np.asarray(st["matrices"], dtype=np.float64).reshape(-1, 3, 3))
+            if mats.shape[0] != stack.frame_count:
+                raise ValueError("one matrix per frame is required")
+            if st.get("interpolation", "lanczos3") not in interps:
+                raise ValueError("interpolation must be bilinear or lanczos3")
+            dtype = st.get("count_map_dtype", "uint16")
+            if dtype not in ("uint16", "float32"):
+                raise ValueError("count_map_dtype must be float32 or uint16")
+            self._keep.append(mats)
+            arr[k].stack = stack.handle.value
+            arr[k].dev_raw = int(st["dev_raw"])
+            arr[k].host_matrices = mats.ctypes.data
+            arr[k].interpolation = interps[st.get("interpolation", "lanczos3")]
+            arr[k].clamping_threshold = float(st.get("clamping_threshold", -1.0))
+            arr[k].weighting = 1 if st.get("weighting", "simple_snr") == "simple_snr" else 0
+            arr[k].calib = st.get("calib") or _lib.CalibParams(1, 1.0, 1.0e-6, 0.0)
+            arr[k].integrate = _lib.IntegrateParams(
+                int(st.get("rejection", _lib.GG_REJECT_WINSORIZED)), float(st.get("low_sigma", 3.0)),
+                float(st.get("high_sigma", 3.0)), int(st.get("min_samples", 3)),
+                float(st.get("max_reject_fraction", 0.5)),
+                _lib.GG_COUNT_U16 if dtype == "uint16" else _lib.GG_COUNT_F32,
+                int(st.get("linear_fit_iterations", 5)))
+            stack._last_count_dtype = np.dtype(np.uint16 if dtype == "uint16" else np.float32)
+        self._stacks = [st["stack"] for st in steps]
+        self._handle = ctypes.c_void_p()
+        _lib.call("gg_stacks_graph_capture", arr, len(steps), ctypes.c_void_p(cuda_stream),
+                  ctypes.byref(self._handle))
+
+    def launch(self) -> None:
+        _lib.call("gg_stacks_graph_launch", self._handle)
+
+    @property
+    def kernel_count(self) -> int:
+        out = ctypes.c_int32()
+        _lib.call("gg_stacks_graph_kernel_count", self._handle, ctypes.byref(out))
+        return int(out.value)
+
+    def close(self) -> None:
+        if self._handle and self._handle.value:
+            _lib.call("gg_stacks_graph_destroy", self._handle)
+            self._handle = ctypes.c_void_p()
+
+
 class _DeviceView:
     """A resident frame exposed through __cuda_array_interface__ (keeps its stack alive)."""
 

@@ -162,6 +162,19 @@ class IntegrateParams(ctypes.Structure):
     ]
 
 
+class StackStep(ctypes.Structure):
+    _fields_ = [
+        ("stack", ctypes.c_void_p),
+        ("dev_raw", ctypes.c_void_p),
+        ("host_matrices", ctypes.c_void_p),
+        ("interpolation", ctypes.c_int32),
+        ("clamping_threshold", ctypes.c_float),
+        ("weighting", ctypes.c_int32),
+        ("calib", CalibParams),
+        ("integrate", IntegrateParams),
+    ]
+
+
 GG_TRANSFORM_TRANSLATION = 0
 GG_TRANSFORM_SIMILARITY = 1
 GG_TRANSFORM_AFFINE = 2
@@ -399,6 +412,10 @@ PROTOTYPES: dict[str, list] = {
                           ctypes.POINTER(ctypes.c_int32)],
     "gg_stack_graph_kernel_count": [_P, ctypes.POINTER(ctypes.c_int)],
     "gg_stack_graph_destroy": [_P],
+    "gg_stacks_graph_capture": [_P, ctypes.c_int32, _P, _P],
+    "gg_stacks_graph_launch": [_P],
+    "gg_stacks_graph_kernel_count": [_P, _P],
+    "gg_stacks_graph_destroy": [_P],
     "gg_stack_device_ptrs": [_P, ctypes.POINTER(StackDevicePtrs)],
     "gg_stack_frame_device_ptr": [_P, ctypes.c_int64, _P],
     "gg_stack_download_weights": [_P, _P],

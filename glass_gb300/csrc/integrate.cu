@@ -1850,6 +1850,159 @@ extern "C" int gg_stack_graph_capture_step(gg_stack* s, const void* dev_raw, con
   GG_API_END
 }
 
+// ---- several stacks in one graph ------------------------------------------------
+namespace gg {
+void* warp_items_device(gg_stack* s, const int64_t* indices, int64_t count, const double* fwd);
+void launch_warp_items_device(gg_stack* s, void* d_items, int64_t count, int interp, float fill, float clamp);
+}  // namespace gg
+
+struct gg_stacks_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  std::vector<void*> items;       // per step: device warp descriptors (or null)
+  std::vector<int64_t> warped;    // per step: descriptor count
+  int kernels = 0;
+};
+
+namespace gg {
+
+static void stacks_graph_free(gg_stacks_graph* g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  for (void* p : g->items)
+    if (p) cudaFree(p);
+  delete g;
+}
+
+// One stack's step on its (current) stream: decode + calibration of every
+// frame, frame weights, the warp of every frame whose matrix is not the
+// identity, rejection + integration with the device weights.
+static void run_stack_step(const gg_stack_step_t& st, void* d_items, int64_t warped) {
+  gg_stack* s = st.stack;
+  std::vector<int64_t> idx(static_cast<size_t>(s->frames));
+  for (int64_t k = 0; k < s->frames; ++k) idx[static_cast<size_t>(k)] = k;
+  int rc = gg_stack_calibrate_u16_device(s, idx.data(), s->frames, st.dev_raw, 0, &st.calib);
+  if (rc != GG_OK) fail(rc, "stacks graph: calibration failed");
+  rc = gg_stack_compute_weights(s, st.weighting, nullptr, 1.0e-6f, nullptr);
+  if (rc != GG_OK) fail(rc, "stacks graph: frame weighting failed");
+  if (warped > 0) launch_warp_items_device(s, d_items, warped, st.interpolation, NAN, st.clamping_threshold);
+  launch_integrate(s, s->d_weights, st.integrate);
+}
+
+}  // namespace gg
+
+extern "C" int gg_stacks_graph_capture(const gg_stack_step_t* steps, int32_t count, void* cuda_stream,
+                                       gg_stacks_graph** out) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(steps != nullptr && out != nullptr, "null argument");
+  require(count >= 1 && count <= kMaxBatchStacks, "stack count must be in [1, 64]");
+  *out = nullptr;
+  for (int k = 0; k < count; ++k) {
+    const gg_stack_step_t& st = steps[k];
+    require(st.stack != nullptr && st.dev_raw != nullptr && st.host_matrices != nullptr, "null argument");
+    require(st.stack->device == steps[0].stack->device, "stacks of one graph must live on one device");
+    for (int j = 0; j < k; ++j) require(steps[j].stack != st.stack, "a stack appears twice in the graph");
+    require(st.interpolation == GG_INTERP_BILINEAR || st.interpolation == GG_INTERP_LANCZOS3,
+            "interpolation must be bilinear or lanczos3");
+    require(st.weighting == GG_WEIGHTS_PRIOR || st.weighting == GG_WEIGHTS_SIMPLE_SNR, "unsupported weighting mode");
+    validate_integrate(st.integrate);
+    require(st.stack->width < (1 << 24) && st.stack->height < (1 << 24), "frame too large for float coordinates");
+  }
+  gg_stack* first = steps[0].stack;
+  stack_activate(first);
+  auto* g = new gg_stacks_graph();
+  struct Guard {
+    gg_stacks_graph*& g;
+    std::vector<cudaStream_t> saved;
+    const gg_stack_step_t* steps;
+    int count;
+    ~Guard() {
+      for (int k = 0; k < static_cast<int>(saved.size()); ++k) steps[k].stack->stream = saved[k];
+      if (g) stacks_graph_free(g);
+    }
+  } guard{g, {}, steps, count};
+  g->device = first->device;
+  g->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : first->stream;
+  for (int k = 0; k < count; ++k) {
+    const gg_stack_step_t& st = steps[k];
+    std::vector<int64_t> idx;
+    std::vector<double> mats;
+    for (int64_t f = 0; f < st.stack->frames; ++f) {
+      const double* m = st.host_matrices + 9 * f;
+      const bool identity = m[0] == 1.0 && m[1] == 0.0 && m[2] == 0.0 && m[3] == 0.0 && m[4] == 1.0 &&
+                            m[5] == 0.0 && m[6] == 0.0 && m[7] == 0.0 && m[8] == 1.0;
+      if (identity) continue;
+      idx.push_back(f);
+      mats.insert(mats.end(), m, m + 9);
+    }
+    // the frames must hold data for the descriptor checks; the warm-up
+    // calibration below loads them, so calibrate first
+    guard.saved.push_back(st.stack->stream);
+    st.stack->stream = g->stream;
+    std::vector<int64_t> all(static_cast<size_t>(st.stack->frames));
+    for (int64_t f = 0; f < st.stack->frames; ++f) all[static_cast<size_t>(f)] = f;
+    const int rc = gg_stack_calibrate_u16_device(st.stack, all.data(), st.stack->frames, st.dev_raw, 0, &st.calib);
+    if (rc != GG_OK) fail(rc, "stacks graph: calibration failed");
+    g->items.push_back(idx.empty() ? nullptr : warp_items_device(st.stack, idx.data(), static_cast<int64_t>(idx.size()),
+                                                                  mats.data()));
+    g->warped.push_back(static_cast<int64_t>(idx.size()));
+  }
+  // one eager pass sizes every lazily allocated buffer and settles the
+  // autotuner, so the capture records launches and stream-ordered copies only
+  for (int k = 0; k < count; ++k) run_stack_step(steps[k], g->items[k], g->warped[k]);
+  check_cuda(cudaStreamSynchronize(g->stream), "cudaStreamSynchronize(stacks graph warm-up)");
+  const int64_t before = gg::launch_count();
+  check_cuda(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
+  try {
+    for (int k = 0; k < count; ++k) run_stack_step(steps[k], g->items[k], g->warped[k]);
+  } catch (...) {
+    cudaGraph_t broken = nullptr;
+    cudaStreamEndCapture(g->stream, &broken);
+    if (broken) cudaGraphDestroy(broken);
+    note_launch(static_cast<int>(before - gg::launch_count()));
+    throw;
+  }
+  check_cuda(cudaStreamEndCapture(g->stream, &g->graph), "cudaStreamEndCapture");
+  g->kernels = static_cast<int>(gg::launch_count() - before);
+  note_launch(-g->kernels);  // recorded, not executed
+  check_cuda(cudaGraphInstantiate(&g->exec, g->graph, 0), "cudaGraphInstantiate");
+  *out = g;
+  g = nullptr;  // owned by the caller now
+  GG_API_END
+}
+
+extern "C" int gg_stacks_graph_launch(gg_stacks_graph* g) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(g != nullptr && g->exec != nullptr, "null graph");
+  check_cuda(cudaSetDevice(g->device), "cudaSetDevice");
+  check_cuda(cudaGraphLaunch(g->exec, g->stream), "cudaGraphLaunch");
+  note_launch(g->kernels);
+  GG_API_END
+}
+
+extern "C" int gg_stacks_graph_kernel_count(gg_stacks_graph* g, int32_t* out) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(g != nullptr && out != nullptr, "null argument");
+  *out = g->kernels;
+  GG_API_END
+}
+
+extern "C" int gg_stacks_graph_destroy(gg_stacks_graph* g) {
+  using namespace gg;
+  GG_API_BEGIN
+  if (g) {
+    check_cuda(cudaSetDevice(g->device), "cudaSetDevice");
+    stacks_graph_free(g);
+  }
+  GG_API_END
+}
+
 extern "C" int gg_stack_graph_launch(gg_stack* s) {
   using namespace gg;
   GG_API_BEGIN

@@ -45,8 +45,10 @@ constexpr float kPiF = 3.14159265358979323846f;
 // 3/2 (k = -1, 2) and 5/2 (k = -2, 3); each pair is E_c(u) +- O_c(u) with
 // E_c even and O_c odd, evaluated as degree-5 polynomials in u^2 (fit error
 // below 3e-10, coefficients from glass_gb300/lanczos_poly.py), so the six
-// weights cost 36 FMAs and no transcendental or division.  t == 0 (an exact
-// integer source coordinate) gives the exact weights 0, 0, 1, 0, 0, 0.
+// weights cost 36 FMAs and no transcendental or division.  Each weight is
+// within 1.3e-7 of the exact value (float32 rounding included); callers
+// that need the exact weights 0, 0, 1, 0, 0, 0 of an integer coordinate
+// (exact integer translations) take the source sample directly.
 // pair A (c = 0.5): max fit error 7.3e-11
 __device__ __forceinline__ float l3_even_a(float x) {
   float p = 1.680220594e-03f;
@@ -105,13 +107,12 @@ __device__ __forceinline__ void lanczos3_weights(float t, float (&w)[6]) {
   const float ea = l3_even_a(x), oa = __fmul_rn(u, l3_odd_a(x));
   const float eb = l3_even_b(x), ob = __fmul_rn(u, l3_odd_b(x));
   const float ec = l3_even_c(x), oc = __fmul_rn(u, l3_odd_c(x));
-  const bool exact = t == 0.0f;
-  w[0] = exact ? 0.0f : __fadd_rn(ec, oc);
-  w[1] = exact ? 0.0f : __fadd_rn(eb, ob);
-  w[2] = exact ? 1.0f : __fadd_rn(ea, oa);
-  w[3] = exact ? 0.0f : __fsub_rn(ea, oa);
-  w[4] = exact ? 0.0f : __fsub_rn(eb, ob);
-  w[5] = exact ? 0.0f : __fsub_rn(ec, oc);
+  w[0] = __fadd_rn(ec, oc);
+  w[1] = __fadd_rn(eb, ob);
+  w[2] = __fadd_rn(ea, oa);
+  w[3] = __fsub_rn(ea, oa);
+  w[4] = __fsub_rn(eb, ob);
+  w[5] = __fsub_rn(ec, oc);
 }
 
 // Lanczos3 weights with relative (not only absolute) accuracy, for the

@@ -47,7 +47,8 @@ struct WarpItem {
   int dst_slot;     // filled on the device
   unsigned src_nonfinite;
   int affine;
-  int pad[3];
+  int int_shift;  // inverse is an exact integer translation
+  int pad[2];
   float m[9][2];  // inverse matrix, float-float (hi, lo), row-major
 };
 
@@ -128,10 +129,14 @@ __device__ __forceinline__ Coef load_coef(const WarpItem* p) {
 
 // Tile plan: box origin for the source footprint of output tile (tx, ty).
 struct TilePlan {
-  int bx, by, fits;
+  int bx, by, fits, interior;
 };
 
-__device__ __forceinline__ TilePlan plan_tile(const Coef& it, int tile_x, int tile_y, int radius) {
+// interior: an affine map sends the whole tile at least one pixel inside the
+// valid source range (valid_lo <= s <= valid_hi on both axes), so no pixel
+// of the tile needs its own validity test.
+__device__ __forceinline__ TilePlan plan_tile(const Coef& it, int tile_x, int tile_y, int radius, float valid_lo,
+                                              float valid_hi_x, float valid_hi_y) {
   const float x0 = static_cast<float>(tile_x * kTileW), y0 = static_cast<float>(tile_y * kTileH);
   const float cx[4] = {x0, x0 + kTileW - 1, x0, x0 + kTileW - 1};
   const float cy[4] = {y0, y0, y0 + kTileH - 1, y0 + kTileH - 1};
@@ -146,7 +151,7 @@ __device__ __forceinline__ TilePlan plan_tile(const Coef& it, int tile_x, int ti
     miny = fminf(miny, sy.hi);
     maxy = fmaxf(maxy, sy.hi);
   }
-  TilePlan p{0, 0, 0};
+  TilePlan p{0, 0, 0, 0};
   if (!ok || !(maxx - minx < 1.0e6f) || !(maxy - miny < 1.0e6f) || fabsf(minx) > 1.0e8f || fabsf(miny) > 1.0e8f)
     return p;
   // taps span [floor(s) - (radius-1), floor(s) + radius]; one pixel of margin.
@@ -157,6 +162,8 @@ __device__ __forceinline__ TilePlan plan_tile(const Coef& it, int tile_x, int ti
   p.bx = lo_x >= 0 ? (lo_x & ~3) : -((-lo_x + 3) & ~3);  // 16-byte aligned x (TMA rule)
   p.by = lo_y;
   p.fits = (hi_x - p.bx < kBoxW) && (hi_y - p.by < kBoxH);
+  p.interior = it.affine && minx >= valid_lo + 1.0f && maxx <= valid_hi_x - 1.0f && miny >= valid_lo + 1.0f &&
+               maxy <= valid_hi_y - 1.0f;
   return p;
 }
 
@@ -165,7 +172,7 @@ __global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __gri
                                                                   WarpArgs a) {
   __shared__ alignas(128) float tile[2][kBoxH * kBoxW];
   __shared__ alignas(8) uint64_t bar[2];
-  __shared__ int s_bx[2], s_by[2], s_fit[2];
+  __shared__ int s_bx[2], s_by[2], s_fit[2], s_interior[2];
   __shared__ int s_abort;
   constexpr int radius = (INTERP == GG_INTERP_LANCZOS3) ? 3 : 1;
   const int tid = threadIdx.x;
@@ -184,8 +191,13 @@ __global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __gri
     // thread 0 only
     const WarpItem* ip = a.items + item / tiles;
     const int t = item % tiles;
-    TilePlan p = plan_tile(load_coef(ip), t % a.tiles_x, t / a.tiles_x, radius);
+    // validity ranges: bilinear 0 <= s <= W - 1; Lanczos3 2 <= s < W - 3
+    const float vlo = INTERP == GG_INTERP_LANCZOS3 ? 2.0f : 0.0f;
+    const float vhx = static_cast<float>(a.width) - (INTERP == GG_INTERP_LANCZOS3 ? 3.0f : 1.0f);
+    const float vhy = static_cast<float>(a.height) - (INTERP == GG_INTERP_LANCZOS3 ? 3.0f : 1.0f);
+    TilePlan p = plan_tile(load_coef(ip), t % a.tiles_x, t / a.tiles_x, radius, vlo, vhx, vhy);
     if (!USE_TMA) p.fits = 0;
+    s_interior[buf] = p.interior;
     s_bx[buf] = p.bx;
     s_by[buf] = p.by;
     s_fit[buf] = p.fits;
@@ -213,6 +225,8 @@ __global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __gri
     const int t = item % tiles;
     const int tile_x = t % a.tiles_x, tile_y = t / a.tiles_x;
     const bool fit = s_fit[buf] != 0;
+    const bool interior = s_interior[buf] != 0;
+    const bool int_shift = __ldg(&ip->int_shift) != 0;
     if (fit) {
       // Bounded wait: on expiry flag the error, give the copy one more
       // bounded wait to land, finish this item (its output is discarded by
@@ -260,7 +274,9 @@ __global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __gri
           FFv sx = sx_row, sy = sy_row;
           if (co.affine ? row_ok : source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx, sy)) {
             const float W = static_cast<float>(a.width), H = static_cast<float>(a.height);
-            if (INTERP != GG_INTERP_LANCZOS3)
+            if (interior)
+              valid = true;
+            else if (INTERP != GG_INTERP_LANCZOS3)
               valid = ff_ge(sx, 0.0f) && ff_le(sx, W - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, H - 1.0f);
             else
               valid = ff_ge(sx, 2.0f) && ff_lt(sx, W - 3.0f) && ff_ge(sy, 2.0f) && ff_lt(sy, H - 3.0f);
@@ -275,14 +291,24 @@ __global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __gri
                 if (ty > 0.5f || (ty == 0.5f && (y0 & 1))) ++y0;
               }
               TapSource src = ts;
-              // Any tap outside the staged box reads global memory instead.
-              if (src.tile && (x0 - (radius - 1) < src.bx || x0 + radius >= src.bx + kBoxW ||
-                               y0 - (radius - 1) < src.by || y0 + radius >= src.by + kBoxH))
+              // Any tap outside the staged box reads global memory instead
+              // (an affine tile that fits the box keeps every tap inside it).
+              if (src.tile && !co.affine &&
+                  (x0 - (radius - 1) < src.bx || x0 + radius >= src.bx + kBoxW || y0 - (radius - 1) < src.by ||
+                   y0 + radius >= src.by + kBoxH))
                 src.tile = nullptr;
               if (INTERP == GG_INTERP_NEAREST) {
                 value = src.at(x0, y0);
               } else if (INTERP == GG_INTERP_BILINEAR) {
                 value = sample_bilinear(src, x0, y0, tx, ty, a.width, a.height);
+              } else if (int_shift) {
+                // exact weights 0, 0, 1, 0, 0, 0: the source sample itself, or
+                // no sample when it is not finite (nothing left to normalise)
+                value = src.at(x0, y0);
+                if (!isfinite(value)) {
+                  valid = false;
+                  value = a.fill;
+                }
               } else {
                 valid = sample_lanczos3(src, x0, y0, tx, ty, all_finite, a.clamp, value);
                 if (!valid) value = a.fill;
@@ -405,8 +431,8 @@ static void launch_warp_tiles(gg_stack* s, const WarpArgs& args, bool use_tma) {
   check_cuda(cudaGetLastError(), "warp kernel launch");
 }
 
-void warp_frames(gg_stack* s, const int64_t* indices, int64_t count, const double* fwd, int interp, float fill,
-                 float clamp, bool track_coverage) {
+// Host descriptors of a warp batch (validated; inverse coefficients).
+static std::vector<WarpItem> warp_items_host(gg_stack* s, const int64_t* indices, int64_t count, const double* fwd) {
   std::vector<WarpItem> items(static_cast<size_t>(count));
   for (int64_t k = 0; k < count; ++k) {
     stack_require_loaded(s, indices[k], "warp");
@@ -419,17 +445,23 @@ void warp_frames(gg_stack* s, const int64_t* indices, int64_t count, const doubl
     std::memset(&it, 0, sizeof(it));
     it.frame = static_cast<int>(indices[k]);
     if (!inverse_coefficients(m, it.m, it.affine)) fail(GG_ERR_INVALID_ARGUMENT, "warp matrix is singular");
+    // an exact integer translation (identity linear part, integer shifts):
+    // its inverse is one too and every source coordinate is an integer
+    it.int_shift = (m[0] == 1.0 && m[1] == 0.0 && m[3] == 0.0 && m[4] == 1.0 && m[6] == 0.0 && m[7] == 0.0 &&
+                    m[8] == 1.0 && m[2] == std::floor(m[2]) && m[5] == std::floor(m[5]) && std::fabs(m[2]) < 1.0e7 &&
+                    std::fabs(m[5]) < 1.0e7)
+                       ? 1
+                       : 0;
   }
-  ensure_warp_items(s, std::max<int64_t>(count, s->spares));
-  if (track_coverage) ensure_warp_coverage(s);
-  // The staging buffer may still feed the previous call's copy.
-  check_cuda(cudaEventSynchronize(s->warp_items_free), "cudaEventSynchronize(warp items)");
-  std::memcpy(s->h_warp_items, items.data(), sizeof(WarpItem) * items.size());
-  check_cuda(cudaMemcpyAsync(s->d_warp_items, s->h_warp_items, sizeof(WarpItem) * items.size(),
-                             cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(warp items)");
-  check_cuda(cudaEventRecord(s->warp_items_free, s->stream), "cudaEventRecord(warp items)");
-  auto* d_items = static_cast<WarpItem*>(s->d_warp_items);
+  return items;
+}
+
+// The kernels of a warp batch whose descriptors are already in device
+// memory (d_items, `count` of them): per group of at most `spares` frames,
+// resolve slots, warp into the spare slots, swap the slot table.  Only
+// launches on the stack's stream (safe inside a stream capture).
+static void launch_warp_items(gg_stack* s, WarpItem* d_items, int64_t count, int interp, float fill, float clamp,
+                              bool track_coverage) {
   const bool use_tma = s->has_slot_tmap;
   for (int64_t k0 = 0; k0 < count; k0 += s->spares) {
     const int nb = static_cast<int>(std::min<int64_t>(s->spares, count - k0));
@@ -465,7 +497,41 @@ void warp_frames(gg_stack* s, const int64_t* indices, int64_t count, const doubl
                                                                 s->d_spare_slot);
     check_cuda(cudaGetLastError(), "warp_finish launch");
   }
+}
+
+void warp_frames(gg_stack* s, const int64_t* indices, int64_t count, const double* fwd, int interp, float fill,
+                 float clamp, bool track_coverage) {
+  const std::vector<WarpItem> items = warp_items_host(s, indices, count, fwd);
+  ensure_warp_items(s, std::max<int64_t>(count, s->spares));
+  if (track_coverage) ensure_warp_coverage(s);
+  // The staging buffer may still feed the previous call's copy.
+  check_cuda(cudaEventSynchronize(s->warp_items_free), "cudaEventSynchronize(warp items)");
+  std::memcpy(s->h_warp_items, items.data(), sizeof(WarpItem) * items.size());
+  check_cuda(cudaMemcpyAsync(s->d_warp_items, s->h_warp_items, sizeof(WarpItem) * items.size(),
+                             cudaMemcpyHostToDevice, s->stream),
+             "cudaMemcpyAsync(warp items)");
+  check_cuda(cudaEventRecord(s->warp_items_free, s->stream), "cudaEventRecord(warp items)");
+  launch_warp_items(s, static_cast<WarpItem*>(s->d_warp_items), count, interp, fill, clamp, track_coverage);
   if (track_coverage) s->warp_coverage_frames += count;
+}
+
+// Warp descriptors in a caller-owned device buffer (for captured graphs):
+// returns the device pointer (cudaMalloc, the caller frees it with cudaFree)
+// and their count through `count_out`.
+void* warp_items_device(gg_stack* s, const int64_t* indices, int64_t count, const double* fwd) {
+  const std::vector<WarpItem> items = warp_items_host(s, indices, count, fwd);
+  void* d = nullptr;
+  check_cuda(cudaMalloc(&d, sizeof(WarpItem) * items.size()), "cudaMalloc(graph warp items)");
+  const cudaError_t err = cudaMemcpy(d, items.data(), sizeof(WarpItem) * items.size(), cudaMemcpyHostToDevice);
+  if (err != cudaSuccess) {
+    cudaFree(d);
+    check_cuda(err, "cudaMemcpy(graph warp items)");
+  }
+  return d;
+}
+
+void launch_warp_items_device(gg_stack* s, void* d_items, int64_t count, int interp, float fill, float clamp) {
+  launch_warp_items(s, static_cast<WarpItem*>(d_items), count, interp, fill, clamp, false);
 }
 
 }  // namespace gg

@@ -316,6 +316,33 @@ int gg_autotune_entry(int32_t index, char* kernel, size_t kernel_len, char* shap
                       size_t choice_len, float* best_ms, int32_t* candidates);
 int gg_stack_graph_kernel_count(gg_stack* stack, int* out);
 int gg_stack_graph_destroy(gg_stack* stack);
+
+/* Several stacks in one CUDA graph (batched uneven stacks; no counterpart in
+ * the reference).  Each step names a stack, its uint16 frames in device
+ * memory (frame_count frames, frame-major), its forward matrices (moving ->
+ * reference, frame_count row-major 3x3 float64; identity matrices are not
+ * warped), interpolation, weighting, calibration and integration parameters.
+ * The capture runs every step once eagerly (buffers, autotuner), then records
+ * calibrate -> weights -> warp -> rejection + integration of every stack, in
+ * order, on cuda_stream (NULL: the first stack's stream); a launch replays
+ * them all.  The graph owns the warp descriptors; it uses each stack's
+ * frames, weights and maps, which later calls may read or overwrite between
+ * replays.  Destroy the graph before its stacks. */
+typedef struct gg_stacks_graph gg_stacks_graph;
+typedef struct {
+  gg_stack* stack;
+  const void* dev_raw;
+  const double* host_matrices;
+  int32_t interpolation;        /* GG_INTERP_BILINEAR or GG_INTERP_LANCZOS3 */
+  float clamping_threshold;     /* < 0: no clamp */
+  int32_t weighting;            /* GG_WEIGHTS_PRIOR (unit) or GG_WEIGHTS_SIMPLE_SNR */
+  gg_calib_params_t calib;
+  gg_integrate_params_t integrate;
+} gg_stack_step_t;
+int gg_stacks_graph_capture(const gg_stack_step_t* steps, int32_t count, void* cuda_stream, gg_stacks_graph** out);
+int gg_stacks_graph_launch(gg_stacks_graph* graph);
+int gg_stacks_graph_kernel_count(gg_stacks_graph* graph, int32_t* out);
+int gg_stacks_graph_destroy(gg_stacks_graph* graph);
 /* Downloads the maps of the last integration; any pointer may be NULL.  Count
  * maps are float32 or uint16 per the count_dtype used. */
 int gg_stack_download_maps(gg_stack* stack, float* host_master, float* host_weight, void* host_coverage,

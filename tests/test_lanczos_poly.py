@@ -1,7 +1,7 @@
 """The Lanczos3 tap-weight polynomials of csrc/sampling.cuh: the table in the
 header is the one glass_gb300/lanczos_poly.py fits, and evaluated in float32
 as the kernel does (Horner with fused multiply-adds, pairs E +- O) it stays
-within 1.5e-7 of sinc(d) sinc(d/3) in float64 and sums to the exact weight
+within 1.5e-7 of sinc(d) sinc(d/3) in float64 (t = 0 included) and sums to the exact weight
 sum within 5e-7 over t in [0, 1)."""
 
 from __future__ import annotations
@@ -59,8 +59,6 @@ def test_float32_weights_match_lanczos3():
         eb, ob = poly(table["EB"]), f32(u * poly(table["OB"]))
         ec, oc = poly(table["EC"]), f32(u * poly(table["OC"]))
         w = [f32(ec + oc), f32(eb + ob), f32(ea + oa), f32(ea - oa), f32(eb - ob), f32(ec - oc)]
-        if t == 0.0:
-            w = [0.0, 0.0, 1.0, 0.0, 0.0, 0.0]
         exact = lanczos3(float(t) - np.arange(-2, 4, dtype=np.float64))
         worst = max(worst, float(np.abs(np.asarray(w, np.float64) - exact).max()))
         worst_sum = max(worst_sum, abs(float(np.sum(np.asarray(w, np.float64))) - float(exact.sum())))
