@@ -787,7 +787,7 @@ def c3_side_report(local: int, frames: int = 64, size: int = 4096) -> dict:
     linear terms, +-0.5 px shifts): the catalog-matching start (triangle
     similarity, the plain registration) against three refinements on the same
     GPU and frames - the NCC translation grid (the reference's), the device
-    Gauss-Newton (affine model) and L-BFGS on the masked NCC of the star
+    Gauss-Newton (affine model, 20 steps at most) and L-BFGS on the masked NCC of the star
     regions with every gradient from the hand-written warp adjoint behind
     torch.autograd (20 evaluations at most) - as RMS distance to the true
     maps (px) and wall time."""
@@ -833,7 +833,7 @@ def c3_side_report(local: int, frames: int = 64, size: int = 4096) -> dict:
         ncc, t = timed(lambda: pipe.refine(tri, 0))
         out["ncc_translation_grid"] = {"rms_px": rms(ncc), "s": t}
         pipe.config.refine_method = "gradient"
-        pipe.config.gradient_refine = {"model": "affine"}
+        pipe.config.gradient_refine = {"model": "affine", "iterations": 20}
         gn, t = timed(lambda: pipe.refine(tri, 0))
         out["device_gauss_newton_affine"] = {"rms_px": rms(gn), "s": t}
         ref = pipe.stack.frame_tensor(0)

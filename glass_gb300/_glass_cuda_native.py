@@ -1139,30 +1139,33 @@ class ResidentCalibratedStack:
                "affine": _lib.GG_TRANSFORM_AFFINE}
     _INTERPS = {"bilinear": _lib.GG_INTERP_BILINEAR, "lanczos3": _lib.GG_INTERP_LANCZOS3}
 
-    def _gradient_params(self, model, interpolation, sample_stride, stats_passes, iterations, min_samples,
-                         clip_sigma, mask_shift_px, tolerance_px, max_step_px) -> _lib.GradientRefineParams:
+    def _gradient_params(self, model, interpolation, sample_stride, row_stride, stats_passes, iterations,
+                         min_samples, clip_sigma, mask_shift_px, tolerance_px, max_step_px) -> _lib.GradientRefineParams:
         if model not in self._MODELS:
             raise ValueError("model must be translation, similarity or affine")
         if interpolation not in self._INTERPS:
             raise ValueError("interpolation must be bilinear or lanczos3")
         return _lib.GradientRefineParams(self._MODELS[model], self._INTERPS[interpolation], int(sample_stride),
-                                         int(stats_passes), int(iterations), int(min_samples), float(clip_sigma),
-                                         float(mask_shift_px), float(tolerance_px), float(max_step_px))
+                                         int(row_stride), int(stats_passes), int(iterations), int(min_samples), 0,
+                                         float(clip_sigma), float(mask_shift_px), float(tolerance_px),
+                                         float(max_step_px))
 
     def refine_matrix_gradient_batch_to_reference(
             self, reference_index: int, moving_indices: Any, matrices: Any, model: str = "similarity",
             interpolation: str = "lanczos3", sample_stride: int = 2, stats_passes: int = 3, iterations: int = 8,
             min_samples: int = 256, clip_sigma: float = 5.0, mask_shift_px: float = 1.0,
-            tolerance_px: float = 1.0e-3, max_step_px: float = 2.0) -> list[dict[str, Any]]:
+            tolerance_px: float = 1.0e-3, max_step_px: float = 2.0, row_stride: int = 0) -> list[dict[str, Any]]:
         """Gauss-Newton refinement of each moving frame's affine matrix against
         the reference frame on the device (masked, photometrically matched
-        sum of squares; the warp adjoint's position derivatives)."""
+        sum of squares; the warp adjoint's position derivatives).  Samples
+        every sample_stride-th column of every row_stride-th row (0: a square
+        grid of sample_stride)."""
         idx = np.ascontiguousarray(np.asarray(moving_indices, dtype=np.int64).reshape(-1))
         if idx.size == 0:
             return []
         mats = self._matrices(matrices, idx.size)
-        params = self._gradient_params(model, interpolation, sample_stride, stats_passes, iterations, min_samples,
-                                       clip_sigma, mask_shift_px, tolerance_px, max_step_px)
+        params = self._gradient_params(model, interpolation, sample_stride, row_stride, stats_passes, iterations,
+                                       min_samples, clip_sigma, mask_shift_px, tolerance_px, max_step_px)
         out = (_lib.GradientRefineResult * idx.size)()
         _lib.call("gg_stack_refine_gradient", self._handle, ctypes.c_int64(int(reference_index)), _lib.ptr(idx),
                   ctypes.c_int64(idx.size), _lib.ptr(mats), ctypes.byref(params), out)
@@ -1175,14 +1178,15 @@ class ResidentCalibratedStack:
 
     def gradient_normal_equations(self, reference_index: int, moving_indices: Any, thetas: Any, photometric: Any,
                                   model: str = "similarity", interpolation: str = "lanczos3", sample_stride: int = 2,
-                                  clip_sigma: float = 5.0, mask_shift_px: float = 1.0) -> np.ndarray:
+                                  clip_sigma: float = 5.0, mask_shift_px: float = 1.0,
+                                  row_stride: int = 0) -> np.ndarray:
         """One accumulation pass of the gradient refinement -> (n, 48) sums:
         J^T J upper triangle (36), J^T r (8), sum r^2, kept count, 0, 0."""
         idx = np.ascontiguousarray(np.asarray(moving_indices, dtype=np.int64).reshape(-1))
         th = np.ascontiguousarray(np.asarray(thetas, dtype=np.float64).reshape(idx.size, 6))
         ph = np.ascontiguousarray(np.asarray(photometric, dtype=np.float64).reshape(idx.size, 3))
-        params = self._gradient_params(model, interpolation, sample_stride, 1, 1, 16, clip_sigma, mask_shift_px,
-                                       0.0, 1.0)
+        params = self._gradient_params(model, interpolation, sample_stride, row_stride, 1, 1, 16, clip_sigma,
+                                       mask_shift_px, 0.0, 1.0)
         out = np.zeros((idx.size, 48), dtype=np.float64)
         _lib.call("gg_stack_gradient_normal_equations", self._handle, ctypes.c_int64(int(reference_index)),
                   _lib.ptr(idx), ctypes.c_int64(idx.size), _lib.ptr(th), _lib.ptr(ph), ctypes.byref(params),

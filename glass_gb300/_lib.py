@@ -309,9 +309,11 @@ class GradientRefineParams(ctypes.Structure):
         ("transform_model", ctypes.c_int32),
         ("interpolation", ctypes.c_int32),
         ("sample_stride", ctypes.c_int32),
+        ("row_stride", ctypes.c_int32),
         ("stats_passes", ctypes.c_int32),
         ("iterations", ctypes.c_int32),
         ("min_samples", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
         ("clip_sigma", ctypes.c_float),
         ("mask_shift_px", ctypes.c_float),
         ("tolerance_px", ctypes.c_double),

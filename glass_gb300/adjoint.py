@@ -406,16 +406,19 @@ def refine_affine_lbfgs(reference: torch.Tensor, moving: torch.Tensor, matrix, c
         raise ValueError("too few star pixels to refine")
     theta0 = torch.from_numpy(theta_from_matrix(matrix))
     basis = torch.from_numpy(_basis(cfg.model, h, w))
-    refd = torch.where(mask, reference, torch.zeros_like(reference)).double()
+    # the loss reads only the star pixels: gathered once from the reference,
+    # and from each warped frame (whose gradient scatters back to them)
+    star_idx = mask.reshape(-1).nonzero().squeeze(1)
+    ref_stars = reference.reshape(-1)[star_idx].double()
     u = torch.zeros(basis.shape[1], dtype=torch.float64, requires_grad=True)
     history: list[float] = []
 
     def loss_of(uu):
-        warped = warp_fn(moving, theta0 + basis @ uu)
-        m = mask & torch.isfinite(warped)
+        warped = warp_fn(moving, theta0 + basis @ uu).reshape(-1)[star_idx]
+        m = torch.isfinite(warped)
         md = m.double()
         n = md.sum()
-        a = refd * md
+        a = ref_stars * md
         b = torch.where(m, warped, torch.zeros_like(warped)).double()
         am, bm = a.sum() / n, b.sum() / n
         da, db = (a - am) * md, (b - bm) * md

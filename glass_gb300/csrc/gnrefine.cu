@@ -4,8 +4,10 @@
 // affine map theta (reference pixel -> moving pixel) and a photometric match
 // (alpha, beta) minimise the masked sum of squares
 //     sum_p m_p (O_p(theta) - alpha a_p - beta)^2
-// over the reference pixels p on a sample grid (every sample_stride-th row
-// and column), where O_p is the moving frame sampled at theta(p) (bilinear or
+// over the reference pixels p on a sample grid (every row_stride-th row and
+// every sample_stride-th column of it; row_stride 0 means sample_stride, a
+// square grid, and whole rows - sample_stride 1 - keep the loads of a warp
+// contiguous on large frames), where O_p is the moving frame sampled at theta(p) (bilinear or
 // Lanczos3, engine/warp.py:99-152 sampling) and a_p the reference pixel.  The
 // mask m_p drops invalid samples (outside the sampler's valid range or a
 // non-finite tap or reference pixel) and single-frame outliers (cosmic rays,
@@ -121,7 +123,7 @@ struct GnArgs {
   double* sums_out;  // [job][kGnSums] (normal-equation export) or nullptr
   unsigned* hist;    // [job][kGnHistWords] residual magnitude and value histograms, zeroed by the solve
   int width, height;
-  int sample_stride, nsx, nsy;
+  int sample_stride, row_stride, nsx, nsy;
   int blocks_per_job;
   int phase;  // 1, 2: the photometric-start passes (value, ratio histograms)
   float clip_sigma, shift_px;
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__(kGnThreads, K == 8 ? 1 : 3) gn_accumulate_kern
   for (int64_t it = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; it < items;
        it += static_cast<int64_t>(a.blocks_per_job) * blockDim.x) {
     const int iy = static_cast<int>(it / a.nsx), ix = static_cast<int>(it - static_cast<int64_t>(iy) * a.nsx);
-    gn_sample<INTERP, K, UNROLL>(a, s_coef, ref, mov, ix * a.sample_stride, iy * a.sample_stride, alpha, beta,
+    gn_sample<INTERP, K, UNROLL>(a, s_coef, ref, mov, ix * a.sample_stride, iy * a.row_stride, alpha, beta,
                                  clip, sigma, s_hist, s_vhist, s_start, acc);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -571,6 +573,7 @@ static void validate_params(const gg_gradient_refine_params_t& p) {
   require(p.interpolation == GG_INTERP_BILINEAR || p.interpolation == GG_INTERP_LANCZOS3,
           "interpolation must be bilinear or lanczos3");
   require(p.sample_stride >= 1 && p.sample_stride <= 64, "sample_stride must be in [1, 64]");
+  require(p.row_stride >= 0 && p.row_stride <= 4096, "row_stride must be in [0, 4096] (0: sample_stride)");
   require(p.stats_passes >= 1 && p.stats_passes <= 16, "stats_passes must be in [1, 16]");
   require(p.iterations >= 1 && p.iterations <= 100, "iterations must be in [1, 100]");
   require(p.min_samples >= 16, "min_samples must be at least 16");
@@ -578,6 +581,23 @@ static void validate_params(const gg_gradient_refine_params_t& p) {
   require(std::isfinite(p.mask_shift_px) && p.mask_shift_px >= 0.0f, "mask_shift_px must be non-negative");
   require(std::isfinite(p.tolerance_px) && p.tolerance_px >= 0.0, "tolerance_px must be non-negative");
   require(std::isfinite(p.max_step_px) && p.max_step_px > 0.0, "max_step_px must be positive");
+}
+
+// Column and row steps of a sample grid.  The fine grid is the caller's; the
+// photometric and statistics passes use one twice as coarse (both steps of a
+// square grid, the row step of a whole-row grid).
+struct SampleGrid {
+  int cols, rows;
+};
+
+static SampleGrid fine_grid(const gg_gradient_refine_params_t& p) {
+  return {p.sample_stride, p.row_stride > 0 ? p.row_stride : p.sample_stride};
+}
+
+static SampleGrid coarse_grid(const gg_gradient_refine_params_t& p) {
+  if (p.row_stride > 0) return {p.sample_stride, std::min(2 * p.row_stride, 8192)};
+  const int c = std::min(2 * p.sample_stride, 64);
+  return {c, c};
 }
 
 // Shared setup: jobs, start states (theta from forward matrices or given
@@ -589,8 +609,8 @@ struct GnPlan {
 };
 
 static GnPlan gn_prepare(gg_stack* s, int64_t reference_index, const int64_t* moving, int64_t count,
-                         const std::vector<GnState>& states, int interp, int sample_stride, float clip_sigma,
-                         float shift_px) {
+                         const std::vector<GnState>& states, int interp, int sample_stride, int row_stride,
+                         float clip_sigma, float shift_px) {
   stack_require_loaded(s, reference_index, "gradient refinement");
   for (int64_t k = 0; k < count; ++k) stack_require_loaded(s, moving[k], "gradient refinement");
   require(s->pixels <= (int64_t{1} << 31) - 1, "gradient refinement supports frames of fewer than 2^31 pixels");
@@ -599,7 +619,7 @@ static GnPlan gn_prepare(gg_stack* s, int64_t reference_index, const int64_t* mo
   plan.jobs = static_cast<int>(count);
   plan.interp = interp;
   const int64_t nsx = (s->width + sample_stride - 1) / sample_stride;
-  const int64_t nsy = (s->height + sample_stride - 1) / sample_stride;
+  const int64_t nsy = (s->height + row_stride - 1) / row_stride;
   // partial sums for up to two waves of 8 resident CTAs per SM
   const int bpj = std::max(1, (2 * 8 * sm_count() + plan.jobs - 1) / plan.jobs);
   GnScratch& g = gn_scratch(s, plan.jobs, bpj);
@@ -624,6 +644,7 @@ static GnPlan gn_prepare(gg_stack* s, int64_t reference_index, const int64_t* mo
   a.width = static_cast<int>(s->width);
   a.height = static_cast<int>(s->height);
   a.sample_stride = sample_stride;
+  a.row_stride = row_stride;
   a.nsx = static_cast<int>(nsx);
   a.nsy = static_cast<int>(nsy);
   a.blocks_per_job = bpj;
@@ -678,12 +699,13 @@ static int gn_blocks_per_job(GnKernelFn fn, int jobs, int64_t samples, int cap) 
 // One pass over the samples: K = 0 statistics, else the model's projected
 // columns (see GnLayout).  Lanczos3 passes tune row-by-row against
 // whole-window tap loads per shape.
-static void gn_accumulate(gg_stack* s, GnPlan& plan, int sample_stride, int K, int phase = 0) {
+static void gn_accumulate(gg_stack* s, GnPlan& plan, SampleGrid grid_step, int K, int phase = 0) {
   GnArgs a = plan.args;
-  a.sample_stride = sample_stride;
+  a.sample_stride = grid_step.cols;
+  a.row_stride = grid_step.rows;
   a.phase = phase;
-  a.nsx = static_cast<int>((s->width + sample_stride - 1) / sample_stride);
-  a.nsy = static_cast<int>((s->height + sample_stride - 1) / sample_stride);
+  a.nsx = static_cast<int>((s->width + grid_step.cols - 1) / grid_step.cols);
+  a.nsy = static_cast<int>((s->height + grid_step.rows - 1) / grid_step.rows);
   const int64_t samples = static_cast<int64_t>(a.nsx) * a.nsy;
   GnScratch& g = *static_cast<GnScratch*>(s->gn_scratch);
   auto run = [&](int variant) {
@@ -743,23 +765,24 @@ int gg_stack_refine_gradient(gg_stack* s, int64_t reference_index, const int64_t
     st.beta = 0.0;
     st.sigma = std::numeric_limits<double>::infinity();
   }
-  GnPlan plan = gn_prepare(s, reference_index, moving, count, states, p.interpolation, p.sample_stride,
+  const SampleGrid fine = fine_grid(p), coarse = coarse_grid(p);
+  GnPlan plan = gn_prepare(s, reference_index, moving, count, states, p.interpolation, fine.cols, fine.rows,
                            p.clip_sigma, p.mask_shift_px);
   const int model_k = p.transform_model == GG_TRANSFORM_TRANSLATION ? 4
                       : p.transform_model == GG_TRANSFORM_SIMILARITY ? 6
                                                                       : 8;
   // photometric start (alpha, beta), then statistics passes (offset and
-  // noise), all on a grid twice as coarse
-  gn_accumulate(s, plan, std::min(2 * p.sample_stride, 64), 0, 1);
+  // noise), all on the coarse grid
+  gn_accumulate(s, plan, coarse, 0, 1);
   gn_solve(s, plan, 3, p.transform_model, p.min_samples, p.tolerance_px, p.max_step_px, 0);
-  gn_accumulate(s, plan, std::min(2 * p.sample_stride, 64), 0, 2);
+  gn_accumulate(s, plan, coarse, 0, 2);
   gn_solve(s, plan, 4, p.transform_model, p.min_samples, p.tolerance_px, p.max_step_px, 0);
   for (int k = 0; k < p.stats_passes; ++k) {
-    gn_accumulate(s, plan, std::min(2 * p.sample_stride, 64), 0);
+    gn_accumulate(s, plan, coarse, 0);
     gn_solve(s, plan, 0, p.transform_model, p.min_samples, p.tolerance_px, p.max_step_px, 0);
   }
   for (int k = 0; k < p.iterations; ++k) {
-    gn_accumulate(s, plan, p.sample_stride, model_k);
+    gn_accumulate(s, plan, fine, model_k);
     gn_solve(s, plan, 1, p.transform_model, p.min_samples, p.tolerance_px, p.max_step_px,
              k == p.iterations - 1 ? 1 : 0);
   }
@@ -818,9 +841,10 @@ int gg_stack_gradient_normal_equations(gg_stack* s, int64_t reference_index, con
     require(std::isfinite(st.alpha) && std::isfinite(st.beta) && !(st.sigma < 0.0),
             "alpha and beta must be finite and sigma non-negative");
   }
-  GnPlan plan = gn_prepare(s, reference_index, moving, count, states, params->interpolation,
-                           params->sample_stride, params->clip_sigma, params->mask_shift_px);
-  gn_accumulate(s, plan, params->sample_stride, 8);
+  const SampleGrid fine = fine_grid(*params);
+  GnPlan plan = gn_prepare(s, reference_index, moving, count, states, params->interpolation, fine.cols, fine.rows,
+                           params->clip_sigma, params->mask_shift_px);
+  gn_accumulate(s, plan, fine, 8);
   gn_solve(s, plan, 2, params->transform_model, params->min_samples, 0.0, 1.0, 0);
   GnScratch& g = *static_cast<GnScratch*>(s->gn_scratch);
   check_cuda(cudaMemcpyAsync(host_sums, g.sums, sizeof(double) * kGnSums * count, cudaMemcpyDeviceToHost, s->stream),

@@ -349,18 +349,27 @@ __global__ void __launch_bounds__(256) bracket_pass_kernel(BracketArgs a) {
       }
     }
   };
-  // every lane of a warp runs the same trip count (the ballot needs them all)
+  // every lane of a warp runs the same trip count (the ballot needs them
+  // all); four float4 loads per thread are issued before any is visited
+  constexpr int kLoads = 4;
   const int64_t n4 = a.pixels / 4;
   const float4* src4 = reinterpret_cast<const float4*>(src);
-  const int64_t gstride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t base = blockIdx.x * int64_t(blockDim.x); base < n4; base += gstride) {
-    const int64_t i = base + threadIdx.x;
-    const bool present = i < n4;
-    const float4 q = present ? __ldg(src4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-    visit(q.x, present);
-    visit(q.y, present);
-    visit(q.z, present);
-    visit(q.w, present);
+  const int64_t gstride = int64_t(gridDim.x) * blockDim.x * kLoads;
+  for (int64_t base = blockIdx.x * int64_t(blockDim.x) * kLoads; base < n4; base += gstride) {
+    float4 q[kLoads];
+#pragma unroll
+    for (int u = 0; u < kLoads; ++u) {
+      const int64_t i = base + u * int64_t(blockDim.x) + threadIdx.x;
+      q[u] = i < n4 ? __ldg(src4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kLoads; ++u) {
+      const bool present = base + u * int64_t(blockDim.x) + threadIdx.x < n4;
+      visit(q[u].x, present);
+      visit(q[u].y, present);
+      visit(q[u].z, present);
+      visit(q[u].w, present);
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x < 32) {
     for (int64_t p = n4 * 4 + threadIdx.x; p - threadIdx.x < a.pixels; p += 32) {
@@ -610,48 +619,62 @@ __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
   const int W = a.width, H = a.height;
   unsigned* out = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
   // rows are dealt to blocks, columns to the block's threads (coalesced, no
-  // division); every thread of a row pass runs the same trip count, so the
-  // warp ballot below always sees the full warp
+  // division), kPer columns per thread and pass with their loads issued
+  // first; every thread of a row pass runs the same trip count, so the warp
+  // ballot below always sees the full warp
+  constexpr int kPer = 4;
   const int cols = W - 2;
-  const int passes = (cols + static_cast<int>(blockDim.x) - 1) / static_cast<int>(blockDim.x);
+  const int span = static_cast<int>(blockDim.x) * kPer;
+  const int passes = (cols + span - 1) / span;
+  const int lane = threadIdx.x & 31;
   for (int y = 1 + static_cast<int>(blockIdx.x); y < H - 1; y += static_cast<int>(gridDim.x)) {
-   for (int pass = 0; pass < passes; ++pass) {
-    const int x = 1 + pass * static_cast<int>(blockDim.x) + static_cast<int>(threadIdx.x);
-    bool hit = false;
-    const int64_t idx = static_cast<int64_t>(y) * W + x;
-    if (x <= cols) {
-      const float c = __ldg(img + idx);
-      bool above;
-      if (a.mesh.bg) {
-        double bg, nz;
-        mesh_at(a.mesh, k, x, y, bg, nz);
-        const double nzc = (nz >= 1.0e-6 || isnan(nz)) ? nz : 1.0e-6;  // np.maximum keeps NaN
-        above = static_cast<double>(c) > __dadd_rn(bg, __dmul_rn(a.k_sigma, nzc));
-      } else {
-        above = c > thr;
+    const float* row = img + static_cast<int64_t>(y) * W;
+    for (int pass = 0; pass < passes; ++pass) {
+      const int x0 = 1 + pass * span + static_cast<int>(threadIdx.x);
+      float c[kPer];
+#pragma unroll
+      for (int u = 0; u < kPer; ++u) {
+        const int x = x0 + u * static_cast<int>(blockDim.x);
+        c[u] = x <= cols ? __ldg(row + x) : 0.0f;
       }
-      if (isfinite(c) && above) {
-        hit = true;
 #pragma unroll
-        for (int dy = -1; dy <= 1; ++dy)
+      for (int u = 0; u < kPer; ++u) {
+        const int x = x0 + u * static_cast<int>(blockDim.x);
+        bool hit = false;
+        if (x <= cols) {
+          bool above;
+          if (a.mesh.bg) {
+            double bg, nz;
+            mesh_at(a.mesh, k, x, y, bg, nz);
+            const double nzc = (nz >= 1.0e-6 || isnan(nz)) ? nz : 1.0e-6;  // np.maximum keeps NaN
+            above = static_cast<double>(c[u]) > __dadd_rn(bg, __dmul_rn(a.k_sigma, nzc));
+          } else {
+            above = c[u] > thr;
+          }
+          if (isfinite(c[u]) && above) {
+            hit = true;
+            const float* p = row + x;
 #pragma unroll
-          for (int dx = -1; dx <= 1; ++dx)
-            if (dx || dy) hit &= (c >= __ldg(img + idx + static_cast<int64_t>(dy) * W + dx));
+            for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+              for (int dx = -1; dx <= 1; ++dx)
+                if (dx || dy) hit &= (c[u] >= __ldg(p + static_cast<int64_t>(dy) * W + dx));
+          }
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, hit);
+        if (mask) {
+          const int leader = __ffs(mask) - 1;
+          unsigned base = 0;
+          if (lane == leader) base = atomicAdd(&a.state[k].candidates, static_cast<unsigned>(__popc(mask)));
+          base = __shfl_sync(0xffffffffu, base, leader);
+          if (hit) {
+            const unsigned pos = base + __popc(mask & ((1u << lane) - 1u));
+            if (pos < static_cast<unsigned>(kMaxCandidates))
+              out[pos] = static_cast<unsigned>(static_cast<int64_t>(y) * W + x);
+          }
+        }
       }
     }
-    const unsigned mask = __ballot_sync(0xffffffffu, hit);
-    if (mask) {
-      const int lane = threadIdx.x & 31;
-      const int leader = __ffs(mask) - 1;
-      unsigned base = 0;
-      if (lane == leader) base = atomicAdd(&a.state[k].candidates, static_cast<unsigned>(__popc(mask)));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (hit) {
-        const unsigned pos = base + __popc(mask & ((1u << lane) - 1u));
-        if (pos < static_cast<unsigned>(kMaxCandidates)) out[pos] = static_cast<unsigned>(idx);
-      }
-    }
-   }
   }
 }
 

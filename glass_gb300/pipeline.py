@@ -134,23 +134,29 @@ DEFAULT_AGREEMENT = {"min_score": None, "rms_scale_adu": 200.0, "action": "fail"
 DEFAULT_REFINE = {"search_radius_px": 1.0, "coarse_step_px": 0.25, "fine_radius_px": 0.25, "fine_step_px": 0.0625,
                   "coarse_sample_stride": 4, "final_sample_stride": 8}
 
-# similarity model, Lanczos3 derivatives, every 3rd row and column (or a
-# coarser grid that still samples about target_samples pixels of a large
-# frame), three noise passes on a grid twice as coarse, at most five steps,
-# stop below 1e-3 px
+# similarity model, Lanczos3 derivatives, every 3rd row and column (or, on a
+# frame where that grid would exceed target_samples, whole rows spaced to
+# about target_samples pixels), three noise passes on a grid twice as coarse,
+# at most five steps, stop below 1e-3 px
 DEFAULT_GRADIENT_REFINE = {"model": "similarity", "interpolation": "lanczos3", "sample_stride": 3,
                            "target_samples": 1_000_000, "stats_passes": 3, "iterations": 5, "min_samples": 256,
                            "clip_sigma": 5.0, "mask_shift_px": 1.0, "tolerance_px": 1.0e-3, "max_step_px": 2.0}
 
 
-def gradient_sample_stride(params: dict, height: int, width: int) -> int:
-    """sample_stride, raised so that a frame of height x width is sampled at
-    about params["target_samples"] pixels (None: no limit)."""
+def gradient_sample_grid(params: dict, height: int, width: int) -> tuple[int, int]:
+    """(sample_stride, row_stride) of the gradient refinement on a frame of
+    height x width: the square grid of params["sample_stride"] while it holds
+    at most params["target_samples"] pixels (None: no limit), else whole rows
+    (column step 1) spaced so that about target_samples pixels are sampled.
+    A warp then reads consecutive pixels of a row and its Lanczos windows
+    overlap, where a sparse square grid touches one pixel per 32-byte sector
+    and re-reads nothing."""
     stride = int(params["sample_stride"])
     target = params.get("target_samples")
-    if target:
-        stride = max(stride, int(np.ceil(np.sqrt(height * width / float(target)))))
-    return min(stride, 32)
+    if target and -(-height // stride) * -(-width // stride) > target:
+        rows = int(np.ceil(height * width / float(target)))
+        return 1, int(min(max(rows, 1), 4096))
+    return stride, stride
 
 
 class ResidentPipeline:
@@ -249,7 +255,7 @@ class ResidentPipeline:
             if good.size == 0:
                 return out
             gp = dict(DEFAULT_GRADIENT_REFINE, **(cfg.gradient_refine or {}))
-            gp["sample_stride"] = gradient_sample_stride(gp, self.height, self.width)
+            gp["sample_stride"], gp["row_stride"] = gradient_sample_grid(gp, self.height, self.width)
             gp.pop("target_samples", None)
             res = self.stack.refine_matrix_gradient_batch_to_reference(reference_index, good, out[good], **gp)
             self.last_refinement = [dict(r, frame=int(k)) for k, r in zip(good, res)]

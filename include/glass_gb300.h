@@ -719,10 +719,13 @@ int gg_warp_affine_backward_f32_device(const float* dev_src, int64_t height, int
 typedef struct {
   int32_t transform_model; /* GG_TRANSFORM_TRANSLATION, _SIMILARITY or _AFFINE */
   int32_t interpolation;   /* GG_INTERP_BILINEAR or GG_INTERP_LANCZOS3 */
-  int32_t sample_stride;   /* every stride-th row and column of the reference, 1..64 */
-  int32_t stats_passes;    /* photometric offset / noise passes first (stride x 2), 1..16 */
+  int32_t sample_stride;   /* every stride-th column of the reference, 1..64 */
+  int32_t row_stride;      /* every row_stride-th row, 0..4096; 0: sample_stride (a square grid) */
+  int32_t stats_passes;    /* photometric offset / noise passes first, on a grid twice as coarse
+                              (both steps; the row step alone when row_stride > 0), 1..16 */
   int32_t iterations;      /* Gauss-Newton steps, 1..100 */
   int32_t min_samples;     /* fewer kept samples fail the frame (>= 16) */
+  int32_t reserved;        /* 0 */
   float clip_sigma;
   float mask_shift_px;
   double tolerance_px;     /* converged when a step moves no image corner farther */

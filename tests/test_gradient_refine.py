@@ -34,10 +34,12 @@ def _matrix_of(theta):
     return m
 
 
-def gn_sums_reference(ref, mov, theta, alpha, beta, stride, interp="lanczos3"):
-    """float64 J^T J (upper, 36), J^T r (8), sum r^2, count over all valid samples."""
+def gn_sums_reference(ref, mov, theta, alpha, beta, stride, interp="lanczos3", row_stride=None):
+    """float64 J^T J (upper, 36), J^T r (8), sum r^2, count over all valid
+    samples of the grid (every row_stride-th row, default stride, and every
+    stride-th column)."""
     h, w = ref.shape
-    ys, xs = np.mgrid[0:h:stride, 0:w:stride].astype(np.float64)
+    ys, xs = np.mgrid[0:h:row_stride or stride, 0:w:stride].astype(np.float64)
     sx = theta[0] * xs + theta[1] * ys + theta[2]
     sy = theta[3] * xs + theta[4] * ys + theta[5]
     o, ox, oy = (t.numpy() for t in value_and_position_gradient(torch.tensor(mov, dtype=torch.float64),
@@ -232,6 +234,27 @@ def test_gpu_normal_equations_scaled(native, interp):
 
 
 @pytest.mark.gpu
+def test_gpu_normal_equations_whole_rows(native):
+    """The whole-row grid (every column of every 5th row) sums the same
+    samples as the restatement on that grid."""
+    h, w = 120, 136
+    ref, mov = _pair(2, h, w, _similarity(0.003, 1.0, 2.6, -3.1), gain=1.1, offset=-30.0)
+    theta = _theta_of(_similarity(0.0035, 1.0, 2.9, -3.3))
+    s = _stack(native, [ref, mov])
+    try:
+        got = s.gradient_normal_equations(0, [1], [theta], [(1.05, -20.0, np.inf)], sample_stride=1, row_stride=5)[0]
+    finally:
+        s.close()
+    exp = gn_sums_reference(ref, mov, theta, 1.05, -20.0, 1, row_stride=5)
+    assert got[45] == exp[45]
+    H = np.zeros((8, 8))
+    H[np.triu_indices(8)] = exp[:36]
+    d = np.sqrt(np.diag(H + np.triu(H, 1).T))
+    assert np.all(np.abs(got[:36] - exp[:36]) <= 2e-5 * np.outer(d, d)[np.triu_indices(8)])
+    assert np.all(np.abs(got[36:44] - exp[36:44]) <= 2e-5 * d * np.sqrt(exp[44]))
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("model", ["similarity", "affine"])
 def test_gpu_gradient_refine_recovers_truth(native, model):
     h, w = 256, 288
@@ -252,6 +275,25 @@ def test_gpu_gradient_refine_recovers_truth(native, model):
         assert after < 0.005, (k, before, after, res[k])
     assert abs(res[0]["alpha"] - 0.85) < 0.02
     np.testing.assert_allclose(single[0]["matrix"], res[1]["matrix"], rtol=0, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_gpu_gradient_refine_whole_rows_recovers_truth(native):
+    """Whole rows (every column of every 4th row; the statistics passes on
+    every 8th row) land as close as the square grid."""
+    h, w = 256, 288
+    truth = _similarity(0.004, 1.0, 5.3, -2.2)
+    start = _similarity(0.0052, 1.0, 5.3 + 0.45, -2.2 - 0.35)
+    ref, mov = _pair(4, h, w, truth, gain=0.85, offset=60.0, cosmic=40)
+    s = _stack(native, [ref, mov])
+    try:
+        res = s.refine_matrix_gradient_batch_to_reference(0, [1], start[None], sample_stride=1, row_stride=4)[0]
+    finally:
+        s.close()
+    assert res["ok"], res
+    assert _rms(res["matrix"], truth, h, w) < 0.005, res
+    assert res["samples"] <= (h // 4) * w
+    assert abs(res["alpha"] - 0.85) < 0.02
 
 
 @pytest.mark.gpu
@@ -287,6 +329,10 @@ def test_gpu_gradient_refine_arguments(native):
         with pytest.raises(ValueError):
             s.refine_matrix_gradient_batch_to_reference(0, [1], eye, sample_stride=0)
         with pytest.raises(ValueError):
+            s.refine_matrix_gradient_batch_to_reference(0, [1], eye, row_stride=-1)
+        with pytest.raises(ValueError):
+            s.refine_matrix_gradient_batch_to_reference(0, [1], eye, row_stride=5000)
+        with pytest.raises(ValueError):
             s.refine_matrix_gradient_batch_to_reference(0, [1], np.array([[[1, 0, 0], [0, 1, 0], [1e-3, 0, 1.0]]]))
         with pytest.raises(IndexError):
             s.refine_matrix_gradient_batch_to_reference(0, [5], eye)
@@ -298,13 +344,14 @@ def test_gpu_gradient_refine_arguments(native):
         s.close()
 
 
-def test_gradient_sample_stride_targets_sample_count():
-    from glass_gb300.pipeline import DEFAULT_GRADIENT_REFINE, gradient_sample_stride
+def test_gradient_sample_grid_targets_sample_count():
+    from glass_gb300.pipeline import DEFAULT_GRADIENT_REFINE, gradient_sample_grid
 
     p = dict(DEFAULT_GRADIENT_REFINE)
-    assert gradient_sample_stride(p, 2048, 2048) == 3  # 466k samples: the minimum stride holds
-    assert gradient_sample_stride(p, 6422, 9600) == 8  # c5 frame: about 1e6 samples
-    assert (6422 // 8) * (9600 // 8) < 1.1e6
-    assert gradient_sample_stride(dict(p, target_samples=None), 6422, 9600) == 3
-    assert gradient_sample_stride(dict(p, sample_stride=5), 512, 512) == 5
-    assert gradient_sample_stride(dict(p, target_samples=1), 6422, 9600) == 32
+    assert gradient_sample_grid(p, 2048, 2048) == (3, 3)  # 466k samples: the square grid holds
+    cols, rows = gradient_sample_grid(p, 6422, 9600)  # 9600 x 6422 frame: whole rows
+    assert (cols, rows) == (1, 62)
+    assert 0.9e6 < -(-6422 // rows) * 9600 <= 1.0e6
+    assert gradient_sample_grid(dict(p, target_samples=None), 6422, 9600) == (3, 3)
+    assert gradient_sample_grid(dict(p, sample_stride=5), 512, 512) == (5, 5)
+    assert gradient_sample_grid(dict(p, target_samples=1), 6422, 9600) == (1, 4096)
