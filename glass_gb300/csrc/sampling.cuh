@@ -166,15 +166,29 @@ __device__ __forceinline__ float sample_bilinear(const TapSource& ts, int x0, in
 
 // Non-finite taps present: skip them and renormalise.  Dropping taps can
 // leave a small weight sum (lobes cancel), which amplifies rounding, so the
-// sums are float-float here.  Kept out of line: it is the rare path.
-static __device__ __noinline__ bool lanczos3_nonfinite(const TapSource& ts, int x0, int y0, float tx, float ty,
-                                                       float& value, float& vmin, float& vmax) {
+// sums are float-float here.  Kept out of line: it is the rare path.  Its
+// arguments and result are plain values (registers): a reference argument
+// would make every caller keep the tap source in local memory.
+struct L3Renorm {
+  float value, vmin, vmax;
+  int ok;
+};
+
+static __device__ __noinline__ L3Renorm lanczos3_nonfinite(const float* tile, const float* src, int bx, int by,
+                                                           int width, int x0, int y0, float tx, float ty) {
+  TapSource ts;
+  ts.tile = tile;
+  ts.src = src;
+  ts.bx = bx;
+  ts.by = by;
+  ts.width = width;
   // Dropped taps can leave a small sum, so the weights here carry relative
   // accuracy (the polynomial pairs are accurate to ~1e-7 absolute only).
   float wx[6], wy[6];
   lanczos3_weights_trig(tx, wx);
   lanczos3_weights_trig(ty, wy);
   FF facc, fw;
+  L3Renorm r{0.0f, kInfF, -kInfF, 0};
   for (int j = 0; j < 6; ++j) {
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
@@ -183,21 +197,25 @@ static __device__ __noinline__ bool lanczos3_nonfinite(const TapSource& ts, int 
         const float w = wy[j] * wx[i];
         facc.add_prod(w, v);
         fw.add(w);
-        vmin = fminf(vmin, v);
-        vmax = fmaxf(vmax, v);
+        r.vmin = fminf(r.vmin, v);
+        r.vmax = fmaxf(r.vmax, v);
       }
     }
   }
-  if (!(fabsf(__fadd_rn(fw.hi, fw.lo)) > 1.0e-12f)) return false;
-  value = ff_div_ff(facc.hi, facc.lo, fw.hi, fw.lo);
-  return true;
+  if (!(fabsf(__fadd_rn(fw.hi, fw.lo)) > 1.0e-12f)) return r;
+  r.value = ff_div_ff(facc.hi, facc.lo, fw.hi, fw.lo);
+  r.ok = 1;
+  return r;
 }
 
 // Returns false when the tap weights sum to (almost) zero.  CLAMP = false
-// compiles the window loops without the min/max tracking (clamp < 0).
-template <bool CLAMP>
+// compiles the window loops without the min/max tracking (clamp < 0);
+// FINITE = 1 compiles only the all-finite branch (a frame known to hold no
+// non-finite sample), 0 both, chosen by all_finite.
+template <bool CLAMP, int FINITE = 0>
 __device__ __forceinline__ bool sample_lanczos3_impl(const TapSource& ts, int x0, int y0, float tx, float ty,
                                                      bool all_finite, float clamp, float& out) {
+  if (FINITE) all_finite = true;
   float wx[6], wy[6];
   lanczos3_weights(tx, wx);
   lanczos3_weights(ty, wy);
@@ -244,8 +262,12 @@ __device__ __forceinline__ bool sample_lanczos3_impl(const TapSource& ts, int x0
       }
     }
     wsum = sx * sy;
-  } else {
-    if (!lanczos3_nonfinite(ts, x0, y0, tx, ty, acc, vmin, vmax)) return false;
+  } else if (!FINITE) {
+    const L3Renorm r = lanczos3_nonfinite(ts.tile, ts.src, ts.bx, ts.by, ts.width, x0, y0, tx, ty);
+    if (!r.ok) return false;
+    acc = r.value;
+    vmin = r.vmin;
+    vmax = r.vmax;
     wsum = 1.0f;
   }
   if (!(fabsf(wsum) > 1.0e-12f)) return false;
@@ -265,6 +287,13 @@ __device__ __forceinline__ bool sample_lanczos3(const TapSource& ts, int x0, int
                                                 bool all_finite, float clamp, float& out) {
   return clamp >= 0.0f ? sample_lanczos3_impl<true>(ts, x0, y0, tx, ty, all_finite, clamp, out)
                        : sample_lanczos3_impl<false>(ts, x0, y0, tx, ty, all_finite, clamp, out);
+}
+
+// The same for a source frame known to hold only finite samples.
+__device__ __forceinline__ bool sample_lanczos3_finite(const TapSource& ts, int x0, int y0, float tx, float ty,
+                                                       float clamp, float& out) {
+  return clamp >= 0.0f ? sample_lanczos3_impl<true, 1>(ts, x0, y0, tx, ty, true, clamp, out)
+                       : sample_lanczos3_impl<false, 1>(ts, x0, y0, tx, ty, true, clamp, out);
 }
 
 }  // namespace gg

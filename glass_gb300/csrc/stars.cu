@@ -31,6 +31,8 @@
 #include <cstring>
 #include <vector>
 
+#include <math_constants.h>
+
 #include "stack.cuh"
 
 namespace gg {
@@ -322,59 +324,92 @@ __global__ void __launch_bounds__(1024) bracket_sample_kernel(BracketArgs a) {
   }
 }
 
-__global__ void __launch_bounds__(256) bracket_pass_kernel(BracketArgs a) {
+// One pass over a frame: the finite samples below the band and the band's
+// keys (appended to the frame's band buffer in no particular order).  Each
+// block iteration covers 16 samples per thread (four float4 loads issued
+// first) and reserves the band slots of all its in-band samples with one
+// atomic, so the per-frame counter sees one atomic per 4096 samples.
+constexpr int kBracketThreads = 256;
+
+__global__ void __launch_bounds__(kBracketThreads) bracket_pass_kernel(BracketArgs a) {
+  __shared__ unsigned s_warp[kBracketThreads / 32];
+  __shared__ unsigned s_base;
   const int k = blockIdx.y;
   StarFrameState& st = a.state[k];
   const unsigned lo = st.band_lo, hi = st.band_hi;
   const float median = st.median;
   const float* src = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
   unsigned* band = a.band + static_cast<int64_t>(k) * a.band_cap;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned below = 0, valid = 0;
-  auto visit = [&](float v, bool present) {
-    unsigned key = 0;
-    const bool fin = present && bracket_key(v, a.mode, median, key);
-    valid += fin ? 1u : 0u;
-    below += (fin && key < lo) ? 1u : 0u;
-    const bool in = fin && key >= lo && key <= hi;
-    const unsigned mask = __ballot_sync(0xffffffffu, in);
-    if (mask) {
-      const int leader = __ffs(mask) - 1;
-      unsigned base = 0;
-      if (lane == leader) base = atomicAdd(&st.inside, static_cast<unsigned>(__popc(mask)));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (in) {
-        const int64_t pos = static_cast<int64_t>(base) + __popc(mask & ((1u << lane) - 1u));
-        if (pos < a.band_cap) band[pos] = key;
-      }
-    }
-  };
-  // every lane of a warp runs the same trip count (the ballot needs them
-  // all); four float4 loads per thread are issued before any is visited
   constexpr int kLoads = 4;
   const int64_t n4 = a.pixels / 4;
   const float4* src4 = reinterpret_cast<const float4*>(src);
   const int64_t gstride = int64_t(gridDim.x) * blockDim.x * kLoads;
+  // every thread of the block runs the same trip count (the barriers need them all)
   for (int64_t base = blockIdx.x * int64_t(blockDim.x) * kLoads; base < n4; base += gstride) {
     float4 q[kLoads];
 #pragma unroll
     for (int u = 0; u < kLoads; ++u) {
       const int64_t i = base + u * int64_t(blockDim.x) + threadIdx.x;
-      q[u] = i < n4 ? __ldg(src4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+      q[u] = i < n4 ? __ldg(src4 + i) : make_float4(CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, CUDART_INF_F);  // not finite: skipped
     }
+    unsigned key[4 * kLoads];
+    unsigned in_mask = 0u;
 #pragma unroll
     for (int u = 0; u < kLoads; ++u) {
-      const bool present = base + u * int64_t(blockDim.x) + threadIdx.x < n4;
-      visit(q[u].x, present);
-      visit(q[u].y, present);
-      visit(q[u].z, present);
-      visit(q[u].w, present);
+      const float v4[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int j = 4 * u + c;
+        key[j] = 0u;
+        const bool fin = bracket_key(v4[c], a.mode, median, key[j]);
+        valid += fin ? 1u : 0u;
+        below += (fin && key[j] < lo) ? 1u : 0u;
+        in_mask |= (fin && key[j] >= lo && key[j] <= hi) ? (1u << j) : 0u;
+      }
     }
+    // block-wide exclusive prefix of the in-band counts, one reservation
+    const unsigned mine = __popc(in_mask);
+    unsigned incl = mine;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned n = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += n;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned total = 0;
+#pragma unroll
+      for (int w = 0; w < kBracketThreads / 32; ++w) {
+        const unsigned c = s_warp[w];
+        s_warp[w] = total;
+        total += c;
+      }
+      s_base = total ? atomicAdd(&st.inside, total) : 0u;
+    }
+    __syncthreads();
+    int64_t pos = static_cast<int64_t>(s_base) + s_warp[warp] + (incl - mine);
+    while (in_mask) {
+      const int j = __ffs(in_mask) - 1;
+      in_mask &= in_mask - 1u;
+      if (pos < a.band_cap) band[pos] = key[j];
+      ++pos;
+    }
+    __syncthreads();  // s_warp and s_base are rewritten by the next iteration
   }
+  // the last pixels % 4 samples: one warp, one atomic per in-band sample
   if (blockIdx.x == 0 && threadIdx.x < 32) {
-    for (int64_t p = n4 * 4 + threadIdx.x; p - threadIdx.x < a.pixels; p += 32) {
-      const bool present = p < a.pixels;
-      visit(present ? __ldg(src + p) : 0.0f, present);
+    for (int64_t p = n4 * 4 + threadIdx.x; p < a.pixels; p += 32) {
+      unsigned key = 0u;
+      const bool fin = bracket_key(__ldg(src + p), a.mode, median, key);
+      valid += fin ? 1u : 0u;
+      below += (fin && key < lo) ? 1u : 0u;
+      if (fin && key >= lo && key <= hi) {
+        const unsigned at = atomicAdd(&st.inside, 1u);
+        if (at < a.band_cap) band[at] = key;
+      }
     }
   }
   below = __reduce_add_sync(0xffffffffu, below);
@@ -611,67 +646,98 @@ struct DetectArgs {
   double k_sigma;
 };
 
-// Local-maximum candidates (star_detect.py:142-151).
+// Local-maximum candidates (star_detect.py:142-151).  Rows are dealt to
+// blocks, columns to the block's threads (coalesced, no division).  VEC: the
+// row is read as aligned float4 (width and frame stride multiples of 4), four
+// per thread and pass with all loads issued first; otherwise four scalar
+// columns per thread and pass.  Every thread of a row pass runs the same
+// trip count, so the warp ballot always sees the full warp.
+template <bool VEC>
 __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
   const int k = blockIdx.y;
   const float* img = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
   const float thr = a.state[k].threshold_f32;
   const int W = a.width, H = a.height;
   unsigned* out = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
-  // rows are dealt to blocks, columns to the block's threads (coalesced, no
-  // division), kPer columns per thread and pass with their loads issued
-  // first; every thread of a row pass runs the same trip count, so the warp
-  // ballot below always sees the full warp
-  constexpr int kPer = 4;
-  const int cols = W - 2;
-  const int span = static_cast<int>(blockDim.x) * kPer;
-  const int passes = (cols + span - 1) / span;
   const int lane = threadIdx.x & 31;
-  for (int y = 1 + static_cast<int>(blockIdx.x); y < H - 1; y += static_cast<int>(gridDim.x)) {
-    const float* row = img + static_cast<int64_t>(y) * W;
-    for (int pass = 0; pass < passes; ++pass) {
-      const int x0 = 1 + pass * span + static_cast<int>(threadIdx.x);
-      float c[kPer];
-#pragma unroll
-      for (int u = 0; u < kPer; ++u) {
-        const int x = x0 + u * static_cast<int>(blockDim.x);
-        c[u] = x <= cols ? __ldg(row + x) : 0.0f;
+  // one pixel: threshold (global or mesh), local maximum, warp-aggregated append
+  auto visit = [&](float c, int x, int y, const float* p, bool present) {
+    bool hit = false;
+    if (present && x >= 1 && x <= W - 2) {
+      bool above;
+      if (a.mesh.bg) {
+        double bg, nz;
+        mesh_at(a.mesh, k, x, y, bg, nz);
+        const double nzc = (nz >= 1.0e-6 || isnan(nz)) ? nz : 1.0e-6;  // np.maximum keeps NaN
+        above = static_cast<double>(c) > __dadd_rn(bg, __dmul_rn(a.k_sigma, nzc));
+      } else {
+        above = c > thr;
       }
+      if (isfinite(c) && above) {
+        hit = true;
 #pragma unroll
-      for (int u = 0; u < kPer; ++u) {
-        const int x = x0 + u * static_cast<int>(blockDim.x);
-        bool hit = false;
-        if (x <= cols) {
-          bool above;
-          if (a.mesh.bg) {
-            double bg, nz;
-            mesh_at(a.mesh, k, x, y, bg, nz);
-            const double nzc = (nz >= 1.0e-6 || isnan(nz)) ? nz : 1.0e-6;  // np.maximum keeps NaN
-            above = static_cast<double>(c[u]) > __dadd_rn(bg, __dmul_rn(a.k_sigma, nzc));
-          } else {
-            above = c[u] > thr;
-          }
-          if (isfinite(c[u]) && above) {
-            hit = true;
-            const float* p = row + x;
+        for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
-            for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx)
+            if (dx || dy) hit &= (c >= __ldg(p + static_cast<int64_t>(dy) * W + dx));
+      }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, hit);
+    if (mask) {
+      const int leader = __ffs(mask) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(&a.state[k].candidates, static_cast<unsigned>(__popc(mask)));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (hit) {
+        const unsigned pos = base + __popc(mask & ((1u << lane) - 1u));
+        if (pos < static_cast<unsigned>(kMaxCandidates)) out[pos] = static_cast<unsigned>(static_cast<int64_t>(y) * W + x);
+      }
+    }
+  };
+  if constexpr (VEC) {
+    constexpr int kPer = 4;
+    const int quads = W / 4;
+    const int span = static_cast<int>(blockDim.x) * kPer;
+    const int passes = (quads + span - 1) / span;
+    for (int y = 1 + static_cast<int>(blockIdx.x); y < H - 1; y += static_cast<int>(gridDim.x)) {
+      const float* row = img + static_cast<int64_t>(y) * W;
+      const float4* row4 = reinterpret_cast<const float4*>(row);
+      for (int pass = 0; pass < passes; ++pass) {
+        const int q0 = pass * span + static_cast<int>(threadIdx.x);
+        float4 c4[kPer];
 #pragma unroll
-              for (int dx = -1; dx <= 1; ++dx)
-                if (dx || dy) hit &= (c[u] >= __ldg(p + static_cast<int64_t>(dy) * W + dx));
-          }
+        for (int u = 0; u < kPer; ++u) {
+          const int q = q0 + u * static_cast<int>(blockDim.x);
+          c4[u] = q < quads ? __ldg(row4 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        const unsigned mask = __ballot_sync(0xffffffffu, hit);
-        if (mask) {
-          const int leader = __ffs(mask) - 1;
-          unsigned base = 0;
-          if (lane == leader) base = atomicAdd(&a.state[k].candidates, static_cast<unsigned>(__popc(mask)));
-          base = __shfl_sync(0xffffffffu, base, leader);
-          if (hit) {
-            const unsigned pos = base + __popc(mask & ((1u << lane) - 1u));
-            if (pos < static_cast<unsigned>(kMaxCandidates))
-              out[pos] = static_cast<unsigned>(static_cast<int64_t>(y) * W + x);
-          }
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+          const int q = q0 + u * static_cast<int>(blockDim.x);
+          const bool present = q < quads;
+          const float v4[4] = {c4[u].x, c4[u].y, c4[u].z, c4[u].w};
+#pragma unroll
+          for (int c = 0; c < 4; ++c) visit(v4[c], 4 * q + c, y, row + 4 * q + c, present);
+        }
+      }
+    }
+  } else {
+    constexpr int kPer = 4;
+    const int span = static_cast<int>(blockDim.x) * kPer;
+    const int passes = (W - 2 + span - 1) / span;
+    for (int y = 1 + static_cast<int>(blockIdx.x); y < H - 1; y += static_cast<int>(gridDim.x)) {
+      const float* row = img + static_cast<int64_t>(y) * W;
+      for (int pass = 0; pass < passes; ++pass) {
+        const int x0 = 1 + pass * span + static_cast<int>(threadIdx.x);
+        float c[kPer];
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+          const int x = x0 + u * static_cast<int>(blockDim.x);
+          c[u] = x <= W - 2 ? __ldg(row + x) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+          const int x = x0 + u * static_cast<int>(blockDim.x);
+          visit(c[u], x, y, row + x, x <= W - 2);
         }
       }
     }
@@ -1438,7 +1504,7 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
       ba.mode = mode;
       note_launch(3);
       bracket_sample_kernel<<<static_cast<unsigned>(count), 1024, sample_smem, s->stream>>>(ba);
-      bracket_pass_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), 256, 0, s->stream>>>(ba);
+      bracket_pass_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), kBracketThreads, 0, s->stream>>>(ba);
       bracket_resolve_kernel<<<static_cast<unsigned>(count), 1024, 0, s->stream>>>(ba);
       check_cuda(cudaGetLastError(), "bracket select launch");
       // frames the bracket could not settle: three-pass radix select
@@ -1536,7 +1602,11 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
   note_launch();
   const unsigned detect_rows = static_cast<unsigned>(std::max<int64_t>(
       1, std::min<int64_t>(s->height - 2, std::max<int64_t>(1, sm_count() * 8 / std::max(count, 1)))));
-  star_detect_kernel<<<dim3(detect_rows, static_cast<unsigned>(count)), 256, 0, s->stream>>>(da);
+  // aligned float4 rows: width and slot stride multiples of 4 (the slot array is cudaMalloc-aligned)
+  if ((s->width & 3) == 0 && (s->stride & 3) == 0)
+    star_detect_kernel<true><<<dim3(detect_rows, static_cast<unsigned>(count)), 256, 0, s->stream>>>(da);
+  else
+    star_detect_kernel<false><<<dim3(detect_rows, static_cast<unsigned>(count)), 256, 0, s->stream>>>(da);
   check_cuda(cudaGetLastError(), "star_detect launch");
   CatalogArgs ca{};
   ca.slots = s->d_slots;

@@ -167,6 +167,142 @@ __device__ __forceinline__ TilePlan plan_tile(const Coef& it, int tile_x, int ti
   return p;
 }
 
+// The 4 output rows of one thread in a 64 x 16 tile (rows ly, ly + 4, ...).
+// FINITE: the source frame holds no non-finite sample (every Lanczos3 window
+// takes the plain normalised sum); returns the count of non-finite outputs.
+template <int INTERP, bool FINITE>
+__device__ __forceinline__ unsigned warp_tile_rows(const WarpArgs& a, const Coef& co, const TapSource& ts, float* dst,
+                                                   int tile_x, int tile_y, int lx, int ly, bool interior,
+                                                   bool int_shift) {
+  constexpr int radius = (INTERP == GG_INTERP_LANCZOS3) ? 3 : 1;
+  const int ox = tile_x * kTileW + lx;
+  unsigned bad = 0;
+  // Affine source coordinates step by 4 output rows: (sx, sy) += 4 (b, e)
+  // in float-float (exact scaling by 4, one TwoSum per axis) instead of
+  // a fresh evaluation per pixel.
+  FFv sx_row{0.0f, 0.0f}, sy_row{0.0f, 0.0f};
+  bool row_ok = false;
+  const float step_x_hi = 4.0f * co.m[1][0], step_x_lo = 4.0f * co.m[1][1];
+  const float step_y_hi = 4.0f * co.m[4][0], step_y_lo = 4.0f * co.m[4][1];
+#pragma unroll 1
+  for (int r = 0; r < 4; ++r) {
+    const int oy = tile_y * kTileH + ly + 4 * r;
+    const bool inside = ox < a.width && oy < a.height;
+    bool valid = false;
+    float value = a.fill;
+    if (co.affine) {
+      if (r == 0) {
+        row_ok = source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx_row, sy_row);
+      } else {
+        sx_row = ff_add_ff(sx_row, step_x_hi, step_x_lo);
+        sy_row = ff_add_ff(sy_row, step_y_hi, step_y_lo);
+      }
+    }
+    if (inside) {
+      FFv sx = sx_row, sy = sy_row;
+      if (co.affine ? row_ok : source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx, sy)) {
+        const float W = static_cast<float>(a.width), H = static_cast<float>(a.height);
+        if (interior)
+          valid = true;
+        else if (INTERP != GG_INTERP_LANCZOS3)
+          valid = ff_ge(sx, 0.0f) && ff_le(sx, W - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, H - 1.0f);
+        else
+          valid = ff_ge(sx, 2.0f) && ff_lt(sx, W - 3.0f) && ff_ge(sy, 2.0f) && ff_lt(sy, H - 3.0f);
+        if (valid) {
+          int x0, y0;
+          float tx, ty;
+          ff_floor_frac(sx, x0, tx);
+          ff_floor_frac(sy, y0, ty);
+          if (INTERP == GG_INTERP_NEAREST) {
+            // np.rint: round half to even (engine/warp.py:87-96).
+            if (tx > 0.5f || (tx == 0.5f && (x0 & 1))) ++x0;
+            if (ty > 0.5f || (ty == 0.5f && (y0 & 1))) ++y0;
+          }
+          TapSource src = ts;
+          // Any tap outside the staged box reads global memory instead
+          // (an affine tile that fits the box keeps every tap inside it).
+          if (src.tile && !co.affine &&
+              (x0 - (radius - 1) < src.bx || x0 + radius >= src.bx + kBoxW || y0 - (radius - 1) < src.by ||
+               y0 + radius >= src.by + kBoxH))
+            src.tile = nullptr;
+          if (INTERP == GG_INTERP_NEAREST) {
+            value = src.at(x0, y0);
+          } else if (INTERP == GG_INTERP_BILINEAR) {
+            value = sample_bilinear(src, x0, y0, tx, ty, a.width, a.height);
+          } else if (int_shift) {
+            // exact weights 0, 0, 1, 0, 0, 0: the source sample itself, or
+            // no sample when it is not finite (nothing left to normalise)
+            value = src.at(x0, y0);
+            if (!isfinite(value)) {
+              valid = false;
+              value = a.fill;
+            }
+          } else {
+            valid = FINITE ? sample_lanczos3_finite(src, x0, y0, tx, ty, a.clamp, value)
+                           : sample_lanczos3(src, x0, y0, tx, ty, false, a.clamp, value);
+            if (!valid) value = a.fill;
+          }
+        }
+      }
+      dst[static_cast<int64_t>(oy) * a.width + ox] = value;
+      if (a.coverage && valid) atomicAdd(a.coverage + static_cast<int64_t>(oy) * a.width + ox, 1.0f);
+      bad += isfinite(value) ? 0u : 1u;
+    }
+  }
+  return bad;
+}
+
+// The common Lanczos3 tile in straight-line form: an affine map, the whole
+// 64 x 16 tile inside the output and mapped at least one pixel inside the
+// valid source range, its footprint staged in the shared-memory box, a source
+// frame without non-finite samples, no clamp and no coverage map.  Every
+// pixel is then valid and takes the plain normalised 6 x 6 sum, so the rows
+// need no per-pixel tests (same arithmetic as the general path).
+__device__ __forceinline__ unsigned warp_tile_rows_fast(const WarpArgs& a, const Coef& co, const float* box, int bx,
+                                                        int by, float* dst, int ox, int oy0) {
+  FFv sx, sy;
+  source_coord(co, static_cast<float>(ox), static_cast<float>(oy0), sx, sy);
+  const float step_x_hi = 4.0f * co.m[1][0], step_x_lo = 4.0f * co.m[1][1];
+  const float step_y_hi = 4.0f * co.m[4][0], step_y_lo = 4.0f * co.m[4][1];
+  float* out = dst + static_cast<int64_t>(oy0) * a.width + ox;
+  const int64_t out_step = 4 * static_cast<int64_t>(a.width);
+  unsigned bad = 0;
+#pragma unroll 1
+  for (int r = 0; r < 4; ++r) {
+    if (r) {
+      sx = ff_add_ff(sx, step_x_hi, step_x_lo);
+      sy = ff_add_ff(sy, step_y_hi, step_y_lo);
+    }
+    int x0, y0;
+    float tx, ty;
+    ff_floor_frac(sx, x0, tx);
+    ff_floor_frac(sy, y0, ty);
+    float wx[6], wy[6];
+    lanczos3_weights(tx, wx);
+    lanczos3_weights(ty, wy);
+    float swx = 0.0f, swy = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      swx += wx[i];
+      swy += wy[i];
+    }
+    const float* r0 = box + (y0 - 2 - by) * kBoxW + (x0 - 2 - bx);
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      float row = 0.0f;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) row = __fmaf_rn(wx[i], r0[j * kBoxW + i], row);
+      acc = __fmaf_rn(wy[j], row, acc);
+    }
+    const float wsum = swx * swy;
+    const float value = fabsf(wsum) > 1.0e-12f ? __fdividef(acc, wsum) : a.fill;
+    out[r * out_step] = value;
+    bad += isfinite(value) ? 0u : 1u;
+  }
+  return bad;
+}
+
 template <int INTERP, bool USE_TMA>
 __global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                   WarpArgs a) {
@@ -216,17 +352,18 @@ __global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __gri
     const int buf = i & 1;
     const int next = item + gridDim.x;
     if (tid == 0 && next < items) issue(next, buf ^ 1);
-    const WarpItem* ip = a.items + item / tiles;
+    const int item_index = item / tiles;
+    const WarpItem* ip = a.items + item_index;
     const Coef co = load_coef(ip);
     const int it_frame = __ldg(&ip->frame);
     const int it_src = __ldg(&ip->src_slot);
     const int it_dst = __ldg(&ip->dst_slot);
     const unsigned it_nonfinite = __ldg(&ip->src_nonfinite);
-    const int t = item % tiles;
+    const bool int_shift = __ldg(&ip->int_shift) != 0;
+    const int t = item - item_index * tiles;
     const int tile_x = t % a.tiles_x, tile_y = t / a.tiles_x;
     const bool fit = s_fit[buf] != 0;
     const bool interior = s_interior[buf] != 0;
-    const bool int_shift = __ldg(&ip->int_shift) != 0;
     if (fit) {
       // Bounded wait: on expiry flag the error, give the copy one more
       // bounded wait to land, finish this item (its output is discarded by
@@ -246,80 +383,18 @@ __global__ void __launch_bounds__(kWarpThreads, 3) warp_tiles_kernel(const __gri
       ts.by = s_by[buf];
       ts.width = a.width;
       float* dst = a.slots + static_cast<int64_t>(it_dst) * a.stride;
-      const int ox = tile_x * kTileW + lx;
-      const bool all_finite = it_nonfinite == 0u;
-      unsigned bad = 0;
-      // Affine source coordinates step by 4 output rows: (sx, sy) += 4 (b, e)
-      // in float-float (exact scaling by 4, one TwoSum per axis) instead of
-      // a fresh evaluation per pixel.
-      FFv sx_row{0.0f, 0.0f}, sy_row{0.0f, 0.0f};
-      bool row_ok = false;
-      const float step_x_hi = 4.0f * co.m[1][0], step_x_lo = 4.0f * co.m[1][1];
-      const float step_y_hi = 4.0f * co.m[4][0], step_y_lo = 4.0f * co.m[4][1];
-#pragma unroll 1
-      for (int r = 0; r < 4; ++r) {
-        const int oy = tile_y * kTileH + ly + 4 * r;
-        const bool inside = ox < a.width && oy < a.height;
-        bool valid = false;
-        float value = a.fill;
-        if (co.affine) {
-          if (r == 0) {
-            row_ok = source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx_row, sy_row);
-          } else {
-            sx_row = ff_add_ff(sx_row, step_x_hi, step_x_lo);
-            sy_row = ff_add_ff(sy_row, step_y_hi, step_y_lo);
-          }
-        }
-        if (inside) {
-          FFv sx = sx_row, sy = sy_row;
-          if (co.affine ? row_ok : source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx, sy)) {
-            const float W = static_cast<float>(a.width), H = static_cast<float>(a.height);
-            if (interior)
-              valid = true;
-            else if (INTERP != GG_INTERP_LANCZOS3)
-              valid = ff_ge(sx, 0.0f) && ff_le(sx, W - 1.0f) && ff_ge(sy, 0.0f) && ff_le(sy, H - 1.0f);
-            else
-              valid = ff_ge(sx, 2.0f) && ff_lt(sx, W - 3.0f) && ff_ge(sy, 2.0f) && ff_lt(sy, H - 3.0f);
-            if (valid) {
-              int x0, y0;
-              float tx, ty;
-              ff_floor_frac(sx, x0, tx);
-              ff_floor_frac(sy, y0, ty);
-              if (INTERP == GG_INTERP_NEAREST) {
-                // np.rint: round half to even (engine/warp.py:87-96).
-                if (tx > 0.5f || (tx == 0.5f && (x0 & 1))) ++x0;
-                if (ty > 0.5f || (ty == 0.5f && (y0 & 1))) ++y0;
-              }
-              TapSource src = ts;
-              // Any tap outside the staged box reads global memory instead
-              // (an affine tile that fits the box keeps every tap inside it).
-              if (src.tile && !co.affine &&
-                  (x0 - (radius - 1) < src.bx || x0 + radius >= src.bx + kBoxW || y0 - (radius - 1) < src.by ||
-                   y0 + radius >= src.by + kBoxH))
-                src.tile = nullptr;
-              if (INTERP == GG_INTERP_NEAREST) {
-                value = src.at(x0, y0);
-              } else if (INTERP == GG_INTERP_BILINEAR) {
-                value = sample_bilinear(src, x0, y0, tx, ty, a.width, a.height);
-              } else if (int_shift) {
-                // exact weights 0, 0, 1, 0, 0, 0: the source sample itself, or
-                // no sample when it is not finite (nothing left to normalise)
-                value = src.at(x0, y0);
-                if (!isfinite(value)) {
-                  valid = false;
-                  value = a.fill;
-                }
-              } else {
-                valid = sample_lanczos3(src, x0, y0, tx, ty, all_finite, a.clamp, value);
-                if (!valid) value = a.fill;
-              }
-            }
-          }
-          dst[static_cast<int64_t>(oy) * a.width + ox] = value;
-          if (a.coverage && valid) atomicAdd(a.coverage + static_cast<int64_t>(oy) * a.width + ox, 1.0f);
-          bad += isfinite(value) ? 0u : 1u;
-        }
-      }
+      // the renormalising path (and its out-of-line call) only for frames
+      // that hold non-finite samples; the straight-line form for the common
+      // interior tile
+      const bool full_tile = (tile_x + 1) * kTileW <= a.width && (tile_y + 1) * kTileH <= a.height;
+      unsigned bad;
+      if (INTERP == GG_INTERP_LANCZOS3 && fit && interior && co.affine && it_nonfinite == 0u && !int_shift &&
+          a.clamp < 0.0f && a.coverage == nullptr && full_tile)
+        bad = warp_tile_rows_fast(a, co, ts.tile, ts.bx, ts.by, dst, tile_x * kTileW + lx, tile_y * kTileH + ly);
+      else if (INTERP == GG_INTERP_LANCZOS3 && it_nonfinite == 0u)
+        bad = warp_tile_rows<INTERP, true>(a, co, ts, dst, tile_x, tile_y, lx, ly, interior, int_shift);
+      else
+        bad = warp_tile_rows<INTERP, false>(a, co, ts, dst, tile_x, tile_y, lx, ly, interior, int_shift);
       const unsigned warp_bad = __reduce_add_sync(0xffffffffu, bad);
       if ((tid & 31) == 0 && warp_bad) atomicAdd(a.nonfinite + it_frame, warp_bad);
     }

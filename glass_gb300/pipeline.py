@@ -385,7 +385,7 @@ class ResidentPipeline:
 
     def capture_graph(self, dev_raw_ptr: int, matrices: np.ndarray) -> int:
         """Captures calibrate -> weights -> fused warp + rejection + integration
-        with fixed matrices into a CUDA graph (at most 32 frames); returns the
+        with fixed matrices into a CUDA graph (at most 512 frames); returns the
         number of kernels one replay launches."""
         cfg = self.config
         return self.stack.capture_step_graph(dev_raw_ptr, matrices, self._calib_params(), cfg.interpolation,
