@@ -647,12 +647,12 @@ struct DetectArgs {
 };
 
 // Local-maximum candidates (star_detect.py:142-151).  Rows are dealt to
-// blocks, columns to the block's threads (coalesced, no division).  VEC: the
-// row is read as aligned float4 (width and frame stride multiples of 4), four
-// per thread and pass with all loads issued first; otherwise four scalar
-// columns per thread and pass.  Every thread of a row pass runs the same
-// trip count, so the warp ballot always sees the full warp.
-template <bool VEC>
+// blocks, columns to the block's threads (coalesced, no division), kPer
+// columns per thread and pass with all their loads issued first.  Every
+// thread of a row pass runs the same trip count, so the warp ballot always
+// sees the full warp.  MESH: per-pixel threshold from the background mesh
+// (float64), else the frame's float32 threshold.
+template <bool MESH>
 __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
   const int k = blockIdx.y;
   const float* img = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
@@ -660,84 +660,54 @@ __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
   const int W = a.width, H = a.height;
   unsigned* out = a.cand + static_cast<int64_t>(k) * kMaxCandidates;
   const int lane = threadIdx.x & 31;
-  // one pixel: threshold (global or mesh), local maximum, warp-aggregated append
-  auto visit = [&](float c, int x, int y, const float* p, bool present) {
-    bool hit = false;
-    if (present && x >= 1 && x <= W - 2) {
-      bool above;
-      if (a.mesh.bg) {
-        double bg, nz;
-        mesh_at(a.mesh, k, x, y, bg, nz);
-        const double nzc = (nz >= 1.0e-6 || isnan(nz)) ? nz : 1.0e-6;  // np.maximum keeps NaN
-        above = static_cast<double>(c) > __dadd_rn(bg, __dmul_rn(a.k_sigma, nzc));
-      } else {
-        above = c > thr;
-      }
-      if (isfinite(c) && above) {
-        hit = true;
+  constexpr int kPer = MESH ? 4 : 8;
+  const int span = static_cast<int>(blockDim.x) * kPer;
+  const int passes = (W - 2 + span - 1) / span;
+  for (int y = 1 + static_cast<int>(blockIdx.x); y < H - 1; y += static_cast<int>(gridDim.x)) {
+    const float* row = img + static_cast<int64_t>(y) * W;
+    for (int pass = 0; pass < passes; ++pass) {
+      const int x0 = 1 + pass * span + static_cast<int>(threadIdx.x);
+      float c[kPer];
 #pragma unroll
-        for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-          for (int dx = -1; dx <= 1; ++dx)
-            if (dx || dy) hit &= (c >= __ldg(p + static_cast<int64_t>(dy) * W + dx));
+      for (int u = 0; u < kPer; ++u) {
+        const int x = x0 + u * static_cast<int>(blockDim.x);
+        c[u] = x <= W - 2 ? __ldg(row + x) : 0.0f;
       }
-    }
-    const unsigned mask = __ballot_sync(0xffffffffu, hit);
-    if (mask) {
-      const int leader = __ffs(mask) - 1;
-      unsigned base = 0;
-      if (lane == leader) base = atomicAdd(&a.state[k].candidates, static_cast<unsigned>(__popc(mask)));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (hit) {
-        const unsigned pos = base + __popc(mask & ((1u << lane) - 1u));
-        if (pos < static_cast<unsigned>(kMaxCandidates)) out[pos] = static_cast<unsigned>(static_cast<int64_t>(y) * W + x);
-      }
-    }
-  };
-  if constexpr (VEC) {
-    constexpr int kPer = 4;
-    const int quads = W / 4;
-    const int span = static_cast<int>(blockDim.x) * kPer;
-    const int passes = (quads + span - 1) / span;
-    for (int y = 1 + static_cast<int>(blockIdx.x); y < H - 1; y += static_cast<int>(gridDim.x)) {
-      const float* row = img + static_cast<int64_t>(y) * W;
-      const float4* row4 = reinterpret_cast<const float4*>(row);
-      for (int pass = 0; pass < passes; ++pass) {
-        const int q0 = pass * span + static_cast<int>(threadIdx.x);
-        float4 c4[kPer];
 #pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-          const int q = q0 + u * static_cast<int>(blockDim.x);
-          c4[u] = q < quads ? __ldg(row4 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int u = 0; u < kPer; ++u) {
+        const int x = x0 + u * static_cast<int>(blockDim.x);
+        bool hit = false;
+        if (x <= W - 2) {
+          bool above;
+          if constexpr (MESH) {
+            double bg, nz;
+            mesh_at(a.mesh, k, x, y, bg, nz);
+            const double nzc = (nz >= 1.0e-6 || isnan(nz)) ? nz : 1.0e-6;  // np.maximum keeps NaN
+            above = static_cast<double>(c[u]) > __dadd_rn(bg, __dmul_rn(a.k_sigma, nzc));
+          } else {
+            above = c[u] > thr;
+          }
+          if (isfinite(c[u]) && above) {
+            hit = true;
+            const float* p = row + x;
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+              for (int dx = -1; dx <= 1; ++dx)
+                if (dx || dy) hit &= (c[u] >= __ldg(p + static_cast<int64_t>(dy) * W + dx));
+          }
         }
-#pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-          const int q = q0 + u * static_cast<int>(blockDim.x);
-          const bool present = q < quads;
-          const float v4[4] = {c4[u].x, c4[u].y, c4[u].z, c4[u].w};
-#pragma unroll
-          for (int c = 0; c < 4; ++c) visit(v4[c], 4 * q + c, y, row + 4 * q + c, present);
-        }
-      }
-    }
-  } else {
-    constexpr int kPer = 4;
-    const int span = static_cast<int>(blockDim.x) * kPer;
-    const int passes = (W - 2 + span - 1) / span;
-    for (int y = 1 + static_cast<int>(blockIdx.x); y < H - 1; y += static_cast<int>(gridDim.x)) {
-      const float* row = img + static_cast<int64_t>(y) * W;
-      for (int pass = 0; pass < passes; ++pass) {
-        const int x0 = 1 + pass * span + static_cast<int>(threadIdx.x);
-        float c[kPer];
-#pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-          const int x = x0 + u * static_cast<int>(blockDim.x);
-          c[u] = x <= W - 2 ? __ldg(row + x) : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-          const int x = x0 + u * static_cast<int>(blockDim.x);
-          visit(c[u], x, y, row + x, x <= W - 2);
+        const unsigned mask = __ballot_sync(0xffffffffu, hit);
+        if (mask) {
+          const int leader = __ffs(mask) - 1;
+          unsigned base = 0;
+          if (lane == leader) base = atomicAdd(&a.state[k].candidates, static_cast<unsigned>(__popc(mask)));
+          base = __shfl_sync(0xffffffffu, base, leader);
+          if (hit) {
+            const unsigned pos = base + __popc(mask & ((1u << lane) - 1u));
+            if (pos < static_cast<unsigned>(kMaxCandidates))
+              out[pos] = static_cast<unsigned>(static_cast<int64_t>(y) * W + x);
+          }
         }
       }
     }
@@ -1602,8 +1572,7 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
   note_launch();
   const unsigned detect_rows = static_cast<unsigned>(std::max<int64_t>(
       1, std::min<int64_t>(s->height - 2, std::max<int64_t>(1, sm_count() * 8 / std::max(count, 1)))));
-  // aligned float4 rows: width and slot stride multiples of 4 (the slot array is cudaMalloc-aligned)
-  if ((s->width & 3) == 0 && (s->stride & 3) == 0)
+  if (da.mesh.bg)
     star_detect_kernel<true><<<dim3(detect_rows, static_cast<unsigned>(count)), 256, 0, s->stream>>>(da);
   else
     star_detect_kernel<false><<<dim3(detect_rows, static_cast<unsigned>(count)), 256, 0, s->stream>>>(da);
