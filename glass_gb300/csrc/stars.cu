@@ -328,15 +328,25 @@ __global__ void __launch_bounds__(1024) bracket_sample_kernel(BracketArgs a) {
 // keys (appended to the frame's band buffer in no particular order).  Each
 // block iteration covers 16 samples per thread (four float4 loads issued
 // first) and reserves the band slots of all its in-band samples with one
-// atomic, so the per-frame counter sees one atomic per 4096 samples.
+// atomic, so the per-frame counter sees one atomic per 4096 samples.  The
+// per-sample tests are unsigned range checks on the order-preserving keys:
+// a finite float32 has a key in [0x00800000, 0xff7fffff] (float_key), so
+// mode 0 needs no separate isfinite; mode 1 (|v - median|) tests the sample
+// itself.
 constexpr int kBracketThreads = 256;
 
+template <int MODE>
 __global__ void __launch_bounds__(kBracketThreads) bracket_pass_kernel(BracketArgs a) {
   __shared__ unsigned s_warp[kBracketThreads / 32];
   __shared__ unsigned s_base;
   const int k = blockIdx.y;
   StarFrameState& st = a.state[k];
   const unsigned lo = st.band_lo, hi = st.band_hi;
+  const unsigned span = hi - lo;  // the band is [lo, lo + span]
+  constexpr unsigned kFiniteLo = 0x00800000u, kFiniteSpan = 0xff7fffffu - 0x00800000u;
+  // mode 0: key < lo for a finite key <=> (key - kFiniteLo) < (lo - kFiniteLo),
+  // nothing is below a band that starts below the finite keys
+  const unsigned lo_f = lo >= kFiniteLo ? lo - kFiniteLo : 0u;
   const float median = st.median;
   const float* src = a.slots + static_cast<int64_t>(a.slot_of_frame[a.frames[k]]) * a.stride;
   unsigned* band = a.band + static_cast<int64_t>(k) * a.band_cap;
@@ -352,7 +362,7 @@ __global__ void __launch_bounds__(kBracketThreads) bracket_pass_kernel(BracketAr
 #pragma unroll
     for (int u = 0; u < kLoads; ++u) {
       const int64_t i = base + u * int64_t(blockDim.x) + threadIdx.x;
-      q[u] = i < n4 ? __ldg(src4 + i) : make_float4(CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, CUDART_INF_F);  // not finite: skipped
+      q[u] = i < n4 ? __ldg(src4 + i) : make_float4(CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, CUDART_INF_F);
     }
     unsigned key[4 * kLoads];
     unsigned in_mask = 0u;
@@ -362,11 +372,20 @@ __global__ void __launch_bounds__(kBracketThreads) bracket_pass_kernel(BracketAr
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const int j = 4 * u + c;
-        key[j] = 0u;
-        const bool fin = bracket_key(v4[c], a.mode, median, key[j]);
-        valid += fin ? 1u : 0u;
-        below += (fin && key[j] < lo) ? 1u : 0u;
-        in_mask |= (fin && key[j] >= lo && key[j] <= hi) ? (1u << j) : 0u;
+        bool fin;
+        if constexpr (MODE == 0) {
+          const unsigned bits = __float_as_uint(v4[c]);
+          key[j] = bits ^ (static_cast<unsigned>(static_cast<int>(bits) >> 31) | 0x80000000u);  // float_key
+          const unsigned kf = key[j] - kFiniteLo;
+          fin = kf <= kFiniteSpan;
+          valid += fin ? 1u : 0u;
+          below += (kf < lo_f) ? 1u : 0u;  // implies finite
+        } else {
+          fin = (__float_as_uint(v4[c]) & 0x7f800000u) != 0x7f800000u;
+          key[j] = __float_as_uint(fabsf(__fsub_rn(v4[c], median))) | 0x80000000u;  // float_key of a |d|
+          below += (fin && key[j] < lo) ? 1u : 0u;
+        }
+        in_mask |= (fin && key[j] - lo <= span) ? (1u << j) : 0u;
       }
     }
     // block-wide exclusive prefix of the in-band counts, one reservation
@@ -403,7 +422,7 @@ __global__ void __launch_bounds__(kBracketThreads) bracket_pass_kernel(BracketAr
   if (blockIdx.x == 0 && threadIdx.x < 32) {
     for (int64_t p = n4 * 4 + threadIdx.x; p < a.pixels; p += 32) {
       unsigned key = 0u;
-      const bool fin = bracket_key(__ldg(src + p), a.mode, median, key);
+      const bool fin = bracket_key(__ldg(src + p), MODE, median, key);
       valid += fin ? 1u : 0u;
       below += (fin && key < lo) ? 1u : 0u;
       if (fin && key >= lo && key <= hi) {
@@ -416,7 +435,7 @@ __global__ void __launch_bounds__(kBracketThreads) bracket_pass_kernel(BracketAr
   valid = __reduce_add_sync(0xffffffffu, valid);
   if (lane == 0) {
     if (below) atomicAdd(&st.below, below);
-    if (a.mode == 0 && valid) atomicAdd(&st.count, valid);
+    if (MODE == 0 && valid) atomicAdd(&st.count, valid);
   }
 }
 
@@ -673,29 +692,36 @@ __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
         const int x = x0 + u * static_cast<int>(blockDim.x);
         c[u] = x <= W - 2 ? __ldg(row + x) : 0.0f;
       }
+      // threshold first: most passes hold no candidate in the whole warp
+      unsigned above_bits = 0u;
 #pragma unroll
       for (int u = 0; u < kPer; ++u) {
         const int x = x0 + u * static_cast<int>(blockDim.x);
-        bool hit = false;
-        if (x <= W - 2) {
-          bool above;
-          if constexpr (MESH) {
+        bool above = false;
+        if constexpr (MESH) {
+          if (x <= W - 2) {  // the mesh is read inside the frame only
             double bg, nz;
             mesh_at(a.mesh, k, x, y, bg, nz);
             const double nzc = (nz >= 1.0e-6 || isnan(nz)) ? nz : 1.0e-6;  // np.maximum keeps NaN
             above = static_cast<double>(c[u]) > __dadd_rn(bg, __dmul_rn(a.k_sigma, nzc));
-          } else {
-            above = c[u] > thr;
           }
-          if (isfinite(c[u]) && above) {
-            hit = true;
-            const float* p = row + x;
+        } else {
+          above = c[u] > thr;
+        }
+        above_bits |= (x <= W - 2 && isfinite(c[u]) && above) ? (1u << u) : 0u;
+      }
+      if (!__any_sync(0xffffffffu, above_bits != 0u)) continue;
 #pragma unroll
-            for (int dy = -1; dy <= 1; ++dy)
+      for (int u = 0; u < kPer; ++u) {
+        const int x = x0 + u * static_cast<int>(blockDim.x);
+        bool hit = (above_bits >> u) & 1u;
+        if (hit) {
+          const float* p = row + x;
 #pragma unroll
-              for (int dx = -1; dx <= 1; ++dx)
-                if (dx || dy) hit &= (c[u] >= __ldg(p + static_cast<int64_t>(dy) * W + dx));
-          }
+          for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx)
+              if (dx || dy) hit &= (c[u] >= __ldg(p + static_cast<int64_t>(dy) * W + dx));
         }
         const unsigned mask = __ballot_sync(0xffffffffu, hit);
         if (mask) {
@@ -1474,7 +1500,10 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
       ba.mode = mode;
       note_launch(3);
       bracket_sample_kernel<<<static_cast<unsigned>(count), 1024, sample_smem, s->stream>>>(ba);
-      bracket_pass_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), kBracketThreads, 0, s->stream>>>(ba);
+      if (mode == 0)
+        bracket_pass_kernel<0><<<dim3(per_frame, static_cast<unsigned>(count)), kBracketThreads, 0, s->stream>>>(ba);
+      else
+        bracket_pass_kernel<1><<<dim3(per_frame, static_cast<unsigned>(count)), kBracketThreads, 0, s->stream>>>(ba);
       bracket_resolve_kernel<<<static_cast<unsigned>(count), 1024, 0, s->stream>>>(ba);
       check_cuda(cudaGetLastError(), "bracket select launch");
       // frames the bracket could not settle: three-pass radix select
