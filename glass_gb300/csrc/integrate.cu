@@ -980,16 +980,23 @@ __device__ __forceinline__ void ff_warp_reduce(FF& s) {
 }
 
 // Ascending bitonic sort of the warp's 32 * NPL values; rank e lives in lane
-// e / NPL, register e % NPL.
+// e / NPL, register e % NPL.  Steps with partner distance >= NPL exchange
+// across lanes (shuffles); the shorter ones stay in a lane.  From merge size
+// NPL up, a lane's direction is the same for all its registers, so its
+// in-register steps always sort ascending (compile-time directions: a min
+// and a max per pair) and a lane whose block sorts descending reverses its
+// registers afterwards; below NPL the direction of a pair is a compile-time
+// function of its register index.
 template <int NPL>
 __device__ __forceinline__ void warp_bitonic_sort(float (&v)[NPL], int lane) {
   constexpr int LOGM = (NPL == 2) ? 6 : (NPL == 4) ? 7 : (NPL == 8) ? 8 : 9;
   static_assert((32 * NPL) == (1 << LOGM), "NPL must be 2, 4, 8 or 16");
 #pragma unroll
   for (int ls = 1; ls <= LOGM; ++ls) {
+    const int size = 1 << ls;
 #pragma unroll
     for (int lj = ls - 1; lj >= 0; --lj) {
-      const int size = 1 << ls, j = 1 << lj;
+      const int j = 1 << lj;
       if (j >= NPL) {
         const int lm = j / NPL;
         const bool up = ((lane * NPL) & size) == 0;  // always true in the last merge
@@ -999,16 +1006,37 @@ __device__ __forceinline__ void warp_bitonic_sort(float (&v)[NPL], int lane) {
           const float o = __shfl_xor_sync(0xffffffffu, v[k], lm);
           v[k] = keep_min ? fminf(v[k], o) : fmaxf(v[k], o);
         }
+      } else if (size < NPL) {
+#pragma unroll
+        for (int k = 0; k < NPL; ++k) {
+          if ((k ^ j) > k) {
+            const int q = k ^ j;
+            const float lo = fminf(v[k], v[q]), hi = fmaxf(v[k], v[q]);
+            const bool up = (k & size) == 0;  // compile time: lane * NPL has no bit below NPL
+            v[k] = up ? lo : hi;
+            v[q] = up ? hi : lo;
+          }
+        }
       } else {
 #pragma unroll
         for (int k = 0; k < NPL; ++k) {
           if ((k ^ j) > k) {
             const int q = k ^ j;
-            const bool up = ((lane * NPL + k) & size) == 0;
             const float lo = fminf(v[k], v[q]), hi = fmaxf(v[k], v[q]);
-            v[k] = up ? lo : hi;
-            v[q] = up ? hi : lo;
+            v[k] = lo;
+            v[q] = hi;
           }
+        }
+      }
+    }
+    if (size >= NPL && size < 32 * NPL) {
+      // descending blocks of this merge: reverse the ascending registers
+      if (((lane * NPL) & size) != 0) {
+#pragma unroll
+        for (int k = 0; k < NPL / 2; ++k) {
+          const float t = v[k];
+          v[k] = v[NPL - 1 - k];
+          v[NPL - 1 - k] = t;
         }
       }
     }
