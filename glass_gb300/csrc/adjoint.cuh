@@ -112,17 +112,93 @@ __device__ __forceinline__ void lanczos3_weights_grad(float t, float (&w)[6], fl
   }
 }
 
+// Derivatives d/dx of the paired Lanczos3 polynomials of sampling.cuh
+// (printed by glass_gb300/lanczos_poly.py --derivatives from the same
+// float32 coefficients).
+__device__ __forceinline__ float l3_even_a_dx(float x) {
+  float p = 8.401103318e-03f;
+  p = __fmaf_rn(p, x, -3.910817578e-02f);
+  p = __fmaf_rn(p, x, 6.560242176e-02f);
+  p = __fmaf_rn(p, x, 1.272828728e-01f);
+  return __fmaf_rn(p, x, -4.488392770e-01f);
+}
+__device__ __forceinline__ float l3_odd_a_dx(float x) {
+  float p = 1.338174939e-02f;
+  p = __fmaf_rn(p, x, -1.017850712e-01f);
+  p = __fmaf_rn(p, x, 4.797004461e-01f);
+  p = __fmaf_rn(p, x, -1.296258688e+00f);
+  return __fmaf_rn(p, x, 1.468628168e+00f);
+}
+__device__ __forceinline__ float l3_even_b_dx(float x) {
+  float p = -2.127639204e-02f;
+  p = __fmaf_rn(p, x, 1.010670736e-01f);
+  p = __fmaf_rn(p, x, -1.926717758e-01f);
+  p = __fmaf_rn(p, x, -1.327898800e-01f);
+  return __fmaf_rn(p, x, 5.606142282e-01f);
+}
+__device__ __forceinline__ float l3_odd_b_dx(float x) {
+  float p = -9.153226390e-03f;
+  p = __fmaf_rn(p, x, 7.287412882e-02f);
+  p = __fmaf_rn(p, x, -3.514715135e-01f);
+  p = __fmaf_rn(p, x, 9.126434922e-01f);
+  return __fmaf_rn(p, x, -8.275418282e-01f);
+}
+__device__ __forceinline__ float l3_even_c_dx(float x) {
+  float p = 2.460771054e-02f;
+  p = __fmaf_rn(p, x, -1.213750690e-01f);
+  p = __fmaf_rn(p, x, 2.724962831e-01f);
+  p = __fmaf_rn(p, x, -1.289147735e-01f);
+  return __fmaf_rn(p, x, -8.637610078e-02f);
+}
+__device__ __forceinline__ float l3_odd_c_dx(float x) {
+  float p = 2.943186555e-03f;
+  p = __fmaf_rn(p, x, -3.018763475e-02f);
+  p = __fmaf_rn(p, x, 1.672878861e-01f);
+  p = __fmaf_rn(p, x, -4.329387546e-01f);
+  return __fmaf_rn(p, x, 3.049877286e-01f);
+}
+
+// Lanczos3 weights and their t-derivatives from the paired polynomials the
+// warp samples with: with u = t - 1/2 and x = u^2 each pair is E(u) +- O(u),
+// E = P_e(x), O = u P_o(x), so dE/dt = 2u P_e'(x) and
+// dO/dt = P_o(x) + 2x P_o'(x).  Absolute accuracy (about 1e-7), enough for
+// sums over windows whose taps are all finite.
+__device__ __forceinline__ void lanczos3_weights_grad_poly(float t, float (&w)[6], float (&dw)[6]) {
+  const float u = __fsub_rn(t, 0.5f);
+  const float x = __fmul_rn(u, u);
+  const float u2 = __fadd_rn(u, u), x2 = __fadd_rn(x, x);
+  const float ea = l3_even_a(x), pa = l3_odd_a(x), oa = __fmul_rn(u, pa);
+  const float eb = l3_even_b(x), pb = l3_odd_b(x), ob = __fmul_rn(u, pb);
+  const float ec = l3_even_c(x), pc = l3_odd_c(x), oc = __fmul_rn(u, pc);
+  const float dea = __fmul_rn(u2, l3_even_a_dx(x)), doa = __fmaf_rn(x2, l3_odd_a_dx(x), pa);
+  const float deb = __fmul_rn(u2, l3_even_b_dx(x)), dob = __fmaf_rn(x2, l3_odd_b_dx(x), pb);
+  const float dec = __fmul_rn(u2, l3_even_c_dx(x)), doc = __fmaf_rn(x2, l3_odd_c_dx(x), pc);
+  w[0] = __fadd_rn(ec, oc);
+  w[1] = __fadd_rn(eb, ob);
+  w[2] = __fadd_rn(ea, oa);
+  w[3] = __fsub_rn(ea, oa);
+  w[4] = __fsub_rn(eb, ob);
+  w[5] = __fsub_rn(ec, oc);
+  dw[0] = __fadd_rn(dec, doc);
+  dw[1] = __fadd_rn(deb, dob);
+  dw[2] = __fadd_rn(dea, doa);
+  dw[3] = __fsub_rn(dea, doa);
+  dw[4] = __fsub_rn(deb, dob);
+  dw[5] = __fsub_rn(dec, doc);
+}
+
 // Lanczos3 value and its derivatives with respect to the sample position
-// over a window whose 36 taps are all finite; false when a tap is not finite
-// or the weights cancel (|D| <= 1e-12).
+// over a window whose 36 taps are all finite (the warp's polynomial weights
+// and their exact derivatives); false when a tap is not finite or the
+// weights cancel (|D| <= 1e-12).
 // UNROLL = true issues all 36 tap loads of the window at once (more loads in
 // flight, more registers); false walks it row by row.
 template <bool UNROLL = false>
 __device__ __forceinline__ bool lanczos3_value_grad(const float* src, int W, int x0, int y0, float tx, float ty,
                                                     float& O, float& Ox, float& Oy) {
   float wx[6], wy[6], dwx[6], dwy[6];
-  lanczos3_weights_grad(tx, wx, dwx);
-  lanczos3_weights_grad(ty, wy, dwy);
+  lanczos3_weights_grad_poly(tx, wx, dwx);
+  lanczos3_weights_grad_poly(ty, wy, dwy);
   float sx = 0.0f, sy = 0.0f, dsx = 0.0f, dsy = 0.0f;
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
