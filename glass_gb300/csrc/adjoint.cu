@@ -106,7 +106,14 @@ __global__ void __launch_bounds__(256) affine_backward_kernel(AdjointArgs a) {
         atomicAdd(a.grad_src + static_cast<int64_t>(y1) * W + x0, g * ox * ty);
         atomicAdd(a.grad_src + static_cast<int64_t>(y1) * W + x1, g * tx * ty);
       }
+    } else if (float Os, Osx, Osy;
+               !a.grad_src && lanczos3_value_grad<true>(a.src, W, x0, y0, tx, ty, Os, Osx, Osy)) {
+      // parameter gradient only over a window of finite taps: the separable
+      // sums with the warp's polynomial weights and their exact derivatives
+      gsx = g * Osx;
+      gsy = g * Osy;
     } else {
+      // source gradient, or non-finite taps (renormalised over the finite ones)
       float wx[6], wy[6], dwx[6], dwy[6];
       lanczos3_weights_grad(tx, wx, dwx);
       lanczos3_weights_grad(ty, wy, dwy);

@@ -159,9 +159,11 @@ __device__ __forceinline__ float percentile_valid(const float* S, int T, int cnt
 }
 
 // engine/rejection.py:352-366: whole-stack frame count, lo + (hi-lo)*f.
-__device__ __forceinline__ float percentile_all(const float* S, int T, int n, float percent) {
+// `fraction` is float32(percent / 100): the callers' 0.25, 0.5 and 0.75 are
+// exactly the quotients of 25, 50 and 75 by 100.
+__device__ __forceinline__ float percentile_all(const float* S, int T, int n, float fraction) {
   if (n == 1) return S[0];
-  const float pos = __fmul_rn(__fdiv_rn(percent, 100.0f), static_cast<float>(n - 1));
+  const float pos = __fmul_rn(fraction, static_cast<float>(n - 1));
   const int lower = static_cast<int>(floorf(pos));
   const int upper = static_cast<int>(ceilf(pos));
   const float f = __fsub_rn(pos, static_cast<float>(lower));
@@ -248,9 +250,9 @@ __device__ __forceinline__ CenterScale winsorized_stats(const Sorted& sorted, co
   if (cnt <= 0) return r;
   float med, q25, q75;
   if (allvalid) {
-    med = percentile_all(S, T, nframes, 50.0f);
-    q25 = percentile_all(S, T, nframes, 25.0f);
-    q75 = percentile_all(S, T, nframes, 75.0f);
+    med = percentile_all(S, T, nframes, 0.5f);
+    q25 = percentile_all(S, T, nframes, 0.25f);
+    q75 = percentile_all(S, T, nframes, 0.75f);
   } else {
     med = percentile_valid(S, T, cnt, 0.5f);
     q25 = percentile_valid(S, T, cnt, 0.25f);
@@ -594,9 +596,9 @@ __device__ __forceinline__ CenterScale winsorized_sorted(const float* S, int T, 
   if (cnt <= 0) return r;
   float med, q25, q75;
   if (allvalid) {
-    med = percentile_all(S, T, nframes, 50.0f);
-    q25 = percentile_all(S, T, nframes, 25.0f);
-    q75 = percentile_all(S, T, nframes, 75.0f);
+    med = percentile_all(S, T, nframes, 0.5f);
+    q25 = percentile_all(S, T, nframes, 0.25f);
+    q75 = percentile_all(S, T, nframes, 0.75f);
   } else {
     med = percentile_valid(S, T, cnt, 0.5f);
     q25 = percentile_valid(S, T, cnt, 0.25f);
@@ -1043,14 +1045,29 @@ __device__ __forceinline__ void warp_bitonic_sort(float (&v)[NPL], int lane) {
   }
 }
 
-// Value of warp-uniform rank i.
+// Value of warp-uniform rank i; the register index i % NPL is warp-uniform,
+// so a switch on it (uniform branch) replaces a per-lane select chain.
 template <int NPL>
 __device__ __forceinline__ float warp_rank(const float (&v)[NPL], int i) {
-  const int k = i % NPL;
   float t = v[0];
-#pragma unroll
-  for (int q = 1; q < NPL; ++q)
-    if (q == k) t = v[q];
+  switch (i & (NPL - 1)) {
+    case 0: if constexpr (0 < NPL) t = v[0]; break;
+    case 1: if constexpr (1 < NPL) t = v[1]; break;
+    case 2: if constexpr (2 < NPL) t = v[2]; break;
+    case 3: if constexpr (3 < NPL) t = v[3]; break;
+    case 4: if constexpr (4 < NPL) t = v[4]; break;
+    case 5: if constexpr (5 < NPL) t = v[5]; break;
+    case 6: if constexpr (6 < NPL) t = v[6]; break;
+    case 7: if constexpr (7 < NPL) t = v[7]; break;
+    case 8: if constexpr (8 < NPL) t = v[8]; break;
+    case 9: if constexpr (9 < NPL) t = v[9]; break;
+    case 10: if constexpr (10 < NPL) t = v[10]; break;
+    case 11: if constexpr (11 < NPL) t = v[11]; break;
+    case 12: if constexpr (12 < NPL) t = v[12]; break;
+    case 13: if constexpr (13 < NPL) t = v[13]; break;
+    case 14: if constexpr (14 < NPL) t = v[14]; break;
+    case 15: if constexpr (15 < NPL) t = v[15]; break;
+  }
   return __shfl_sync(0xffffffffu, t, i / NPL);
 }
 
@@ -1068,9 +1085,9 @@ __device__ __forceinline__ float warp_percentile_valid(const float (&v)[NPL], in
 }
 
 template <int NPL>
-__device__ __forceinline__ float warp_percentile_all(const float (&v)[NPL], int n, float percent) {
+__device__ __forceinline__ float warp_percentile_all(const float (&v)[NPL], int n, float fraction) {
   if (n == 1) return warp_rank(v, 0);
-  const float pos = __fmul_rn(__fdiv_rn(percent, 100.0f), static_cast<float>(n - 1));
+  const float pos = __fmul_rn(fraction, static_cast<float>(n - 1));
   const int lower = static_cast<int>(floorf(pos));
   const int upper = static_cast<int>(ceilf(pos));
   const float f = __fsub_rn(pos, static_cast<float>(lower));
@@ -1213,9 +1230,9 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
         if (cnt > 0 && a.rejection == GG_REJECT_WINSORIZED) {
           float med, q25, q75;
           if (allvalid) {
-            med = warp_percentile_all(v, N, 50.0f);
-            q25 = warp_percentile_all(v, N, 25.0f);
-            q75 = warp_percentile_all(v, N, 75.0f);
+            med = warp_percentile_all(v, N, 0.5f);
+            q25 = warp_percentile_all(v, N, 0.25f);
+            q75 = warp_percentile_all(v, N, 0.75f);
           } else {
             med = warp_percentile_valid(v, cnt, 0.5f);
             q25 = warp_percentile_valid(v, cnt, 0.25f);
