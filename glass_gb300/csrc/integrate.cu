@@ -967,17 +967,31 @@ constexpr int kWarpTilePx = 32;
 constexpr int kWarpTileRow = kWarpTilePx + 1;
 constexpr int kWarpThreads = 256;
 
-// (hi, lo) float-float sum of the whole warp, in every lane.  TwoSum is exact
-// and symmetric, so both partners of each butterfly step hold the same pair.
+// (hi, lo) float-float sum over each segment of LANES lanes (the whole warp
+// by default), in every lane of the segment.  TwoSum is exact and
+// symmetric, so both partners of each butterfly step hold the same pair.
+template <int LANES = 32>
 __device__ __forceinline__ void ff_warp_reduce(FF& s) {
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
+  for (int off = LANES / 2; off > 0; off >>= 1) {
     const float oh = __shfl_xor_sync(0xffffffffu, s.hi, off);
     const float ol = __shfl_xor_sync(0xffffffffu, s.lo, off);
     float h, e;
     two_sum(s.hi, oh, h, e);
     s.hi = h;
     s.lo = __fadd_rn(__fadd_rn(s.lo, ol), e);
+  }
+}
+
+// Integer sum over each segment of LANES lanes, in every lane of it.
+template <int LANES>
+__device__ __forceinline__ int seg_sum(int x) {
+  if constexpr (LANES == 32) {
+    return __reduce_add_sync(0xffffffffu, x);
+  } else {
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    return x;
   }
 }
 
@@ -989,10 +1003,14 @@ __device__ __forceinline__ void ff_warp_reduce(FF& s) {
 // and a max per pair) and a lane whose block sorts descending reverses its
 // registers afterwards; below NPL the direction of a pair is a compile-time
 // function of its register index.
-template <int NPL>
+// With LANES = 16 the two half-warps sort two columns of 16 * NPL values
+// independently (every partner distance stays below 16); `lane` is then the
+// lane within the half.
+template <int NPL, int LANES = 32>
 __device__ __forceinline__ void warp_bitonic_sort(float (&v)[NPL], int lane) {
-  constexpr int LOGM = (NPL == 2) ? 6 : (NPL == 4) ? 7 : (NPL == 8) ? 8 : 9;
-  static_assert((32 * NPL) == (1 << LOGM), "NPL must be 2, 4, 8 or 16");
+  constexpr int M = LANES * NPL;
+  constexpr int LOGM = (M == 64) ? 6 : (M == 128) ? 7 : (M == 256) ? 8 : 9;
+  static_assert(M == (1 << LOGM) && NPL >= 2 && NPL <= 16, "LANES * NPL must be 64 .. 512");
 #pragma unroll
   for (int ls = 1; ls <= LOGM; ++ls) {
     const int size = 1 << ls;
@@ -1031,7 +1049,7 @@ __device__ __forceinline__ void warp_bitonic_sort(float (&v)[NPL], int lane) {
         }
       }
     }
-    if (size >= NPL && size < 32 * NPL) {
+    if (size >= NPL && size < M) {
       // descending blocks of this merge: reverse the ascending registers
       if (((lane * NPL) & size) != 0) {
 #pragma unroll
@@ -1047,8 +1065,8 @@ __device__ __forceinline__ void warp_bitonic_sort(float (&v)[NPL], int lane) {
 
 // Value of warp-uniform rank i; the register index i % NPL is warp-uniform,
 // so a switch on it (uniform branch) replaces a per-lane select chain.
-template <int NPL>
-__device__ __forceinline__ float warp_rank(const float (&v)[NPL], int i) {
+template <int NPL, int LANES = 32>
+__device__ __forceinline__ float warp_rank(const float (&v)[NPL], int i, int seg = 0) {
   float t = v[0];
   switch (i & (NPL - 1)) {
     case 0: if constexpr (0 < NPL) t = v[0]; break;
@@ -1068,46 +1086,49 @@ __device__ __forceinline__ float warp_rank(const float (&v)[NPL], int i) {
     case 14: if constexpr (14 < NPL) t = v[14]; break;
     case 15: if constexpr (15 < NPL) t = v[15]; break;
   }
-  return __shfl_sync(0xffffffffu, t, i / NPL);
+  return __shfl_sync(0xffffffffu, t, seg * LANES + i / NPL);
 }
 
-// percentile_valid / percentile_all on the warp's sorted column.
-template <int NPL>
-__device__ __forceinline__ float warp_percentile_valid(const float (&v)[NPL], int cnt, float fraction) {
-  if (cnt <= 0) return 0.0f;
-  const float pos = __fmul_rn(static_cast<float>(cnt - 1), fraction);
+// percentile_valid / percentile_all on the warp's sorted column.  With
+// LANES = 16 the two halves rank their own columns; the shuffles run in
+// every lane whatever the counts (a half with no samples gets 0).
+template <int NPL, int LANES = 32>
+__device__ __forceinline__ float warp_percentile_valid(const float (&v)[NPL], int cnt, float fraction, int seg = 0) {
+  const int c = cnt > 0 ? cnt : 1;
+  const float pos = __fmul_rn(static_cast<float>(c - 1), fraction);
   const int lower = static_cast<int>(floorf(pos));
-  const int upper = min(lower + 1, cnt - 1);
+  const int upper = min(lower + 1, c - 1);
   const float t = __fsub_rn(pos, static_cast<float>(lower));
-  const float lv = warp_rank(v, lower);
-  const float uv = warp_rank(v, upper);
+  const float lv = warp_rank<NPL, LANES>(v, lower, seg);
+  const float uv = warp_rank<NPL, LANES>(v, upper, seg);
+  if (cnt <= 0) return 0.0f;
   return __fadd_rn(__fmul_rn(lv, __fsub_rn(1.0f, t)), __fmul_rn(uv, t));
 }
 
-template <int NPL>
-__device__ __forceinline__ float warp_percentile_all(const float (&v)[NPL], int n, float fraction) {
-  if (n == 1) return warp_rank(v, 0);
+template <int NPL, int LANES = 32>
+__device__ __forceinline__ float warp_percentile_all(const float (&v)[NPL], int n, float fraction, int seg = 0) {
+  if (n == 1) return warp_rank<NPL, LANES>(v, 0, seg);
   const float pos = __fmul_rn(fraction, static_cast<float>(n - 1));
   const int lower = static_cast<int>(floorf(pos));
   const int upper = static_cast<int>(ceilf(pos));
   const float f = __fsub_rn(pos, static_cast<float>(lower));
-  const float lv = warp_rank(v, lower);
+  const float lv = warp_rank<NPL, LANES>(v, lower, seg);
   if (upper == lower) return lv;
-  const float uv = warp_rank(v, upper);
+  const float uv = warp_rank<NPL, LANES>(v, upper, seg);
   return __fadd_rn(lv, __fmul_rn(__fsub_rn(uv, lv), f));
 }
 
 // Mean (hi, lo) and float-float squared deviations of the valid ranks after
 // clipping to [lo, hi] (+-inf: no clipping); the two passes of std_of_valid
 // and winsorized_stats.
-template <int NPL>
+template <int NPL, int LANES = 32>
 __device__ __forceinline__ float warp_clipped_std(const float (&v)[NPL], int lane, int cnt, bool allvalid, float lo,
                                                   float hi, float& mean_out) {
   FF s1;
 #pragma unroll
   for (int k = 0; k < NPL; ++k)
     if (lane * NPL + k < cnt) s1.add(clipf(v[k], lo, hi));
-  ff_warp_reduce(s1);
+  ff_warp_reduce<LANES>(s1);
   float mh, ml;
   if (allvalid) {
     ff_div_pair(s1.hi, s1.lo, static_cast<float>(cnt), mh, ml);
@@ -1121,7 +1142,7 @@ __device__ __forceinline__ float warp_clipped_std(const float (&v)[NPL], int lan
 #pragma unroll
   for (int k = 0; k < NPL; ++k)
     if (lane * NPL + k < cnt) ff_add_sqdev(sv, clipf(v[k], lo, hi), mh, ml);
-  ff_warp_reduce(sv);
+  ff_warp_reduce<LANES>(sv);
   float q, ql;
   ff_div_pair(sv.hi, sv.lo, static_cast<float>(cnt), q, ql);
   return ff_sqrt_f32(q, ql);
@@ -1141,8 +1162,12 @@ __device__ __forceinline__ void cp_async_wait() {
 // PIPE (resident frames only): two tile buffers; the copies of the next tile
 // (cp.async, one 4-byte sample per thread and step) are in flight while the
 // warps integrate the current one.
-template <int NPL, int WARP, bool PIPE = false>
-__global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateArgs a) {
+// LANES = 16: two pixels per warp, one per half (columns of at most
+// 16 * NPL frames): the per-pixel scalar work and the butterfly reductions
+// are shared by two pixels.
+template <int NPL, int WARP, bool PIPE = false, int LANES = 32>
+__global__ void __launch_bounds__(kWarpThreads, LANES == 16 ? (NPL >= 16 ? 3 : 4) : 1)
+    integrate_warp_kernel(IntegrateArgs a) {
   extern __shared__ float smem_tiles[];  // [frames][kWarpTileRow] (x2 with PIPE), then (fused) [frames] FusedFrame
   __shared__ FrameTable<32 * NPL> tab;
   __shared__ int s_geo[kWarpTilePx];
@@ -1154,6 +1179,7 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
   const bool allvalid = tab.allvalid != 0;
   const bool unit = tab.unit != 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int hl = lane & (LANES - 1), seg = lane / LANES;
   const int N = a.frames;
   const int64_t P = a.pixels;
   const int64_t tiles = (P + kWarpTilePx - 1) / kWarpTilePx;
@@ -1205,56 +1231,69 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
       }
     }
     __syncthreads();
-    for (int px = warp; px < kWarpTilePx; px += kWarpThreads / 32) {
+    // LANES = 32: one warp per pixel; LANES = 16: each half-warp takes a
+    // pixel, the halves 16 tile columns apart (their column loads fall in
+    // disjoint shared-memory banks).  Every shuffle below runs in all 32
+    // lanes; a half whose pixel lies past the frame works on the tile's zero
+    // padding and writes nothing.
+    constexpr int kPixelsPerPass = 32 / LANES;
+    for (int pb = warp; pb < kWarpTilePx / kPixelsPerPass; pb += kWarpThreads / 32) {
+      const int px = pb + seg * (kWarpTilePx / kPixelsPerPass);
       const int64_t p = p0 + px;
-      if (p >= P) break;
+      const bool in_frame = p < P;
+      if (!__any_sync(0xffffffffu, in_frame)) break;
       const float* col = tile + px;
-      // column: lane l holds frames l, l + 32, ... (+inf when invalid)
+      // column: lane l of the segment holds frames l, l + LANES, ... (+inf when invalid)
       float v[NPL];
       int c = 0;
 #pragma unroll
       for (int k = 0; k < NPL; ++k) {
-        const int f = k * 32 + lane;
+        const int f = k * LANES + hl;
         const float x = f < N ? col[f * kWarpTileRow] : kInf;
-        const bool ok = f < N && tab.w[f] > 0.0f && isfinite(x);
+        const bool ok = in_frame && f < N && tab.w[f] > 0.0f && isfinite(x);
         v[k] = ok ? x : kInf;
         c += ok ? 1 : 0;
       }
-      const int cnt = __reduce_add_sync(0xffffffffu, c);
+      const int cnt = seg_sum<LANES>(c);
       int nl = 0, nh = 0;
       float lt = -kInf, ht = kInf;
       bool use_thresholds = false;
       if (a.rejection != GG_REJECT_NONE) {
-        warp_bitonic_sort<NPL>(v, lane);
+        warp_bitonic_sort<NPL, LANES>(v, hl);
         CenterScale cs{0.0f, 0.0f};
-        if (cnt > 0 && a.rejection == GG_REJECT_WINSORIZED) {
+        if (a.rejection == GG_REJECT_WINSORIZED) {
           float med, q25, q75;
           if (allvalid) {
-            med = warp_percentile_all(v, N, 0.5f);
-            q25 = warp_percentile_all(v, N, 0.25f);
-            q75 = warp_percentile_all(v, N, 0.75f);
+            med = warp_percentile_all<NPL, LANES>(v, N, 0.5f, seg);
+            q25 = warp_percentile_all<NPL, LANES>(v, N, 0.25f, seg);
+            q75 = warp_percentile_all<NPL, LANES>(v, N, 0.75f, seg);
           } else {
-            med = warp_percentile_valid(v, cnt, 0.5f);
-            q25 = warp_percentile_valid(v, cnt, 0.25f);
-            q75 = warp_percentile_valid(v, cnt, 0.75f);
+            med = warp_percentile_valid<NPL, LANES>(v, cnt, 0.5f, seg);
+            q25 = warp_percentile_valid<NPL, LANES>(v, cnt, 0.25f, seg);
+            q75 = warp_percentile_valid<NPL, LANES>(v, cnt, 0.75f, seg);
           }
           float scale1 = __fdiv_rn(__fsub_rn(q75, q25), 1.349f);
           const bool ok1 = allvalid ? (scale1 > 0.0f) : (scale1 > 0.0f && isfinite(scale1));
-          float unused;
-          if (!ok1) scale1 = warp_clipped_std(v, lane, cnt, allvalid, -kInf, kInf, unused);
+          if (__any_sync(0xffffffffu, !ok1)) {
+            float unused;
+            const float sd = warp_clipped_std<NPL, LANES>(v, hl, cnt, allvalid, -kInf, kInf, unused);
+            if (!ok1) scale1 = sd;
+          }
           const float lo1 = __fsub_rn(med, __fmul_rn(ls, scale1));
           const float hi1 = __fadd_rn(med, __fmul_rn(hs, scale1));
-          const float scale = warp_clipped_std(v, lane, cnt, allvalid, lo1, hi1, cs.center);
+          const float scale = warp_clipped_std<NPL, LANES>(v, hl, cnt, allvalid, lo1, hi1, cs.center);
           const bool ok2 = allvalid ? (scale > 0.0f) : (scale > 0.0f && isfinite(scale));
           cs.scale = ok2 ? scale : scale1;
-        } else if (cnt > 0) {
+          if (cnt <= 0) cs = CenterScale{0.0f, 0.0f};
+        } else {
           // sigma clip: median, then float32 frame-order sums (sequential, as
           // NumPy reduces over the frame axis)
-          const int h = cnt / 2;
-          const int l = (cnt & 1) ? h : h - 1;
-          cs.center = __fmul_rn(__fadd_rn(warp_rank(v, l), warp_rank(v, h)), 0.5f);
+          const int cc = cnt > 0 ? cnt : 1;
+          const int h = cc / 2;
+          const int l = (cc & 1) ? h : h - 1;
+          const float ml = warp_rank<NPL, LANES>(v, l, seg), mh = warp_rank<NPL, LANES>(v, h, seg);
           float scale = 0.0f;
-          if (lane == 0) {
+          if (hl == 0 && cnt > 0) {
             float sum = 0.0f;
             for (int f = 0; f < N; ++f) {
               const float x = col[f * kWarpTileRow];
@@ -1271,20 +1310,24 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
             }
             scale = __fsqrt_rn(__fdiv_rn(var, static_cast<float>(cnt)));
           }
-          cs.scale = __shfl_sync(0xffffffffu, scale, 0);
+          scale = __shfl_sync(0xffffffffu, scale, seg * LANES);
+          if (cnt > 0) {
+            cs.center = __fmul_rn(__fadd_rn(ml, mh), 0.5f);
+            cs.scale = scale;
+          }
         }
         lt = __fsub_rn(cs.center, __fmul_rn(ls, cs.scale));
         ht = __fadd_rn(cs.center, __fmul_rn(hs, cs.scale));
         int cl = 0, ch = 0;
 #pragma unroll
         for (int k = 0; k < NPL; ++k) {
-          if (lane * NPL + k < cnt) {
+          if (hl * NPL + k < cnt) {
             cl += v[k] < lt;
             ch += v[k] > ht;
           }
         }
-        nl = __reduce_add_sync(0xffffffffu, cl);
-        nh = __reduce_add_sync(0xffffffffu, ch);
+        nl = seg_sum<LANES>(cl);
+        nh = seg_sum<LANES>(ch);
         use_thresholds = true;
         if (nl + nh > 0) {
           // cpu/integration.py:85-99
@@ -1303,13 +1346,13 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
 #pragma unroll
         for (int k = 0; k < NPL; ++k) {
           const float x = v[k];
-          if (lane * NPL + k < cnt && !(use_thresholds && (x < lt || x > ht))) {
+          if (hl * NPL + k < cnt && !(use_thresholds && (x < lt || x > ht))) {
             ws.add(x);
             ++kept;
           }
         }
-        ff_warp_reduce(ws);
-        kept = __reduce_add_sync(0xffffffffu, kept);
+        ff_warp_reduce<LANES>(ws);
+        kept = seg_sum<LANES>(kept);
         if (kept > 0) {
           master = ff_div_f32(ws.hi, ws.lo, static_cast<float>(kept));
           weight = static_cast<float>(kept);
@@ -1318,8 +1361,8 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
         FF ws, wsum;
 #pragma unroll
         for (int k = 0; k < NPL; ++k) {
-          const int f = k * 32 + lane;
-          if (f < N) {
+          const int f = k * LANES + hl;
+          if (in_frame && f < N) {
             const float x = col[f * kWarpTileRow];
             const float w = tab.w[f];
             if (w > 0.0f && isfinite(x) && !(use_thresholds && (x < lt || x > ht))) {
@@ -1329,15 +1372,15 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
             }
           }
         }
-        ff_warp_reduce(ws);
-        ff_warp_reduce(wsum);
-        kept = __reduce_add_sync(0xffffffffu, kept);
+        ff_warp_reduce<LANES>(ws);
+        ff_warp_reduce<LANES>(wsum);
+        kept = seg_sum<LANES>(kept);
         if (kept > 0 && wsum.hi > 0.0f) {
           master = ff_div_ff(ws.hi, ws.lo, wsum.hi, wsum.lo);
           weight = wsum.value_f32();
         }
       }
-      if (lane == 0) {
+      if (hl == 0 && in_frame) {
         if constexpr (WARP != 0) a.geometric_out[p] = static_cast<float>(s_geo[px]);
         write_outputs(a, p, master, weight, kept, nl, nh, tab.active);
       }
@@ -1346,7 +1389,7 @@ __global__ void __launch_bounds__(kWarpThreads) integrate_warp_kernel(IntegrateA
   }
 }
 
-template <int NPL, int WARP = 0>
+template <int NPL, int WARP = 0, int LANES = 32>
 static void launch_warp(const IntegrateArgs& args, cudaStream_t stream) {
   const size_t tile_bytes = static_cast<size_t>(args.frames) * kWarpTileRow * sizeof(float);
   // resident frames: double-buffered tiles while two of them stay under 100 KB
@@ -1354,7 +1397,7 @@ static void launch_warp(const IntegrateArgs& args, cudaStream_t stream) {
   const bool pipe = kCanPipe && 2 * tile_bytes <= 100 * 1024;
   const size_t smem = tile_bytes * (pipe ? 2 : 1) +
                       (WARP != 0 ? static_cast<size_t>(args.frames) * sizeof(FusedFrame) : 0);
-  auto kern = pipe ? integrate_warp_kernel<NPL, WARP, kCanPipe> : integrate_warp_kernel<NPL, WARP, false>;
+  auto kern = pipe ? integrate_warp_kernel<NPL, WARP, kCanPipe, LANES> : integrate_warp_kernel<NPL, WARP, false, LANES>;
   check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
              "cudaFuncSetAttribute(integrate_warp)");
   int per_sm = 0;
@@ -1520,9 +1563,10 @@ void launch_integrate(gg_stack* s, const float* d_weights, const gg_integrate_pa
   }
   else if (p.rejection != GG_REJECT_LINEAR_FIT && n <= 512) {
     // one warp per pixel (the linear fit's serial rank walks stay below)
-    if (n <= 64) launch_warp<2>(a, s->stream);
-    else if (n <= 128) launch_warp<4>(a, s->stream);
-    else if (n <= 256) launch_warp<8>(a, s->stream);
+    // two pixels per warp up to 256 frames (16 lanes x NPL values each)
+    if (n <= 64) launch_warp<4, 0, 16>(a, s->stream);
+    else if (n <= 128) launch_warp<8, 0, 16>(a, s->stream);
+    else if (n <= 256) launch_warp<16, 0, 16>(a, s->stream);
     else launch_warp<16>(a, s->stream);
   }
   else if (n <= 64) launch_reg<64>(a, s->stream);
