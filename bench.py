@@ -787,7 +787,9 @@ def c3_side_report(local: int, frames: int = 64, size: int = 4096) -> dict:
     """Differentiable registration on 64 calibrated float32 frames of 4096 x
     4096 (~30 stars per 128 x 128, true affine = I + N(0, 1e-3) on the
     linear terms, +-0.5 px shifts): the catalog-matching start (triangle
-    similarity, the plain registration) against three refinements on the same
+    similarity, the plain registration; and the same catalogs with the affine
+    model, alone and followed by the device Gauss-Newton) against three
+    refinements on the same
     GPU and frames - the NCC translation grid (the reference's), the device
     Gauss-Newton (affine model, 20 steps at most) and L-BFGS on the masked NCC of the star
     regions with every gradient from the hand-written warp adjoint behind
@@ -831,6 +833,12 @@ def c3_side_report(local: int, frames: int = 64, size: int = 4096) -> dict:
 
         out = {"frames": frames, "size": size, "registered": len(good) + 1,
                "plain_catalog_similarity": {"rms_px": rms(tri), "s": t_plain}}
+        # the same catalogs with the reference's affine model
+        pipe.config.registration_model = "affine"
+        (aff, ok_aff), t_aff = timed(lambda: pipe.register(0))
+        pipe.config.registration_model = "similarity"
+        out["plain_catalog_affine"] = {"rms_px": rms(aff), "s": t_aff,
+                                       "registered": int(sum(ok_aff[k] for k in range(1, frames))) + 1}
         pipe.config.refine_method = "ncc"
         ncc, t = timed(lambda: pipe.refine(tri, 0))
         out["ncc_translation_grid"] = {"rms_px": rms(ncc), "s": t}
@@ -838,6 +846,9 @@ def c3_side_report(local: int, frames: int = 64, size: int = 4096) -> dict:
         pipe.config.gradient_refine = {"model": "affine", "iterations": 20}
         gn, t = timed(lambda: pipe.refine(tri, 0))
         out["device_gauss_newton_affine"] = {"rms_px": rms(gn), "s": t}
+        # Gauss-Newton from the affine catalog solution (inside its capture range)
+        gna, t = timed(lambda: pipe.refine(aff, 0))
+        out["affine_catalog_then_gauss_newton"] = {"rms_px": rms(gna), "s": t + t_aff}
         ref = pipe.stack.frame_tensor(0)
         cfg = LbfgsConfig(iterations=20)
 

@@ -393,18 +393,22 @@ def _points_xy(points: Any) -> np.ndarray:
     return np.ascontiguousarray(arr)
 
 
+_REG_MODELS = {"similarity": _lib.GG_TRANSFORM_SIMILARITY, "affine": _lib.GG_TRANSFORM_AFFINE}
+
+
 def _register_params(transform_model: str, min_inliers: int, tolerance_px: float, max_stars: int, neighbors: int,
                      descriptor_radius: float, max_descriptors: int, max_candidates: int) -> _lib.RegisterParams:
-    if transform_model != "similarity":
-        raise ValueError("triangle asterism registration on the GPU supports the similarity model")
-    return _lib.RegisterParams(_lib.GG_TRANSFORM_SIMILARITY, int(min_inliers), float(tolerance_px),
+    if transform_model not in _REG_MODELS:
+        raise ValueError("triangle asterism registration supports similarity or affine transforms")
+    return _lib.RegisterParams(_REG_MODELS[transform_model], int(min_inliers), float(tolerance_px),
                                float(descriptor_radius), int(max_stars), int(neighbors), int(max_descriptors),
                                int(max_candidates))
 
 
-def _registration_dict(r: _lib.Registration, pairs: np.ndarray | None = None) -> dict[str, Any]:
+def _registration_dict(r: _lib.Registration, pairs: np.ndarray | None = None,
+                       transform_model: str = "similarity") -> dict[str, Any]:
     out = {
-        "transform_model": "similarity",
+        "transform_model": transform_model,
         "matrix": np.asarray(r.matrix, dtype=np.float64).reshape(3, 3),
         "matched_stars": int(r.inliers),
         "inliers": int(r.inliers),
@@ -532,7 +536,7 @@ def estimate_triangle_asterism_transform(reference: Any, moving: Any, transform_
     pairs = np.full((_REG_MAX_STARS, 2), -1, dtype=np.int32)
     _lib.call("gg_register_star_lists", _lib.ptr(ref), ctypes.c_int64(len(ref)), _lib.ptr(mov),
               ctypes.c_int64(len(mov)), ctypes.byref(params), ctypes.byref(res), _lib.ptr(pairs))
-    return _registration_dict(res, pairs)
+    return _registration_dict(res, pairs, transform_model)
 
 
 # ---- alignment metrics / sub-pixel refinement (glass_cuda.py:706-1245) -------------
@@ -1078,7 +1082,7 @@ class ResidentCalibratedStack:
         out = (_lib.Registration * idx.size)()
         _lib.call("gg_stack_register_frames", self._handle, ctypes.c_int64(int(reference_index)), _lib.ptr(idx),
                   ctypes.c_int64(idx.size), ctypes.byref(params), out)
-        return [_registration_dict(r) for r in out]
+        return [_registration_dict(r, None, transform_model) for r in out]
 
     # ---- alignment metrics / refinement (native_bindings.cpp:10186-10417) ------------
     def _matrices(self, matrices: Any, count: int) -> np.ndarray:

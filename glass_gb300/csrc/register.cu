@@ -12,6 +12,9 @@
 //        two reference orientations per match, best = most pairs then
 //        smallest rms (first wins), three guarded refits
 //   _fit_similarity_matrix       :140-162  Procrustes fit
+//   _fit_affine_matrix           :106-119  least-squares affine fit (the
+//        transform_model = "affine" estimator: 3-point affine hypotheses,
+//        affine refits)
 //   _greedy_pairs / _score_matrix :177-215 pairs within tolerance, greedy by
 //        distance, rms of the residuals
 // and, in descriptor-list mode, the reference's similarity-from-descriptors
@@ -113,6 +116,7 @@ struct RegArgs {
   int max_desc;
   int max_cand;
   int min_inliers;
+  int model;  // GG_TRANSFORM_SIMILARITY or GG_TRANSFORM_AFFINE
 };
 
 // ---- float64 arithmetic rounded step by step like NumPy ---------------------
@@ -200,6 +204,65 @@ __device__ bool fit_similarity(const double* mx, const double* my, const double*
   m[4] = l11;
   m[5] = dsub(mry, dadd(dmul(mmx, l10), dmul(mmy, l11)));
   return true;
+}
+
+// Affine fit of n >= 3 point pairs (registration.py:106-119: the least-squares
+// solution of the 2n x 6 system).  The same solution from the normal
+// equations about the means, which decouple the translation: with centred
+// moving (a) and reference (b) coordinates,
+//   [Sxx Sxy; Sxy Syy] (l00, l01) = (S(ax bx), S(ay bx)), likewise for row 1,
+// solved by Cramer's rule; t = mean(b) - L mean(a).  False for fewer than 3
+// pairs or a (numerically) singular system — collinear moving points, where
+// the reference returns the minimum-norm solution instead; the descriptor
+// filter (area >= 2 px^2) keeps those out of the 3-point fits.
+struct AffineSums {
+  double mmx, mmy, mrx, mry, sxx, sxy, syy, sxr, syr, sxs, sys;
+};
+
+__device__ __forceinline__ bool affine_from_sums(const AffineSums& q, double (&m)[6]) {
+  const double det = dsub(dmul(q.sxx, q.syy), dmul(q.sxy, q.sxy));
+  if (!(q.sxx > 0.0 && q.syy > 0.0 && det > dmul(1.0e-12, dmul(q.sxx, q.syy)))) return false;
+  const double l00 = __ddiv_rn(dsub(dmul(q.sxr, q.syy), dmul(q.syr, q.sxy)), det);
+  const double l01 = __ddiv_rn(dsub(dmul(q.syr, q.sxx), dmul(q.sxr, q.sxy)), det);
+  const double l10 = __ddiv_rn(dsub(dmul(q.sxs, q.syy), dmul(q.sys, q.sxy)), det);
+  const double l11 = __ddiv_rn(dsub(dmul(q.sys, q.sxx), dmul(q.sxs, q.sxy)), det);
+  m[0] = l00;
+  m[1] = l01;
+  m[2] = dsub(q.mrx, dadd(dmul(l00, q.mmx), dmul(l01, q.mmy)));
+  m[3] = l10;
+  m[4] = l11;
+  m[5] = dsub(q.mry, dadd(dmul(l10, q.mmx), dmul(l11, q.mmy)));
+  return true;
+}
+
+__device__ bool fit_affine(const double* mx, const double* my, const double* rx, const double* ry, int n,
+                           double (&m)[6]) {
+  if (n < 3) return false;
+  AffineSums q{};
+  double smx = 0.0, smy = 0.0, srx = 0.0, sry = 0.0;
+  for (int i = 0; i < n; ++i) {
+    smx = dadd(smx, mx[i]);
+    smy = dadd(smy, my[i]);
+    srx = dadd(srx, rx[i]);
+    sry = dadd(sry, ry[i]);
+  }
+  const double dn = static_cast<double>(n);
+  q.mmx = __ddiv_rn(smx, dn);
+  q.mmy = __ddiv_rn(smy, dn);
+  q.mrx = __ddiv_rn(srx, dn);
+  q.mry = __ddiv_rn(sry, dn);
+  for (int i = 0; i < n; ++i) {
+    const double ax = dsub(mx[i], q.mmx), ay = dsub(my[i], q.mmy);
+    const double bx = dsub(rx[i], q.mrx), by = dsub(ry[i], q.mry);
+    q.sxx = dadd(q.sxx, dmul(ax, ax));
+    q.sxy = dadd(q.sxy, dmul(ax, ay));
+    q.syy = dadd(q.syy, dmul(ay, ay));
+    q.sxr = dadd(q.sxr, dmul(ax, bx));
+    q.syr = dadd(q.syr, dmul(ay, bx));
+    q.sxs = dadd(q.sxs, dmul(ax, by));
+    q.sys = dadd(q.sys, dmul(ay, by));
+  }
+  return affine_from_sums(q, m);
 }
 
 // ---- point pairs of a transform (registration.py:177-215) ------------------------
@@ -494,6 +557,43 @@ __device__ bool warp_fit_similarity(const double* mx, const double* my, const do
   m[4] = l11;
   m[5] = dsub(mry, dadd(dmul(mmx, l10), dmul(mmy, l11)));
   return true;
+}
+
+// Warp-cooperative affine fit of n <= 80 pairs: fit_affine's sums, one per
+// lane (each in pair order).  Every lane returns the result.
+__device__ bool warp_fit_affine(const double* mx, const double* my, const double* rx, const double* ry, int n,
+                                double (&m)[6]) {
+  const int lane = threadIdx.x & 31;
+  if (n < 3) return false;
+  double s = 0.0;
+  if (lane < 4) {
+    const double* v = lane == 0 ? mx : (lane == 1 ? my : (lane == 2 ? rx : ry));
+    for (int i = 0; i < n; ++i) s = dadd(s, v[i]);
+  }
+  const double dn = static_cast<double>(n);
+  AffineSums q{};
+  q.mmx = __ddiv_rn(__shfl_sync(0xffffffffu, s, 0), dn);
+  q.mmy = __ddiv_rn(__shfl_sync(0xffffffffu, s, 1), dn);
+  q.mrx = __ddiv_rn(__shfl_sync(0xffffffffu, s, 2), dn);
+  q.mry = __ddiv_rn(__shfl_sync(0xffffffffu, s, 3), dn);
+  double c = 0.0;
+  if (lane < 7) {
+    // lane: 0 ax ax, 1 ax ay, 2 ay ay, 3 ax bx, 4 ay bx, 5 ax by, 6 ay by
+    for (int i = 0; i < n; ++i) {
+      const double ax = dsub(mx[i], q.mmx), ay = dsub(my[i], q.mmy);
+      const double u = (lane == 0 || lane == 1 || lane == 3 || lane == 5) ? ax : ay;
+      const double v = lane == 0 ? ax : (lane <= 2 ? ay : (lane <= 4 ? dsub(rx[i], q.mrx) : dsub(ry[i], q.mry)));
+      c = dadd(c, dmul(u, v));
+    }
+  }
+  q.sxx = __shfl_sync(0xffffffffu, c, 0);
+  q.sxy = __shfl_sync(0xffffffffu, c, 1);
+  q.syy = __shfl_sync(0xffffffffu, c, 2);
+  q.sxr = __shfl_sync(0xffffffffu, c, 3);
+  q.syr = __shfl_sync(0xffffffffu, c, 4);
+  q.sxs = __shfl_sync(0xffffffffu, c, 5);
+  q.sys = __shfl_sync(0xffffffffu, c, 6);
+  return affine_from_sums(q, m);
 }
 
 // ---- K1: triangle descriptors, one CTA per catalog row ----------------------------------
@@ -972,6 +1072,7 @@ __device__ void load_job_points(const RegArgs& a, const RegJob& job, JobPoints& 
 constexpr int kScoreWarps = 4;
 
 // Cand::valid bits: 1 = fit succeeded, 2 = count and rms are exact.
+template <int MODEL>
 __global__ void __launch_bounds__(32 * kScoreWarps) reg_score_kernel(RegArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   WarpScratch* ws = reinterpret_cast<WarpScratch*>(smem);
@@ -1008,7 +1109,10 @@ __global__ void __launch_bounds__(32 * kScoreWarps) reg_score_kernel(RegArgs a) 
       const double try_[3] = {jp.ry[rv0], jp.ry[rv1], jp.ry[dr.v[2]]};
       double scratch[6];
       double m[6];
-      ok = fit_similarity(tmx, tmy, trx, try_, 3, scratch, m) ? 1 : 0;
+      if constexpr (MODEL == GG_TRANSFORM_AFFINE)
+        ok = fit_affine(tmx, tmy, trx, try_, 3, m) ? 1 : 0;
+      else
+        ok = fit_similarity(tmx, tmy, trx, try_, 3, scratch, m) ? 1 : 0;
       Cand& cd = cands[c];
       for (int q = 0; q < 6; ++q) {
         cm[warp][lane][q] = ok ? m[q] : 0.0;
@@ -1140,7 +1244,9 @@ __global__ void __launch_bounds__(32) reg_best_kernel(RegArgs a) {
     }
     __syncwarp();
     double m[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    if (!warp_fit_similarity(fx, fy, gx, gy, best_n, buf, m)) break;
+    const bool fitted = a.model == GG_TRANSFORM_AFFINE ? warp_fit_affine(fx, fy, gx, gy, best_n, m)
+                                                       : warp_fit_similarity(fx, fy, gx, gy, best_n, buf, m);
+    if (!fitted) break;
     int n2;
     double r2;
     warp_score_exact(m, jp, a.tol, ws, n2, r2, prs2, a.overflow);
@@ -1255,8 +1361,8 @@ static void reg_scratch_ensure(RegScratch& r, int rows, int jobs, int match_cap,
 }
 
 static void validate_reg(const gg_register_params_t& p) {
-  require(p.transform_model == GG_TRANSFORM_SIMILARITY,
-          "triangle asterism registration on the device supports the similarity model");
+  require(p.transform_model == GG_TRANSFORM_SIMILARITY || p.transform_model == GG_TRANSFORM_AFFINE,
+          "triangle asterism registration supports similarity or affine transforms");
   require(std::isfinite(p.tolerance_px) && p.tolerance_px >= 0.0, "tolerance_px must be non-negative");
   require(std::isfinite(p.descriptor_radius) && p.descriptor_radius >= 0.0, "descriptor_radius must be non-negative");
   require(p.neighbors <= kMaxNeighbors, "neighbors must be at most 6");
@@ -1291,6 +1397,7 @@ static RegArgs make_args(RegScratch& r, int mode, double tol, double radius) {
   a.max_desc = kMaxDesc;
   a.max_cand = kMaxSel;
   a.min_inliers = 0;
+  a.model = GG_TRANSFORM_SIMILARITY;  // the descriptor-list fallback fits similarities
   return a;
 }
 
@@ -1300,6 +1407,7 @@ static void apply_params(RegArgs& a, const gg_register_params_t& p) {
   a.max_desc = std::min(p.max_descriptors, kMaxDesc);
   a.max_cand = p.max_candidates;
   a.min_inliers = p.min_inliers;
+  a.model = p.transform_model;
 }
 
 static void launch_desc(const RegArgs& a, int rows, cudaStream_t stream) {
@@ -1323,11 +1431,12 @@ static void launch_match_score_best(const RegArgs& a, int njobs, int64_t max_sel
   const int64_t per_job = (2 * max_sel + 32 * kScoreWarps - 1) / (32 * kScoreWarps);
   const unsigned gx = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(per_job, 1024)));
   const size_t score_smem = sizeof(WarpScratch) * kScoreWarps;
-  check_cuda(cudaFuncSetAttribute(reg_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(score_smem)),
+  auto score = a.model == GG_TRANSFORM_AFFINE ? reg_score_kernel<GG_TRANSFORM_AFFINE>
+                                              : reg_score_kernel<GG_TRANSFORM_SIMILARITY>;
+  check_cuda(cudaFuncSetAttribute(score, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(score_smem)),
              "cudaFuncSetAttribute(reg_score)");
   note_launch();
-  reg_score_kernel<<<dim3(gx, static_cast<unsigned>(njobs)), 32 * kScoreWarps, score_smem, stream>>>(a);
+  score<<<dim3(gx, static_cast<unsigned>(njobs)), 32 * kScoreWarps, score_smem, stream>>>(a);
   check_cuda(cudaGetLastError(), "reg_score launch");
   note_launch();
   reg_best_kernel<<<njobs, 32, 0, stream>>>(a);

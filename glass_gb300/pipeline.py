@@ -108,6 +108,9 @@ class StepConfig:
     local_normalization_tile: int = 0
     registration_tolerance_px: float = 3.0
     registration_min_inliers: int = 6
+    # "similarity" (the resident triangle path) or "affine" (3-point affine
+    # hypotheses and least-squares affine refits, cpu/registration.py:106-119)
+    registration_model: str = "similarity"
     # sub-pixel translation refinement of the triangle matrices (a coarse
     # +-1 px grid of 0.25 px at stride 4, then +-0.25 px of 0.0625 px at
     # stride 8: the resident run's settings); None skips it
@@ -220,7 +223,10 @@ class ResidentPipeline:
         device catalogs -> (matrices [frames, 3, 3], ok [frames]).  Frames that
         fail keep the identity matrix and are weighted 0 by weights()."""
         cfg = self.config
-        params = _lib.RegisterParams(_lib.GG_TRANSFORM_SIMILARITY, int(cfg.registration_min_inliers),
+        models = {"similarity": _lib.GG_TRANSFORM_SIMILARITY, "affine": _lib.GG_TRANSFORM_AFFINE}
+        if cfg.registration_model not in models:
+            raise ValueError("registration_model must be similarity or affine")
+        params = _lib.RegisterParams(models[cfg.registration_model], int(cfg.registration_min_inliers),
                                      float(cfg.registration_tolerance_px), 0.1, 80, 5, 1200, 1500)
         idx = np.array([i for i in range(self.frames) if i != reference_index], dtype=np.int64)
         matrices = np.tile(np.eye(3), (self.frames, 1, 1))

@@ -547,7 +547,8 @@ int gg_stack_apply_invalid_mask(gg_stack* stack, int64_t index, const uint8_t* h
 /* Parameters of estimate_triangle_asterism_transform
  * (cpu/registration.py:361-373). */
 typedef struct {
-  int32_t transform_model;  /* GG_TRANSFORM_SIMILARITY */
+  int32_t transform_model;  /* GG_TRANSFORM_SIMILARITY (Procrustes fits) or GG_TRANSFORM_AFFINE
+                               (least-squares affine fits, cpu/registration.py:106-119) */
   int32_t min_inliers;      /* 6 */
   double tolerance_px;      /* 3.0 */
   double descriptor_radius; /* 0.1 */

@@ -1,11 +1,12 @@
 """Oracle: triangle-asterism star registration.
 
-Restates src/glass/cpu/registration.py:140-475 (similarity model) with the
-same NumPy arithmetic:
+Restates src/glass/cpu/registration.py:106-475 (similarity and affine
+models) with the same NumPy arithmetic:
 
 - ``local_triangle_descriptors``  :273-303 (+ ``_ordered_triangle_by_sides``
   :242-270, ``_triangle_area`` :236-239)
 - ``fit_similarity``              :140-162 (Procrustes through a 2x2 SVD)
+- ``fit_affine``                  :106-119 (least squares of the 2n x 6 system)
 - ``greedy_pairs`` / ``score``    :177-215
 - ``estimate_triangle_asterism_transform`` :361-475
 - ``similarity_from_descriptors`` the descriptor-list fallback of
@@ -103,6 +104,28 @@ def fit_similarity(moving: np.ndarray, reference: np.ndarray) -> np.ndarray | No
                       dtype=np.float64)
 
 
+def fit_affine(moving: np.ndarray, reference: np.ndarray) -> np.ndarray | None:
+    """registration.py:106-119; None where the reference raises ValueError."""
+    if len(moving) < 3:
+        return None
+    rows, rhs = [], []
+    for (x, y), (rx, ry) in zip(moving, reference):
+        rows.append([x, y, 1.0, 0.0, 0.0, 0.0])
+        rows.append([0.0, 0.0, 0.0, x, y, 1.0])
+        rhs.extend([rx, ry])
+    p, *_ = np.linalg.lstsq(np.asarray(rows, dtype=np.float64), np.asarray(rhs, dtype=np.float64), rcond=None)
+    return np.asarray([[p[0], p[1], p[2]], [p[3], p[4], p[5]], [0.0, 0.0, 1.0]], dtype=np.float64)
+
+
+def fit_model(transform_model: str, moving: np.ndarray, reference: np.ndarray) -> np.ndarray | None:
+    """registration.py:165-174 for the two models of the asterism estimator."""
+    if transform_model == "similarity":
+        return fit_similarity(moving, reference)
+    if transform_model == "affine":
+        return fit_affine(moving, reference)
+    raise ValueError("triangle asterism registration supports similarity or affine transforms")
+
+
 def apply_matrix(points: np.ndarray, matrix: np.ndarray) -> np.ndarray:
     """registration.py:46-51."""
     hom = np.hstack([points, np.ones((points.shape[0], 1), dtype=np.float64)])
@@ -147,8 +170,11 @@ def _failed(reason: str, ndesc=(0, 0), matches=0) -> dict:
 
 def estimate_triangle_asterism_transform(reference, moving, min_inliers: int = 6, tolerance_px: float = 3.0,
                                          max_stars: int = 80, neighbors: int = 5, descriptor_radius: float = 0.1,
-                                         max_descriptors: int = 1200, max_candidates: int = 1500) -> dict:
-    """registration.py:361-475 (similarity)."""
+                                         max_descriptors: int = 1200, max_candidates: int = 1500,
+                                         transform_model: str = "similarity") -> dict:
+    """registration.py:361-475 (similarity or affine fits)."""
+    if transform_model not in ("similarity", "affine"):
+        raise ValueError("triangle asterism registration supports similarity or affine transforms")
     ref = np.asarray(reference, dtype=np.float64).reshape(-1, 2)[: max(0, int(max_stars))]
     mov = np.asarray(moving, dtype=np.float64).reshape(-1, 2)[: max(0, int(max_stars))]
     if len(ref) < 3 or len(mov) < 3:
@@ -170,7 +196,7 @@ def estimate_triangle_asterism_transform(reference, moving, min_inliers: int = 6
         mt = mov[list(midx)]
         rt = ref[list(ridx)]
         for o, rto in enumerate((rt, rt[[1, 0, 2]])):
-            m = fit_similarity(mt, rto)
+            m = fit_model(transform_model, mt, rto)
             if m is None:
                 continue
             pairs, rms = score(ref, mov, m, tolerance_px)
@@ -179,7 +205,7 @@ def estimate_triangle_asterism_transform(reference, moving, min_inliers: int = 6
     for _ in range(3):
         if len(best_pairs) < 3:
             break
-        m = fit_similarity(mov[[p[0] for p in best_pairs]], ref[[p[1] for p in best_pairs]])
+        m = fit_model(transform_model, mov[[p[0] for p in best_pairs]], ref[[p[1] for p in best_pairs]])
         if m is None:
             break
         pairs, rms = score(ref, mov, m, tolerance_px)

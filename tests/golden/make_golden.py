@@ -788,6 +788,84 @@ def make_tile_local(ref_src: Path) -> None:
     np.savez_compressed(HERE / "tile_local.npz", **out)
 
 
+def _affine_catalog(rng, n, linear, dx, dy, noise, extent=2000.0, drop=0, add=0, swap=0):
+    """Reference catalog (n, 2) and a moving catalog that the affine map
+    (linear, (dx, dy)) sends back onto it, with centroid noise, dropped and
+    spurious stars and a perturbed brightness order."""
+    ref = rng.uniform(20.0, extent - 20.0, size=(n, 2))
+    lin = np.asarray(linear, dtype=np.float64)
+    mov = (ref - np.array([dx, dy])) @ np.linalg.inv(lin).T + noise * rng.standard_normal((n, 2))
+    keep = np.sort(rng.permutation(n)[: n - drop])
+    mov = mov[keep]
+    if add:
+        mov = np.vstack([mov, rng.uniform(0.0, extent, size=(add, 2))])
+    order = np.arange(len(mov))
+    for _ in range(swap):
+        i = int(rng.integers(0, len(mov) - 1))
+        order[i], order[i + 1] = order[i + 1], order[i]
+    return ref, mov[order]
+
+
+def make_registration_affine(ref_src: Path) -> None:
+    """estimate_triangle_asterism_transform with transform_model="affine"
+    (src/glass/cpu/registration.py:106-119, 361-475) on seeded catalogs under
+    affine maps (shear and anisotropic scale that a similarity cannot
+    represent), the reference test's similarity case and degenerate inputs."""
+    sys.path.insert(0, str(ref_src))
+    from glass.cpu.registration import estimate_triangle_asterism_transform
+    from glass.cpu.star_detect import Star
+
+    rng = np.random.default_rng(31415)
+    cases = []
+    pts = np.array([(10, 10), (20, 10), (10, 25), (30, 30), (5, 35), (35, 5), (25, 18), (14, 32)], dtype=np.float64)
+    ang = np.deg2rad(-7.0)
+    lin = 0.98 * np.array([[np.cos(ang), -np.sin(ang)], [np.sin(ang), np.cos(ang)]])
+    mov = np.vstack([(pts - np.array([-4.0, 3.0])) @ np.linalg.inv(lin).T, [[100.0, 100.0]]])
+    cases.append(("reftest_outlier", pts, mov, dict(min_inliers=8, tolerance_px=0.5)))
+    specs = [  # (n, linear perturbation sigma, rotation deg, dx, dy, noise, drop, add, swap, params)
+        (80, 1e-3, 0.0, 0.4, -0.3, 0.05, 0, 0, 0, {}),
+        (80, 3e-3, 0.3, 12.5, -7.25, 0.05, 0, 0, 0, {}),
+        (80, 1e-2, -2.0, -40.0, 33.0, 0.1, 5, 5, 6, {}),
+        (60, 2e-2, 4.5, 3.0, 150.0, 0.2, 8, 10, 10, dict(tolerance_px=2.0)),
+        (40, 5e-3, 0.0, 0.5, 0.25, 0.0, 0, 0, 0, dict(neighbors=4)),
+        (80, 2e-3, 1.0, -5.0, 5.0, 0.05, 0, 0, 0, dict(neighbors=6, max_candidates=200)),
+        (80, 4e-3, -0.7, 8.0, -2.0, 0.05, 2, 3, 4, dict(max_descriptors=100, max_candidates=50)),
+        (50, 1e-2, 10.0, 100.0, -80.0, 0.1, 0, 0, 0, dict(max_stars=30)),
+        (25, 1e-3, 0.2, 1.0, 1.0, 0.05, 10, 12, 0, dict(min_inliers=10)),
+        (12, 0.0, 0.0, 2.0, 3.0, 0.0, 0, 0, 0, dict(tolerance_px=1.0)),
+        (80, 1e-3, 180.0, 2000.0, 2000.0, 0.05, 0, 0, 0, {}),
+        (80, 2e-3, 0.5, 3.0, 4.0, 0.05, 0, 0, 0, dict(descriptor_radius=0.02)),
+    ]
+    for k, (n, sig, th, dx, dy, noise, drop, add, swap, params) in enumerate(specs):
+        t = np.deg2rad(th)
+        rot = np.array([[np.cos(t), -np.sin(t)], [np.sin(t), np.cos(t)]])
+        linear = rot @ (np.eye(2) + rng.normal(0.0, sig, (2, 2)))
+        ref, mov = _affine_catalog(rng, n, linear, dx, dy, noise, drop=drop, add=add, swap=swap)
+        cases.append((f"affine{k}", ref, mov, params))
+    line = np.column_stack([np.arange(10) * 7.0, np.arange(10) * 3.0])
+    cases.append(("collinear", line, line + 1.0, {}))
+    cases.append(("two_stars", np.array([[1.0, 2.0], [30.0, 40.0]]), np.array([[2.0, 2.0], [31.0, 40.0]]), {}))
+    cases.append(("empty_moving", rng.uniform(0, 100, (10, 2)), np.zeros((0, 2)), {}))
+
+    arrays: dict[str, np.ndarray] = {}
+    names = []
+    for name, ref, mov, params in cases:
+        rstars = [Star(float(x), float(y), 1000.0 - i) for i, (x, y) in enumerate(ref)]
+        mstars = [Star(float(x), float(y), 1000.0 - i) for i, (x, y) in enumerate(mov)]
+        res = estimate_triangle_asterism_transform(rstars, mstars, "affine", **params)
+        arrays[f"{name}/ref"] = np.asarray(ref, dtype=np.float64).reshape(-1, 2)
+        arrays[f"{name}/mov"] = np.asarray(mov, dtype=np.float64).reshape(-1, 2)
+        arrays[f"{name}/params"] = np.asarray(repr(params))
+        arrays[f"{name}/matrix"] = np.asarray(res.matrix, dtype=np.float64)
+        arrays[f"{name}/inliers"] = np.asarray(res.inliers)
+        arrays[f"{name}/rms_px"] = np.asarray(res.rms_px)
+        arrays[f"{name}/status"] = np.asarray(res.status)
+        arrays[f"{name}/pairs"] = np.asarray(res.pairs, dtype=np.int32).reshape(-1, 2)
+        names.append(name)
+    arrays["_names"] = np.asarray(names)
+    np.savez_compressed(HERE / "registration_affine.npz", **arrays)
+
+
 # ---------------------------------------------------------------------------
 # registration-quality policy (resident_cuda.py:4905-4998,
 # engine/resident_registration_quality.py:41-136)
@@ -847,7 +925,8 @@ def main() -> int:
     ref = Path(args.reference)
     src = ref / "src"
     jobs = {"integration": make_integration, "calibration": make_calibration, "warp": make_warp,
-            "stars": make_stars, "registration": make_registration, "alignment": make_alignment,
+            "stars": make_stars, "registration": make_registration,
+            "registration_affine": make_registration_affine, "alignment": make_alignment,
             "local_norm": make_local_norm, "cosmetic": make_cosmetic, "dq": make_dq,
             "tile_local": make_tile_local, "quality": make_quality}
     only = [j for j in args.only.split(",") if j] or list(jobs)
