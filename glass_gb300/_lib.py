@@ -374,6 +374,8 @@ PROTOTYPES: dict[str, list] = {
                                       ctypes.c_int64, _P],
     "gg_stack_calibrate_u16": [_P, _P, ctypes.c_int64, _P, ctypes.c_int, ctypes.POINTER(CalibParams)],
     "gg_stack_calibrate_u16_device": [_P, _P, ctypes.c_int64, _P, ctypes.c_int, ctypes.POINTER(CalibParams)],
+    "gg_stack_upload_raw_u16": [_P, _P, ctypes.c_int64, _P],
+    "gg_stack_calibrate_u16_staged": [_P, _P, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(CalibParams)],
     "gg_stack_calibrate_f32": [_P, ctypes.c_int64, _P, ctypes.POINTER(CalibParams)],
     "gg_stack_frame_stats": [_P, _P, ctypes.c_int64, _P],
     "gg_stack_compute_weights": [_P, ctypes.c_int, _P, ctypes.c_float, _P],

@@ -279,6 +279,45 @@ int gg_stack_calibrate_u16(gg_stack* s, const int64_t* indices, int64_t count, c
   GG_API_END
 }
 
+// ---- staged ingest: uploads run ahead of the per-frame stages ---------------
+// A device copy of every frame's raw uint16 samples (frames x P) filled from
+// pinned host memory on the copy stream, one event per frame when its copy
+// has landed and one when its calibration has read it: the caller enqueues
+// the uploads of a whole stack at once and calibrates (and processes) the
+// frames in chunks while later chunks are still in flight.
+struct RawStage {
+  uint16_t* d_raw = nullptr;
+  std::vector<cudaEvent_t> ready;     // the frame's upload has landed
+  std::vector<cudaEvent_t> consumed;  // the frame's calibration has read it
+  std::vector<unsigned char> uploaded;
+};
+
+static void raw_stage_release(RawStage* r) {
+  if (r->d_raw) cudaFree(r->d_raw);
+  for (cudaEvent_t e : r->ready) cudaEventDestroy(e);
+  for (cudaEvent_t e : r->consumed) cudaEventDestroy(e);
+  delete r;
+}
+
+static RawStage& raw_stage(gg_stack* s) {
+  if (!s->raw_stage) {
+    auto* r = new RawStage();
+    s->raw_stage = r;
+    s->raw_stage_free = [](void* q) { raw_stage_release(static_cast<RawStage*>(q)); };
+    const size_t bytes = static_cast<size_t>(s->frames) * static_cast<size_t>(s->pixels) * 2;
+    check_cuda(cudaMalloc(&r->d_raw, bytes), "cudaMalloc(raw staging)");
+    s->bytes_allocated += static_cast<int64_t>(bytes);
+    r->ready.assign(static_cast<size_t>(s->frames), nullptr);
+    r->consumed.assign(static_cast<size_t>(s->frames), nullptr);
+    r->uploaded.assign(static_cast<size_t>(s->frames), 0);
+    for (int64_t k = 0; k < s->frames; ++k) {
+      check_cuda(cudaEventCreateWithFlags(&r->ready[k], cudaEventDisableTiming), "cudaEventCreate(raw ready)");
+      check_cuda(cudaEventCreateWithFlags(&r->consumed[k], cudaEventDisableTiming), "cudaEventCreate(raw read)");
+    }
+  }
+  return *static_cast<RawStage*>(s->raw_stage);
+}
+
 int gg_stack_calibrate_u16_device(gg_stack* s, const int64_t* indices, int64_t count, const void* dev_raw,
                                   int big_endian_bzero, const gg_calib_params_t* params) {
   GG_API_BEGIN
@@ -296,6 +335,62 @@ int gg_stack_calibrate_u16_device(gg_stack* s, const int64_t* indices, int64_t c
     job.nframes = nb;
     for (int i = 0; i < nb; ++i) job.frame[i] = static_cast<int>(indices[k0 + i]);
     launch_calibrate(s, job, *params);
+  }
+  for (int64_t k = 0; k < count; ++k) stack_mark_loaded(s, indices[k]);
+  GG_API_END
+}
+
+int gg_stack_upload_raw_u16(gg_stack* s, const int64_t* indices, int64_t count, const void* host_raw) {
+  GG_API_BEGIN
+  require(s != nullptr && indices != nullptr && host_raw != nullptr, "null argument");
+  require(count > 0, "indices must contain at least one frame index");
+  for (int64_t k = 0; k < count; ++k) stack_require_index(s, indices[k]);
+  require(is_pinned(host_raw), "staged uploads need page-locked (pinned) host memory");
+  stack_activate(s);
+  RawStage& r = raw_stage(s);
+  const size_t frame_bytes = static_cast<size_t>(s->pixels) * 2;
+  const auto* src = static_cast<const unsigned char*>(host_raw);
+  for (int64_t k = 0; k < count; ++k) {
+    const int64_t f = indices[k];
+    // the previous calibration of this frame must have read its staged copy
+    check_cuda(cudaStreamWaitEvent(s->copy_stream, r.consumed[f], 0), "cudaStreamWaitEvent(raw read)");
+    check_cuda(cudaMemcpyAsync(reinterpret_cast<unsigned char*>(r.d_raw) + static_cast<size_t>(f) * frame_bytes,
+                               src + static_cast<size_t>(k) * frame_bytes, frame_bytes, cudaMemcpyHostToDevice,
+                               s->copy_stream),
+               "cudaMemcpyAsync(raw staging)");
+    check_cuda(cudaEventRecord(r.ready[f], s->copy_stream), "cudaEventRecord(raw ready)");
+    r.uploaded[f] = 1;
+  }
+  GG_API_END
+}
+
+int gg_stack_calibrate_u16_staged(gg_stack* s, const int64_t* indices, int64_t count, int big_endian_bzero,
+                                  const gg_calib_params_t* params) {
+  GG_API_BEGIN
+  require(s != nullptr && indices != nullptr, "null argument");
+  require(count > 0, "indices must contain at least one frame index");
+  validate_calib(params);
+  for (int64_t k = 0; k < count; ++k) stack_require_index(s, indices[k]);
+  require(s->raw_stage != nullptr, "no staged raw frames: call gg_stack_upload_raw_u16 first");
+  RawStage& r = raw_stage(s);
+  for (int64_t k = 0; k < count; ++k) require(r.uploaded[indices[k]] != 0, "frame has no staged raw samples");
+  stack_activate(s);
+  // runs of consecutive frame indices share one launch (their staged copies are contiguous)
+  int64_t k0 = 0;
+  while (k0 < count) {
+    int64_t k1 = k0 + 1;
+    while (k1 < count && k1 - k0 < GG_MAX_BATCH_FRAMES && indices[k1] == indices[k1 - 1] + 1) ++k1;
+    for (int64_t k = k0; k < k1; ++k)
+      check_cuda(cudaStreamWaitEvent(s->stream, r.ready[indices[k]], 0), "cudaStreamWaitEvent(raw ready)");
+    CalibLaunch job{};
+    job.raw = r.d_raw + static_cast<size_t>(indices[k0]) * static_cast<size_t>(s->pixels);
+    job.big_endian_bzero = big_endian_bzero;
+    job.nframes = static_cast<int>(k1 - k0);
+    for (int64_t k = k0; k < k1; ++k) job.frame[k - k0] = static_cast<int>(indices[k]);
+    launch_calibrate(s, job, *params);
+    for (int64_t k = k0; k < k1; ++k)
+      check_cuda(cudaEventRecord(r.consumed[indices[k]], s->stream), "cudaEventRecord(raw read)");
+    k0 = k1;
   }
   for (int64_t k = 0; k < count; ++k) stack_mark_loaded(s, indices[k]);
   GG_API_END

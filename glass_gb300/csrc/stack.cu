@@ -147,6 +147,7 @@ static void stack_free(gg_stack* s) {
   if (s->gn_scratch && s->gn_scratch_free) s->gn_scratch_free(s->gn_scratch);
   if (s->step_graph && s->step_graph_free) s->step_graph_free(s->step_graph);
   if (s->ln_scratch && s->ln_scratch_free) s->ln_scratch_free(s->ln_scratch);
+  if (s->raw_stage && s->raw_stage_free) s->raw_stage_free(s->raw_stage);
   void* dev_ptrs[] = {s->d_slots,    s->d_slot_of_frame, s->d_spare_slot, s->d_frame_nonfinite,
                       s->d_bias,     s->d_dark,          s->d_flat,       s->d_master,
                       s->d_weight,   s->d_coverage,      s->d_low,        s->d_high,

@@ -106,6 +106,8 @@ struct gg_stack {
   void (*step_graph_free)(void*) = nullptr;
   void* ln_scratch = nullptr;  // local normalisation (localnorm.cu)
   void (*ln_scratch_free)(void*) = nullptr;
+  void* raw_stage = nullptr;  // staged raw frames for pipelined ingest (calibrate.cu)
+  void (*raw_stage_free)(void*) = nullptr;
 
   // Fused warp-integration: per-frame inverse matrices, per-frame
   // non-finite sample counts of the virtual warped stack and the geometric

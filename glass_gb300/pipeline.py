@@ -196,67 +196,93 @@ class ResidentPipeline:
         _lib.call("gg_stack_calibrate_u16_device", self.stack.handle, _lib.ptr(self._indices),
                   ctypes.c_int64(self.frames), ctypes.c_void_p(dev_raw_ptr), 0, ctypes.byref(self._calib_params()))
 
+    def upload_raw(self, host_raw: np.ndarray) -> None:
+        """Enqueues the host-to-device copies of every frame's raw uint16
+        samples (page-locked host memory) and returns at once; calibrate_staged
+        then waits, on the device, for the frames it calibrates."""
+        _lib.call("gg_stack_upload_raw_u16", self.stack.handle, _lib.ptr(self._indices), ctypes.c_int64(self.frames),
+                  _lib.ptr(host_raw))
+
+    def calibrate_staged(self, frames) -> None:
+        """Calibrates `frames` from their staged raw samples (upload_raw)."""
+        idx = np.ascontiguousarray(np.asarray(frames, dtype=np.int64))
+        _lib.call("gg_stack_calibrate_u16_staged", self.stack.handle, _lib.ptr(idx), ctypes.c_int64(idx.size), 0,
+                  ctypes.byref(self._calib_params()))
+
     def calibrate_host(self, host_raw: np.ndarray) -> None:
         """uint16 frames in host memory (pinned for full-speed copies)."""
         _lib.call("gg_stack_calibrate_u16", self.stack.handle, _lib.ptr(self._indices),
                   ctypes.c_int64(self.frames), _lib.ptr(host_raw), 0, ctypes.byref(self._calib_params()))
 
-    def detect(self, info: bool = False) -> list[dict] | None:
-        """Star catalogs of every frame; they stay on the device for register().
-        info=True also returns each frame's background statistics, candidate
-        count and catalog size."""
+    def detect(self, info: bool = False, frames=None) -> list[dict] | None:
+        """Star catalogs of every frame (or of `frames`); they stay on the
+        device for register().  info=True also returns each frame's background
+        statistics, candidate count and catalog size."""
         cfg = self.config
+        indices = self._indices if frames is None else np.ascontiguousarray(np.asarray(frames, dtype=np.int64))
         params = _lib.StarParams(float(cfg.star_threshold_sigma), int(cfg.star_max_stars), 4, 2.0, np.nan, np.nan,
                                  float(cfg.catalog_min_fwhm), float(cfg.catalog_max_eccentricity),
                                  int(cfg.background_mesh_cell))
-        host_info = (_lib.StarFrameInfo * self.frames)() if info else None
-        counts = np.zeros(self.frames, dtype=np.int32) if info else None
-        _lib.call("gg_stack_detect_stars", self.stack.handle, _lib.ptr(self._indices), ctypes.c_int64(self.frames),
+        host_info = (_lib.StarFrameInfo * indices.size)() if info else None
+        counts = np.zeros(indices.size, dtype=np.int32) if info else None
+        _lib.call("gg_stack_detect_stars", self.stack.handle, _lib.ptr(indices), ctypes.c_int64(indices.size),
                   ctypes.byref(params), None, None if counts is None else _lib.ptr(counts), host_info)
         if not info:
             return None
-        return [{"frame": k, "median": float(r.median), "noise": float(r.noise), "threshold": float(r.threshold),
-                 "candidates": int(r.candidates), "stars": int(counts[k])} for k, r in enumerate(host_info)]
+        return [{"frame": int(k), "median": float(r.median), "noise": float(r.noise), "threshold": float(r.threshold),
+                 "candidates": int(r.candidates), "stars": int(counts[pos])}
+                for pos, (k, r) in enumerate(zip(indices, host_info))]
 
-    def register(self, reference_index: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    def register(self, reference_index: int = 0, frames=None) -> tuple[np.ndarray, np.ndarray]:
         """Triangle registration of every frame to the reference frame from the
         device catalogs -> (matrices [frames, 3, 3], ok [frames]).  Frames that
-        fail keep the identity matrix and are weighted 0 by weights()."""
+        fail keep the identity matrix and are weighted 0 by weights().  With
+        `frames`, only those are registered and the earlier results of the
+        others are kept (chunked processing; start with a call that includes
+        the reference frame or with frames=None)."""
         cfg = self.config
         models = {"similarity": _lib.GG_TRANSFORM_SIMILARITY, "affine": _lib.GG_TRANSFORM_AFFINE}
         if cfg.registration_model not in models:
             raise ValueError("registration_model must be similarity or affine")
         params = _lib.RegisterParams(models[cfg.registration_model], int(cfg.registration_min_inliers),
                                      float(cfg.registration_tolerance_px), 0.1, 80, 5, 1200, 1500)
-        idx = np.array([i for i in range(self.frames) if i != reference_index], dtype=np.int64)
-        matrices = np.tile(np.eye(3), (self.frames, 1, 1))
-        ok = np.ones(self.frames, dtype=bool)
+        subset = list(range(self.frames)) if frames is None else [int(k) for k in frames]
+        idx = np.array([i for i in subset if i != reference_index], dtype=np.int64)
+        fresh = frames is None or reference_index in subset or getattr(self, "_reg_matrices", None) is None
+        if fresh:
+            self._reg_matrices = np.tile(np.eye(3), (self.frames, 1, 1))
+            self._registered = np.ones(self.frames, dtype=bool)
+            self._accepted = self._registered.copy()
+            self._multipliers = np.ones(self.frames, dtype=np.float64)
+            self.last_registration = []
+            self.last_refinement = []
+            self.last_quality = []
+        matrices, ok = self._reg_matrices, self._registered
         if idx.size:
             out = (_lib.Registration * idx.size)()
             _lib.call("gg_stack_register_frames", self.stack.handle, ctypes.c_int64(int(reference_index)),
                       _lib.ptr(idx), ctypes.c_int64(idx.size), ctypes.byref(params), out)
             for pos, k in enumerate(idx):
                 ok[k] = out[pos].status == 1
-                if ok[k]:
-                    matrices[k] = np.asarray(out[pos].matrix, dtype=np.float64).reshape(3, 3)
-            self.last_registration = [
+                matrices[k] = np.asarray(out[pos].matrix, dtype=np.float64).reshape(3, 3) if ok[k] else np.eye(3)
+                self._accepted[k] = ok[k]
+                self._multipliers[k] = 1.0
+            self.last_registration = [r for r in self.last_registration if r["frame"] not in set(idx.tolist())] + [
                 {"frame": int(k), "status": int(r.status), "inliers": int(r.inliers), "matches": int(r.matches),
                  "descriptors_reference": int(r.descriptors_reference),
                  "descriptors_moving": int(r.descriptors_moving), "rms_px": float(r.rms_px)}
                 for k, r in zip(idx, out)]
-        self._registered = ok
-        self._accepted = ok.copy()
-        self._multipliers = np.ones(self.frames, dtype=np.float64)
-        return matrices, ok
+        return matrices.copy(), ok.copy()
 
-    def refine(self, matrices: np.ndarray, reference_index: int = 0) -> np.ndarray:
+    def refine(self, matrices: np.ndarray, reference_index: int = 0, frames=None) -> np.ndarray:
         """Sub-pixel translation refinement (config.refine) of the registered
-        frames' matrices against the reference frame; returns new matrices."""
+        frames' matrices (all, or `frames`) against the reference frame;
+        returns new matrices."""
         cfg = self.config
         ok = getattr(self, "_registered", None)
         out = np.array(matrices, dtype=np.float64, copy=True)
-        good = np.array([k for k in range(self.frames) if k != reference_index and (ok is None or ok[k])],
-                        dtype=np.int64)
+        subset = range(self.frames) if frames is None else [int(k) for k in frames]
+        good = np.array([k for k in subset if k != reference_index and (ok is None or ok[k])], dtype=np.int64)
         if cfg.refine_method == "gradient":
             if good.size == 0:
                 return out
@@ -264,7 +290,9 @@ class ResidentPipeline:
             gp["sample_stride"], gp["row_stride"] = gradient_sample_grid(gp, self.height, self.width)
             gp.pop("target_samples", None)
             res = self.stack.refine_matrix_gradient_batch_to_reference(reference_index, good, out[good], **gp)
-            self.last_refinement = [dict(r, frame=int(k)) for k, r in zip(good, res)]
+            done = set(good.tolist()) if frames is not None else None
+            kept = [r for r in getattr(self, "last_refinement", []) if done is not None and r["frame"] not in done]
+            self.last_refinement = kept + [dict(r, frame=int(k)) for k, r in zip(good, res)]
             for k, r in zip(good, res):
                 if r["ok"]:
                     out[k] = r["matrix"]
@@ -306,21 +334,31 @@ class ResidentPipeline:
             outcomes.append(res)
         return out, outcomes
 
-    def assess(self, matrices: np.ndarray, reference_index: int = 0) -> list[dict]:
-        """Registration quality of every registered frame under its final
-        matrix (run before warp()): the inlier / fit-RMS gate, then the
-        pixel-agreement score and policy.  Frames that fail get weight 0 in
-        weights(); downweighted frames get the policy's multiplier.  Returns
-        one record per moving frame (one host synchronisation)."""
+    def assess(self, matrices: np.ndarray, reference_index: int = 0, frames=None) -> list[dict]:
+        """Registration quality of every registered frame (or of `frames`)
+        under its final matrix (run before warp()): the inlier / fit-RMS gate,
+        then the pixel-agreement score and policy.  Frames that fail get
+        weight 0 in weights(); downweighted frames get the policy's
+        multiplier.  Returns one record per assessed moving frame (one host
+        synchronisation)."""
         from glass_gb300 import quality
 
         cfg = self.config
         ag = dict(DEFAULT_AGREEMENT, **(cfg.agreement or {}))
-        ok = getattr(self, "_registered", np.ones(self.frames, dtype=bool)).copy()
+        registered = getattr(self, "_registered", np.ones(self.frames, dtype=bool))
+        subset = range(self.frames) if frames is None else [int(k) for k in frames]
+        if frames is None or not hasattr(self, "_accepted"):
+            ok = registered.copy()
+            mult = np.ones(self.frames, dtype=np.float64)
+        else:
+            ok = self._accepted.copy()
+            mult = self._multipliers.copy()
+            for k in subset:
+                ok[k] = registered[k]
+                mult[k] = 1.0
         regs = {r["frame"]: r for r in getattr(self, "last_registration", [])}
-        mult = np.ones(self.frames, dtype=np.float64)
         records = []
-        for k in range(self.frames):
+        for k in subset:
             if k == reference_index or not ok[k] or k not in regs:
                 continue
             r = regs[k]
@@ -348,14 +386,19 @@ class ResidentPipeline:
                 mult[k] = pol["weight_multiplier"]
         self._accepted = ok
         self._multipliers = mult
-        self.last_quality = records
+        if frames is None:
+            self.last_quality = records
+        else:
+            done = {rec["frame"] for rec in records}
+            self.last_quality = [r for r in getattr(self, "last_quality", []) if r["frame"] not in done] + records
         return records
 
-    def warp(self, matrices: np.ndarray, reference_index: int = 0) -> None:
-        """Warps every frame but the reference through its moving->reference matrix."""
+    def warp(self, matrices: np.ndarray, reference_index: int = 0, frames=None) -> None:
+        """Warps every frame (or every one of `frames`) but the reference
+        through its moving->reference matrix."""
         ok = getattr(self, "_registered", None)
-        idx = np.array([i for i in range(self.frames) if i != reference_index and (ok is None or ok[i])],
-                       dtype=np.int64)
+        subset = range(self.frames) if frames is None else [int(k) for k in frames]
+        idx = np.array([i for i in subset if i != reference_index and (ok is None or ok[i])], dtype=np.int64)
         if idx.size == 0:
             return
         mats = np.ascontiguousarray(np.asarray(matrices, dtype=np.float64)[idx])
@@ -419,19 +462,45 @@ class ResidentPipeline:
         self.local_normalize()
         self.integrate()
 
+    def frame_chunks(self, parts: int = 2) -> list[list[int]]:
+        """Frame chunks of the staged step: `parts` runs of consecutive frames
+        (the first holds the reference frame 0, whose catalog every
+        registration needs).  Few, large chunks: the catalog and registration
+        kernels run one CTA per frame, so small chunks leave SMs idle, while
+        the second half's copy (about 60 ms of a 9600 x 6422 x 200 stack) still
+        hides behind the first half's stages."""
+        parts = max(1, min(int(parts), self.frames))
+        bounds = [round(i * self.frames / parts) for i in range(parts + 1)]
+        return [list(range(a, b)) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+
     def step_host(self, host_raw: np.ndarray, matrices: np.ndarray | None = None, register: bool = False,
-                  out: tuple | None = None):
+                  out: tuple | None = None, staged: bool = True):
         """Public-API step from host memory to host maps (end to end).  With
-        register=True the matrices come from detect() + register(); `out`
+        register=True the matrices come from detect() + register() + refine()
+        + assess().  With staged=True (page-locked host_raw) the raw frames of
+        the whole stack are uploaded on the copy stream up front and the
+        per-frame stages run chunk by chunk (frame_chunks) while the later
+        chunks are still in flight, so the host-to-device copy overlaps the
+        step's own work; the integration waits for every frame.  `out`
         optionally supplies the six map buffers (see download_maps)."""
-        self.calibrate_host(host_raw)
-        if register:
-            self.detect()
-            matrices, _ok = self.register()
-            matrices = self.refine(matrices)
-            self.assess(matrices)
-        if matrices is not None:
-            self.warp(matrices)
+        if staged and register:
+            self.upload_raw(host_raw)
+            for chunk in self.frame_chunks():
+                self.calibrate_staged(chunk)
+                self.detect(frames=chunk)
+                mats, _ok = self.register(0, frames=chunk)
+                mats = self.refine(mats, 0, frames=chunk)
+                self.assess(mats, 0, frames=chunk)
+                self.warp(mats, 0, frames=chunk)
+        else:
+            self.calibrate_host(host_raw)
+            if register:
+                self.detect()
+                matrices, _ok = self.register()
+                matrices = self.refine(matrices)
+                self.assess(matrices)
+            if matrices is not None:
+                self.warp(matrices)
         self.weights()
         self.local_normalize()
         self.integrate()

@@ -149,6 +149,20 @@ int gg_stack_calibrate_u16(gg_stack* stack, const int64_t* indices, int64_t coun
 int gg_stack_calibrate_u16_device(gg_stack* stack, const int64_t* indices, int64_t count,
                                   const void* dev_raw, int big_endian_bzero,
                                   const gg_calib_params_t* params);
+/* Staged ingest (no counterpart in the reference, whose resident path reads,
+ * uploads and calibrates frame by frame): gg_stack_upload_raw_u16 enqueues
+ * the host-to-device copies of `count` frames (host_raw: page-locked,
+ * count*H*W uint16 in the order of indices) into a device staging copy of
+ * the stack's raw samples (allocated on first use: frames*H*W*2 bytes) on
+ * the stack's copy stream and returns at once; gg_stack_calibrate_u16_staged
+ * then calibrates any subset of the staged frames on the stack stream, each
+ * launch waiting (on the device) only for its own frames' copies.  A caller
+ * uploads a whole stack and processes it chunk by chunk while the later
+ * chunks are still in flight.  A frame's staged samples may be uploaded
+ * again once its calibration has been enqueued. */
+int gg_stack_upload_raw_u16(gg_stack* stack, const int64_t* indices, int64_t count, const void* host_raw);
+int gg_stack_calibrate_u16_staged(gg_stack* stack, const int64_t* indices, int64_t count, int big_endian_bzero,
+                                  const gg_calib_params_t* params);
 /* Replaces calibrate_frame(i, light_f32, t_L, t_D, policy) (native_bindings.cpp:5979). */
 int gg_stack_calibrate_f32(gg_stack* stack, int64_t index, const float* host_light,
                            const gg_calib_params_t* params);
