@@ -62,6 +62,9 @@ struct StarFrameState {
   unsigned below;             // finite keys under band_lo
   unsigned inside;            // keys in the band (appended, may exceed capacity)
   int resolved[2];            // 1: the order statistic came from the band
+  // radix select inside the band (bracket_band_* kernels)
+  unsigned band_prefix[2], band_rank[2];
+  int band_ok, band_shift;
 };
 
 __device__ __forceinline__ unsigned float_key(float v) {
@@ -263,6 +266,9 @@ struct BracketArgs {
   unsigned* band;      // [count][band_cap]
   int64_t band_cap;
   int mode;            // 0: v, 1: |v - median|
+  unsigned* ghist;     // [count][2][256] band histograms (zero between passes)
+  int pass;            // radix pass of the band select (0..3)
+  int count_frames;
 };
 
 __device__ __forceinline__ bool bracket_key(float v, int mode, float median, unsigned& key) {
@@ -439,70 +445,101 @@ __global__ void __launch_bounds__(kBracketThreads) bracket_pass_kernel(BracketAr
   }
 }
 
-// One CTA per frame: the two middle ranks' keys inside the band by an MSB-
-// first radix select over key - band_lo (8 bits per pass, shared
-// histograms), then the median / MAD as the float32 mean of the two middle
-// values (np.median).
-__global__ void __launch_bounds__(1024) bracket_resolve_kernel(BracketArgs a) {
-  __shared__ unsigned hist[2][256];
-  __shared__ unsigned s_prefix[2], s_rank[2];
-  __shared__ int s_ok;
+// The two middle ranks' keys inside the band by an MSB-first radix select
+// over key - band_lo (8 bits per pass), then the median / MAD as the float32
+// mean of the two middle values (np.median).  The band of a 9600 x 6422
+// frame holds ~1.6 M keys, so each pass spreads it over several CTAs per
+// frame (shared histograms merged into a per-frame global histogram) and one
+// warp per frame picks the digit:
+//   bracket_band_init   the ranks inside the band (or no band select when
+//                       the order statistics lie outside it: the radix
+//                       fallback then takes the frame), passes from the
+//                       bits of the band's key range
+//   bracket_band_hist   per pass, CTAs x frames
+//   bracket_band_digit  per pass, one warp per frame
+//   bracket_band_finish the value of the two ranks
+__global__ void bracket_band_init_kernel(BracketArgs a) {
   const int k = blockIdx.x;
   StarFrameState& st = a.state[k];
-  const unsigned* band = a.band + static_cast<int64_t>(k) * a.band_cap;
-  if (threadIdx.x == 0) {
-    const unsigned n = st.count;
-    const unsigned rhi = n / 2, rlo = (n & 1u) ? rhi : (rhi > 0 ? rhi - 1 : 0);
-    const bool ok = n > 0 && static_cast<int64_t>(st.inside) <= a.band_cap && st.below <= rlo &&
-                    rhi < st.below + st.inside;
-    s_ok = ok ? 1 : 0;
-    s_rank[0] = ok ? rlo - st.below : 0u;
-    s_rank[1] = ok ? rhi - st.below : 0u;
-    s_prefix[0] = s_prefix[1] = 0u;
-    st.resolved[a.mode] = 0;
-    if (!ok && a.mode == 0) st.count = 0u;  // the radix passes count the finite pixels again
-  }
-  __syncthreads();
-  if (!s_ok) return;
-  const unsigned lo = st.band_lo;
-  const unsigned range = st.band_hi - lo;
+  unsigned* g = a.ghist + static_cast<int64_t>(k) * 512;
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) g[i] = 0u;
+  if (threadIdx.x != 0) return;
+  const unsigned n = st.count;
+  const unsigned rhi = n / 2, rlo = (n & 1u) ? rhi : (rhi > 0 ? rhi - 1 : 0);
+  const bool ok = n > 0 && static_cast<int64_t>(st.inside) <= a.band_cap && st.below <= rlo &&
+                  rhi < st.below + st.inside;
+  st.band_ok = ok ? 1 : 0;
+  st.band_rank[0] = ok ? rlo - st.below : 0u;
+  st.band_rank[1] = ok ? rhi - st.below : 0u;
+  st.band_prefix[0] = st.band_prefix[1] = 0u;
+  st.resolved[a.mode] = 0;
+  if (!ok && a.mode == 0) st.count = 0u;  // the radix passes count the finite pixels again
+  const unsigned range = st.band_hi - st.band_lo;
   int top = 0;  // bits of the key range
   while (top < 32 && (range >> top) != 0u) ++top;
-  const int m = static_cast<int>(st.inside);
-  for (int shift = ((top + 7) / 8) * 8 - 8; shift >= 0; shift -= 8) {
-    for (int i = threadIdx.x; i < 512; i += blockDim.x) (&hist[0][0])[i] = 0u;
-    __syncthreads();
-    const unsigned pre0 = s_prefix[0], pre1 = s_prefix[1];
-    const int hi_shift = shift + 8;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-      const unsigned d = band[i] - lo;
-      const unsigned hp = hi_shift >= 32 ? 0u : (d >> hi_shift);
-      const unsigned digit = (d >> shift) & 255u;
-      if (hp == pre0) atomicAdd(&hist[0][digit], 1u);
-      if (hp == pre1 && pre1 != pre0) atomicAdd(&hist[1][digit], 1u);
-    }
-    __syncthreads();
-    if (threadIdx.x < 2) {
-      const int r = threadIdx.x;
-      const unsigned* h = (r == 1 && s_prefix[1] == s_prefix[0]) ? hist[0] : hist[r];
-      unsigned rank = s_rank[r];
-      int b = 0;
-      while (b < 255 && rank >= h[b]) {
-        rank -= h[b];
-        ++b;
-      }
-      s_rank[r] = rank;
-      s_prefix[r] = (s_prefix[r] << 8) | static_cast<unsigned>(b);
-    }
-    __syncthreads();
+  st.band_shift = ((top + 7) / 8) * 8 - 8;  // first pass's digit shift (< 0: a one-value band)
+}
+
+__global__ void __launch_bounds__(256) bracket_band_hist_kernel(BracketArgs a) {
+  __shared__ unsigned hist[2][256];
+  const int k = blockIdx.y;
+  const StarFrameState& st = a.state[k];
+  const int shift = st.band_shift - 8 * a.pass;
+  if (!st.band_ok || shift < 0) return;
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) (&hist[0][0])[i] = 0u;
+  __syncthreads();
+  const unsigned lo = st.band_lo, pre0 = st.band_prefix[0], pre1 = st.band_prefix[1];
+  const int hi_shift = shift + 8;
+  const unsigned* band = a.band + static_cast<int64_t>(k) * a.band_cap;
+  const int64_t m = st.inside;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < m; i += int64_t(gridDim.x) * blockDim.x) {
+    const unsigned d = band[i] - lo;
+    const unsigned hp = hi_shift >= 32 ? 0u : (d >> hi_shift);
+    const unsigned digit = (d >> shift) & 255u;
+    if (hp == pre0) atomicAdd(&hist[0][digit], 1u);
+    if (hp == pre1 && pre1 != pre0) atomicAdd(&hist[1][digit], 1u);
   }
-  if (threadIdx.x == 0) {
-    const float vlo = key_float(lo + s_prefix[0]);
-    const float vhi = key_float(lo + s_prefix[1]);
-    const float med = __fmul_rn(__fadd_rn(vlo, vhi), 0.5f);
-    if (a.mode == 0) st.median = med; else st.mad = med;
-    st.resolved[a.mode] = 1;
+  __syncthreads();
+  unsigned* g = a.ghist + static_cast<int64_t>(k) * 512;
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+    const unsigned c = (&hist[0][0])[i];
+    if (c) atomicAdd(g + i, c);
   }
+}
+
+__global__ void bracket_band_digit_kernel(BracketArgs a) {
+  const int k = blockIdx.x;
+  StarFrameState& st = a.state[k];
+  const int shift = st.band_shift - 8 * a.pass;
+  if (!st.band_ok || shift < 0) return;
+  unsigned* g = a.ghist + static_cast<int64_t>(k) * 512;
+  if (threadIdx.x < 2) {
+    const int r = threadIdx.x;
+    const unsigned* h = (r == 1 && st.band_prefix[1] == st.band_prefix[0]) ? g : g + 256 * r;
+    unsigned rank = st.band_rank[r];
+    int b = 0;
+    while (b < 255 && rank >= h[b]) {
+      rank -= h[b];
+      ++b;
+    }
+    __syncwarp(0x3u);
+    st.band_rank[r] = rank;
+    st.band_prefix[r] = (st.band_prefix[r] << 8) | static_cast<unsigned>(b);
+  }
+  __syncwarp();
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) g[i] = 0u;  // ready for the next pass
+}
+
+__global__ void bracket_band_finish_kernel(BracketArgs a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.count_frames) return;
+  StarFrameState& st = a.state[k];
+  if (!st.band_ok) return;
+  const float vlo = key_float(st.band_lo + st.band_prefix[0]);
+  const float vhi = key_float(st.band_lo + st.band_prefix[1]);
+  const float med = __fmul_rn(__fadd_rn(vlo, vhi), 0.5f);
+  if (a.mode == 0) st.median = med; else st.mad = med;
+  st.resolved[a.mode] = 1;
 }
 
 // Threshold from median / MAD (star_detect.py:29-43, 133-137).
@@ -1488,6 +1525,10 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
       sc.band_elems = band_cap * count;
     }
     BracketArgs ba{s->d_slots, s->d_slot_of_frame, s->stride, s->pixels, sc.frames, sc.state, sc.band, band_cap, 0};
+    ba.ghist = sc.hist;  // [count][2][kSelBins] >= 512 words per frame; the radix fallback zeroes it again
+    ba.count_frames = count;
+    // CTAs per frame for the band histograms: about eight waves of the GPU's SMs over all frames
+    const unsigned band_ctas = static_cast<unsigned>(std::max(1, std::min(64, sm_count() * 8 / std::max(count, 1))));
     const int samples = static_cast<int>(std::min<int64_t>(kBracketSamples, s->pixels));
     int sample_pow2 = 1;
     while (sample_pow2 < samples) sample_pow2 <<= 1;
@@ -1504,8 +1545,17 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
         bracket_pass_kernel<0><<<dim3(per_frame, static_cast<unsigned>(count)), kBracketThreads, 0, s->stream>>>(ba);
       else
         bracket_pass_kernel<1><<<dim3(per_frame, static_cast<unsigned>(count)), kBracketThreads, 0, s->stream>>>(ba);
-      bracket_resolve_kernel<<<static_cast<unsigned>(count), 1024, 0, s->stream>>>(ba);
       check_cuda(cudaGetLastError(), "bracket select launch");
+      note_launch(2);
+      bracket_band_init_kernel<<<static_cast<unsigned>(count), 32, 0, s->stream>>>(ba);
+      for (int pass = 0; pass < 4; ++pass) {
+        ba.pass = pass;
+        note_launch(2);
+        bracket_band_hist_kernel<<<dim3(band_ctas, static_cast<unsigned>(count)), 256, 0, s->stream>>>(ba);
+        bracket_band_digit_kernel<<<static_cast<unsigned>(count), 32, 0, s->stream>>>(ba);
+      }
+      bracket_band_finish_kernel<<<(count + 127) / 128, 128, 0, s->stream>>>(ba);
+      check_cuda(cudaGetLastError(), "bracket band select launch");
       // frames the bracket could not settle: three-pass radix select
       for (int pass = 0; pass < 3; ++pass) {
         sa.pass = pass;
