@@ -10,6 +10,7 @@
 #include <cmath>
 #include <mutex>
 
+#include "sampling.cuh"
 #include "stack.cuh"
 
 namespace gg {
@@ -315,7 +316,7 @@ int gg_stack_create(int64_t frame_count, int64_t height, int64_t width, gg_stack
     s->d_error = static_cast<int*>(device_alloc(s, sizeof(int), "device error word"));
     check_cuda(cudaMemsetAsync(s->d_error, 0, sizeof(int), s->stream), "cudaMemsetAsync(error)");
     check_cuda(cudaEventCreateWithFlags(&s->warp_items_free, cudaEventDisableTiming), "cudaEventCreate");
-    s->has_slot_tmap = (s->width % 4 == 0) && make_slot_tensor_map(s, 80, 32);
+    s->has_slot_tmap = (s->width % 4 == 0) && make_slot_tensor_map(s, kBoxW, kBoxH);
 
     check_cuda(cudaMemsetAsync(s->d_slots, 0, slot_bytes, s->stream), "cudaMemsetAsync(stack)");
     check_cuda(cudaMemsetAsync(s->d_frame_nonfinite, 0, sizeof(unsigned) * frame_count, s->stream),

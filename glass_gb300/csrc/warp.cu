@@ -16,7 +16,7 @@
 //   - source coordinates are evaluated in float-float (TwoProd/TwoSum) from
 //     the float64 inverse, so floor/validity decisions agree with the float64
 //     reference without float64 arithmetic on the device;
-//   - each CTA owns a 64x16 output tile; its source footprint (an 80x32 box
+//   - each CTA owns a 64x32 output tile; its source footprint (an 80x48 box
 //     for the small rotations registration produces) is copied to shared
 //     memory by one cp.async.bulk.tensor (TMA) load, double-buffered against
 //     the previous tile's compute.  Footprints that do not fit the box (large
@@ -24,8 +24,9 @@
 //     read the taps straight from global memory instead;
 //   - output goes to a spare slot; a follow-up kernel swaps the frame->slot
 //     table, so nothing is copied back (8 B/pixel instead of 16 B);
-//   - Lanczos weights use sin(pi d) = (-1)^k sin(pi t) and the angle-sum form
-//     of sin(pi d / 3), i.e. one sinpif and one sincospif per axis.
+//   - Lanczos3 weights are paired even/odd polynomials in (t - 1/2)^2
+//     (sampling.cuh); interior tiles of finite frames run a straight-line
+//     form without per-pixel tests.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -38,8 +39,14 @@
 namespace gg {
 
 constexpr int kTileW = 64;
-constexpr int kTileH = 16;
-constexpr int kWarpThreads = 256;  // 64 x 4; each thread covers 4 rows
+constexpr int kTileH = 32;
+constexpr int kWarpThreads = 256;  // 64 x 4; each thread covers kTileH / 4 rows
+constexpr int kRowsPerThread = kTileH / 4;
+// Affine source coordinates are stepped by 4 output rows in float-float and
+// evaluated afresh every kFreshRows rows: at most three steps of rounding
+// separate a coordinate from the float64-faithful evaluation, so floor and
+// fraction decisions stay those of a direct evaluation.
+constexpr int kFreshRows = 4;
 
 struct WarpItem {
   int frame;
@@ -167,7 +174,7 @@ __device__ __forceinline__ TilePlan plan_tile(const Coef& it, int tile_x, int ti
   return p;
 }
 
-// The 4 output rows of one thread in a 64 x 16 tile (rows ly, ly + 4, ...).
+// The output rows of one thread in a 64 x 32 tile (rows ly, ly + 4, ...).
 // FINITE: the source frame holds no non-finite sample (every Lanczos3 window
 // takes the plain normalised sum); returns the count of non-finite outputs.
 template <int INTERP, bool FINITE>
@@ -178,20 +185,20 @@ __device__ __forceinline__ unsigned warp_tile_rows(const WarpArgs& a, const Coef
   const int ox = tile_x * kTileW + lx;
   unsigned bad = 0;
   // Affine source coordinates step by 4 output rows: (sx, sy) += 4 (b, e)
-  // in float-float (exact scaling by 4, one TwoSum per axis) instead of
-  // a fresh evaluation per pixel.
+  // in float-float (exact scaling by 4, one TwoSum per axis), with a fresh
+  // evaluation every kFreshRows rows.
   FFv sx_row{0.0f, 0.0f}, sy_row{0.0f, 0.0f};
   bool row_ok = false;
   const float step_x_hi = 4.0f * co.m[1][0], step_x_lo = 4.0f * co.m[1][1];
   const float step_y_hi = 4.0f * co.m[4][0], step_y_lo = 4.0f * co.m[4][1];
 #pragma unroll 1
-  for (int r = 0; r < 4; ++r) {
+  for (int r = 0; r < kRowsPerThread; ++r) {
     const int oy = tile_y * kTileH + ly + 4 * r;
     const bool inside = ox < a.width && oy < a.height;
     bool valid = false;
     float value = a.fill;
     if (co.affine) {
-      if (r == 0) {
+      if (r % kFreshRows == 0) {
         row_ok = source_coord(co, static_cast<float>(ox), static_cast<float>(oy), sx_row, sy_row);
       } else {
         sx_row = ff_add_ff(sx_row, step_x_hi, step_x_lo);
@@ -253,7 +260,7 @@ __device__ __forceinline__ unsigned warp_tile_rows(const WarpArgs& a, const Coef
 }
 
 // The common Lanczos3 tile in straight-line form: an affine map, the whole
-// 64 x 16 tile inside the output and mapped at least one pixel inside the
+// 64 x 32 tile inside the output and mapped at least one pixel inside the
 // valid source range, its footprint staged in the shared-memory box, a source
 // frame without non-finite samples, no clamp and no coverage map.  Every
 // pixel is then valid and takes the plain normalised 6 x 6 sum, so the rows
@@ -261,15 +268,16 @@ __device__ __forceinline__ unsigned warp_tile_rows(const WarpArgs& a, const Coef
 __device__ __forceinline__ unsigned warp_tile_rows_fast(const WarpArgs& a, const Coef& co, const float* box, int bx,
                                                         int by, float* dst, int ox, int oy0) {
   FFv sx, sy;
-  source_coord(co, static_cast<float>(ox), static_cast<float>(oy0), sx, sy);
   const float step_x_hi = 4.0f * co.m[1][0], step_x_lo = 4.0f * co.m[1][1];
   const float step_y_hi = 4.0f * co.m[4][0], step_y_lo = 4.0f * co.m[4][1];
   float* out = dst + static_cast<int64_t>(oy0) * a.width + ox;
   const int64_t out_step = 4 * static_cast<int64_t>(a.width);
   unsigned bad = 0;
 #pragma unroll 1
-  for (int r = 0; r < 4; ++r) {
-    if (r) {
+  for (int r = 0; r < kRowsPerThread; ++r) {
+    if (r % kFreshRows == 0) {
+      source_coord(co, static_cast<float>(ox), static_cast<float>(oy0 + 4 * r), sx, sy);
+    } else {
       sx = ff_add_ff(sx, step_x_hi, step_x_lo);
       sy = ff_add_ff(sy, step_y_hi, step_y_lo);
     }
