@@ -10,7 +10,7 @@ namespace gg {
 constexpr float kInfF = __builtin_huge_valf();
 // Shared-memory source box of the tiled warp (columns x rows).
 constexpr int kBoxW = 80;
-constexpr int kBoxH = 48;
+constexpr int kBoxH = 64;
 
 // sin(pi u) for |u| <= 1/2 and sin / cos of |x| <= pi/3 by their Taylor
 // series (truncation below 1e-9 on these ranges), evaluated by Horner.

@@ -16,7 +16,7 @@
 //   - source coordinates are evaluated in float-float (TwoProd/TwoSum) from
 //     the float64 inverse, so floor/validity decisions agree with the float64
 //     reference without float64 arithmetic on the device;
-//   - each CTA owns a 64x32 output tile; its source footprint (an 80x48 box
+//   - each CTA owns a 64x48 output tile; its source footprint (an 80x64 box
 //     for the small rotations registration produces) is copied to shared
 //     memory by one cp.async.bulk.tensor (TMA) load, double-buffered against
 //     the previous tile's compute.  Footprints that do not fit the box (large
@@ -39,7 +39,7 @@
 namespace gg {
 
 constexpr int kTileW = 64;
-constexpr int kTileH = 32;
+constexpr int kTileH = 48;
 constexpr int kWarpThreads = 256;  // 64 x 4; each thread covers kTileH / 4 rows
 constexpr int kRowsPerThread = kTileH / 4;
 // Affine source coordinates are stepped by 4 output rows in float-float and
@@ -174,7 +174,7 @@ __device__ __forceinline__ TilePlan plan_tile(const Coef& it, int tile_x, int ti
   return p;
 }
 
-// The output rows of one thread in a 64 x 32 tile (rows ly, ly + 4, ...).
+// The output rows of one thread in a 64 x 48 tile (rows ly, ly + 4, ...).
 // FINITE: the source frame holds no non-finite sample (every Lanczos3 window
 // takes the plain normalised sum); returns the count of non-finite outputs.
 template <int INTERP, bool FINITE>
@@ -260,7 +260,7 @@ __device__ __forceinline__ unsigned warp_tile_rows(const WarpArgs& a, const Coef
 }
 
 // The common Lanczos3 tile in straight-line form: an affine map, the whole
-// 64 x 32 tile inside the output and mapped at least one pixel inside the
+// 64 x 48 tile inside the output and mapped at least one pixel inside the
 // valid source range, its footprint staged in the shared-memory box, a source
 // frame without non-finite samples, no clamp and no coverage map.  Every
 // pixel is then valid and takes the plain normalised 6 x 6 sum, so the rows
