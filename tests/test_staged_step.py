@@ -8,7 +8,8 @@ inliers) and quality decisions, refined matrices within 1e-6 px of each
 other (the Gauss-Newton partial sums are reduced over a different number of
 blocks when fewer frames share a launch), the same zero-weight frames and
 count maps, and masters within 1e-5 of the batched ones relative to their
-range; a second staged step reproduces the first bit for bit.
+range; a second staged step reproduces the first bit for bit, also when its
+upload was started (prefetched) behind the previous step's integration.
 """
 
 from __future__ import annotations
@@ -46,8 +47,9 @@ def test_staged_step_matches_batched_step(native):
     a, b = _pipe(data), _pipe(data)
     try:
         maps_a = a.step_host(pinned, register=True, staged=False)
-        assert [len(c) for c in b.frame_chunks()] == [20, 20]
+        assert [len(c) for c in b.frame_chunks(2)] == [20, 20]
         assert [len(c) for c in b.frame_chunks(3)] == [13, 14, 13]
+        b.staged_chunks = 2  # chunked processing, the second half still in flight
         maps_b = b.step_host(pinned, register=True, staged=True)
         reg_a = {r["frame"]: r for r in a.last_registration}
         reg_b = {r["frame"]: r for r in b.last_registration}
@@ -69,9 +71,15 @@ def test_staged_step_matches_batched_step(native):
         span = float(np.nanmax(maps_a[0]) - np.nanmin(maps_a[0]))
         assert np.max(np.abs(maps_a[0][fin] - maps_b[0][fin])) <= 1e-5 * span
 
-        again = b.step_host(pinned, register=True, staged=True)
+        again = b.step_host(pinned, register=True, staged=True, prefetch=pinned)
         for k in range(5):
             np.testing.assert_array_equal(again[k], maps_b[k], err_msg=f"map {k}")
+        # the prefetched upload serves the next step, which skips its own
+        assert b._prefetched == pinned.ctypes.data
+        third = b.step_host(pinned, register=True, staged=True)
+        assert b._prefetched is None
+        for k in range(5):
+            np.testing.assert_array_equal(third[k], maps_b[k], err_msg=f"map {k}")
     finally:
         a.close()
         b.close()
