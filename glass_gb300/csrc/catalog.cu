@@ -401,8 +401,7 @@ extern "C" int gg_stack_star_grid_catalog(gg_stack* s, const int64_t* indices, i
 
   std::vector<int> frames(n);
   for (int k = 0; k < n; ++k) frames[k] = static_cast<int>(indices[k]);
-  check_cuda(cudaMemcpyAsync(d_frames, frames.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(grid catalog frames)");
+  upload_params(s->stream, d_frames, frames.data(), sizeof(int) * n, "cudaMemcpyAsync(grid catalog frames)");
   check_cuda(cudaMemsetAsync(d_found, 0, sizeof(unsigned) * n, s->stream), "cudaMemsetAsync(grid catalog)");
   check_cuda(cudaMemsetAsync(d_planes, 0, sizeof(float) * 5 * cat, s->stream), "cudaMemsetAsync(grid catalog)");
   check_cuda(cudaMemsetAsync(d_status, 0, cat, s->stream), "cudaMemsetAsync(grid catalog)");

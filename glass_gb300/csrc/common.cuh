@@ -46,6 +46,18 @@ inline void check_cuda(cudaError_t err, const char* what) {
 void note_launch(int n = 1);
 long long launch_count();
 
+// Stream-ordered host-to-device copy of a small block (launch descriptors,
+// frame lists, per-frame priors) that keeps off the copy engines: up to
+// kParamUploadMax bytes travel in the launch parameters of a one-CTA kernel,
+// larger blocks fall back to cudaMemcpyAsync.  A copy-engine copy on the stack
+// stream queues behind bulk copies already submitted to the same engine by
+// another stream (the next step's raw frames on the copy stream), so a stage
+// that needs a few hundred bytes of parameters would otherwise wait for
+// gigabytes of unrelated upload.  The host block may be reused as soon as the
+// call returns.
+constexpr std::size_t kParamUploadMax = 64 * 1024;
+void upload_params(cudaStream_t stream, void* dst, const void* src, std::size_t bytes, const char* what);
+
 // Grid sizing for streaming kernels: a whole number of waves over the SMs.
 int sm_count();
 inline unsigned grid_for(std::size_t work_items, int threads, int ctas_per_sm = 8) {

@@ -626,10 +626,8 @@ static GnPlan gn_prepare(gg_stack* s, int64_t reference_index, const int64_t* mo
   std::vector<int2> jobs(static_cast<size_t>(count));
   for (int64_t k = 0; k < count; ++k) jobs[k] = make_int2(static_cast<int>(reference_index), static_cast<int>(moving[k]));
   std::memcpy(g.h_state, states.data(), sizeof(GnState) * states.size());
-  check_cuda(cudaMemcpyAsync(g.jobs, jobs.data(), sizeof(int2) * count, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(gradient refine jobs)");
-  check_cuda(cudaMemcpyAsync(g.state, g.h_state, sizeof(GnState) * count, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(gradient refine state)");
+  upload_params(s->stream, g.jobs, jobs.data(), sizeof(int2) * count, "cudaMemcpyAsync(gradient refine jobs)");
+  upload_params(s->stream, g.state, g.h_state, sizeof(GnState) * count, "cudaMemcpyAsync(gradient refine state)");
   GnArgs& a = plan.args;
   a.slots = s->d_slots;
   a.slot_of_frame = s->d_slot_of_frame;

@@ -1671,9 +1671,7 @@ static void integrate_batch(std::vector<gg_stack*>& stacks, const gg_integrate_p
     IntegrateArgs* d_args = nullptr;
     check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&d_args), sizeof(IntegrateArgs) * count, lead->stream),
                "cudaMallocAsync(batch args)");
-    check_cuda(cudaMemcpyAsync(d_args, args.data(), sizeof(IntegrateArgs) * count, cudaMemcpyHostToDevice,
-                               lead->stream),
-               "cudaMemcpyAsync(batch args)");
+    upload_params(lead->stream, d_args, args.data(), sizeof(IntegrateArgs) * count, "cudaMemcpyAsync(batch args)");
     for (int b = 0; b < 3; ++b) {
       if (bucket_start[b + 1] == bucket_start[b]) continue;
       const std::vector<IntegrateArgs> sub(args.begin() + bucket_start[b], args.begin() + bucket_start[b + 1]);
@@ -1848,9 +1846,8 @@ static void integrate_warped(gg_stack* s, const double* fwd, int interp, float c
   const std::vector<FusedFrame> frames = fused_frames_host(fwd, static_cast<int>(s->frames));
   ensure_fused_buffers(s);
   auto* d_frames = static_cast<FusedFrame*>(s->d_fused_frames);
-  check_cuda(cudaMemcpyAsync(d_frames, frames.data(), sizeof(FusedFrame) * frames.size(), cudaMemcpyHostToDevice,
-                             s->stream),
-             "cudaMemcpyAsync(fused frames)");
+  upload_params(s->stream, d_frames, frames.data(), sizeof(FusedFrame) * frames.size(),
+                "cudaMemcpyAsync(fused frames)");
   launch_fused_sequence(s, d_frames, interp, clamp, d_weights, p);
 }
 
@@ -2131,9 +2128,7 @@ int gg_stack_integrate(gg_stack* s, const float* host_weights, const gg_integrat
   stack_require_all_loaded(s, "integration");
   stack_activate(s);
   for (int64_t f = 0; f < s->frames; ++f) s->h_weights_pinned[f] = host_weights ? host_weights[f] : 1.0f;
-  check_cuda(cudaMemcpyAsync(s->d_weights, s->h_weights_pinned, sizeof(float) * s->frames, cudaMemcpyHostToDevice,
-                             s->stream),
-             "cudaMemcpyAsync(weights)");
+  upload_params(s->stream, s->d_weights, s->h_weights_pinned, sizeof(float) * s->frames, "cudaMemcpyAsync(weights)");
   launch_integrate(s, s->d_weights, *params);
   GG_API_END
 }
@@ -2176,9 +2171,7 @@ int gg_stack_integrate_warped(gg_stack* s, const double* host_matrices, int inte
   stack_require_all_loaded(s, "fused warp-integration");
   stack_activate(s);
   for (int64_t f = 0; f < s->frames; ++f) s->h_weights_pinned[f] = host_weights ? host_weights[f] : 1.0f;
-  check_cuda(cudaMemcpyAsync(s->d_weights, s->h_weights_pinned, sizeof(float) * s->frames, cudaMemcpyHostToDevice,
-                             s->stream),
-             "cudaMemcpyAsync(weights)");
+  upload_params(s->stream, s->d_weights, s->h_weights_pinned, sizeof(float) * s->frames, "cudaMemcpyAsync(weights)");
   integrate_warped(s, host_matrices, interpolation, clamping_threshold, s->d_weights, *params);
   GG_API_END
 }

@@ -240,8 +240,7 @@ static LnArgs ln_args(gg_stack* s, int tile_h, int tile_w, int rows, int cols, i
 
 static void upload_frames(gg_stack* s, LnScratch& g, const int64_t* idx, int64_t count) {
   for (int64_t k = 0; k < count; ++k) g.h_frames[k] = static_cast<int>(idx[k]);
-  check_cuda(cudaMemcpyAsync(g.frames, g.h_frames, sizeof(int) * count, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(local norm frames)");
+  upload_params(s->stream, g.frames, g.h_frames, sizeof(int) * count, "cudaMemcpyAsync(local norm frames)");
 }
 
 static unsigned apply_grid_x(gg_stack* s, int pairs) {
@@ -336,11 +335,9 @@ int gg_stack_apply_grid_normalization(gg_stack* s, const int64_t* indices, int64
   const int64_t tiles = static_cast<int64_t>(grid_rows) * grid_cols;
   LnScratch& g = ln_scratch(s, static_cast<int>(count), tiles);
   upload_frames(s, g, indices, count);
-  check_cuda(cudaMemcpyAsync(g.scales, host_scales, sizeof(float) * tiles * count, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(local norm scales)");
-  check_cuda(cudaMemcpyAsync(g.offsets, host_offsets, sizeof(float) * tiles * count, cudaMemcpyHostToDevice,
-                             s->stream),
-             "cudaMemcpyAsync(local norm offsets)");
+  upload_params(s->stream, g.scales, host_scales, sizeof(float) * tiles * count, "cudaMemcpyAsync(local norm scales)");
+  upload_params(s->stream, g.offsets, host_offsets, sizeof(float) * tiles * count,
+                "cudaMemcpyAsync(local norm offsets)");
   LnArgs a = ln_args(s, tile_h, tile_w, grid_rows, grid_cols, 0, g);
   note_launch();
   ln_apply_kernel<<<dim3(apply_grid_x(s, static_cast<int>(count)), static_cast<unsigned>(count)), 256, 0,
@@ -386,10 +383,8 @@ int gg_stack_apply_global_normalization(gg_stack* s, int64_t index, float scale,
   stack_activate(s);
   LnScratch& g = ln_scratch(s, 1, 1);
   upload_frames(s, g, &index, 1);
-  check_cuda(cudaMemcpyAsync(g.scales, &scale, sizeof(float), cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(global scale)");
-  check_cuda(cudaMemcpyAsync(g.offsets, &offset, sizeof(float), cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(global offset)");
+  upload_params(s->stream, g.scales, &scale, sizeof(float), "cudaMemcpyAsync(global scale)");
+  upload_params(s->stream, g.offsets, &offset, sizeof(float), "cudaMemcpyAsync(global offset)");
   LnArgs a = ln_args(s, static_cast<int>(s->height), static_cast<int>(s->width), 1, 1, 0, g);
   note_launch();
   ln_apply_kernel<<<dim3(apply_grid_x(s, 1), 1), 256, 0, s->stream>>>(a, 0);

@@ -403,10 +403,8 @@ static std::vector<double> evaluate_candidates(gg_stack* s, const std::vector<Pa
     m.bands_cap = bc;
     s->bytes_allocated += bytes(jc, cc, bc) - before;
   }
-  check_cuda(cudaMemcpyAsync(m.jobs, jobs.data(), sizeof(MetricJob) * nj, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(metric jobs)");
-  check_cuda(cudaMemcpyAsync(m.cands, cands.data(), sizeof(MetricCand) * ncand, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(metric candidates)");
+  upload_params(s->stream, m.jobs, jobs.data(), sizeof(MetricJob) * nj, "cudaMemcpyAsync(metric jobs)");
+  upload_params(s->stream, m.cands, cands.data(), sizeof(MetricCand) * ncand, "cudaMemcpyAsync(metric candidates)");
   MetricArgs a{};
   a.slots = s->d_slots;
   a.slot_of_frame = s->d_slot_of_frame;

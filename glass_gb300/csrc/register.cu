@@ -1682,10 +1682,8 @@ int gg_stack_register_frames(gg_stack* s, int64_t reference_index, const int64_t
     row_frames[static_cast<size_t>(k + 1)] = static_cast<int>(indices[k]);
     jobs[static_cast<size_t>(k)] = RegJob{0, static_cast<int>(k + 1)};
   }
-  check_cuda(cudaMemcpyAsync(r.row_frames, row_frames.data(), sizeof(int) * rows, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(registration rows)");
-  check_cuda(cudaMemcpyAsync(r.jobs, jobs.data(), sizeof(RegJob) * count, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(registration jobs)");
+  upload_params(s->stream, r.row_frames, row_frames.data(), sizeof(int) * rows, "cudaMemcpyAsync(registration rows)");
+  upload_params(s->stream, r.jobs, jobs.data(), sizeof(RegJob) * count, "cudaMemcpyAsync(registration jobs)");
   check_cuda(cudaMemsetAsync(r.overflow, 0, sizeof(int), s->stream), "cudaMemsetAsync(overflow)");
   note_launch();
   reg_copy_catalogs_kernel<<<rows, 128, 0, s->stream>>>(s->d_cat_xy, s->d_cat_n, r.row_frames, rows, r.pts, r.npts);

@@ -29,6 +29,57 @@ static std::atomic<long long> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
+namespace {
+template <unsigned BYTES>
+struct ParamBlock {
+  unsigned char* dst;
+  unsigned bytes;
+  alignas(16) unsigned char data[BYTES];
+};
+
+// Writes the block carried in the launch parameters to its destination;
+// whole 32-bit words when the destination and the size allow it.
+template <unsigned BYTES>
+__global__ void __launch_bounds__(256) param_block_kernel(const __grid_constant__ ParamBlock<BYTES> b) {
+  if ((reinterpret_cast<uintptr_t>(b.dst) & 3u) == 0 && (b.bytes & 3u) == 0) {
+    const unsigned* src = reinterpret_cast<const unsigned*>(b.data);
+    unsigned* dst = reinterpret_cast<unsigned*>(b.dst);
+    for (unsigned i = threadIdx.x; i < b.bytes / 4; i += blockDim.x) dst[i] = src[i];
+  } else {
+    for (unsigned i = threadIdx.x; i < b.bytes; i += blockDim.x) b.dst[i] = b.data[i];
+  }
+}
+
+template <unsigned BYTES>
+void launch_param_block(cudaStream_t stream, unsigned char* dst, const unsigned char* src, unsigned bytes,
+                        const char* what) {
+  ParamBlock<BYTES> b;
+  b.dst = dst;
+  b.bytes = bytes;
+  std::memcpy(b.data, src, bytes);
+  note_launch();
+  param_block_kernel<BYTES><<<1, 256, 0, stream>>>(b);
+  check_cuda(cudaGetLastError(), what);
+}
+}  // namespace
+
+void upload_params(cudaStream_t stream, void* dst, const void* src, std::size_t bytes, const char* what) {
+  if (bytes == 0) return;
+  if (bytes > kParamUploadMax) {
+    check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream), what);
+    return;
+  }
+  // 16 KB blocks stay well inside the 32,764-byte kernel parameter limit
+  constexpr unsigned kLarge = 16384, kSmall = 1024;
+  auto* d = static_cast<unsigned char*>(dst);
+  const auto* h = static_cast<const unsigned char*>(src);
+  for (std::size_t off = 0; off < bytes; off += kLarge) {
+    const unsigned n = static_cast<unsigned>(std::min<std::size_t>(kLarge, bytes - off));
+    if (n <= kSmall) launch_param_block<kSmall>(stream, d + off, h + off, n, what);
+    else launch_param_block<kLarge>(stream, d + off, h + off, n, what);
+  }
+}
+
 int sm_count() {
   static int cached = 0;
   if (cached == 0) {

@@ -1496,8 +1496,7 @@ void detect_stars(gg_stack* s, const int64_t* indices, int count, const gg_star_
   ensure_star_scratch(sc, count, p.max_stars);
   std::vector<int> frames(static_cast<size_t>(count));
   for (int k = 0; k < count; ++k) frames[static_cast<size_t>(k)] = static_cast<int>(indices[k]);
-  check_cuda(cudaMemcpyAsync(sc.frames, frames.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(star frames)");
+  upload_params(s->stream, sc.frames, frames.data(), sizeof(int) * count, "cudaMemcpyAsync(star frames)");
   check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(star frames)");
   check_cuda(cudaMemsetAsync(sc.state, 0, sizeof(StarFrameState) * count, s->stream), "cudaMemsetAsync(state)");
   const bool need_stats = !std::isfinite(p.background) || !std::isfinite(p.noise);

@@ -149,8 +149,7 @@ int gg_stack_compute_weights(gg_stack* s, int mode, const float* host_prior, flo
     h_frames[k] = static_cast<int>(k);
     h_prior[k] = host_prior ? host_prior[k] : 1.0f;
   }
-  check_cuda(cudaMemcpyAsync(d_frames, h_frames, sizeof(int) * count * 2, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(weights frames)");
+  upload_params(s->stream, d_frames, h_frames, sizeof(int) * count * 2, "cudaMemcpyAsync(weights frames)");
   if (mode == GG_WEIGHTS_SIMPLE_SNR) {
     note_launch();
     frame_stats_kernel<<<dim3(blocks, static_cast<unsigned>(count)), 256, 0, s->stream>>>(
@@ -186,8 +185,7 @@ int gg_stack_frame_stats(gg_stack* s, const int64_t* indices, int64_t count, gg_
   for (int64_t k = 0; k < count; ++k) frames[static_cast<size_t>(k)] = static_cast<int>(indices[k]);
   int* h_frames = reinterpret_cast<int*>(s->h_partials_pinned + static_cast<size_t>(count) * blocks * 3);
   std::copy(frames.begin(), frames.end(), h_frames);
-  check_cuda(cudaMemcpyAsync(d_frames, h_frames, sizeof(int) * count, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(stats frames)");
+  upload_params(s->stream, d_frames, h_frames, sizeof(int) * count, "cudaMemcpyAsync(stats frames)");
   note_launch();
   frame_stats_kernel<<<dim3(blocks, static_cast<unsigned>(count)), 256, 0, s->stream>>>(
       s->d_slots, s->d_slot_of_frame, s->stride, s->pixels, d_frames, s->d_partials);

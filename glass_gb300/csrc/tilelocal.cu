@@ -214,8 +214,7 @@ int gg_stack_integrate_tile_local(gg_stack* s, int mode, const float* host_weigh
   std::memcpy(host.data() + off_m, host_multipliers, sizeof(float) * tile_count);
   unsigned char* dev = nullptr;
   check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&dev), bytes, s->stream), "cudaMallocAsync(tile-local params)");
-  check_cuda(cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(tile-local params)");
+  upload_params(s->stream, dev, host.data(), bytes, "cudaMemcpyAsync(tile-local params)");
   TileLocalArgs a{};
   a.slots = s->d_slots;
   a.slot_of_frame = s->d_slot_of_frame;

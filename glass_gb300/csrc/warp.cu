@@ -590,9 +590,8 @@ void warp_frames(gg_stack* s, const int64_t* indices, int64_t count, const doubl
   // The staging buffer may still feed the previous call's copy.
   check_cuda(cudaEventSynchronize(s->warp_items_free), "cudaEventSynchronize(warp items)");
   std::memcpy(s->h_warp_items, items.data(), sizeof(WarpItem) * items.size());
-  check_cuda(cudaMemcpyAsync(s->d_warp_items, s->h_warp_items, sizeof(WarpItem) * items.size(),
-                             cudaMemcpyHostToDevice, s->stream),
-             "cudaMemcpyAsync(warp items)");
+  upload_params(s->stream, s->d_warp_items, s->h_warp_items, sizeof(WarpItem) * items.size(),
+                "cudaMemcpyAsync(warp items)");
   check_cuda(cudaEventRecord(s->warp_items_free, s->stream), "cudaEventRecord(warp items)");
   launch_warp_items(s, static_cast<WarpItem*>(s->d_warp_items), count, interp, fill, clamp, track_coverage);
   if (track_coverage) s->warp_coverage_frames += count;
