@@ -53,6 +53,8 @@
 namespace gg {
 
 constexpr int kGnThreads = 256;
+constexpr int kGnSamplesPerThread = 64;
+constexpr int kGnMaxBlocksPerJob = 64;
 constexpr int kGnSums = 48;  // 36 (J^T J upper) + 8 (J^T r) + sum r^2 + count, padded
 constexpr int kGnUsed = 46;
 // Residual scale: sigma = 1.4826 * median |r| over the valid samples (robust
@@ -566,6 +568,20 @@ static GnScratch& gn_scratch(gg_stack* s, int jobs, int blocks) {
   return g;
 }
 
+// Blocks per job: about kGnSamplesPerThread samples per thread (at most
+// kGnMaxBlocksPerJob blocks, and at most 2^18 block partials over all jobs).
+// A launch is then many short CTAs, so its time follows the jobs still
+// running: the CTAs of converged jobs return at once, where a few long CTAs
+// per job would keep every iteration as long as the first.  The count
+// depends on the samples alone (below 4,096 jobs), so a job's sums do not
+// depend on which frames share its launch.
+static int gn_blocks_per_job(int64_t samples, int jobs) {
+  constexpr int64_t per_block = int64_t{kGnThreads} * kGnSamplesPerThread;
+  const int64_t want = std::min<int64_t>(kGnMaxBlocksPerJob, std::max<int64_t>(1, (samples + per_block - 1) / per_block));
+  const int64_t cap = std::max<int64_t>(1, (int64_t{1} << 18) / std::max(jobs, 1));
+  return static_cast<int>(std::min(want, cap));
+}
+
 static void validate_params(const gg_gradient_refine_params_t& p) {
   require(p.transform_model == GG_TRANSFORM_TRANSLATION || p.transform_model == GG_TRANSFORM_SIMILARITY ||
               p.transform_model == GG_TRANSFORM_AFFINE,
@@ -620,8 +636,8 @@ static GnPlan gn_prepare(gg_stack* s, int64_t reference_index, const int64_t* mo
   plan.interp = interp;
   const int64_t nsx = (s->width + sample_stride - 1) / sample_stride;
   const int64_t nsy = (s->height + row_stride - 1) / row_stride;
-  // partial sums for up to two waves of 8 resident CTAs per SM
-  const int bpj = std::max(1, (2 * 8 * sm_count() + plan.jobs - 1) / plan.jobs);
+  // partial sums for the sample grid given here (the finest one a call uses)
+  const int bpj = gn_blocks_per_job(nsx * nsy, plan.jobs);
   GnScratch& g = gn_scratch(s, plan.jobs, bpj);
   std::vector<int2> jobs(static_cast<size_t>(count));
   for (int64_t k = 0; k < count; ++k) jobs[k] = make_int2(static_cast<int>(reference_index), static_cast<int>(moving[k]));
@@ -671,28 +687,6 @@ static GnKernelFn gn_kernel(int interp, int K, bool unroll) {
   }
 }
 
-// Blocks per job: whole waves of the kernel's resident CTAs (the first count
-// that fills at least 98 % of its last wave, unless a later wave count fills
-// noticeably more), at most `cap` and at least two samples per thread.
-static int gn_blocks_per_job(GnKernelFn fn, int jobs, int64_t samples, int cap) {
-  int occ = 0;
-  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kGnThreads, 0), "cudaOccupancy(gn_accumulate)");
-  const int64_t resident = static_cast<int64_t>(std::max(occ, 1)) * sm_count();
-  const int64_t limit = std::max<int64_t>(1, std::min<int64_t>(cap, (samples + 2 * kGnThreads - 1) / (2 * kGnThreads)));
-  const int64_t bmax = std::min<int64_t>(limit, std::max<int64_t>(1, (2 * resident + jobs - 1) / jobs));
-  int64_t best = 1;
-  double best_eff = -1.0;
-  for (int64_t b = 1; b <= bmax; ++b) {
-    const int64_t total = b * jobs;
-    const int64_t waves = (total + resident - 1) / resident;
-    const double eff = static_cast<double>(total) / static_cast<double>(waves * resident);
-    if (eff > best_eff + 0.02) {
-      best_eff = eff;
-      best = b;
-    }
-  }
-  return static_cast<int>(best);
-}
 
 // One pass over the samples: K = 0 statistics, else the model's projected
 // columns (see GnLayout).  Lanczos3 passes tune row-by-row against
@@ -708,7 +702,7 @@ static void gn_accumulate(gg_stack* s, GnPlan& plan, SampleGrid grid_step, int K
   GnScratch& g = *static_cast<GnScratch*>(s->gn_scratch);
   auto run = [&](int variant) {
     GnKernelFn fn = gn_kernel(plan.interp, K, variant == 1);
-    a.blocks_per_job = gn_blocks_per_job(fn, plan.jobs, samples, g.block_cap);
+    a.blocks_per_job = std::min(gn_blocks_per_job(samples, plan.jobs), g.block_cap);
     check_cuda(cudaMemsetAsync(g.hist, 0, sizeof(unsigned) * kGnHistWords * plan.jobs, s->stream),
                "cudaMemsetAsync(gradient refine histogram)");
     const dim3 grid(static_cast<unsigned>(a.blocks_per_job), static_cast<unsigned>(plan.jobs));

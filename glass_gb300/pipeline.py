@@ -141,9 +141,13 @@ DEFAULT_REFINE = {"search_radius_px": 1.0, "coarse_step_px": 0.25, "fine_radius_
 # frame where that grid would exceed target_samples, whole rows spaced to
 # about target_samples pixels), three noise passes on a grid twice as coarse,
 # at most five steps, stop below 1e-3 px
+# Gauss-Newton defaults.  On the 200-frame 9600 x 6422 stack (registration
+# error 0.0146 px RMS against the rendered truth) three statistics passes and
+# a 1e-3 px step tolerance gave the same error in 33.6 ms with 6 frames at the
+# iteration cap; two passes and 3e-3 px take 27.6 ms and every frame converges.
 DEFAULT_GRADIENT_REFINE = {"model": "similarity", "interpolation": "lanczos3", "sample_stride": 3,
-                           "target_samples": 1_000_000, "stats_passes": 3, "iterations": 5, "min_samples": 256,
-                           "clip_sigma": 5.0, "mask_shift_px": 1.0, "tolerance_px": 1.0e-3, "max_step_px": 2.0}
+                           "target_samples": 1_000_000, "stats_passes": 2, "iterations": 5, "min_samples": 256,
+                           "clip_sigma": 5.0, "mask_shift_px": 1.0, "tolerance_px": 3.0e-3, "max_step_px": 2.0}
 
 
 def gradient_sample_grid(params: dict, height: int, width: int) -> tuple[int, int]:
