@@ -477,9 +477,10 @@ class ResidentPipeline:
         integration took 379 ms end to end in one chunk (the device step
         alone: 379 ms); a step that uploads its own 24.7 GB took 535 ms in one
         chunk, 468 ms in two, 465 ms in three and 483 ms in eight.  One chunk
-        stays the default: the Gauss-Newton sums are split over a number of
-        blocks that depends on the frames sharing a launch, so a chunked step
-        reproduces an unchunked one to 1e-6 px, not bit for bit."""
+        stays the default: the registration-quality sums are split over a
+        number of CTAs that depends on the frames sharing a launch, so a
+        chunked step reproduces an unchunked one to rounding, not bit for
+        bit."""
         parts = self.staged_chunks if parts is None else parts
         parts = max(1, min(int(parts), self.frames))
         bounds = [round(i * self.frames / parts) for i in range(parts + 1)]

@@ -5,8 +5,8 @@ are still in flight.
 
 It must give the batched step's answers: the same registrations (status,
 inliers) and quality decisions, refined matrices within 1e-6 px of each
-other (the Gauss-Newton partial sums are reduced over a different number of
-blocks when fewer frames share a launch), the same zero-weight frames and
+other (the registration-quality sums are reduced over a CTA count that
+depends on the frames sharing a launch), the same zero-weight frames and
 count maps, and masters within 1e-5 of the batched ones relative to their
 range; a second staged step reproduces the first bit for bit, also when its
 upload was started (prefetched) behind the previous step's integration.
