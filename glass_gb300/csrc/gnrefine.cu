@@ -41,6 +41,7 @@
 // CUDA graph.  The Jacobian uses centred, scaled coordinates
 // ((x - cx) / R, (y - cy) / R), R = max(W, H) / 2, so that a unit step of
 // every parameter moves the image corners by about one pixel.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -568,18 +569,23 @@ static GnScratch& gn_scratch(gg_stack* s, int jobs, int blocks) {
   return g;
 }
 
-// Blocks per job: about kGnSamplesPerThread samples per thread (at most
-// kGnMaxBlocksPerJob blocks, and at most 2^18 block partials over all jobs).
-// A launch is then many short CTAs, so its time follows the jobs still
-// running: the CTAs of converged jobs return at once, where a few long CTAs
-// per job would keep every iteration as long as the first.  The count
-// depends on the samples alone (below 4,096 jobs), so a job's sums do not
+// Blocks per job: about kGnSamplesPerThread samples per thread, or more
+// when that leaves the GPU short of two waves of three CTAs per SM; at least
+// two samples per thread, at most kGnMaxBlocksPerJob blocks and 2^18 block
+// partials over all jobs.  A launch is then many short CTAs, so its time
+// follows the jobs still running: the CTAs of converged jobs return at once,
+// where a few long CTAs per job would keep every iteration as long as the
+// first.  On frames large enough to fill the GPU (the c5 stack: 1 M samples
+// per frame) the count depends on the samples alone, so a job's sums do not
 // depend on which frames share its launch.
 static int gn_blocks_per_job(int64_t samples, int jobs) {
   constexpr int64_t per_block = int64_t{kGnThreads} * kGnSamplesPerThread;
-  const int64_t want = std::min<int64_t>(kGnMaxBlocksPerJob, std::max<int64_t>(1, (samples + per_block - 1) / per_block));
-  const int64_t cap = std::max<int64_t>(1, (int64_t{1} << 18) / std::max(jobs, 1));
-  return static_cast<int>(std::min(want, cap));
+  const int64_t j = std::max(jobs, 1);
+  const int64_t by_samples = (samples + per_block - 1) / per_block;
+  const int64_t by_fill = (int64_t{6} * sm_count() + j - 1) / j;
+  const int64_t floor_cap = std::max<int64_t>(1, (samples + 2 * kGnThreads - 1) / (2 * kGnThreads));
+  const int64_t cap = std::min<int64_t>({kGnMaxBlocksPerJob, floor_cap, std::max<int64_t>(1, (int64_t{1} << 18) / j)});
+  return static_cast<int>(std::max<int64_t>(1, std::min(std::max(by_samples, by_fill), cap)));
 }
 
 static void validate_params(const gg_gradient_refine_params_t& p) {
