@@ -748,18 +748,26 @@ __global__ void __launch_bounds__(256) star_detect_kernel(DetectArgs a) {
         above_bits |= (x <= W - 2 && isfinite(c[u]) && above) ? (1u << u) : 0u;
       }
       if (!__any_sync(0xffffffffu, above_bits != 0u)) continue;
+      // every column's 3 x 3 test first (their loads all in flight
+      // together), then one ballot per column
+      unsigned hit_bits = 0u;
 #pragma unroll
       for (int u = 0; u < kPer; ++u) {
-        const int x = x0 + u * static_cast<int>(blockDim.x);
-        bool hit = (above_bits >> u) & 1u;
-        if (hit) {
-          const float* p = row + x;
+        if ((above_bits >> u) & 1u) {
+          const float* p = row + x0 + u * static_cast<int>(blockDim.x);
+          bool hit = true;
 #pragma unroll
           for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
             for (int dx = -1; dx <= 1; ++dx)
               if (dx || dy) hit &= (c[u] >= __ldg(p + static_cast<int64_t>(dy) * W + dx));
+          hit_bits |= hit ? (1u << u) : 0u;
         }
+      }
+#pragma unroll
+      for (int u = 0; u < kPer; ++u) {
+        const int x = x0 + u * static_cast<int>(blockDim.x);
+        const bool hit = (hit_bits >> u) & 1u;
         const unsigned mask = __ballot_sync(0xffffffffu, hit);
         if (mask) {
           const int leader = __ffs(mask) - 1;
