@@ -1057,6 +1057,89 @@ class ResidentCalibratedStack:
                  "sigma": float(r.sigma), "star_count": int(r.star_count), "applied": bool(apply),
                  "model": model} for k, r in enumerate(out)]
 
+    # ---- source DQ: threshold-only cosmetic mask (native_bindings.cpp:3243-3400, 4307-4620) ----
+    def _cosmetic_threshold(self, indices: Any, lows: Any, highs: Any, apply: bool) -> tuple[np.ndarray, np.ndarray,
+                                                                                               np.ndarray, np.ndarray,
+                                                                                               dict[str, float]]:
+        idx = np.ascontiguousarray(np.asarray(list(indices), dtype=np.int64).reshape(-1))
+        lo = np.ascontiguousarray(np.asarray(list(lows), dtype=np.float32).reshape(-1))
+        hi = np.ascontiguousarray(np.asarray(list(highs), dtype=np.float32).reshape(-1))
+        if idx.size != lo.size or idx.size != hi.size:
+            raise ValueError("indices, low_thresholds, and high_thresholds must have the same length")
+        if idx.size > 65535:
+            raise ValueError("batch cosmetic threshold application supports at most 65535 frames per launch")
+        counts = np.zeros((idx.size, 3), dtype=np.int64)
+        t0 = perf_counter()
+        if idx.size:
+            _lib.call("gg_stack_cosmetic_threshold", self._handle, _lib.ptr(idx), ctypes.c_int64(idx.size),
+                      _lib.ptr(lo), _lib.ptr(hi), ctypes.c_int32(int(bool(apply))), _lib.ptr(counts))
+        t1 = perf_counter()
+        return idx, lo, hi, counts, {"kernel_enqueue_s": t1 - t0, "sync_s": 0.0, "device_counts_download_s": 0.0,
+                                     "mask_upload_s": 0.0}
+
+    def _cosmetic_threshold_frame(self, index: int, low_threshold: float, high_threshold: float, apply: bool):
+        t0 = perf_counter()
+        _, lo, hi, counts, timing = self._cosmetic_threshold([int(index)], [low_threshold], [high_threshold], apply)
+        hot, cold, nonfinite = (int(x) for x in counts[0])
+        name = "apply" if apply else "count"
+        return {"schema_version": 1, "native_method": f"ResidentCalibratedStack.{name}_cosmetic_threshold_mask_frame",
+                "frame_index": int(index), "total_pixels": int(self.height * self.width),
+                "low_threshold": float(lo[0]), "high_threshold": float(hi[0]), "hot_samples": hot,
+                "cold_samples": cold, "nonfinite_samples": nonfinite, "cosmetic_corrected_samples": hot + cold,
+                "invalid_samples": hot + cold + nonfinite, "applied": bool(apply) and hot + cold + nonfinite > 0,
+                **timing, "total_s": perf_counter() - t0, "detector_execution": f"cuda_threshold_{name}"}
+
+    def apply_cosmetic_threshold_mask_frame(self, index: int, low_threshold: float,
+                                            high_threshold: float) -> dict[str, Any]:
+        """Samples of frame `index` above high_threshold (hot), below
+        low_threshold (cold) or non-finite become NaN; returns the counts."""
+        return self._cosmetic_threshold_frame(index, low_threshold, high_threshold, True)
+
+    def count_cosmetic_threshold_mask_frame(self, index: int, low_threshold: float,
+                                            high_threshold: float) -> dict[str, Any]:
+        """The counts of apply_cosmetic_threshold_mask_frame; the frame is not changed."""
+        return self._cosmetic_threshold_frame(index, low_threshold, high_threshold, False)
+
+    def _cosmetic_threshold_frames(self, indices: Any, low_thresholds: Any, high_thresholds: Any, apply: bool):
+        t0 = perf_counter()
+        idx, lo, hi, counts, timing = self._cosmetic_threshold(indices, low_thresholds, high_thresholds, apply)
+        name = "apply" if apply else "count"
+        method = f"ResidentCalibratedStack.{name}_cosmetic_threshold_mask_frames"
+        frames = []
+        for k in range(idx.size):
+            hot, cold, nonfinite = (int(x) for x in counts[k])
+            frames.append({"schema_version": 1, "native_method": method,
+                           "per_frame_native_method": f"ResidentCalibratedStack.{name}_cosmetic_threshold_mask_frame",
+                           "frame_index": int(idx[k]), "batch_position": k,
+                           "total_pixels": int(self.height * self.width), "low_threshold": float(lo[k]),
+                           "high_threshold": float(hi[k]), "hot_samples": hot, "cold_samples": cold,
+                           "nonfinite_samples": nonfinite, "cosmetic_corrected_samples": hot + cold,
+                           "invalid_samples": hot + cold + nonfinite,
+                           "applied": bool(apply) and hot + cold + nonfinite > 0,
+                           "batch_single_kernel_launch": True, "batch_single_sync": True,
+                           "batch_frame_count": int(idx.size), **timing,
+                           "detector_execution": f"cuda_threshold_{name}_batch"})
+        tot = counts.sum(axis=0) if idx.size else np.zeros(3, dtype=np.int64)
+        hot, cold, nonfinite = (int(x) for x in tot)
+        return {"schema_version": 1, "native_method": method, "frame_count": int(idx.size),
+                "total_pixels_per_frame": int(self.height * self.width), "hot_samples": hot, "cold_samples": cold,
+                "nonfinite_samples": nonfinite, "cosmetic_corrected_samples": hot + cold,
+                "invalid_samples": hot + cold + nonfinite, "applied": bool(apply) and hot + cold + nonfinite > 0,
+                **timing, "batch_single_kernel_launch": True, "batch_single_sync": True,
+                "detector_execution": f"cuda_threshold_{name}_batch", "total_s": perf_counter() - t0,
+                "frames": frames}
+
+    def apply_cosmetic_threshold_mask_frames(self, indices: Any, low_thresholds: Any,
+                                             high_thresholds: Any) -> dict[str, Any]:
+        """apply_cosmetic_threshold_mask_frame over several frames (one
+        threshold pair per frame) in one launch."""
+        return self._cosmetic_threshold_frames(indices, low_thresholds, high_thresholds, True)
+
+    def count_cosmetic_threshold_mask_frames(self, indices: Any, low_thresholds: Any,
+                                             high_thresholds: Any) -> dict[str, Any]:
+        """count_cosmetic_threshold_mask_frame over several frames in one launch."""
+        return self._cosmetic_threshold_frames(indices, low_thresholds, high_thresholds, False)
+
     def apply_invalid_mask_frame(self, index: int, invalid_mask: Any) -> dict[str, Any]:
         """Source-DQ invalid samples (non-zero mask entries) become NaN."""
         mask = np.ascontiguousarray(np.asarray(invalid_mask).astype(np.uint8))

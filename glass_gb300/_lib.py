@@ -396,6 +396,7 @@ PROTOTYPES: dict[str, list] = {
     "gg_read_queue_destroy": [_P],
     "gg_stack_cosmetic_mask": [_P, _P, ctypes.c_int64, ctypes.POINTER(CosmeticParams), _P],
     "gg_stack_apply_invalid_mask": [_P, ctypes.c_int64, _P, _P],
+    "gg_stack_cosmetic_threshold": [_P, _P, ctypes.c_int64, _P, _P, ctypes.c_int32, _P],
     "gg_stack_integrate_tile_local": [_P, ctypes.c_int, _P, _P, _P, _P, ctypes.c_int32, ctypes.c_float,
                                       ctypes.c_float],
     "gg_stack_integrate_warped_device_weights": [_P, _P, ctypes.c_int, ctypes.c_float,

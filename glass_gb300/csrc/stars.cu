@@ -2064,3 +2064,112 @@ extern "C" int gg_stack_apply_invalid_mask(gg_stack* s, int64_t index, const uin
   }
   GG_API_END
 }
+
+namespace gg {
+
+// Threshold-only cosmetic mask (apply / count_cosmetic_threshold_mask_frame(s)
+// semantics, integration_kernels.cu:181-232, 266-330): per listed frame a
+// sample is non-finite, hot (> high) or cold (< low), tested in that order;
+// with `apply` all three become NaN and the frame's non-finite counter grows
+// by the hot and cold samples (a non-finite sample was already counted).
+// float4 grid-stride loop per frame (slots start 256-byte aligned), one
+// store per quad that changed, counts folded per warp.
+struct ThresholdFrame {
+  int frame;
+  float low, high;
+  int pad;
+};
+
+__device__ __forceinline__ bool threshold_classify(float& x, float low, float high, bool apply, unsigned& hot,
+                                                   unsigned& cold, unsigned& nonfinite) {
+  bool hit = true;
+  if (!isfinite(x)) ++nonfinite;
+  else if (x > high) ++hot;
+  else if (x < low) ++cold;
+  else hit = false;
+  if (hit && apply) x = __int_as_float(0x7fc00000);
+  return hit && apply;
+}
+
+__global__ void __launch_bounds__(256) cosmetic_threshold_kernel(float* slots, const int* slot_of_frame, int64_t stride,
+                                                                 int64_t pixels, const ThresholdFrame* frames,
+                                                                 int apply, unsigned long long* counts,
+                                                                 unsigned* frame_nonfinite) {
+  const int k = blockIdx.y;
+  const ThresholdFrame tf = frames[k];
+  float* img = slots + static_cast<int64_t>(slot_of_frame[tf.frame]) * stride;
+  const bool ap = apply != 0;
+  unsigned hot = 0, cold = 0, nonf = 0;
+  const int64_t quads = pixels / 4;
+  const int64_t t0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t step = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  float4* img4 = reinterpret_cast<float4*>(img);
+  for (int64_t q = t0; q < quads; q += step) {
+    float4 v = img4[q];
+    bool changed = threshold_classify(v.x, tf.low, tf.high, ap, hot, cold, nonf);
+    changed |= threshold_classify(v.y, tf.low, tf.high, ap, hot, cold, nonf);
+    changed |= threshold_classify(v.z, tf.low, tf.high, ap, hot, cold, nonf);
+    changed |= threshold_classify(v.w, tf.low, tf.high, ap, hot, cold, nonf);
+    if (changed) img4[q] = v;
+  }
+  for (int64_t p = quads * 4 + t0; p < pixels; p += step) {
+    float x = img[p];
+    if (threshold_classify(x, tf.low, tf.high, ap, hot, cold, nonf)) img[p] = x;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    hot += __shfl_xor_sync(0xffffffffu, hot, off);
+    cold += __shfl_xor_sync(0xffffffffu, cold, off);
+    nonf += __shfl_xor_sync(0xffffffffu, nonf, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    unsigned long long* c = counts + static_cast<int64_t>(k) * 3;
+    if (hot) atomicAdd(c, static_cast<unsigned long long>(hot));
+    if (cold) atomicAdd(c + 1, static_cast<unsigned long long>(cold));
+    if (nonf) atomicAdd(c + 2, static_cast<unsigned long long>(nonf));
+    if (ap && hot + cold) atomicAdd(frame_nonfinite + tf.frame, hot + cold);
+  }
+}
+
+}  // namespace gg
+
+extern "C" int gg_stack_cosmetic_threshold(gg_stack* s, const int64_t* indices, int64_t count,
+                                           const float* low_thresholds, const float* high_thresholds, int32_t apply,
+                                           int64_t* host_counts) {
+  using namespace gg;
+  GG_API_BEGIN
+  require(s != nullptr && indices != nullptr && low_thresholds != nullptr && high_thresholds != nullptr,
+          "null argument");
+  require(count > 0 && count <= 65535, "batch cosmetic threshold application supports at most 65535 frames per launch");
+  std::vector<ThresholdFrame> frames(static_cast<size_t>(count));
+  for (int64_t k = 0; k < count; ++k) {
+    const float lo = low_thresholds[k], hi = high_thresholds[k];
+    require(!std::isnan(lo) && !std::isnan(hi) && lo <= hi,
+            "cosmetic thresholds must be finite-or-infinite values with low <= high");
+    stack_require_loaded(s, indices[k], "source-DQ cosmetic threshold mask");
+    frames[static_cast<size_t>(k)] = ThresholdFrame{static_cast<int>(indices[k]), lo, hi, 0};
+  }
+  stack_activate(s);
+  const size_t count_bytes = sizeof(unsigned long long) * 3 * static_cast<size_t>(count);
+  const size_t frame_bytes = sizeof(ThresholdFrame) * static_cast<size_t>(count);
+  unsigned char* buf = nullptr;
+  check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&buf), count_bytes + frame_bytes, s->stream),
+             "cudaMallocAsync(cosmetic threshold)");
+  auto* d_counts = reinterpret_cast<unsigned long long*>(buf);
+  auto* d_frames = reinterpret_cast<ThresholdFrame*>(buf + count_bytes);
+  check_cuda(cudaMemsetAsync(d_counts, 0, count_bytes, s->stream), "cudaMemsetAsync(cosmetic threshold counts)");
+  upload_params(s->stream, d_frames, frames.data(), frame_bytes, "cudaMemcpyAsync(cosmetic threshold frames)");
+  const unsigned per_frame = grid_for(static_cast<size_t>((s->pixels + 3) / 4), 256,
+                                      std::max(1, 8 / static_cast<int>(std::min<int64_t>(count, 8))));
+  note_launch();
+  cosmetic_threshold_kernel<<<dim3(per_frame, static_cast<unsigned>(count)), 256, 0, s->stream>>>(
+      s->d_slots, s->d_slot_of_frame, s->stride, s->pixels, d_frames, apply ? 1 : 0, d_counts, s->d_frame_nonfinite);
+  check_cuda(cudaGetLastError(), "cosmetic_threshold launch");
+  std::vector<unsigned long long> host(3 * static_cast<size_t>(count));
+  check_cuda(cudaMemcpyAsync(host.data(), d_counts, count_bytes, cudaMemcpyDeviceToHost, s->stream),
+             "cudaMemcpyAsync(cosmetic threshold counts)");
+  check_cuda(cudaFreeAsync(buf, s->stream), "cudaFreeAsync(cosmetic threshold)");
+  check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize(cosmetic threshold)");
+  if (host_counts)
+    for (size_t i = 0; i < host.size(); ++i) host_counts[i] = static_cast<int64_t>(host[i]);
+  GG_API_END
+}

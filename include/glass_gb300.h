@@ -545,6 +545,17 @@ typedef struct {
 
 int gg_stack_cosmetic_mask(gg_stack* stack, const int64_t* indices, int64_t count,
                            const gg_cosmetic_params_t* params, gg_cosmetic_result_t* host_out);
+/* Replaces apply_cosmetic_threshold_mask_frame(s) and
+ * count_cosmetic_threshold_mask_frame(s) (native_bindings.cpp:3243-3400,
+ * 4307-4620; kernels integration_kernels.cu:181-330): for frame indices[k]
+ * a sample is non-finite, hot (> high_thresholds[k]) or cold
+ * (< low_thresholds[k]), tested in that order; apply = 1 sets all three to
+ * NaN (and counts the hot and cold ones in the frame's non-finite counter),
+ * 0 only counts.  Thresholds may be infinite, not NaN, low <= high; at most
+ * 65535 distinct frames.  host_counts (may be NULL) receives [count][3] =
+ * hot, cold, non-finite.  Synchronises. */
+int gg_stack_cosmetic_threshold(gg_stack* stack, const int64_t* indices, int64_t count, const float* low_thresholds,
+                                const float* high_thresholds, int32_t apply, int64_t* host_counts);
 /* apply_invalid_mask (integration_kernels.cu:159-179): frame `index` samples
  * whose host_mask byte (H*W) is non-zero become NaN; host_invalid_samples
  * (may be NULL) receives the number of flagged samples.  Synchronises. */

@@ -100,3 +100,27 @@ def star_protected_defects(data, hot_sigma=8.0, cold_sigma=8.0, structure_sigma=
     out["cold"] = iso["cold"] & ~protected
     out["star_count"] = len(catalog)
     return out
+
+
+def threshold_mask(frame, low_threshold, high_threshold, apply=True):
+    """Threshold-only cosmetic mask of one frame, as
+    ResidentCalibratedStack.apply_cosmetic_threshold_mask_frame /
+    count_cosmetic_threshold_mask_frame do it on the device
+    (cpp/src/native_bindings.cpp:3243-3400 over
+    cpp/cuda/integration_kernels.cu:181-232): every sample is tested in the
+    order non-finite, > high (hot), < low (cold), the thresholds compared as
+    float32.  Returns (frame after the call, hot, cold, non-finite counts);
+    with apply the three classes become NaN, otherwise the frame is returned
+    unchanged."""
+    x = np.asarray(frame, dtype=_F32)
+    lo, hi = _F32(low_threshold), _F32(high_threshold)
+    if np.isnan(lo) or np.isnan(hi) or lo > hi:
+        raise ValueError("cosmetic thresholds must be finite-or-infinite values with low <= high")
+    nonfinite = ~np.isfinite(x)
+    with np.errstate(invalid="ignore"):
+        hot = ~nonfinite & (x > hi)
+        cold = ~nonfinite & ~hot & (x < lo)
+    out = x.copy()
+    if apply:
+        out[nonfinite | hot | cold] = np.nan
+    return out, int(hot.sum()), int(cold.sum()), int(nonfinite.sum())
